@@ -1,0 +1,289 @@
+/*
+ * scone_gpu.h -- C ABI of libsconegpu, a GB300 (sm_103a) implementation of SCONE's
+ * Monte Carlo particle-tracking cycle.
+ *
+ * The ABI is what a Fortran physicsPackage binds with ISO_C_BINDING: plain pointers,
+ * sizes and int32 status codes, no C++ or torch types.  Every entry point returns
+ * SG_OK (0) or a negative SG_ERR_* code; sg_last_error() gives the message.
+ *
+ * Conventions shared with SCONE (so arrays can be passed straight from the Fortran side):
+ *   - material indices are 1-based (matIdx); 0 is OUTSIDE_MAT, 2147483647 is VOID_MAT
+ *     (SharedModules/universalVariables.f90:45-48);
+ *   - a cell/universe fill is matIdx (>= 0) or -uniIdx (1-based universe index)
+ *     (Geometry/Universes/universe_inter.f90:477-507);
+ *   - energy groups are 1-based; the MG scattering matrix P0 is stored with the incident
+ *     group as the row, exactly as in an MG xsFile (multiScatterMG_class.f90:321-336);
+ *   - bins of one tally admin are returned as SCONE's scoreMemory `bins(N,{BIN,CSUM,CSUM2})`,
+ *     Fortran column-major (Tallies/scoreMemory_class.f90:16-18,87-97).
+ *
+ * The library is one handle per GPU stream; a handle is not thread-safe and is called from
+ * the master thread (outside `!$omp parallel`).
+ */
+#ifndef SCONE_GPU_H
+#define SCONE_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define SG_OK              0
+#define SG_ERR_BAD_ARG    -1
+#define SG_ERR_OOM        -2
+#define SG_ERR_BANK_OVERFLOW -3
+#define SG_ERR_UNDEF_MAT  -4
+#define SG_ERR_OVERLAP    -5
+#define SG_ERR_NAN        -6
+#define SG_ERR_TIMEOUT    -7
+#define SG_ERR_CUDA       -8
+#define SG_ERR_STATE      -9
+#define SG_ERR_LOST      -10
+
+/* ---------------------------------------------------------------- constants */
+#define SG_MAX_NEST       12      /* HARDCODED_MAX_NEST, universalVariables.f90:10 */
+#define SG_SURF_NPAR       6
+#define SG_VOID_MAT       2147483647
+#define SG_UNDEF_MAT      2147483646
+#define SG_OVERLAP_MAT    2147483645
+
+/* surface types (Geometry/Surfaces) */
+#define SG_SURF_XPLANE     1      /* aPlane_class.f90   par: a0                          */
+#define SG_SURF_YPLANE     2
+#define SG_SURF_ZPLANE     3
+#define SG_SURF_PLANE      4      /* plane_class.f90    par: c1 c2 c3 c4 (normalised here) */
+#define SG_SURF_XCYL       5      /* cylinder_class.f90 par: ox oy oz r                  */
+#define SG_SURF_YCYL       6
+#define SG_SURF_ZCYL       7
+#define SG_SURF_SPHERE     8      /* sphere_class.f90   par: ox oy oz r                  */
+#define SG_SURF_BOX        9      /* box_class.f90      par: ox oy oz hx hy hz           */
+#define SG_SURF_XSQCYL    10      /* squareCylinder_class.f90 par: ox oy oz hx hy hz     */
+#define SG_SURF_YSQCYL    11
+#define SG_SURF_ZSQCYL    12
+
+/* universe types (Geometry/Universes) */
+#define SG_UNI_ROOT        1      /* ipar: border surface (0-based)        fills: [inside]        */
+#define SG_UNI_CELL        2      /* ipar: cell indices (0-based)          fills: one per cell    */
+#define SG_UNI_PIN         3      /* dpar: finite radii, ascending         fills: n_radii + 1     */
+#define SG_UNI_LAT         4      /* ipar: nx ny nz(0 = 2D) offset(0/1)    dpar: px py pz
+                                     fills: nx*ny*nz in local-ID order (x fastest, y, z) + pad   */
+
+/* boundary conditions (universalVariables.f90:57-59) */
+#define SG_BC_VACUUM       0
+#define SG_BC_REFLECTIVE   1
+#define SG_BC_PERIODIC     2
+
+/* precision forms */
+#define SG_PREC_FP64       0      /* all-FP64 verification mode                                  */
+#define SG_PREC_MIXED      1      /* FP32 XS/distances/sampling, FP64 positions and tally sums   */
+
+/* transport operators (transportOperatorFactory_func.f90:48-60) */
+#define SG_TRANSPORT_ST    1      /* transportOperatorST, distance cache on                      */
+#define SG_TRANSPORT_DT    2      /* transportOperatorDT                                         */
+#define SG_TRANSPORT_ST_NOCACHE 3 /* transportOperatorST { cache 0; }                           */
+
+/* tally clerks (Tallies/TallyClerks) */
+#define SG_CLERK_COLLISION      1 /* collisionClerk_class.f90                                    */
+#define SG_CLERK_TRACK          2 /* trackClerk_class.f90                                        */
+#define SG_CLERK_KEFF_ANALOG    3 /* keffAnalogClerk_class.f90  (3 bins)                         */
+#define SG_CLERK_KEFF_IMPLICIT  4 /* keffImplicitClerk_class.f90 (5 bins)                        */
+
+/* tally map axes (Tallies/TallyMaps) */
+#define SG_AXIS_X          1      /* spaceMap axis x, lin grid                                   */
+#define SG_AXIS_Y          2
+#define SG_AXIS_Z          3
+#define SG_AXIS_GROUP      4      /* MG group axis (no SCONE counterpart: energyMap maps MG to 0) */
+#define SG_AXIS_MATERIAL   5      /* materialMap over 1..n                                       */
+
+/* tally responses: 0 = fluxResponse, otherwise a macroResponse MT (endfConstants.f90:116-130) */
+#define SG_RESP_FLUX       0
+
+/* ---------------------------------------------------------------- descriptions */
+
+typedef struct sg_geometry_desc {
+  int32_t        n_surf;
+  const int32_t* surf_type;     /* [n_surf]                     */
+  const double*  surf_par;      /* [n_surf][SG_SURF_NPAR]       */
+  int32_t        border_surf;   /* 0-based index of the root border surface  */
+  int32_t        bc[6];         /* -x +x -y +y -z +z, applied to the border (geometryStd `boundary`) */
+  int32_t        n_cell;
+  const int32_t* cell_ptr;      /* [n_cell+1] into cell_surf    */
+  const int32_t* cell_surf;     /* signed 1-based surface index (-k: -ve halfspace of surface k) */
+  int32_t        n_uni;
+  const int32_t* uni_type;      /* [n_uni]                      */
+  const double*  uni_origin;    /* [n_uni][3]                   */
+  const int32_t* uni_iptr;      /* [n_uni+1] into uni_ipar      */
+  const int32_t* uni_ipar;
+  const int32_t* uni_dptr;      /* [n_uni+1] into uni_dpar      */
+  const double*  uni_dpar;
+  const int32_t* uni_fptr;      /* [n_uni+1] into uni_fill      */
+  const int32_t* uni_fill;      /* fills per local cell: matIdx or -uniIdx */
+  int32_t        root_uni;      /* 0-based index of the root universe */
+} sg_geometry_desc;
+
+typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN = P0 */
+  int32_t        n_mat;
+  int32_t        n_g;
+  const double*  capture;       /* [n_mat][n_g]                 */
+  const double*  fission;       /* [n_mat][n_g], read where fissile */
+  const double*  nu;            /* [n_mat][n_g]                 */
+  const double*  chi;           /* [n_mat][n_g]                 */
+  const double*  p0;            /* [n_mat][n_g (in)][n_g (out)] */
+  const double*  prod;          /* [n_mat][n_g (in)][n_g (out)] scatteringMultiplicity */
+  const int32_t* fissile;       /* [n_mat] 0/1                  */
+  double         avg_dist;      /* `avgDist`; <= 0 means none   */
+} sg_mg_desc;
+
+typedef struct sg_axis_desc {
+  int32_t kind;                 /* SG_AXIS_*                    */
+  int32_t n;                    /* number of bins               */
+  double  min, max;             /* lin grid bounds (space axes) */
+} sg_axis_desc;
+
+typedef struct sg_clerk_desc {
+  int32_t      type;            /* SG_CLERK_*                   */
+  int32_t      handle_virtual;  /* collision clerks: 1 (default) scores virtual collisions with Sigma_track */
+  int32_t      n_resp;          /* 1..4                         */
+  int32_t      resp[4];         /* SG_RESP_FLUX or macro MT     */
+  int32_t      n_axes;          /* 0..3 (multiMap, first axis fastest) */
+  sg_axis_desc axes[3];
+  int32_t      filter_g_top;    /* energyFilter for MG: pass if g_top <= G <= g_low; 0 = no filter */
+  int32_t      filter_g_low;
+} sg_clerk_desc;
+
+typedef struct sg_tally_desc {  /* tallyAdmin_class.f90:162-255 */
+  int32_t              n_clerks;
+  const sg_clerk_desc* clerks;
+  int32_t              batch_size;    /* cycles per batch (>= 1) */
+  int32_t              norm_clerk;    /* -1: no `norm`; else clerk index whose first bin normalises */
+  double               norm_val;
+} sg_tally_desc;
+
+typedef struct sg_point_source_desc {  /* pointSource_class.f90:189-270, MG */
+  double  r[3];
+  double  dir[3];
+  int32_t isotropic;
+  int32_t G;                    /* used when n_prob_g == 0       */
+  int32_t n_prob_g;
+  const double* prob_g;         /* [n_prob_g]                    */
+} sg_point_source_desc;
+
+typedef struct sg_config {
+  int32_t precision;            /* SG_PREC_*                     */
+  int32_t transport;            /* SG_TRANSPORT_*                */
+  int32_t device;               /* CUDA device ordinal           */
+  int32_t max_bank;             /* capacity of each device bank (particles) */
+  int32_t record_histories;     /* 1: keep per-history collision counts and end RNG states */
+} sg_config;
+
+/* A particle bank as SoA host arrays of SCONE's particleStateData (particle_class.f90:50-65).
+ * Unused arrays may be NULL on input; on output every non-NULL array is written. */
+typedef struct sg_bank {
+  double*  wgt;                 /* [n]    */
+  double*  r;                   /* [n][3] */
+  double*  dir;                 /* [n][3] */
+  int32_t* G;                   /* [n]    */
+  double*  time;                /* [n]    */
+  int32_t* brood_id;            /* [n]    */
+} sg_bank;
+
+typedef struct sg_cycle_stats {
+  int64_t n_histories;
+  int64_t n_events;             /* flight segments incl. virtual collisions (device-counted) */
+  int64_t n_collisions;         /* real collisions */
+  int64_t n_next;               /* fission sites written to the next bank */
+  double  start_weight;         /* popWeight of the transported bank */
+  double  end_weight;           /* popWeight of the produced bank    */
+  double  k_eff;                /* k used for this cycle              */
+  double  k_new;                /* k estimate after the cycle (eigen device cycles) */
+} sg_cycle_stats;
+
+typedef struct sg_handle_t* sg_handle;
+
+/* ---------------------------------------------------------------- lifetime */
+
+/* new transportOperatorGPU: transportOperatorFactory_func.f90:36-60 + transportOperator%init */
+int32_t sg_create(const sg_config* cfg, sg_handle* out);
+int32_t sg_destroy(sg_handle h);
+/* copies the last error message (NUL-terminated, truncated to len) */
+int32_t sg_last_error(sg_handle h, char* buf, size_t len);
+
+/* ---------------------------------------------------------------- uploads (host arrays copied) */
+
+/* geometryStd%init: csg_class.f90:50-207 and geomGraph_class.f90:60-232 (shrunk graph) */
+int32_t sg_upload_geometry(sg_handle h, const sg_geometry_desc* g);
+/* baseMgNeutronDatabase%init + activate/initMajorant: baseMgNeutronDatabase_class.f90:340-503 */
+int32_t sg_upload_mg(sg_handle h, const sg_mg_desc* mg);
+/* tallyAdmin%init: tallyAdmin_class.f90:162-255; returns an admin id */
+int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out);
+/* tallyAdmin%push: tallyAdmin_class.f90 (attachment receives every report first) */
+int32_t sg_attach_tally(sg_handle h, int32_t admin, int32_t attachment);
+/* pointSource%init for fixed-source runs: pointSource_class.f90 */
+int32_t sg_set_point_source(sg_handle h, const sg_point_source_desc* src);
+
+/* ---------------------------------------------------------------- cycle (host banks) */
+
+/* source%generate (source_inter.f90:98-119): particle i uses master + stride(i), i = 1..n */
+int32_t sg_generate_source(sg_handle h, uint64_t master_state, int32_t n, sg_bank* out);
+
+/* The `gen:` history loop of fixedSource/eigenPhysicsPackage%cycles
+ * (fixedSourcePhysicsPackage_class.f90:198-261, eigenPhysicsPackage_class.f90:211-252):
+ * history n (1-based) of `in` starts with RNG master + stride(n), is placed, transported and
+ * collided until death, scoring into tally admin `admin` (and its attachment).
+ * Fission sites are returned in `next` sorted by brood ID (the order normSize_Repr sorts to);
+ * `next_cap` is its capacity.  `k_eff` is the k used for fission-site weights. */
+int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t n,
+                          uint64_t master_state, double k_eff,
+                          sg_bank* next, int32_t next_cap, sg_cycle_stats* stats);
+
+/* tallyAdmin%reportCycleStart / reportCycleEnd (tallyAdmin_class.f90:672-788):
+ * pop weights are popWeight() of the start and end dungeons, k_end is end%k_eff. */
+int32_t sg_tally_cycle_start(sg_handle h, int32_t admin, double start_pop_weight);
+int32_t sg_tally_cycle_end(sg_handle h, int32_t admin, double end_pop_weight, double k_end);
+
+/* scoreMemory bins(N,3) column-major of one admin (N from sg_tally_size) */
+int32_t sg_tally_size(sg_handle h, int32_t admin, int64_t* n_bins);
+int32_t sg_get_bins(sg_handle h, int32_t admin, double* bins, int64_t n_bins);
+/* keffResult of the first k clerk of an admin: mean and STD (keff clerks getResult) */
+int32_t sg_get_keff(sg_handle h, int32_t admin, double* k, double* std);
+
+/* ---------------------------------------------------------------- device-resident cycles */
+
+/* fissionSource (fissionSource_class.f90:149-271) sampled on the device into the resident
+ * bank: particle i uses master + stride(i); afterwards master is strided by pop
+ * (eigenPhysicsPackage_class.f90:348-366). */
+int32_t sg_eigen_init(sg_handle h, int32_t pop, uint64_t master_state, double k0);
+/* One whole eigenvalue cycle on the resident banks: gen loop, cleanPop, stride(pop+1),
+ * reportCycleEnd, normSize_Repr, stride(1), dungeon flip and k update
+ * (eigenPhysicsPackage_class.f90:203-338).  `admin` is the cycle's tally admin; the
+ * k estimate is read from attachment `atch`. */
+int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats* stats);
+/* current master RNG state and k of the resident eigen run */
+int32_t sg_eigen_state(sg_handle h, uint64_t* master_state, double* k);
+/* copy the resident "this cycle" bank to the host (pop particles) */
+int32_t sg_eigen_get_bank(sg_handle h, sg_bank* out, int32_t cap, int32_t* pop);
+
+/* fixedSourcePhysicsPackage%cycles, one batch, fully on the device: point source generation,
+ * stride(n), gen loop, stride(n), reportCycleEnd.  master_state is updated in place. */
+int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* master_state,
+                              sg_cycle_stats* stats);
+
+/* ---------------------------------------------------------------- verification records */
+
+/* Per-history records of the last gen loop (needs cfg.record_histories): number of real
+ * collisions (particle%collisionN increments) and the RNG state at history end. */
+int32_t sg_get_history_records(sg_handle h, int32_t* collisions, uint64_t* rng_end, int32_t n);
+
+/* ---------------------------------------------------------------- RNG (RNG_class.f90) */
+
+/* n draws of `get` starting from *state (state advanced); writes xi in [0,1) */
+int32_t sg_rng_draws(uint64_t* state, double* out, int32_t n);
+/* skip(k) (RNG_class.f90:251-304), k may be negative */
+uint64_t sg_rng_skip(uint64_t state, int64_t k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCONE_GPU_H */

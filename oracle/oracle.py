@@ -1,0 +1,317 @@
+"""TEST INFRASTRUCTURE: ctypes loader of the CPU oracle (liboracle built from scone_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this module.  The oracle is a
+scalar restatement of SCONE's algorithm and is never a product code path.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from scone_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libsconeoracle.so")
+
+
+def build(force=False):
+    src = os.path.join(HERE, "scone_oracle.cpp")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        i32, i64, u64, f64 = C.c_int32, C.c_int64, C.c_uint64, C.c_double
+        P = C.POINTER
+        sig = {
+            "or_create": (i32, [i32, P(vp)]), "or_destroy": (i32, [vp]),
+            "or_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+            "or_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
+            "or_upload_mg": (i32, [vp, P(abi.MGDesc)]),
+            "or_upload_tally": (i32, [vp, P(abi.TallyDesc), P(i32)]),
+            "or_attach_tally": (i32, [vp, i32, i32]),
+            "or_set_point_source": (i32, [vp, P(abi.PointSourceDesc)]),
+            "or_generate_source": (i32, [vp, u64, i32, P(abi.Bank)]),
+            "or_transport_bank": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(abi.CycleStats)]),
+            "or_tally_cycle_start": (i32, [vp, i32, f64]), "or_tally_cycle_end": (i32, [vp, i32, f64, f64]),
+            "or_tally_size": (i32, [vp, i32, P(i64)]), "or_get_bins": (i32, [vp, i32, P(f64), i64]),
+            "or_get_keff": (i32, [vp, i32, P(f64), P(f64)]),
+            "or_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
+            "or_eigen_init": (i32, [vp, i32, u64, f64]), "or_eigen_cycle": (i32, [vp, i32, i32, P(abi.CycleStats)]),
+            "or_eigen_state": (i32, [vp, P(u64), P(f64)]), "or_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
+            "or_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
+            "or_rng_draws": (i32, [P(u64), P(f64), i32]), "or_rng_skip": (u64, [u64, i64]),
+            "or_surf_eval": (i32, [i32, P(f64), P(i32), P(f64), P(f64), P(f64)]),
+            "or_surf_bc": (i32, [i32, P(f64), P(i32), i32, P(f64), P(f64)]),
+            "or_coords_init": (i32, [vp, P(f64), P(f64)]), "or_coords_place": (i32, [vp]),
+            "or_coords_move": (i32, [vp, i32, P(f64), P(i32)]),
+            "or_coords_get": (i32, [vp, i32, P(f64), P(f64), P(i32)]),
+            "or_what_is_at": (i32, [vp, P(f64), P(f64), P(i32), P(i32)]),
+            "or_bounds": (i32, [vp, P(f64)]), "or_mg_info": (i32, [vp, i32, i32, P(f64)]),
+            "or_rotate_vector": (i32, [P(f64), f64, f64, P(f64)]),
+            "or_scoremem_new": (i32, [i64, i32, P(vp)]), "or_scoremem_free": (i32, [vp]),
+            "or_scoremem_score": (i32, [vp, f64, i64]), "or_scoremem_accumulate": (i32, [vp, f64, i64]),
+            "or_scoremem_close": (i32, [vp, f64]), "or_scoremem_result": (i32, [vp, i64, i32, P(f64), P(f64)]),
+            "or_timed_gen_loop": (i64, [vp, i32, P(abi.Bank), i32, u64, f64, i32, P(i64)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = res, args
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """Python face of the oracle with the same methods as scone_gb300.TransportOperatorGPU."""
+
+    def __init__(self, problem=None, transport=abi.TRANSPORT_ST):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self._keep = []
+        self._check(self.L.or_create(transport, C.byref(self.h)))
+        if problem is not None:
+            self.upload_geometry(problem.geometry)
+            if problem.mg is not None:
+                self.upload_mg(problem.mg)
+            if problem.source:
+                self.set_point_source(**problem.source)
+
+    def _check(self, rc):
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            self.L.or_last_error(self.h, buf, 512)
+            raise RuntimeError(f"oracle error {rc}: {buf.value.decode()}")
+        return rc
+
+    def close(self):
+        if self.h:
+            self.L.or_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_geometry(self, g):
+        s, keep = abi.geometry_struct(g)
+        self._keep.append(keep)
+        self._check(self.L.or_upload_geometry(self.h, C.byref(s)))
+
+    def upload_mg(self, m):
+        s, keep = abi.mg_struct(m)
+        self._keep.append(keep)
+        self._check(self.L.or_upload_mg(self.h, C.byref(s)))
+
+    def upload_tally(self, clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
+        t, arr = abi.tally_struct(clerks, batch_size, norm_clerk, norm_val)
+        self._keep.append(arr)
+        a = C.c_int32()
+        self._check(self.L.or_upload_tally(self.h, C.byref(t), C.byref(a)))
+        return a.value
+
+    def attach_tally(self, admin, atch):
+        self._check(self.L.or_attach_tally(self.h, admin, atch))
+
+    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
+        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g)
+        self._keep.append((s, keep))
+        self._check(self.L.or_set_point_source(self.h, C.byref(s)))
+
+    def generate_source(self, master, n):
+        b = abi.HostBank(n)
+        self._check(self.L.or_generate_source(self.h, C.c_uint64(master), n, C.byref(b.struct)))
+        return b
+
+    def transport_bank(self, admin, bank, master, k_eff=1.0, next_cap=None):
+        n = bank.n
+        cap = next_cap if next_cap is not None else max(4 * n, 16)
+        nxt = abi.HostBank(cap)
+        st = abi.CycleStats()
+        self._check(self.L.or_transport_bank(self.h, admin, C.byref(bank.struct), n, C.c_uint64(master),
+                                             k_eff, C.byref(nxt.struct), cap, C.byref(st)))
+        return nxt, st
+
+    def tally_cycle_start(self, admin, w):
+        self._check(self.L.or_tally_cycle_start(self.h, admin, w))
+
+    def tally_cycle_end(self, admin, w, k=1.0):
+        self._check(self.L.or_tally_cycle_end(self.h, admin, w, k))
+
+    def bins(self, admin):
+        n = C.c_int64()
+        self._check(self.L.or_tally_size(self.h, admin, C.byref(n)))
+        out = np.zeros(3 * n.value)
+        self._check(self.L.or_get_bins(self.h, admin, out.ctypes.data_as(C.POINTER(C.c_double)), n.value))
+        return out.reshape(3, n.value).T.copy()
+
+    def keff(self, admin):
+        k, s = C.c_double(), C.c_double()
+        self._check(self.L.or_get_keff(self.h, admin, C.byref(k), C.byref(s)))
+        return k.value, s.value
+
+    def history_records(self, n):
+        c = np.zeros(n, np.int32)
+        r = np.zeros(n, np.uint64)
+        self._check(self.L.or_get_history_records(self.h, c.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  r.ctypes.data_as(C.POINTER(C.c_uint64)), n))
+        return c, r
+
+    def eigen_init(self, pop, master, k0=1.0):
+        self._check(self.L.or_eigen_init(self.h, pop, C.c_uint64(master), k0))
+
+    def eigen_cycle(self, admin, atch):
+        st = abi.CycleStats()
+        self._check(self.L.or_eigen_cycle(self.h, admin, atch, C.byref(st)))
+        return st
+
+    def eigen_state(self):
+        m, k = C.c_uint64(), C.c_double()
+        self._check(self.L.or_eigen_state(self.h, C.byref(m), C.byref(k)))
+        return m.value, k.value
+
+    def eigen_bank(self, cap):
+        b = abi.HostBank(cap)
+        pop = C.c_int32()
+        self._check(self.L.or_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
+        return b, pop.value
+
+    def fixed_source_cycle(self, admin, n, master):
+        m = C.c_uint64(master)
+        st = abi.CycleStats()
+        self._check(self.L.or_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        return m.value, st
+
+    # geometry probes
+    def coords_init(self, r, u):
+        _, pr = _d(r)
+        _, pu = _d(u)
+        self.L.or_coords_init(self.h, pr, pu)
+
+    def coords_place(self):
+        self.L.or_coords_place(self.h)
+
+    def coords_move(self, mode, max_dist):
+        d = C.c_double(max_dist)
+        ev = C.c_int32()
+        self.L.or_coords_move(self.h, mode, C.byref(d), C.byref(ev))
+        return d.value, ev.value
+
+    def coords_get(self, level=0):
+        r = np.zeros(3)
+        u = np.zeros(3)
+        info = np.zeros(5, np.int32)
+        self.L.or_coords_get(self.h, level, r.ctypes.data_as(C.POINTER(C.c_double)),
+                             u.ctypes.data_as(C.POINTER(C.c_double)), info.ctypes.data_as(C.POINTER(C.c_int32)))
+        return r, u, dict(nesting=int(info[0]), mat=int(info[1]), uid=int(info[2]), local=int(info[3]), uni=int(info[4]))
+
+    def what_is_at(self, r, u=(1.0, 0.0, 0.0)):
+        _, pr = _d(r)
+        _, pu = _d(u)
+        m, i = C.c_int32(), C.c_int32()
+        self.L.or_what_is_at(self.h, pr, pu, C.byref(m), C.byref(i))
+        return m.value, i.value
+
+    def bounds(self):
+        b = np.zeros(6)
+        self.L.or_bounds(self.h, b.ctypes.data_as(C.POINTER(C.c_double)))
+        return b
+
+    def mg_info(self, mat, G):
+        o = np.zeros(6)
+        self.L.or_mg_info(self.h, mat, G, o.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(total=o[0], scatter=o[1], capture=o[2], fission=o[3], nu_fission=o[4], majorant=o[5])
+
+    def timed_gen_loop(self, admin, bank, master, k_eff=1.0, threads=0):
+        ev = C.c_int64()
+        n = self.L.or_timed_gen_loop(self.h, admin, C.byref(bank.struct), bank.n, C.c_uint64(master), k_eff,
+                                     threads, C.byref(ev))
+        return n, ev.value
+
+
+def rng_draws(state, n):
+    s = C.c_uint64(state)
+    out = np.zeros(n)
+    lib().or_rng_draws(C.byref(s), out.ctypes.data_as(C.POINTER(C.c_double)), n)
+    return out, s.value
+
+
+def rng_skip(state, k):
+    return lib().or_rng_skip(C.c_uint64(state), C.c_int64(k))
+
+
+def surf_eval(type_, par, r, u, bc=None):
+    p = np.zeros(abi.SG_SURF_NPAR)
+    p[:len(par)] = par
+    _, pp = _d(p)
+    _, pr = _d(r)
+    _, pu = _d(u)
+    out = np.zeros(5)
+    bcp = None
+    if bc is not None:
+        b = np.ascontiguousarray(bc, np.int32)
+        bcp = b.ctypes.data_as(C.POINTER(C.c_int32))
+    lib().or_surf_eval(type_, pp, bcp, pr, pu, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return dict(evaluate=out[0], distance=out[1], halfspace=bool(out[2]), going=bool(out[3]), tol=out[4])
+
+
+def surf_bc(type_, par, bc, r, u, transform=False):
+    p = np.zeros(abi.SG_SURF_NPAR)
+    p[:len(par)] = par
+    _, pp = _d(p)
+    r = np.array(r, dtype=np.float64)
+    u = np.array(u, dtype=np.float64)
+    b = np.ascontiguousarray(bc, np.int32)
+    lib().or_surf_bc(type_, pp, b.ctypes.data_as(C.POINTER(C.c_int32)), 1 if transform else 0,
+                     r.ctypes.data_as(C.POINTER(C.c_double)), u.ctypes.data_as(C.POINTER(C.c_double)))
+    return r, u
+
+
+def rotate_vector(d, mu, phi):
+    _, pd = _d(d)
+    out = np.zeros(3)
+    lib().or_rotate_vector(pd, mu, phi, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+class ScoreMemory:
+    def __init__(self, n, batch=1):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self.L.or_scoremem_new(n, batch, C.byref(self.h))
+
+    def score(self, s, idx):
+        self.L.or_scoremem_score(self.h, s, idx)
+
+    def accumulate(self, s, idx):
+        self.L.or_scoremem_accumulate(self.h, s, idx)
+
+    def close_cycle(self, f=1.0):
+        self.L.or_scoremem_close(self.h, f)
+
+    def result(self, idx, samples=-1):
+        m, s = C.c_double(), C.c_double()
+        self.L.or_scoremem_result(self.h, idx, samples, C.byref(m), C.byref(s))
+        return m.value, s.value
+
+    def __del__(self):
+        try:
+            self.L.or_scoremem_free(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,1681 @@
+// SPDX-License-Identifier: MIT
+//
+// TEST INFRASTRUCTURE -- NOT PART OF THE PRODUCT.
+//
+// A scalar CPU restatement of SCONE's particle-tracking cycle (Fortran, CambridgeNuclear/SCONE),
+// used as the correctness oracle for libsconegpu.  Only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference legs of bench.py may load it.  Every routine cites the SCONE file:line
+// it restates.  The arithmetic follows SCONE's operation order; build with -ffp-contract=off so
+// no fused multiply-add changes a rounding (gfortran -O3 without -march emits none on x86-64).
+//
+// Parity pinning: SCONE cannot be compiled in this build environment (no Fortran compiler), so the
+// restatement is pinned against the golden values of SCONE's own unit/integration tests
+// (RNG, surfaces, universes, geometryStd, MG data, scoreMemory, clerks) in tests/test_oracle_*.py,
+// and the RNG against a Python big-integer evaluation of the same recurrence.
+//
+// It consumes the same description structs as the product ABI (include/scone_gpu.h) and exposes
+// an `or_*` C ABI with the same meaning as the `sg_*` entry points.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cstdio>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include <map>
+#include <memory>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/scone_gpu.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------- constants
+// SharedModules/universalVariables.f90:21-25, numPrecision.f90:24-25
+static const double INF = 9223372036854775808.0;   // 2**63
+static const double SURF_TOL = 1.0e-12;
+static const double NUDGE = 1.0e-8;
+static const double FP_REL_TOL = 1.0e-7;
+static const double ST_TOL = (double)1.0E-12f;     // transportOperatorST_class.f90:59 (default-real literal)
+static const double ROT_TOL = (double)1.0E-8f;     // genericProcedures.f90:1067 (default-real literal)
+static const double PI = 3.14159265358979323846264338327950288;
+static const double TWO_PI = 2.0 * PI;
+static const int MAX_NEST = 12;
+
+static const int OUTSIDE_MAT = 0;
+static const int VOID_MAT = 2147483647;
+static const int UNDEF_MAT = VOID_MAT - 1;
+static const int OVERLAP_MAT = VOID_MAT - 2;
+
+// geometry events (universalVariables.f90:28-32)
+enum { COLL_EV = 1, BOUNDARY_EV = 2, CROSS_EV = 3 };
+// fates (tallyCodes.f90:23-27)
+enum { NO_FATE = 5000, ABS_FATE = 5001, LEAK_FATE = 5002 };
+// macro MTs (endfConstants.f90:116-130)
+enum { macroTotal = -1, macroDisappearance = -2, macroEscatter = -3, macroIEscatter = -4,
+       macroFission = -6, macroNuFission = -7, macroKappaFission = -80, macroAllScatter = -20,
+       macroAbsorbtion = -21, macroNonElastic = -22 };
+
+// ---------------------------------------------------------------- RNG (RandomNumbers/RNG_class.f90)
+static const uint64_t RNG_G = 2806196910506780709ULL;   // :40
+static const uint64_t RNG_MASK = 0x7FFFFFFFFFFFFFFFULL; // :43 bitMask = huge(0_int64)
+static const int64_t STRIDE = 152917;                   // :128
+
+struct RNG {
+  uint64_t s = 0;
+  // get (:147-168): seed = iand(g*seed, mask); seed = iand(seed+c, mask); rand = seed*2^-63
+  double get() {
+    s = (RNG_G * s) & RNG_MASK;
+    s = (s + 1ULL) & RNG_MASK;
+    return (double)(int64_t)s * 0x1p-63;
+  }
+  // skip (:251-304), F. Brown's O(log k) jump
+  void skip(int64_t k_in) {
+    uint64_t k;
+    if (k_in >= 0) k = (uint64_t)k_in;
+    else k = (uint64_t)INT64_MAX - (uint64_t)(-k_in) + 1ULL;   // huge(M) - abs(k) + 1
+    k &= RNG_MASK;
+    uint64_t Gk = 1, Ck = 0, gsq = RNG_G, L = 1;
+    while (k > 0) {
+      if (k & 1ULL) {
+        Gk = (Gk * gsq) & RNG_MASK;
+        Ck = (Ck * gsq) & RNG_MASK;
+        Ck = (Ck + L) & RNG_MASK;
+      }
+      L = (L * (gsq + 1ULL)) & RNG_MASK;
+      gsq = (gsq * gsq) & RNG_MASK;        // pow_of_gsq table (:61-123) = successive squares
+      k >>= 1;
+    }
+    s = (Gk * s + Ck) & RNG_MASK;
+  }
+  void stride(int32_t n) { skip(STRIDE * (int64_t)n); }   // :310-316
+};
+
+// ---------------------------------------------------------------- helpers
+static inline double sgn(double a, double b) { return std::copysign(std::fabs(a), b); }  // Fortran SIGN
+
+// gfortran NORM2: scaled sum of squares (avoids overflow), used for norm2() calls in SCONE
+static double norm2_3(const double v[3]) {
+  double scale = 1.0, ssq = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0.0) {
+      double a = std::fabs(v[i]);
+      if (scale < a) { double t = scale / a; ssq = 1.0 + ssq * t * t; scale = a; }
+      else { double t = a / scale; ssq = ssq + t * t; }
+    }
+  }
+  return scale * std::sqrt(ssq);
+}
+
+// rotateVector (SharedModules/genericProcedures.f90:1047-1084)
+static void rotateVector(const double dir[3], double mu, double phi, double out[3]) {
+  double sinPol = std::sin(phi);
+  double cosPol = std::cos(phi);
+  double u = dir[0], v = dir[1], w = dir[2];
+  double A = std::sqrt(std::max(0.0, 1.0 - mu * mu));
+  double B = std::sqrt(std::max(0.0, 1.0 - w * w));
+  if (B > ROT_TOL) {
+    out[0] = mu * u + A * (u * w * cosPol - v * sinPol) / B;
+    out[1] = mu * v + A * (v * w * cosPol + u * sinPol) / B;
+    out[2] = mu * w - A * B * cosPol;
+  } else {
+    B = std::sqrt(std::max(0.0, 1.0 - v * v));
+    out[0] = mu * u + A * (u * v * cosPol + w * sinPol) / B;
+    out[1] = mu * v - A * B * cosPol;
+    out[2] = mu * w + A * (v * w * cosPol - u * sinPol) / B;
+  }
+  double n = norm2_3(out);
+  out[0] /= n; out[1] /= n; out[2] /= n;
+}
+
+// ---------------------------------------------------------------- surfaces (Geometry/Surfaces)
+struct Surface {
+  int type = 0;
+  double p[SG_SURF_NPAR] = {0};
+  double tol = SURF_TOL;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  int axis = 2, plane0 = 0, plane1 = 1;   // cylinders / square cylinders
+
+  void build(int t, const double* par) {
+    type = t;
+    for (int i = 0; i < SG_SURF_NPAR; ++i) p[i] = par[i];
+    switch (t) {
+      case SG_SURF_XCYL: case SG_SURF_XSQCYL: axis = 0; plane0 = 1; plane1 = 2; break;
+      case SG_SURF_YCYL: case SG_SURF_YSQCYL: axis = 1; plane0 = 0; plane1 = 2; break;
+      default: axis = 2; plane0 = 0; plane1 = 1; break;
+    }
+    if (t == SG_SURF_PLANE) {                       // plane_class.f90:78-84 coeffs/norm2(coeffs(1:3))
+      double n3[3] = {par[0], par[1], par[2]};
+      double n = norm2_3(n3);
+      for (int i = 0; i < 4; ++i) p[i] = par[i] / n;
+    }
+    if (t == SG_SURF_XCYL || t == SG_SURF_YCYL || t == SG_SURF_ZCYL || t == SG_SURF_SPHERE)
+      tol = 2.0 * p[3] * SURF_TOL;                  // cylinder_class.f90:181, sphere_class.f90:107
+    else
+      tol = SURF_TOL;
+  }
+  int aplaneAxis() const { return type - SG_SURF_XPLANE; }
+
+  double evaluate(const double r[3]) const {
+    switch (type) {
+      case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
+        return r[aplaneAxis()] - p[0];                                   // aPlane_class.f90:139
+      case SG_SURF_PLANE:
+        return (r[0] * p[0] + r[1] * p[1] + r[2] * p[2]) - p[3];        // plane_class.f90:125
+      case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {        // cylinder_class.f90:222
+        double d0 = r[plane0] - p[plane0], d1 = r[plane1] - p[plane1];
+        return (d0 * d0 + d1 * d1) - p[3] * p[3];
+      }
+      case SG_SURF_SPHERE: {                                            // sphere_class.f90:143
+        double d0 = r[0] - p[0], d1 = r[1] - p[1], d2 = r[2] - p[2];
+        return (d0 * d0 + d1 * d1 + d2 * d2) - p[3] * p[3];
+      }
+      case SG_SURF_BOX: {                                               // box_class.f90:134-143
+        double m = -HUGE_VAL;
+        for (int i = 0; i < 3; ++i) m = std::max(m, std::fabs(r[i] - p[i]) - p[3 + i]);
+        return m;
+      }
+      default: {                                                        // squareCylinder evaluate
+        double a = std::fabs(r[plane0] - p[plane0]) - p[3 + plane0];
+        double b = std::fabs(r[plane1] - p[plane1]) - p[3 + plane1];
+        return std::max(a, b);
+      }
+    }
+  }
+
+  double distance(const double r[3], const double u[3]) const {
+    switch (type) {
+      case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE: {  // aPlane_class.f90:157-181
+        int ax = aplaneAxis();
+        double ra = p[0] - r[ax], ua = u[ax], d;
+        if (std::fabs(ra) < tol) d = INF;
+        else if (ua != 0.0) d = ra / ua;
+        else d = INF;
+        if (d <= 0.0 || d > INF) d = INF;
+        return d;
+      }
+      case SG_SURF_PLANE: {                                             // plane_class.f90:144-163
+        double k = u[0] * p[0] + u[1] * p[1] + u[2] * p[2];
+        double c = evaluate(r), d;
+        if (k == 0.0 || std::fabs(c) < tol) d = INF;
+        else { d = -c / k; if (d <= 0.0 || d > INF) d = INF; }
+        return d;
+      }
+      case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {        // cylinder_class.f90:231-270
+        double c = evaluate(r);
+        double k = (r[plane0] - p[plane0]) * u[plane0] + (r[plane1] - p[plane1]) * u[plane1];
+        double a = 1.0 - u[axis] * u[axis];
+        double delta = k * k - a * c, d;
+        if (delta < 0.0 || a == 0.0) d = INF;
+        else if (std::fabs(c) < tol) {
+          if (k >= 0.0) d = INF;
+          else { d = -k + std::sqrt(delta); d = d / a; }
+        } else if (c < 0.0) { d = -k + std::sqrt(delta); d = d / a; }
+        else { d = -k - std::sqrt(delta); d = d / a; if (d <= 0.0) d = INF; }
+        return std::min(d, INF);
+      }
+      case SG_SURF_SPHERE: {                                            // sphere_class.f90:152-183
+        double c = evaluate(r);
+        double k = (r[0] - p[0]) * u[0] + (r[1] - p[1]) * u[1] + (r[2] - p[2]) * u[2];
+        double delta = k * k - c, d;
+        if (delta < 0.0) d = INF;
+        else if (std::fabs(c) < tol) { if (k >= 0.0) d = INF; else d = -k + std::sqrt(delta); }
+        else if (c < 0.0) d = -k + std::sqrt(delta);
+        else { d = -k - std::sqrt(delta); if (d <= 0.0) d = INF; }
+        return d;
+      }
+      case SG_SURF_BOX: {                                               // box_class.f90:168-237
+        static const double FP_MISS_TOL = 1.0 + 10.0 * 2.220446049250313e-16;
+        double far = 1.7976931348623157e308, near = -1.7976931348623157e308;   // huge(far)
+        for (int ax = 0; ax < 3; ++ax) {
+          double rb = r[ax] - p[ax];
+          double a_far = sgn(p[3 + ax], u[ax]);
+          double a_near = -a_far;
+          double tn, tf;
+          if (u[ax] != 0.0) { tn = (a_near - rb) / u[ax]; tf = (a_far - rb) / u[ax]; }
+          else {
+            tn = sgn(INF, a_near - rb); tf = sgn(INF, a_far - rb);
+            if (tn > tf) std::swap(tn, tf);
+          }
+          far = std::min(far, tf);
+          near = std::max(near, tn);
+        }
+        double d;
+        if (far <= near * FP_MISS_TOL) d = INF;
+        else if (std::fabs(evaluate(r)) < tol) d = (std::fabs(far) >= std::fabs(near)) ? far : near;
+        else d = (near <= 0.0) ? far : near;
+        if (d <= 0.0 || d > INF) d = INF;
+        return d;
+      }
+      default: {                                                        // squareCylinder :212-270
+        static const double FP_MISS_TOL = 1.0 + 10.0 * 2.220446049250313e-16;
+        double far = 1.7976931348623157e308, near = -1.7976931348623157e308;
+        int pl[2] = {plane0, plane1};
+        for (int i = 0; i < 2; ++i) {
+          int ax = pl[i];
+          double rb = r[ax] - p[ax];
+          double a_far = sgn(p[3 + ax], u[ax]);
+          double a_near = -a_far;
+          double tn, tf;
+          if (u[ax] != 0.0) { tn = (a_near - rb) / u[ax]; tf = (a_far - rb) / u[ax]; }
+          else {
+            tn = sgn(INF, a_near - rb); tf = sgn(INF, a_far - rb);
+            if (tn > tf) std::swap(tn, tf);
+          }
+          far = std::min(far, tf);
+          near = std::max(near, tn);
+        }
+        double d;
+        if (far <= near * FP_MISS_TOL) d = INF;
+        else if (std::fabs(evaluate(r)) < tol) d = (std::fabs(far) >= std::fabs(near)) ? far : near;
+        else d = (near <= 0.0) ? far : near;
+        if (d <= 0.0 || d > INF) d = INF;
+        return d;
+      }
+    }
+  }
+
+  bool going(const double r[3], const double u[3]) const {
+    switch (type) {
+      case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
+        return u[aplaneAxis()] > 0.0;                                   // aPlane_class.f90:195
+      case SG_SURF_PLANE: {                                             // plane_class.f90:172-186
+        double proj = u[0] * p[0] + u[1] * p[1] + u[2] * p[2];
+        bool hs = proj > 0.0;
+        if (proj == 0.0) hs = evaluate(r) >= 0.0;
+        return hs;
+      }
+      case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL:          // cylinder_class.f90:281
+        return ((r[plane0] - p[plane0]) * u[plane0] + (r[plane1] - p[plane1]) * u[plane1]) >= 0.0;
+      case SG_SURF_SPHERE:                                              // sphere_class.f90:192
+        return ((r[0] - p[0]) * u[0] + (r[1] - p[1]) * u[1] + (r[2] - p[2]) * u[2]) >= 0.0;
+      case SG_SURF_BOX: {                                               // box_class.f90:253-281
+        double rl[3]; int maxCom = 0; double best = -HUGE_VAL;
+        for (int i = 0; i < 3; ++i) {
+          rl[i] = r[i] - p[i];
+          double v = std::fabs(rl[i]) - p[3 + i];
+          if (v > best) { best = v; maxCom = i; }
+        }
+        double proj = u[maxCom] * sgn(1.0, rl[maxCom]);
+        bool hs = proj > 0.0;
+        if (proj == 0.0) hs = evaluate(r) >= 0.0;
+        return hs;
+      }
+      default: {                                                        // squareCylinder :272-300
+        int pl[2] = {plane0, plane1};
+        double rl[2]; int maxCom = 0; double best = -HUGE_VAL;
+        for (int i = 0; i < 2; ++i) {
+          rl[i] = r[pl[i]] - p[pl[i]];
+          double v = std::fabs(rl[i]) - p[3 + pl[i]];
+          if (v > best) { best = v; maxCom = i; }
+        }
+        double proj = u[pl[maxCom]] * sgn(1.0, rl[maxCom]);
+        bool hs = proj > 0.0;
+        if (proj == 0.0) hs = evaluate(r) >= 0.0;
+        return hs;
+      }
+    }
+  }
+
+  // surface_inter.f90:363-378
+  bool halfspace(const double r[3], const double u[3]) const {
+    double c = evaluate(r);
+    bool hs = c > 0.0;
+    if (std::fabs(c) < tol) hs = going(r, u);
+    return hs;
+  }
+
+  // box_class.f90:380-420, squareCylinder_class.f90:430-472 (vacuum for all other surfaces)
+  void explicitBC(double r[3], double u[3]) const {
+    if (type != SG_SURF_BOX && !(type >= SG_SURF_XSQCYL && type <= SG_SURF_ZSQCYL)) return;
+    int axes[3] = {0, 1, 2}; int nax = 3;
+    if (type != SG_SURF_BOX) { axes[0] = plane0; axes[1] = plane1; nax = 2; }
+    for (int i = 0; i < nax; ++i) {
+      int ax = axes[i];
+      double r0 = r[ax] - p[ax];
+      if (std::fabs(r0) <= p[3 + ax] * (1.0 - tol)) continue;
+      int b = (r0 < 0.0) ? bc[2 * ax] : bc[2 * ax + 1];
+      if (b == SG_BC_REFLECTIVE) u[ax] = -u[ax];
+      else if (b == SG_BC_PERIODIC) r[ax] = r[ax] - 2.0 * sgn(p[3 + ax], r0);
+    }
+  }
+
+  // box_class.f90:430-487, squareCylinder_class.f90:482-544
+  void transformBC(double r[3], double u[3]) const {
+    if (type != SG_SURF_BOX && !(type >= SG_SURF_XSQCYL && type <= SG_SURF_ZSQCYL)) return;
+    int axes[3] = {0, 1, 2}; int nax = 3;
+    if (type != SG_SURF_BOX) { axes[0] = plane0; axes[1] = plane1; nax = 2; }
+    int Ri[3];
+    for (int i = 0; i < nax; ++i) {
+      int ax = axes[i];
+      double a_bar = p[3 + ax] * (1.0 - tol);
+      Ri[i] = ((int)std::ceil(std::fabs(r[ax] - p[ax]) / a_bar)) / 2;
+    }
+    for (int i = 0; i < nax; ++i) {
+      int ax = axes[i];
+      for (int t = 1; t <= Ri[i]; ++t) {
+        double r0 = r[ax] - p[ax];
+        int b = (r0 < 0.0) ? bc[2 * ax] : bc[2 * ax + 1];
+        if (b == SG_BC_REFLECTIVE) {
+          double a0 = sgn(p[3 + ax], r0) + p[ax];
+          double d = r[ax] - a0;
+          r[ax] = r[ax] - 2.0 * d;
+          u[ax] = -u[ax];
+        } else if (b == SG_BC_PERIODIC) {
+          double d = sgn(p[3 + ax], r0);
+          r[ax] = r[ax] - 2.0 * d;
+        }
+      }
+    }
+  }
+
+  // axis-aligned bounding box (boundingBox of each surface)
+  void boundingBox(double bb[6]) const {
+    for (int i = 0; i < 3; ++i) { bb[i] = -INF; bb[3 + i] = INF; }
+    if (type == SG_SURF_BOX) for (int i = 0; i < 3; ++i) { bb[i] = p[i] - p[3 + i]; bb[3 + i] = p[i] + p[3 + i]; }
+    else if (type >= SG_SURF_XSQCYL && type <= SG_SURF_ZSQCYL) {
+      int pl[2] = {plane0, plane1};
+      for (int i : pl) { bb[i] = p[i] - p[3 + i]; bb[3 + i] = p[i] + p[3 + i]; }
+    } else if (type == SG_SURF_SPHERE) for (int i = 0; i < 3; ++i) { bb[i] = p[i] - p[3]; bb[3 + i] = p[i] + p[3]; }
+    else if (type >= SG_SURF_XCYL && type <= SG_SURF_ZCYL) {
+      int pl[2] = {plane0, plane1};
+      for (int i : pl) { bb[i] = p[i] - p[3]; bb[3 + i] = p[i] + p[3]; }
+    }
+  }
+};
+
+// ---------------------------------------------------------------- coordinates (Geometry/coord_class.f90)
+struct Coord {
+  double r[3] = {0, 0, 0};
+  double dir[3] = {0, 0, 0};
+  int uniIdx = 0, uniRootID = 0, localID = 0, cellIdx = 0;
+};
+
+struct CoordList {
+  int nesting = 0;
+  Coord lvl[MAX_NEST];
+  int matIdx = UNDEF_MAT;
+  int uniqueID = -3;
+  void init(const double r[3], const double u[3]) {   // :193-203
+    takeAboveGeom();
+    for (int i = 0; i < 3; ++i) { lvl[0].r[i] = r[i]; lvl[0].dir[i] = u[i]; }
+    nesting = 1;
+  }
+  void takeAboveGeom() { nesting = 1; matIdx = UNDEF_MAT; uniqueID = -3; }   // :283-290
+  void moveGlobal(double d) {                                                  // :326-332
+    takeAboveGeom();
+    for (int i = 0; i < 3; ++i) lvl[0].r[i] = lvl[0].r[i] + d * lvl[0].dir[i];
+  }
+  void moveLocal(double d, int n) {                                            // :346-356
+    nesting = n;
+    for (int l = 0; l < n; ++l)
+      for (int i = 0; i < 3; ++i) lvl[l].r[i] = lvl[l].r[i] + d * lvl[l].dir[i];
+  }
+  void assignDirection(const double u[3]) {                                     // :418-434 (no rotated levels)
+    for (int l = 0; l < nesting; ++l) for (int i = 0; i < 3; ++i) lvl[l].dir[i] = u[i];
+  }
+  void rotate(double mu, double phi) {                                          // :367-386
+    double nd[3];
+    rotateVector(lvl[0].dir, mu, phi, nd);
+    for (int i = 0; i < 3; ++i) lvl[0].dir[i] = nd[i];
+    for (int l = 1; l < nesting; ++l) for (int i = 0; i < 3; ++i) lvl[l].dir[i] = lvl[l - 1].dir[i];
+  }
+};
+
+struct distCache {   // geometry_inter.f90:21-25
+  int lvl = 0;
+  double dist[MAX_NEST] = {0};
+  int surf[MAX_NEST] = {0};
+};
+
+// ---------------------------------------------------------------- geometry (csg + universes + graph)
+struct Universe {
+  int type = 0;
+  double origin[3] = {0, 0, 0};
+  std::vector<int> ip;
+  std::vector<double> dp;
+  std::vector<int> fill;
+  int nLocal = 0;
+  // pin
+  std::vector<double> r_sq, ptol;
+  // lattice
+  double pitch[3], corner[3], a_bar[3];
+  int sizeN[3], outLocalID = 0;
+  bool offset = true;
+  Surface outline;
+};
+
+struct Geometry {
+  std::vector<Surface> surfs;
+  std::vector<std::vector<int>> cells;   // signed 1-based surface index per cell
+  std::vector<Universe> unis;
+  std::vector<int> graphIdx, graphId;   // geomGraph array (1-based locations)
+  std::vector<int> uniBase;             // uniRootID per universe (1-based), shrunk graph
+  int rootIdx = 0;                      // 0-based
+  int borderIdx = 0;                    // 0-based
+  int uniqueCells = 0;
+
+  int build(const sg_geometry_desc* g, std::string& err) {
+    surfs.resize(g->n_surf);
+    for (int i = 0; i < g->n_surf; ++i) surfs[i].build(g->surf_type[i], g->surf_par + SG_SURF_NPAR * i);
+    borderIdx = g->border_surf;
+    for (int i = 0; i < 6; ++i) surfs[borderIdx].bc[i] = g->bc[i];
+    cells.resize(g->n_cell);
+    for (int c = 0; c < g->n_cell; ++c)
+      for (int k = g->cell_ptr[c]; k < g->cell_ptr[c + 1]; ++k) cells[c].push_back(g->cell_surf[k]);
+    unis.resize(g->n_uni);
+    for (int u = 0; u < g->n_uni; ++u) {
+      Universe& U = unis[u];
+      U.type = g->uni_type[u];
+      for (int i = 0; i < 3; ++i) U.origin[i] = g->uni_origin[3 * u + i];
+      for (int k = g->uni_iptr[u]; k < g->uni_iptr[u + 1]; ++k) U.ip.push_back(g->uni_ipar[k]);
+      for (int k = g->uni_dptr[u]; k < g->uni_dptr[u + 1]; ++k) U.dp.push_back(g->uni_dpar[k]);
+      for (int k = g->uni_fptr[u]; k < g->uni_fptr[u + 1]; ++k) U.fill.push_back(g->uni_fill[k]);
+      if (U.type == SG_UNI_ROOT) {                     // rootUniverse_class.f90:100-119
+        U.fill.resize(1);
+        U.fill.push_back(OUTSIDE_MAT);
+        U.nLocal = 2;
+      } else if (U.type == SG_UNI_CELL) {              // cellUniverse_class.f90:145-151
+        U.fill.push_back(UNDEF_MAT);
+        U.fill.push_back(OVERLAP_MAT);
+        U.nLocal = (int)U.fill.size();
+      } else if (U.type == SG_UNI_PIN) {               // pinUniverse_class.f90:76-139
+        int N = (int)U.dp.size() + 1;
+        std::vector<double> radii(U.dp);
+        radii.push_back(INF * 1.1);
+        for (int i = 0; i < N; ++i) { U.r_sq.push_back(radii[i] * radii[i]); U.ptol.push_back(2.0 * radii[i] * SURF_TOL); }
+        U.nLocal = N;
+        if ((int)U.fill.size() != N) { err = "pin universe fills mismatch"; return -1; }
+      } else if (U.type == SG_UNI_LAT) {               // latUniverse_class.f90:113-260
+        for (int i = 0; i < 3; ++i) { U.pitch[i] = U.dp[i]; U.sizeN[i] = U.ip[i]; }
+        U.offset = U.ip.size() > 3 ? U.ip[3] != 0 : true;
+        if (U.sizeN[2] == 0) { U.sizeN[2] = 1; U.pitch[2] = 2.0 * INF; }
+        for (int i = 0; i < 3; ++i) {
+          U.a_bar[i] = U.pitch[i] * 0.5 - U.pitch[i] * SURF_TOL;
+          U.corner[i] = -(U.sizeN[i] * 0.5 * U.pitch[i]);
+        }
+        U.outLocalID = U.sizeN[0] * U.sizeN[1] * U.sizeN[2] + 1;
+        double ob[SG_SURF_NPAR] = {0, 0, 0, std::fabs(U.corner[0]), std::fabs(U.corner[1]), std::fabs(U.corner[2])};
+        U.outline.build(SG_SURF_BOX, ob);
+        U.nLocal = U.outLocalID;
+        if ((int)U.fill.size() != U.nLocal) { err = "lattice fills mismatch"; return -1; }
+      }
+    }
+    rootIdx = g->root_uni;
+    // shrunk geomGraph (geomGraph_class.f90:172-232): BFS layout from root, then enumerate sinks
+    uniBase.assign(unis.size(), -1);
+    int top = 1;
+    auto layout = [&](int u) {
+      uniBase[u] = top;
+      for (int f : unis[u].fill) { graphIdx.push_back(f); graphId.push_back(0); }
+      top += (int)unis[u].fill.size();
+    };
+    layout(rootIdx);
+    for (size_t loc = 0; loc < graphIdx.size(); ++loc) {
+      int f = graphIdx[loc];
+      if (f < 0) {
+        int u = -f - 1;
+        if (u < 0 || u >= (int)unis.size()) { err = "bad universe fill"; return -1; }
+        if (uniBase[u] < 0) layout(u);
+        graphId[loc] = uniBase[u];
+      }
+    }
+    int cellsN = 0;                                 // setUniqueIDs (:309-345)
+    for (size_t i = 0; i < graphIdx.size(); ++i) if (graphIdx[i] > 0) graphId[i] = ++cellsN;
+    uniqueCells = cellsN;
+    return 0;
+  }
+
+  // universe%enter (universe_inter.f90:400-424) with findCell; no rotation
+  void enter(int u, Coord& nw, const double r[3], const double dir[3]) {
+    Universe& U = unis[u];
+    for (int i = 0; i < 3; ++i) { nw.r[i] = r[i]; nw.dir[i] = dir[i]; }
+    nw.uniIdx = u + 1;
+    for (int i = 0; i < 3; ++i) nw.r[i] = nw.r[i] - U.origin[i];
+    findCell(u, nw.localID, nw.cellIdx, nw.r, nw.dir);
+  }
+
+  void findCell(int u, int& localID, int& cellIdx, const double r[3], const double dir[3]) {
+    Universe& U = unis[u];
+    cellIdx = 0;
+    switch (U.type) {
+      case SG_UNI_ROOT:                                 // rootUniverse_class.f90:127-145
+        localID = surfs[U.ip[0]].halfspace(r, dir) ? 2 : 1;
+        return;
+      case SG_UNI_CELL: {                               // cellUniverse_class.f90:203-246 (fixed order)
+        int nc = (int)U.ip.size();
+        for (int i = 0; i < nc; ++i) {
+          if (cellInside(U.ip[i], r, dir)) { localID = i + 1; cellIdx = U.ip[i] + 1; return; }
+        }
+        localID = nc + 1;
+        return;
+      }
+      case SG_UNI_PIN: {                                // pinUniverse_class.f90:150-173
+        double rsq = r[0] * r[0] + r[1] * r[1];
+        double mul = (r[0] * dir[0] + r[1] * dir[1] >= 0.0) ? -1.0 : 1.0;
+        int N = (int)U.r_sq.size();
+        for (localID = 1; localID <= N; ++localID)
+          if (rsq < U.r_sq[localID - 1] + mul * U.ptol[localID - 1]) return;
+        return;   // localID = N + 1
+      }
+      case SG_UNI_LAT: {                                // latUniverse_class.f90:270-312
+        int ijk[3];
+        for (int i = 0; i < 3; ++i) ijk[i] = (int)std::floor((r[i] - U.corner[i]) / U.pitch[i]) + 1;
+        for (int i = 0; i < 3; ++i) {
+          double r_bar = r[i] - U.corner[i] - ijk[i] * U.pitch[i] + 0.5 * U.pitch[i];
+          if (std::fabs(r_bar) > U.a_bar[i] && r_bar * dir[i] > 0.0) ijk[i] += (dir[i] < 0.0) ? -1 : 1;
+        }
+        bool out = false;
+        for (int i = 0; i < 3; ++i) if (ijk[i] <= 0 || ijk[i] > U.sizeN[i]) out = true;
+        localID = out ? U.outLocalID : ijk[0] + U.sizeN[0] * (ijk[1] - 1 + U.sizeN[1] * (ijk[2] - 1));
+        return;
+      }
+    }
+  }
+
+  bool cellInside(int c, const double r[3], const double u[3]) {    // simpleCell_class.f90:90-111
+    bool isIt = false;
+    for (int s : cells[c]) {
+      bool sense = s > 0;
+      bool hs = surfs[std::abs(s) - 1].halfspace(r, u);
+      isIt = (hs == sense);
+      if (!isIt) return false;
+    }
+    return isIt;
+  }
+
+  static void get_ijk(int localID, const int sizeN[3], int ijk[3]) {  // latUniverse_class.f90:489-506
+    int temp = localID - 1;
+    int base = temp / sizeN[0];
+    ijk[0] = temp - sizeN[0] * base + 1;
+    temp = base;
+    base = temp / sizeN[1];
+    ijk[1] = temp - sizeN[1] * base + 1;
+    ijk[2] = base + 1;
+  }
+
+  void uniDistance(int u, double& d, int& surfIdx, const Coord& c) {
+    Universe& U = unis[u];
+    switch (U.type) {
+      case SG_UNI_ROOT:                                  // rootUniverse_class.f90:152-162
+        surfIdx = U.ip[0] + 1;
+        d = surfs[U.ip[0]].distance(c.r, c.dir);
+        return;
+      case SG_UNI_CELL: {                                // cellUniverse_class.f90:343-362, simpleCell :120-141
+        int cidx = U.ip[c.localID - 1];
+        d = INF; surfIdx = 0;
+        for (int s : cells[cidx]) {
+          double td = surfs[std::abs(s) - 1].distance(c.r, c.dir);
+          if (td < d) { d = td; surfIdx = std::abs(s); }
+        }
+        return;
+      }
+      case SG_UNI_PIN: {                                 // pinUniverse_class.f90:185-226
+        int id = c.localID, N = (int)U.r_sq.size();
+        double d_out, d_in;
+        if (id > N) d_out = INF;
+        else d_out = pinCylDist(U, id - 1, c.r, c.dir);
+        if (id == 1) d_in = INF;
+        else d_in = pinCylDist(U, id - 2, c.r, c.dir);
+        if (d_in < d_out) { surfIdx = -1; d = d_in; } else { surfIdx = -2; d = d_out; }
+        return;
+      }
+      case SG_UNI_LAT: {                                 // latUniverse_class.f90:319-373
+        if (c.localID == U.outLocalID) { surfIdx = -7; d = U.outline.distance(c.r, c.dir); return; }
+        int ijk[3]; get_ijk(c.localID, U.sizeN, ijk);
+        double r_bar[3], bounds[3];
+        for (int i = 0; i < 3; ++i) {
+          r_bar[i] = c.r[i] - U.corner[i];
+          r_bar[i] = r_bar[i] - (ijk[i] - 0.5) * U.pitch[i];
+          bounds[i] = sgn(U.pitch[i] * 0.5, c.dir[i]);
+        }
+        d = INF; int ax = 0;
+        for (int i = 0; i < 3; ++i) {
+          double td = (bounds[i] - r_bar[i]) / c.dir[i];
+          if (td < d) { d = td; ax = i; }
+        }
+        d = std::max(0.0, d);
+        d = std::min(INF, d);
+        int s = (ax + 1) * 2;
+        if (c.dir[ax] < 0.0) s -= 1;
+        surfIdx = -s;
+        return;
+      }
+    }
+  }
+
+  double pinCylDist(const Universe& U, int k, const double r[3], const double u[3]) {
+    // annulus k is a zCylinder at the origin with r_sq and surfTol = 2 r SURF_TOL
+    double c = (r[0] * r[0] + r[1] * r[1]) - U.r_sq[k];
+    double kk = r[0] * u[0] + r[1] * u[1];
+    double a = 1.0 - u[2] * u[2];
+    double delta = kk * kk - a * c, d;
+    if (delta < 0.0 || a == 0.0) d = INF;
+    else if (std::fabs(c) < U.ptol[k]) {
+      if (kk >= 0.0) d = INF;
+      else { d = -kk + std::sqrt(delta); d = d / a; }
+    } else if (c < 0.0) { d = -kk + std::sqrt(delta); d = d / a; }
+    else { d = -kk - std::sqrt(delta); d = d / a; if (d <= 0.0) d = INF; }
+    return std::min(d, INF);
+  }
+
+  void cross(int u, Coord& c, int surfIdx) {
+    Universe& U = unis[u];
+    switch (U.type) {
+      case SG_UNI_ROOT: findCell(u, c.localID, c.cellIdx, c.r, c.dir); return;   // rootUniverse :170-178
+      case SG_UNI_CELL:                                                             // cellUniverse :388-431
+        for (int i = 0; i < 3; ++i) c.r[i] = c.r[i] + c.dir[i] * NUDGE;
+        findCell(u, c.localID, c.cellIdx, c.r, c.dir);
+        return;
+      case SG_UNI_PIN:                                                              // pinUniverse :236-253
+        if (surfIdx == -1) c.localID -= 1; else c.localID += 1;
+        return;
+      case SG_UNI_LAT: findCell(u, c.localID, c.cellIdx, c.r, c.dir); return;      // latUniverse :380-387
+    }
+  }
+
+  void cellOffset(int u, const Coord& c, double off[3]) {
+    Universe& U = unis[u];
+    off[0] = off[1] = off[2] = 0.0;
+    if (U.type == SG_UNI_LAT && U.offset && c.localID != U.outLocalID) {         // latUniverse :394-414
+      int ijk[3]; get_ijk(c.localID, U.sizeN, ijk);
+      for (int i = 0; i < 3; ++i) off[i] = (ijk[i] - 0.5) * U.pitch[i] + U.corner[i];
+    }
+  }
+
+  // geometryStd%diveToMat (geometryStd_class.f90:565-619)
+  bool diveToMat(CoordList& co, int start) {
+    for (int i = start; i <= MAX_NEST; ++i) {
+      Coord& L = co.lvl[i - 1];
+      int loc = L.uniRootID + L.localID - 1;
+      int fill = graphIdx[loc - 1], id = graphId[loc - 1];
+      if (fill >= 0) { co.matIdx = fill; co.uniqueID = id; return true; }
+      if (i == MAX_NEST) break;
+      int nu = -fill - 1;
+      double off[3]; cellOffset(L.uniIdx - 1, L, off);
+      double r[3];
+      for (int k = 0; k < 3; ++k) r[k] = L.r[k] - off[k];
+      co.nesting += 1;
+      enter(nu, co.lvl[i], r, L.dir);
+      co.lvl[i].uniRootID = id;
+    }
+    return false;
+  }
+
+  // geometryStd%placeCoord (:119-147)
+  void placeCoord(CoordList& co) {
+    co.takeAboveGeom();
+    double r[3], dir[3];
+    for (int i = 0; i < 3; ++i) { r[i] = co.lvl[0].r[i]; dir[i] = co.lvl[0].dir[i]; }
+    enter(rootIdx, co.lvl[0], r, dir);
+    co.lvl[0].uniRootID = 1;
+    diveToMat(co, 1);
+  }
+
+  void whatIsAt(int& matIdx, int& uniqueID, const double r[3], const double u[3]) {  // :152-180
+    CoordList co; co.init(r, u); placeCoord(co);
+    matIdx = co.matIdx; uniqueID = co.uniqueID;
+  }
+
+  void bounds(double bb[6]) {   // :186-205
+    surfs[borderIdx].boundingBox(bb);
+    for (int i = 0; i < 3; ++i)
+      if (bb[i] <= -INF && bb[i + 3] >= INF) { bb[i] = 0.0; bb[i + 3] = 0.0; }
+  }
+
+  // closestDist / closestDist_cache (:633-717)
+  void closestDist(double& dist, int& surfIdx, int& lvl, const CoordList& co) {
+    dist = INF; surfIdx = 0; lvl = 0;
+    for (int l = 1; l <= co.nesting; ++l) {
+      double td; int ti;
+      uniDistance(co.lvl[l - 1].uniIdx - 1, td, ti, co.lvl[l - 1]);
+      if ((dist - td) >= dist * FP_REL_TOL) { dist = td; surfIdx = ti; lvl = l; }
+    }
+  }
+  void closestDist_cache(double& dist, int& surfIdx, int& lvl, const CoordList& co, distCache& cache) {
+    dist = INF; surfIdx = 0; lvl = 0;
+    for (int l = 1; l <= co.nesting; ++l) {
+      if (cache.lvl < l) {
+        uniDistance(co.lvl[l - 1].uniIdx - 1, cache.dist[l - 1], cache.surf[l - 1], co.lvl[l - 1]);
+        cache.lvl += 1;
+      }
+      double td = cache.dist[l - 1]; int ti = cache.surf[l - 1];
+      if ((dist - td) >= dist * FP_REL_TOL) { dist = td; surfIdx = ti; lvl = l; }
+    }
+  }
+
+  // move_noCache (:214-272) / move_withCache (:285-352); no fields: fieldDist = INF
+  void move(CoordList& co, double& maxDist, int& event, distCache* cache) {
+    double dist; int surfIdx, level;
+    if (cache) closestDist_cache(dist, surfIdx, level, co, *cache);
+    else closestDist(dist, surfIdx, level, co);
+    if (maxDist < dist) {
+      co.moveLocal(maxDist, co.nesting);
+      event = COLL_EV;
+      if (cache) cache->lvl = 0;
+    } else if (surfIdx == borderIdx + 1 && level == 1) {
+      co.moveGlobal(dist);
+      event = BOUNDARY_EV;
+      maxDist = dist;
+      if (cache) cache->lvl = 0;
+      surfs[borderIdx].explicitBC(co.lvl[0].r, co.lvl[0].dir);
+      placeCoord(co);
+    } else {
+      co.moveLocal(dist, level);
+      event = CROSS_EV;
+      maxDist = dist;
+      if (cache) {
+        for (int l = 0; l < level - 1; ++l) cache->dist[l] = cache->dist[l] - dist;
+        cache->lvl = level - 1;
+      }
+      cross(co.lvl[level - 1].uniIdx - 1, co.lvl[level - 1], surfIdx);
+      diveToMat(co, level);
+    }
+  }
+
+  // geometryStd%moveGlobal (:355-392)
+  void moveGlobalGeom(CoordList& co, double& maxDist, int& event) {
+    const Surface& s = surfs[borderIdx];
+    double dist = s.distance(co.lvl[0].r, co.lvl[0].dir);
+    if (maxDist < dist) { co.moveGlobal(maxDist); event = COLL_EV; }
+    else { co.moveGlobal(dist); event = BOUNDARY_EV; s.explicitBC(co.lvl[0].r, co.lvl[0].dir); maxDist = dist; }
+    placeCoord(co);
+  }
+
+  // teleport (:492-514)
+  void teleport(CoordList& co, double dist) {
+    co.moveGlobal(dist);
+    placeCoord(co);
+    if (co.matIdx == OUTSIDE_MAT) {
+      surfs[borderIdx].transformBC(co.lvl[0].r, co.lvl[0].dir);
+      placeCoord(co);
+    }
+  }
+};
+
+// ---------------------------------------------------------------- MG data
+// baseMgNeutronMaterial_class.f90:158-291, multiScatterMG_class.f90:199-336, fissionMG_class.f90:183-274
+struct MGData {
+  int nMat = 0, nG = 0;
+  std::vector<double> total, scatter, capture, fission, nuFission, chi, P0, prod;  // [m][g], P0/prod [m][gin][gout]
+  std::vector<int> fissile;
+  std::vector<double> majorant;
+  double collisionXS = 0.0;
+
+  int build(const sg_mg_desc* d, std::string& err) {
+    nMat = d->n_mat; nG = d->n_g;
+    size_t M = (size_t)nMat * nG;
+    total.assign(M, 0); scatter.assign(M, 0); capture.assign(M, 0); fission.assign(M, 0);
+    nuFission.assign(M, 0); chi.assign(M, 0);
+    P0.assign(M * nG, 0); prod.assign(M * nG, 0); fissile.assign(nMat, 0);
+    for (int m = 0; m < nMat; ++m) {
+      fissile[m] = d->fissile[m];
+      for (int gi = 0; gi < nG; ++gi)
+        for (int go = 0; go < nG; ++go) {
+          size_t k = ((size_t)m * nG + gi) * nG + go;
+          P0[k] = d->p0[k]; prod[k] = d->prod[k];
+        }
+      for (int g = 0; g < nG; ++g) {
+        size_t k = (size_t)m * nG + g;
+        double s = 0.0;                                   // scatterXSs = sum(P0, 1)
+        for (int go = 0; go < nG; ++go) s = s + P0[((size_t)m * nG + g) * nG + go];
+        scatter[k] = s;
+        capture[k] = d->capture[k];
+        if (fissile[m]) { fission[k] = d->fission[k]; nuFission[k] = d->nu[k] * d->fission[k]; }
+        total[k] = scatter[k] + capture[k];
+        if (fissile[m]) total[k] = total[k] + fission[k];
+      }
+      if (fissile[m]) {                                   // fissionMG buildFromDict chi normalisation
+        double S = 0.0;
+        for (int g = 0; g < nG; ++g) S = S + d->chi[(size_t)m * nG + g];
+        for (int g = 0; g < nG; ++g) {
+          double c = d->chi[(size_t)m * nG + g];
+          if (std::fabs(S - 1.0) > 0.01 * FP_REL_TOL) c = c / S;
+          chi[(size_t)m * nG + g] = c;
+        }
+      }
+    }
+    if (d->avg_dist > 0.0) collisionXS = 1.0 / d->avg_dist;
+    (void)err;
+    return 0;
+  }
+  void initMajorant(const std::vector<int>& activeMats) {   // baseMgNeutronDatabase_class.f90:458-503
+    majorant.assign(nG, 0.0);
+    for (int g = 0; g < nG; ++g) {
+      double xs = 0.0;
+      for (int m : activeMats) xs = std::max(xs, total[(size_t)(m - 1) * nG + g]);
+      majorant[g] = xs * 1.0;
+    }
+  }
+  double T(int m, int g) const { return total[(size_t)(m - 1) * nG + (g - 1)]; }
+};
+
+// ---------------------------------------------------------------- scoreMemory (Tallies/scoreMemory_class.f90)
+struct ScoreMemory {
+  std::vector<double> bin, csum, csum2;
+  std::vector<double> parallel;   // accumulating scores of the running batch
+  int64_t N = 0;
+  int batchN = 0, cycles = 0, batchSize = 1;
+  void init(int64_t n, int bs) {
+    N = n; bin.assign(n, 0); csum.assign(n, 0); csum2.assign(n, 0); parallel.assign(n, 0);
+    batchN = 0; cycles = 0; batchSize = bs > 0 ? bs : 1;
+  }
+  void score(double s, int64_t idx) { parallel[idx - 1] += s; }          // :215-233
+  void accumulate(double s, int64_t idx) {                                // :255-270
+    csum[idx - 1] = csum[idx - 1] + s; csum2[idx - 1] = csum2[idx - 1] + s * s;
+  }
+  bool lastCycle() const { return (cycles + 1) % batchSize == 0; }       // :377-381
+  void reduceBins() {                                                     // :403-432
+    if (lastCycle()) for (int64_t i = 0; i < N; ++i) { bin[i] = parallel[i]; parallel[i] = 0.0; }
+  }
+  void closeCycle(double normFactor) {                                    // :319-345
+    cycles += 1;
+    if (cycles % batchSize == 0) {
+      for (int64_t i = 0; i < N; ++i) {
+        double res = bin[i] * normFactor;
+        bin[i] = 0.0;
+        csum[i] = csum[i] + res;
+        csum2[i] = csum2[i] + res * res;
+      }
+      batchN += 1;
+    }
+  }
+  double getScore(int64_t idx) const { return (idx <= 0 || idx > N) ? 0.0 : bin[idx - 1]; }  // :597-608
+  void getResult(double& mean, double& STD, int64_t idx, int samples = -1) const {          // :537-573
+    int n = samples > 0 ? samples : batchN;
+    mean = csum[idx - 1] / n;
+    double inv_N = 1.0 / n;
+    double inv_Nm1 = (n != 1) ? 1.0 / (n - 1) : 1.0;
+    STD = csum2[idx - 1] * inv_N * inv_Nm1 - mean * mean * inv_Nm1;
+    STD = std::sqrt(STD);
+  }
+};
+
+// ---------------------------------------------------------------- particle (ParticleObjects/particle_class.f90)
+struct PState {   // particleState subset carried by the banks
+  double wgt = 0, r[3] = {0, 0, 0}, dir[3] = {0, 0, 0}, time = 0;
+  int G = 0, broodID = 0, matIdx = -1;
+};
+
+struct Particle {
+  CoordList coords;
+  int G = 1;
+  double w = 1.0, w0 = 1.0, time = 0.0;
+  bool isDead = false;
+  int fate = NO_FATE;
+  int collisionN = 0, broodID = 0;
+  double k_eff = 1.0;
+  RNG rng;
+  double preHistWgt = 1.0, preCollWgt = 1.0;
+  // prePath snapshot used by track clerks
+  double prePathR[3] = {0, 0, 0};
+  int prePathMat = 0, prePathG = 1;
+  int matIdx() const { return coords.matIdx; }
+};
+
+// ---------------------------------------------------------------- tallies
+struct Clerk {
+  sg_clerk_desc d;
+  int64_t addr = 1;   // 1-based memory address
+  int width = 1;
+  int64_t nbins = 1;
+  int64_t multi[3] = {1, 1, 1};
+  double step[3] = {0, 0, 0};
+  int64_t size() const {
+    if (d.type == SG_CLERK_KEFF_ANALOG) return 3;
+    if (d.type == SG_CLERK_KEFF_IMPLICIT) return 5;
+    return (int64_t)width * nbins;
+  }
+};
+
+struct TallyAdmin {
+  std::vector<Clerk> clerks;
+  ScoreMemory mem;
+  int atch = -1;
+  int64_t normAddr = -1;
+  double normVal = 1.0;
+};
+
+struct Oracle {
+  Geometry geom;
+  MGData mg;
+  std::vector<TallyAdmin> admins;
+  int transport = SG_TRANSPORT_ST;
+  std::string err;
+  sg_point_source_desc src{};
+  std::vector<double> srcProbG;
+  bool hasSource = false;
+  // per-history records of the last gen loop
+  std::vector<int32_t> recColl;
+  std::vector<uint64_t> recRng;
+  // eigen state
+  std::vector<PState> thisCycle;
+  RNG master;
+  double k_new = 1.0, keff0 = 1.0;
+  int pop = 0;
+  double nextK = 1.0;   // k_eff attached to the next-cycle dungeon
+  // probe coords for geometry unit tests
+  CoordList probe;
+  distCache probeCache;
+  int64_t nEvents = 0, nColl = 0;
+
+  // ----- clerk evaluation helpers (Tallies/TallyMaps, TallyFilters, TallyResponses)
+  int mapState(const Clerk& c, const double r[3], int G, int mat) const {
+    if (c.d.n_axes == 0) return 1;
+    int64_t idx = 1;
+    for (int a = 0; a < c.d.n_axes; ++a) {
+      const sg_axis_desc& ax = c.d.axes[a];
+      int b = 0;
+      if (ax.kind >= SG_AXIS_X && ax.kind <= SG_AXIS_Z) {        // spaceMap (spaceMap_class.f90:211-221)
+        double v = r[ax.kind - SG_AXIS_X];
+        b = (int)std::floor((v - ax.min) / c.step[a]) + 1;       // grid%search lin (grid_class.f90:225-245)
+        if (b < 1 || b >= ax.n + 1) b = 0;
+      } else if (ax.kind == SG_AXIS_GROUP) {
+        b = (G >= 1 && G <= ax.n) ? G : 0;
+      } else if (ax.kind == SG_AXIS_MATERIAL) {
+        b = (mat >= 1 && mat <= ax.n) ? mat : 0;
+      }
+      if (b == 0) return 0;                                       // multiMap (multiMap_class.f90:153-173)
+      idx = idx + (int64_t)(b - 1) * c.multi[a];
+    }
+    return (int)idx;
+  }
+  double macroXS(int mat, int G, int MT) const {                 // neutronMacroXSs%get (:143-190)
+    if (mat <= 0 || mat == VOID_MAT) return 0.0;
+    size_t k = (size_t)(mat - 1) * mg.nG + (G - 1);
+    bool f = mg.fissile[mat - 1] != 0;
+    double tot = mg.total[k], ie = mg.scatter[k], cap = mg.capture[k];
+    double fis = f ? mg.fission[k] : 0.0, nuf = f ? mg.nuFission[k] : 0.0;
+    switch (MT) {
+      case macroTotal: return tot;
+      case macroDisappearance: return cap;
+      case macroEscatter: return 0.0;
+      case macroNonElastic: return ie + fis + cap;
+      case macroIEscatter: return ie;
+      case macroAllScatter: return 0.0 + ie;
+      case macroFission: return fis;
+      case macroNuFission: return nuf;
+      case macroAbsorbtion: return cap + fis;
+      default: return 0.0;
+    }
+  }
+  double response(int code, int mat, int G) const {
+    if (code == SG_RESP_FLUX) return 1.0;
+    return macroXS(mat, G, code);                                // macroResponse_class.f90:141-172
+  }
+  bool filterPass(const Clerk& c, int G) const {                 // energyFilter_class.f90:109-127 (MG)
+    if (c.d.filter_g_top <= 0) return true;
+    return (c.d.filter_g_top <= G) && (G <= c.d.filter_g_low);
+  }
+
+  // tallyAdmin report dispatch (tallyAdmin_class.f90:466-704): attachment first, then own clerks
+  void reportInColl(int a, Particle& p, bool virt, double trackXS) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportInColl(A.atch, p, virt, trackXS);
+    for (Clerk& c : A.clerks) {
+      if (c.d.type == SG_CLERK_COLLISION) {                      // collisionClerk_class.f90:192-242
+        if (!c.d.handle_virtual && virt) continue;
+        if (!filterPass(c, p.G)) continue;
+        int bin = mapState(c, p.coords.lvl[0].r, p.G, p.matIdx());
+        if (bin == 0) continue;
+        double flux = c.d.handle_virtual ? p.w / trackXS : p.w / mg.T(p.matIdx(), p.G);
+        int64_t addr = c.addr + (int64_t)c.width * (bin - 1) - 1;
+        for (int i = 0; i < c.width; ++i) A.mem.score(response(c.d.resp[i], p.matIdx(), p.G) * flux, addr + i + 1);
+      } else if (c.d.type == SG_CLERK_KEFF_IMPLICIT) {           // keffImplicitClerk_class.f90:180-227
+        if (p.matIdx() == VOID_MAT) continue;
+        double flux = p.w / trackXS;
+        size_t k = (size_t)(p.matIdx() - 1) * mg.nG + (p.G - 1);
+        bool f = mg.fissile[p.matIdx() - 1] != 0;
+        double nuFiss = f ? mg.nuFission[k] : 0.0;
+        double absXS = mg.capture[k] + (f ? mg.fission[k] : 0.0);
+        double s1 = nuFiss * flux, s2 = absXS * flux;
+        A.mem.score(s1, c.addr + 0);
+        A.mem.score(s2, c.addr + 2);
+      }
+    }
+  }
+  void reportOutColl(int a, Particle& p, int MT) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportOutColl(A.atch, p, MT);
+    for (Clerk& c : A.clerks) {
+      if (c.d.type == SG_CLERK_KEFF_IMPLICIT) {                  // keffImplicitClerk_class.f90:241-268
+        double score = 0.0;
+        if (MT == macroAllScatter || MT == macroIEscatter) score = std::max(p.w - p.preCollWgt, 0.0);
+        if (score > 0.0) A.mem.score(score, c.addr + 1);
+      }
+    }
+  }
+  void reportPath(int a, Particle& p, double L) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportPath(A.atch, p, L);
+    for (Clerk& c : A.clerks) {
+      if (c.d.type == SG_CLERK_TRACK) {                          // trackClerk_class.f90:185-232
+        if (!filterPass(c, p.prePathG)) continue;
+        int bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat);
+        if (bin == 0) continue;
+        int64_t addr = c.addr + (int64_t)c.width * (bin - 1) - 1;
+        for (int i = 0; i < c.width; ++i)
+          A.mem.score(response(c.d.resp[i], p.prePathMat, p.G) * p.w * L, addr + i + 1);
+      }
+    }
+  }
+  void reportHist(int a, Particle& p) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportHist(A.atch, p);
+    for (Clerk& c : A.clerks)
+      if (c.d.type == SG_CLERK_KEFF_IMPLICIT && p.fate == LEAK_FATE) A.mem.score(p.w, c.addr + 3);   // :276-290
+  }
+  void reportCycleStart(int a, double startW) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportCycleStart(A.atch, startW);
+    for (Clerk& c : A.clerks) if (c.d.type == SG_CLERK_KEFF_ANALOG) A.mem.score(startW, c.addr + 0);  // keffAnalog :140-147
+  }
+  void reportCycleEnd(int a, double endW, double kEnd) {          // tallyAdmin_class.f90:721-788
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportCycleEnd(A.atch, endW, kEnd);
+    for (Clerk& c : A.clerks) if (c.d.type == SG_CLERK_KEFF_ANALOG) A.mem.score(endW, c.addr + 1);
+    A.mem.reduceBins();
+    for (Clerk& c : A.clerks) {
+      if (c.d.type == SG_CLERK_KEFF_ANALOG && A.mem.lastCycle()) {                 // keffAnalog :162-181
+        double startW = A.mem.getScore(c.addr + 0), endWs = A.mem.getScore(c.addr + 1);
+        double k = endWs / startW * kEnd;
+        A.mem.accumulate(k, c.addr + 2);
+      } else if (c.d.type == SG_CLERK_KEFF_IMPLICIT && A.mem.lastCycle()) {        // keffImplicit :306-326
+        double nuFiss = A.mem.getScore(c.addr + 0), absorb = A.mem.getScore(c.addr + 2);
+        double leak = A.mem.getScore(c.addr + 3), scatterMul = A.mem.getScore(c.addr + 1);
+        double k = nuFiss / (absorb + leak - scatterMul);
+        A.mem.accumulate(k, c.addr + 4);
+      }
+    }
+    double normFactor = 1.0;
+    if (A.normAddr > 0) {
+      double ns = A.mem.getScore(A.normAddr);
+      normFactor = A.normVal / ns;
+    }
+    A.mem.closeCycle(normFactor);
+  }
+  bool getKeff(int a, double& k, double& sd) {
+    TallyAdmin& A = admins[a];
+    for (Clerk& c : A.clerks) {
+      if (c.d.type == SG_CLERK_KEFF_ANALOG) { A.mem.getResult(k, sd, c.addr + 2); return true; }
+      if (c.d.type == SG_CLERK_KEFF_IMPLICIT) { A.mem.getResult(k, sd, c.addr + 4); return true; }
+    }
+    return false;
+  }
+
+  // ----- transport (TransportOperator)
+  double trackingXS_material(Particle& p) {          // getTrackingXS(MATERIAL_XS) (baseMgNeutronDatabase :95-133)
+    int m = p.matIdx();
+    if (m == VOID_MAT) return mg.collisionXS;
+    return std::max(mg.T(m, p.G), mg.collisionXS);
+  }
+  double trackMatXS(Particle& p) {                   // getTrackMatXS (:137-160)
+    int m = p.matIdx();
+    if (m == VOID_MAT) return 0.0;
+    return mg.T(m, p.G);
+  }
+
+  // surfaceTracking (transportOperatorST_class.f90:48-166); returns tracking XS cache value
+  void surfaceTracking(Particle& p, int admin, double& trackXS, bool useCache) {
+    distCache cache;
+    while (true) {
+      double sigmaTrack = trackingXS_material(p);
+      trackXS = sigmaTrack;
+      double dist, invSigmaTrack, sigmaT;
+      if (sigmaTrack < ST_TOL) { dist = INF; invSigmaTrack = INF; sigmaT = 0.0; }
+      else {
+        invSigmaTrack = 1.0 / sigmaTrack;
+        dist = -std::log(p.rng.get()) * invSigmaTrack;
+        sigmaT = trackMatXS(p);
+      }
+      // MG speed = 1 (particle_class.f90:481-503); timeMax = 0 -> no ageing
+      for (int i = 0; i < 3; ++i) p.prePathR[i] = p.coords.lvl[0].r[i];
+      p.prePathMat = p.matIdx(); p.prePathG = p.G;
+      int event;
+      geom.move(p.coords, dist, event, useCache ? &cache : nullptr);
+      p.time = p.time + dist / 1.0;
+      nEvents++;
+      reportPath(admin, p, dist);
+      if (p.matIdx() == OUTSIDE_MAT) { p.isDead = true; p.fate = LEAK_FATE; }
+      else if (p.matIdx() == UNDEF_MAT) { err = "Particle is in undefined material"; p.isDead = true; }
+      else if (p.matIdx() == OVERLAP_MAT) { err = "Particle is in overlapping cells"; p.isDead = true; }
+      if (p.isDead) break;
+      if (event == COLL_EV) {
+        if (p.rng.get() < sigmaT * invSigmaTrack) break;
+        else reportInColl(admin, p, true, trackXS);
+      }
+    }
+  }
+
+  // deltaTracking (transportOperatorDT_class.f90:47-131)
+  void deltaTracking(Particle& p, int admin, double& trackXS) {
+    double maj = std::max(mg.majorant[p.G - 1], mg.collisionXS);   // getTrackingXS(MAJORANT_XS)
+    trackXS = maj;
+    double majorant_inv = 1.0 / maj;
+    while (true) {
+      double distance = -std::log(p.rng.get()) * majorant_inv;
+      geom.teleport(p.coords, distance);
+      p.time = p.time + distance / 1.0;
+      nEvents++;
+      int m = p.matIdx();
+      if (m == OUTSIDE_MAT) { p.fate = LEAK_FATE; p.isDead = true; break; }
+      if (m == VOID_MAT) { reportInColl(admin, p, true, trackXS); continue; }
+      if (m == UNDEF_MAT || m == OVERLAP_MAT) { err = "Particle is in undefined/overlap material"; p.isDead = true; break; }
+      double sigmaT = trackMatXS(p);
+      if (p.rng.get() < sigmaT * majorant_inv) break;
+      else reportInColl(admin, p, true, trackXS);
+    }
+  }
+
+  // collisionProcessor%collide + neutronMGstd (collisionProcessor_inter.f90:114-195,
+  // neutronMGstd_class.f90:85-297)
+  void collide(Particle& p, int admin, double trackXS, std::vector<PState>* sites) {
+    int matIdx = p.matIdx();
+    // sampleCollision (:85-129): alpha test drawn even for alpha = 0
+    (void)p.rng.get();
+    size_t k = (size_t)(matIdx - 1) * mg.nG + (p.G - 1);
+    bool fiss = mg.fissile[matIdx - 1] != 0;
+    double total = mg.total[k], elastic = 0.0, inel = mg.scatter[k], capture = mg.capture[k];
+    double r = p.rng.get();
+    // neutronMacroXSs%invert (neutronXsPackages_class.f90:211-250)
+    int C = 1;
+    double xs = total * r - elastic;
+    if (xs > 0.0) C = C + 1;
+    xs = xs - inel;
+    if (xs > 0.0) C = C + 1;
+    xs = xs - capture;
+    if (xs > 0.0) C = C + 1;
+    int MT = (C == 1) ? macroEscatter : (C == 2) ? macroIEscatter : (C == 3) ? macroDisappearance : macroFission;
+    reportInColl(admin, p, false, trackXS);
+    p.preCollWgt = p.w;
+    // implicit (:134-201): fission sites
+    if (fiss) {
+      double wgt = p.w, w0 = p.preHistWgt, k_eff = p.k_eff;
+      double rand1 = p.rng.get();
+      double sig_tot = total, sig_nuFiss = mg.nuFission[k];
+      int n = (int)(std::fabs((wgt * sig_nuFiss) / (w0 * sig_tot * k_eff)) + rand1);
+      if (n >= 1) {
+        double sw = sgn(w0, wgt);
+        double r0[3] = {p.coords.lvl[0].r[0], p.coords.lvl[0].r[1], p.coords.lvl[0].r[2]};
+        for (int i = 0; i < n; ++i) {
+          // fissionMG%sampleOut (fissionMG_class.f90:183-206)
+          double mu = 2.0 * p.rng.get() - 1.0;
+          double phi = TWO_PI * p.rng.get();
+          double rem = p.rng.get();
+          int Gout = 1;
+          for (Gout = 1; Gout <= mg.nG; ++Gout) {
+            rem = rem - mg.chi[(size_t)(matIdx - 1) * mg.nG + (Gout - 1)];
+            if (rem < 0.0) break;
+          }
+          if (Gout > mg.nG) { err = "fission G_out sampling failed"; Gout = mg.nG; }
+          PState s;
+          rotateVector(p.coords.lvl[0].dir, mu, phi, s.dir);
+          for (int q = 0; q < 3; ++q) s.r[q] = r0[q];
+          s.G = Gout; s.wgt = sw; s.time = p.time; s.broodID = p.broodID; s.matIdx = matIdx;
+          if (sites) sites->push_back(s);
+        }
+      }
+    }
+    // reaction
+    if (MT == macroIEscatter || MT == macroEscatter) {
+      // inelastic (:221-252): multiScatterMG%sampleOut (:199-238)
+      double rem = p.rng.get() * inel;
+      int Gout;
+      for (Gout = 1; Gout <= mg.nG; ++Gout) {
+        rem = rem - mg.P0[((size_t)(matIdx - 1) * mg.nG + (p.G - 1)) * mg.nG + (Gout - 1)];
+        if (rem < 0.0) break;
+      }
+      if (Gout > mg.nG) { err = "scatter G_out sampling failed"; Gout = mg.nG; }
+      double mu = 2.0 * p.rng.get() - 1.0;
+      double phi = TWO_PI * p.rng.get();
+      double w_mul = mg.prod[((size_t)(matIdx - 1) * mg.nG + (p.G - 1)) * mg.nG + (Gout - 1)];
+      MT = macroIEscatter;
+      p.G = Gout;
+      p.w = p.w * w_mul;
+      p.coords.rotate(mu, phi);
+    } else {
+      p.isDead = true;   // capture / fission
+    }
+    p.collisionN += 1;
+    nColl++;
+    reportOutColl(admin, p, MT);
+    if (p.isDead) { p.fate = ABS_FATE; reportHist(admin, p); }
+  }
+
+  // one history: copy from the bank, place, history loop (eigenPhysicsPackage_class.f90:211-246)
+  void runHistory(const PState& st, int n, uint64_t master, double k, int admin,
+                  std::vector<PState>* sites, int32_t* recC, uint64_t* recR) {
+    Particle p;
+    p.rng.s = master;
+    p.rng.stride(n);
+    p.w = st.wgt; p.w0 = st.wgt;
+    p.coords.takeAboveGeom();
+    for (int i = 0; i < 3; ++i) { p.coords.lvl[0].r[i] = st.r[i]; p.coords.lvl[0].dir[i] = st.dir[i]; }
+    p.G = st.G; p.time = st.time; p.fate = NO_FATE; p.collisionN = 0; p.isDead = false;
+    p.broodID = n;
+    geom.placeCoord(p.coords);
+    p.k_eff = k;
+    p.preHistWgt = p.w; p.preCollWgt = p.w;
+    while (true) {
+      double trackXS = 0.0;
+      if (transport == SG_TRANSPORT_DT) deltaTracking(p, admin, trackXS);
+      else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_ST);
+      if (p.isDead) { reportHist(admin, p); break; }
+      collide(p, admin, trackXS, sites);
+      if (p.isDead) break;
+    }
+    if (recC) *recC = p.collisionN;
+    if (recR) *recR = p.rng.s;
+  }
+
+  int transportBank(int admin, const std::vector<PState>& in, uint64_t master, double k,
+                    std::vector<PState>& next) {
+    int n = (int)in.size();
+    recColl.assign(n, 0); recRng.assign(n, 0);
+    nEvents = 0; nColl = 0;
+    next.clear();
+    for (int i = 0; i < n; ++i) {
+      std::vector<PState> s;
+      runHistory(in[i], i + 1, master, k, admin, &s, &recColl[i], &recRng[i]);
+      next.insert(next.end(), s.begin(), s.end());
+      if (!err.empty()) return SG_ERR_LOST;
+    }
+    return SG_OK;
+  }
+
+  // pointSource / configSource sampleParticle (pointSource_class.f90:189-270)
+  PState samplePoint(RNG& rand) {
+    PState s;
+    for (int i = 0; i < 3; ++i) s.r[i] = src.r[i];
+    if (src.isotropic) {
+      double mu = 2.0 * rand.get() - 1.0;
+      double phi = TWO_PI * rand.get();
+      double x[3] = {1.0, 0.0, 0.0};
+      rotateVector(x, mu, phi, s.dir);
+    } else for (int i = 0; i < 3; ++i) s.dir[i] = src.dir[i];
+    if (!srcProbG.empty()) {
+      double r = rand.get(); int g;
+      for (g = 1; g <= (int)srcProbG.size(); ++g) { r = r - srcProbG[g - 1]; if (r < 0.0) break; }
+      if (g > (int)srcProbG.size()) g = (int)srcProbG.size() + 1;   // Fortran do-loop exit value
+      s.G = g;
+    } else s.G = src.G;
+    s.time = 0.0; s.wgt = 1.0;
+    return s;
+  }
+
+  // fissionSource sampleParticle (fissionSource_class.f90:149-271), MG, G = 1
+  int sampleFission(RNG& rand, PState& s) {
+    double bb[6]; geom.bounds(bb);
+    for (int i = 0; i < 10000; ++i) {
+      double r3[3] = {rand.get(), rand.get(), rand.get()};
+      double r[3];
+      for (int q = 0; q < 3; ++q) r[q] = (bb[3 + q] - bb[q]) * r3[q] + bb[q];
+      int matIdx, uid; double u0[3] = {1.0, 0.0, 0.0};
+      geom.whatIsAt(matIdx, uid, r, u0);
+      if (matIdx == VOID_MAT || matIdx == OUTSIDE_MAT) continue;
+      if (matIdx == UNDEF_MAT || matIdx == OVERLAP_MAT) return -1;
+      if (!mg.fissile[matIdx - 1]) continue;
+      s.matIdx = matIdx; s.wgt = 1.0; s.time = 0.0;
+      for (int q = 0; q < 3; ++q) s.r[q] = r[q];
+      double mu = 2.0 * rand.get() - 1.0;
+      double phi = TWO_PI * rand.get();
+      double rem = rand.get(); int Gout;
+      for (Gout = 1; Gout <= mg.nG; ++Gout) {
+        rem = rem - mg.chi[(size_t)(matIdx - 1) * mg.nG + (Gout - 1)];
+        if (rem < 0.0) break;
+      }
+      s.G = Gout;
+      double x[3] = {1.0, 0.0, 0.0};
+      rotateVector(x, mu, phi, s.dir);
+      return 0;
+    }
+    return -1;
+  }
+
+  // particleDungeon%normSize_Repr for one rank (particleDungeon_class.f90:431-605)
+  void sortByBroodID(std::vector<PState>& b) {   // stable counting sort (:923-981)
+    std::stable_sort(b.begin(), b.end(), [](const PState& x, const PState& y) { return x.broodID < y.broodID; });
+  }
+  void normSizeRepr(std::vector<PState>& b, int totPop, const RNG& rand) {
+    sortByBroodID(b);
+    int totSites = (int)b.size();
+    int excess = totSites - totPop;
+    int heapSize, n_duplicates;
+    if (excess < 0) { n_duplicates = (-excess) % totSites; heapSize = n_duplicates; }
+    else heapSize = excess;
+    double threshold = 1.0;
+    uint64_t seed = 0;
+    if (heapSize != 0) {
+      RNG mr = rand;
+      seed = mr.s;
+      std::vector<double> rn(totSites);
+      for (int j = 0; j < totSites; ++j) rn[j] = mr.get();
+      std::vector<double> tmp(rn);
+      std::nth_element(tmp.begin(), tmp.begin() + (heapSize - 1), tmp.end());
+      threshold = tmp[heapSize - 1];      // heapSize-th smallest = max of the heap
+    }
+    RNG rr; rr.s = seed;
+    if (excess > 0) {
+      std::vector<PState> keep;
+      for (int i = 0; i < totSites; ++i) if (rr.get() > threshold) keep.push_back(b[i]);
+      b.swap(keep);
+    } else if (excess < 0) {
+      int ts = excess + totPop;
+      int n_copies = (-excess) / ts;
+      n_duplicates = (-excess) % ts;
+      int p0 = (int)b.size();
+      std::vector<PState> out(b);
+      for (int c = 0; c < n_copies; ++c) out.insert(out.end(), b.begin(), b.begin() + p0);
+      if (n_duplicates != 0)
+        for (int i = 0; i < p0; ++i) if (rr.get() <= threshold) out.push_back(b[i]);
+      b.swap(out);
+      sortByBroodID(b);
+    }
+  }
+};
+
+}  // namespace orc
+
+using orc::Oracle;
+
+// ====================================================================== C ABI
+extern "C" {
+
+typedef struct or_handle_t* or_handle;
+
+static Oracle* O(or_handle h) { return reinterpret_cast<Oracle*>(h); }
+
+static void bankToStates(const sg_bank* b, int n, std::vector<orc::PState>& v) {
+  v.resize(n);
+  for (int i = 0; i < n; ++i) {
+    orc::PState& s = v[i];
+    s.wgt = b->wgt ? b->wgt[i] : 1.0;
+    for (int q = 0; q < 3; ++q) { s.r[q] = b->r[3 * i + q]; s.dir[q] = b->dir[3 * i + q]; }
+    s.G = b->G ? b->G[i] : 1;
+    s.time = b->time ? b->time[i] : 0.0;
+    s.broodID = b->brood_id ? b->brood_id[i] : 0;
+  }
+}
+static void statesToBank(const std::vector<orc::PState>& v, sg_bank* b, int cap) {
+  int n = std::min((int)v.size(), cap);
+  for (int i = 0; i < n; ++i) {
+    const orc::PState& s = v[i];
+    if (b->wgt) b->wgt[i] = s.wgt;
+    for (int q = 0; q < 3; ++q) { if (b->r) b->r[3 * i + q] = s.r[q]; if (b->dir) b->dir[3 * i + q] = s.dir[q]; }
+    if (b->G) b->G[i] = s.G;
+    if (b->time) b->time[i] = s.time;
+    if (b->brood_id) b->brood_id[i] = s.broodID;
+  }
+}
+
+int32_t or_create(int32_t transport, or_handle* out) {
+  Oracle* o = new Oracle();
+  o->transport = transport;
+  *out = reinterpret_cast<or_handle>(o);
+  return SG_OK;
+}
+int32_t or_destroy(or_handle h) { delete O(h); return SG_OK; }
+int32_t or_last_error(or_handle h, char* buf, size_t len) {
+  std::snprintf(buf, len, "%s", O(h)->err.c_str());
+  return SG_OK;
+}
+int32_t or_upload_geometry(or_handle h, const sg_geometry_desc* g) {
+  return O(h)->geom.build(g, O(h)->err) == 0 ? SG_OK : SG_ERR_BAD_ARG;
+}
+int32_t or_upload_mg(or_handle h, const sg_mg_desc* d) {
+  Oracle* o = O(h);
+  o->mg.build(d, o->err);
+  // activeMats = materials present in the geometry graph (geometryStd%activeMats)
+  std::vector<int> act;
+  for (int f : o->geom.graphIdx) if (f > 0 && f <= o->mg.nMat) act.push_back(f);
+  std::sort(act.begin(), act.end());
+  act.erase(std::unique(act.begin(), act.end()), act.end());
+  o->mg.initMajorant(act);
+  return SG_OK;
+}
+int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
+  Oracle* o = O(h);
+  orc::TallyAdmin A;
+  int64_t memLoc = 1;
+  for (int i = 0; i < t->n_clerks; ++i) {
+    orc::Clerk c; c.d = t->clerks[i];
+    c.width = c.d.n_resp > 0 ? c.d.n_resp : 1;
+    int64_t mul = 1;
+    for (int a = 0; a < c.d.n_axes; ++a) {
+      c.multi[a] = mul; mul *= c.d.axes[a].n;
+      if (c.d.axes[a].kind <= SG_AXIS_Z) c.step[a] = (c.d.axes[a].max - c.d.axes[a].min) / c.d.axes[a].n;
+    }
+    c.nbins = mul;
+    c.addr = memLoc;
+    memLoc += c.size();
+    A.clerks.push_back(c);
+  }
+  A.mem.init(memLoc - 1, t->batch_size);
+  if (t->norm_clerk >= 0) { A.normAddr = A.clerks[t->norm_clerk].addr; A.normVal = t->norm_val; }
+  o->admins.push_back(A);
+  *admin = (int32_t)o->admins.size() - 1;
+  return SG_OK;
+}
+int32_t or_attach_tally(or_handle h, int32_t admin, int32_t atch) { O(h)->admins[admin].atch = atch; return SG_OK; }
+int32_t or_set_point_source(or_handle h, const sg_point_source_desc* s) {
+  Oracle* o = O(h);
+  o->src = *s;
+  o->srcProbG.assign(s->prob_g, s->prob_g + s->n_prob_g);
+  o->hasSource = true;
+  return SG_OK;
+}
+int32_t or_generate_source(or_handle h, uint64_t master, int32_t n, sg_bank* out) {
+  Oracle* o = O(h);
+  std::vector<orc::PState> v(n);
+  for (int i = 1; i <= n; ++i) {                      // source_inter.f90:98-119
+    orc::RNG r; r.s = master; r.stride(i);
+    v[i - 1] = o->samplePoint(r);
+  }
+  statesToBank(v, out, n);
+  return SG_OK;
+}
+int32_t or_transport_bank(or_handle h, int32_t admin, const sg_bank* in, int32_t n, uint64_t master,
+                          double k, sg_bank* next, int32_t cap, sg_cycle_stats* st) {
+  Oracle* o = O(h);
+  std::vector<orc::PState> v, nx;
+  bankToStates(in, n, v);
+  int rc = o->transportBank(admin, v, master, k, nx);
+  if (st) {
+    st->n_histories = n; st->n_events = o->nEvents; st->n_collisions = o->nColl; st->n_next = (int64_t)nx.size();
+    double sw = 0; for (auto& s : v) sw += s.wgt;
+    double ew = 0; for (auto& s : nx) ew += s.wgt;
+    st->start_weight = sw; st->end_weight = ew; st->k_eff = k; st->k_new = k;
+  }
+  if ((int)nx.size() > cap) return SG_ERR_BANK_OVERFLOW;
+  if (next) statesToBank(nx, next, cap);
+  return rc;
+}
+int32_t or_tally_cycle_start(or_handle h, int32_t admin, double w) { O(h)->reportCycleStart(admin, w); return SG_OK; }
+int32_t or_tally_cycle_end(or_handle h, int32_t admin, double w, double k) { O(h)->reportCycleEnd(admin, w, k); return SG_OK; }
+int32_t or_tally_size(or_handle h, int32_t admin, int64_t* n) { *n = O(h)->admins[admin].mem.N; return SG_OK; }
+int32_t or_get_bins(or_handle h, int32_t admin, double* bins, int64_t n) {
+  orc::ScoreMemory& m = O(h)->admins[admin].mem;
+  for (int64_t i = 0; i < n && i < m.N; ++i) { bins[i] = m.bin[i]; bins[n + i] = m.csum[i]; bins[2 * n + i] = m.csum2[i]; }
+  return SG_OK;
+}
+int32_t or_get_keff(or_handle h, int32_t admin, double* k, double* sd) {
+  return O(h)->getKeff(admin, *k, *sd) ? SG_OK : SG_ERR_BAD_ARG;
+}
+int32_t or_get_history_records(or_handle h, int32_t* c, uint64_t* r, int32_t n) {
+  Oracle* o = O(h);
+  for (int i = 0; i < n && i < (int)o->recColl.size(); ++i) { if (c) c[i] = o->recColl[i]; if (r) r[i] = o->recRng[i]; }
+  return SG_OK;
+}
+
+// eigenvalue driver (eigenPhysicsPackage_class.f90:135-412) on the oracle's own banks
+int32_t or_eigen_init(or_handle h, int32_t pop, uint64_t master, double k0) {
+  Oracle* o = O(h);
+  o->pop = pop; o->master.s = master; o->k_new = k0; o->keff0 = k0; o->nextK = 1.0;
+  o->thisCycle.assign(pop, orc::PState());
+  for (int i = 1; i <= pop; ++i) {                    // generateInitialState (:348-366)
+    orc::RNG r = o->master; r.stride(i);
+    if (o->sampleFission(r, o->thisCycle[i - 1]) != 0) { o->err = "fission source failed"; return SG_ERR_STATE; }
+  }
+  o->master.stride(pop);
+  return SG_OK;
+}
+int32_t or_eigen_cycle(or_handle h, int32_t admin, int32_t atch, sg_cycle_stats* st) {
+  Oracle* o = O(h);
+  double startW = 0; for (auto& s : o->thisCycle) startW += s.wgt;
+  o->reportCycleStart(admin, startW);
+  std::vector<orc::PState> next;
+  int rc = o->transportBank(admin, o->thisCycle, o->master.s, o->k_new, next);
+  if (rc) return rc;
+  int n = (int)o->thisCycle.size();
+  o->master.stride(o->pop + 1);                       // :257
+  double endW = 0; for (auto& s : next) endW += s.wgt;
+  o->reportCycleEnd(admin, endW, o->nextK);            // :261 (end%k_eff = k used this cycle)
+  if (next.empty()) { o->err = "empty fission bank"; return SG_ERR_STATE; }
+  o->normSizeRepr(next, o->pop, o->master);            // :269
+  o->master.stride(1);                                 // :275
+  o->thisCycle.swap(next);                             // flip
+  double k = o->k_new, sd = 0.0;
+  o->getKeff(atch, k, sd);                             // :289-298
+  double kUsed = o->k_new;
+  o->k_new = k;
+  o->nextK = k;                                        // nextCycle%k_eff = k_new
+  if (st) {
+    st->n_histories = n; st->n_events = o->nEvents; st->n_collisions = o->nColl; st->n_next = (int64_t)o->thisCycle.size();
+    st->start_weight = startW; st->end_weight = endW; st->k_eff = kUsed; st->k_new = k;
+  }
+  return SG_OK;
+}
+int32_t or_eigen_state(or_handle h, uint64_t* master, double* k) { *master = O(h)->master.s; *k = O(h)->k_new; return SG_OK; }
+int32_t or_eigen_get_bank(or_handle h, sg_bank* out, int32_t cap, int32_t* pop) {
+  Oracle* o = O(h);
+  *pop = (int32_t)o->thisCycle.size();
+  statesToBank(o->thisCycle, out, cap);
+  return SG_OK;
+}
+
+// fixedSourcePhysicsPackage%cycles, one batch (fixedSourcePhysicsPackage_class.f90:183-289)
+int32_t or_fixed_source_cycle(or_handle h, int32_t admin, int32_t n, uint64_t* master, sg_cycle_stats* st) {
+  Oracle* o = O(h);
+  std::vector<orc::PState> bank(n), next;
+  for (int i = 1; i <= n; ++i) { orc::RNG r; r.s = *master; r.stride(i); bank[i - 1] = o->samplePoint(r); }
+  orc::RNG m; m.s = *master; m.stride(n);
+  o->reportCycleStart(admin, (double)n);
+  int rc = o->transportBank(admin, bank, m.s, 1.0, next);
+  m.stride(n);
+  o->reportCycleEnd(admin, 0.0, 1.0);
+  *master = m.s;
+  if (st) { st->n_histories = n; st->n_events = o->nEvents; st->n_collisions = o->nColl; st->n_next = (int64_t)next.size(); }
+  return rc;
+}
+
+// ---- unit-test probes
+int32_t or_rng_draws(uint64_t* state, double* out, int32_t n) {
+  orc::RNG r; r.s = *state;
+  for (int i = 0; i < n; ++i) out[i] = r.get();
+  *state = r.s;
+  return SG_OK;
+}
+uint64_t or_rng_skip(uint64_t state, int64_t k) { orc::RNG r; r.s = state; r.skip(k); return r.s; }
+
+int32_t or_surf_eval(int32_t type, const double* par, const int32_t* bc, const double* r, const double* u,
+                     double* out /* [evaluate, distance, halfspace, going, tol] */) {
+  orc::Surface s; s.build(type, par);
+  if (bc) for (int i = 0; i < 6; ++i) s.bc[i] = bc[i];
+  out[0] = s.evaluate(r); out[1] = s.distance(r, u); out[2] = s.halfspace(r, u) ? 1.0 : 0.0;
+  out[3] = s.going(r, u) ? 1.0 : 0.0; out[4] = s.tol;
+  return SG_OK;
+}
+int32_t or_surf_bc(int32_t type, const double* par, const int32_t* bc, int32_t transform, double* r, double* u) {
+  orc::Surface s; s.build(type, par);
+  for (int i = 0; i < 6; ++i) s.bc[i] = bc[i];
+  if (transform) s.transformBC(r, u); else s.explicitBC(r, u);
+  return SG_OK;
+}
+int32_t or_coords_init(or_handle h, const double* r, const double* u) {
+  Oracle* o = O(h); o->probe = orc::CoordList(); o->probe.init(r, u); o->probeCache = orc::distCache(); return SG_OK;
+}
+int32_t or_coords_place(or_handle h) { O(h)->geom.placeCoord(O(h)->probe); return SG_OK; }
+int32_t or_coords_move(or_handle h, int32_t mode, double* maxDist, int32_t* event) {
+  // mode 0: move_noCache, 1: move_withCache, 2: geometry moveGlobal, 3: teleport
+  Oracle* o = O(h); int ev = 0;
+  if (mode == 0) o->geom.move(o->probe, *maxDist, ev, nullptr);
+  else if (mode == 1) o->geom.move(o->probe, *maxDist, ev, &o->probeCache);
+  else if (mode == 2) o->geom.moveGlobalGeom(o->probe, *maxDist, ev);
+  else o->geom.teleport(o->probe, *maxDist);
+  *event = ev;
+  return SG_OK;
+}
+int32_t or_coords_get(or_handle h, int32_t level, double* r, double* u, int32_t* info /* nesting, matIdx, uniqueID, localID, uniIdx */) {
+  Oracle* o = O(h);
+  const orc::Coord& c = o->probe.lvl[level];
+  for (int i = 0; i < 3; ++i) { r[i] = c.r[i]; u[i] = c.dir[i]; }
+  info[0] = o->probe.nesting; info[1] = o->probe.matIdx; info[2] = o->probe.uniqueID; info[3] = c.localID; info[4] = c.uniIdx;
+  return SG_OK;
+}
+int32_t or_what_is_at(or_handle h, const double* r, const double* u, int32_t* mat, int32_t* uid) {
+  int m, id; O(h)->geom.whatIsAt(m, id, r, u); *mat = m; *uid = id; return SG_OK;
+}
+int32_t or_bounds(or_handle h, double* bb) { O(h)->geom.bounds(bb); return SG_OK; }
+int32_t or_mg_info(or_handle h, int32_t mat, int32_t G, double* out /* total scatter capture fission nuFission majorant */) {
+  Oracle* o = O(h);
+  size_t k = (size_t)(mat - 1) * o->mg.nG + (G - 1);
+  out[0] = o->mg.total[k]; out[1] = o->mg.scatter[k]; out[2] = o->mg.capture[k];
+  out[3] = o->mg.fission[k]; out[4] = o->mg.nuFission[k]; out[5] = o->mg.majorant[G - 1];
+  return SG_OK;
+}
+int32_t or_rotate_vector(const double* dir, double mu, double phi, double* out) { orc::rotateVector(dir, mu, phi, out); return SG_OK; }
+
+// scoreMemory probe: replays the reference scoreMemory unit test pattern
+int32_t or_scoremem_new(int64_t n, int32_t batch, or_handle* out) {
+  orc::ScoreMemory* m = new orc::ScoreMemory(); m->init(n, batch); *out = reinterpret_cast<or_handle>(m); return SG_OK;
+}
+int32_t or_scoremem_free(or_handle h) { delete reinterpret_cast<orc::ScoreMemory*>(h); return SG_OK; }
+int32_t or_scoremem_score(or_handle h, double s, int64_t idx) { reinterpret_cast<orc::ScoreMemory*>(h)->score(s, idx); return SG_OK; }
+int32_t or_scoremem_accumulate(or_handle h, double s, int64_t idx) { reinterpret_cast<orc::ScoreMemory*>(h)->accumulate(s, idx); return SG_OK; }
+int32_t or_scoremem_close(or_handle h, double f) {
+  orc::ScoreMemory* m = reinterpret_cast<orc::ScoreMemory*>(h); m->reduceBins(); m->closeCycle(f); return SG_OK;
+}
+int32_t or_scoremem_result(or_handle h, int64_t idx, int32_t samples, double* mean, double* sd) {
+  reinterpret_cast<orc::ScoreMemory*>(h)->getResult(*mean, *sd, idx, samples); return SG_OK;
+}
+
+// CPU baseline: the gen loop with OpenMP over histories (thread-private tallies merged after the
+// loop, sites concatenated in history order).  Returns histories processed; tallies discarded.
+int64_t or_timed_gen_loop(or_handle h, int32_t admin, const sg_bank* in, int32_t n, uint64_t master,
+                          double k, int32_t threads, int64_t* events) {
+  Oracle* o = O(h);
+  std::vector<orc::PState> v;
+  bankToStates(in, n, v);
+  int64_t ev = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+:ev)
+  {
+    Oracle local = *o;   // thread-private operators, RNG and tallies (eigenPhysicsPackage :181)
+    local.nEvents = 0;
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; ++i) {
+      std::vector<orc::PState> s;
+      local.runHistory(v[i], i + 1, master, k, admin, &s, nullptr, nullptr);
+    }
+    ev += local.nEvents;
+  }
+#else
+  (void)threads;
+  for (int i = 0; i < n; ++i) { std::vector<orc::PState> s; o->runHistory(v[i], i + 1, master, k, admin, &s, nullptr, nullptr); }
+  ev = o->nEvents;
+#endif
+  if (events) *events = ev;
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,225 @@
+"""ctypes mirrors of the C ABI structs declared in include/scone_gpu.h.
+
+The same structs describe a problem to the CUDA library (libsconegpu) and, in the tests, to the
+CPU oracle.  Helper builders keep the numpy arrays they point to alive for as long as the struct.
+"""
+import ctypes as C
+import numpy as np
+
+SG_OK = 0
+SG_SURF_NPAR = 6
+SG_VOID_MAT = 2147483647
+
+# surface types
+XPLANE, YPLANE, ZPLANE, PLANE = 1, 2, 3, 4
+XCYL, YCYL, ZCYL, SPHERE, BOX = 5, 6, 7, 8, 9
+XSQCYL, YSQCYL, ZSQCYL = 10, 11, 12
+# universe types
+UNI_ROOT, UNI_CELL, UNI_PIN, UNI_LAT = 1, 2, 3, 4
+# boundary conditions
+BC_VACUUM, BC_REFLECTIVE, BC_PERIODIC = 0, 1, 2
+# precision forms
+PREC_FP64, PREC_MIXED = 0, 1
+# transport operators
+TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE = 1, 2, 3
+# clerks
+CLERK_COLLISION, CLERK_TRACK, CLERK_KEFF_ANALOG, CLERK_KEFF_IMPLICIT = 1, 2, 3, 4
+# map axes
+AXIS_X, AXIS_Y, AXIS_Z, AXIS_GROUP, AXIS_MATERIAL = 1, 2, 3, 4, 5
+# responses (macro MTs from SharedModules/endfConstants.f90:116-130)
+RESP_FLUX = 0
+MACRO_TOTAL, MACRO_CAPTURE, MACRO_FISSION, MACRO_NUFISSION, MACRO_ABSORPTION = -1, -2, -6, -7, -21
+
+i32p = C.POINTER(C.c_int32)
+f64p = C.POINTER(C.c_double)
+
+
+class GeometryDesc(C.Structure):
+    _fields_ = [
+        ("n_surf", C.c_int32), ("surf_type", i32p), ("surf_par", f64p),
+        ("border_surf", C.c_int32), ("bc", C.c_int32 * 6),
+        ("n_cell", C.c_int32), ("cell_ptr", i32p), ("cell_surf", i32p),
+        ("n_uni", C.c_int32), ("uni_type", i32p), ("uni_origin", f64p),
+        ("uni_iptr", i32p), ("uni_ipar", i32p), ("uni_dptr", i32p), ("uni_dpar", f64p),
+        ("uni_fptr", i32p), ("uni_fill", i32p), ("root_uni", C.c_int32),
+    ]
+
+
+class MGDesc(C.Structure):
+    _fields_ = [
+        ("n_mat", C.c_int32), ("n_g", C.c_int32),
+        ("capture", f64p), ("fission", f64p), ("nu", f64p), ("chi", f64p),
+        ("p0", f64p), ("prod", f64p), ("fissile", i32p), ("avg_dist", C.c_double),
+    ]
+
+
+class AxisDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("n", C.c_int32), ("min", C.c_double), ("max", C.c_double)]
+
+
+class ClerkDesc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("handle_virtual", C.c_int32), ("n_resp", C.c_int32),
+        ("resp", C.c_int32 * 4), ("n_axes", C.c_int32), ("axes", AxisDesc * 3),
+        ("filter_g_top", C.c_int32), ("filter_g_low", C.c_int32),
+    ]
+
+
+class TallyDesc(C.Structure):
+    _fields_ = [
+        ("n_clerks", C.c_int32), ("clerks", C.POINTER(ClerkDesc)), ("batch_size", C.c_int32),
+        ("norm_clerk", C.c_int32), ("norm_val", C.c_double),
+    ]
+
+
+class PointSourceDesc(C.Structure):
+    _fields_ = [
+        ("r", C.c_double * 3), ("dir", C.c_double * 3), ("isotropic", C.c_int32),
+        ("G", C.c_int32), ("n_prob_g", C.c_int32), ("prob_g", f64p),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("transport", C.c_int32), ("device", C.c_int32),
+        ("max_bank", C.c_int32), ("record_histories", C.c_int32),
+    ]
+
+
+class Bank(C.Structure):
+    _fields_ = [
+        ("wgt", f64p), ("r", f64p), ("dir", f64p), ("G", i32p), ("time", f64p), ("brood_id", i32p),
+    ]
+
+
+class CycleStats(C.Structure):
+    _fields_ = [
+        ("n_histories", C.c_int64), ("n_events", C.c_int64), ("n_collisions", C.c_int64),
+        ("n_next", C.c_int64), ("start_weight", C.c_double), ("end_weight", C.c_double),
+        ("k_eff", C.c_double), ("k_new", C.c_double),
+    ]
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class HostBank:
+    """SoA particle bank in (optionally pinned) host numpy arrays, viewable as an sg_bank."""
+
+    def __init__(self, n, arrays=None):
+        self.n = int(n)
+        if arrays is None:
+            arrays = dict(
+                wgt=np.ones(n, np.float64), r=np.zeros((n, 3), np.float64),
+                dir=np.zeros((n, 3), np.float64), G=np.ones(n, np.int32),
+                time=np.zeros(n, np.float64), brood_id=np.zeros(n, np.int32))
+        self.a = arrays
+        for k in ("wgt", "r", "dir", "time"):
+            self.a[k] = np.ascontiguousarray(self.a[k], dtype=np.float64)
+        for k in ("G", "brood_id"):
+            self.a[k] = np.ascontiguousarray(self.a[k], dtype=np.int32)
+        self.struct = Bank(_p(self.a["wgt"], C.c_double), _p(self.a["r"], C.c_double),
+                           _p(self.a["dir"], C.c_double), _p(self.a["G"], C.c_int32),
+                           _p(self.a["time"], C.c_double), _p(self.a["brood_id"], C.c_int32))
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+    def head(self, m):
+        return {k: v[:m].copy() for k, v in self.a.items()}
+
+
+def geometry_struct(g):
+    """Build a GeometryDesc from a dict of numpy arrays (see problems.Geometry)."""
+    keep = {}
+
+    def arr(name, dt):
+        a = np.ascontiguousarray(g[name], dtype=dt)
+        if a.size == 0:
+            a = np.zeros(1, dtype=dt)
+        keep[name] = a
+        return _p(a, C.c_int32 if dt == np.int32 else C.c_double)
+
+    s = GeometryDesc()
+    s.n_surf = len(g["surf_type"])
+    s.surf_type = arr("surf_type", np.int32)
+    s.surf_par = arr("surf_par", np.float64)
+    s.border_surf = int(g["border_surf"])
+    for i in range(6):
+        s.bc[i] = int(g["bc"][i])
+    s.n_cell = len(g["cell_ptr"]) - 1
+    s.cell_ptr = arr("cell_ptr", np.int32)
+    s.cell_surf = arr("cell_surf", np.int32)
+    s.n_uni = len(g["uni_type"])
+    s.uni_type = arr("uni_type", np.int32)
+    s.uni_origin = arr("uni_origin", np.float64)
+    s.uni_iptr = arr("uni_iptr", np.int32)
+    s.uni_ipar = arr("uni_ipar", np.int32)
+    s.uni_dptr = arr("uni_dptr", np.int32)
+    s.uni_dpar = arr("uni_dpar", np.float64)
+    s.uni_fptr = arr("uni_fptr", np.int32)
+    s.uni_fill = arr("uni_fill", np.int32)
+    s.root_uni = int(g["root_uni"])
+    return s, keep
+
+
+def mg_struct(m):
+    keep = {}
+
+    def arr(name, dt):
+        a = np.ascontiguousarray(m[name], dtype=dt)
+        keep[name] = a
+        return _p(a, C.c_int32 if dt == np.int32 else C.c_double)
+
+    s = MGDesc()
+    s.n_mat, s.n_g = int(m["n_mat"]), int(m["n_g"])
+    s.capture = arr("capture", np.float64)
+    s.fission = arr("fission", np.float64)
+    s.nu = arr("nu", np.float64)
+    s.chi = arr("chi", np.float64)
+    s.p0 = arr("p0", np.float64)
+    s.prod = arr("prod", np.float64)
+    s.fissile = arr("fissile", np.int32)
+    s.avg_dist = float(m.get("avg_dist", 0.0))
+    return s, keep
+
+
+def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None):
+    """Describe one tally clerk; axes = [(kind, n, min, max), ...] (multiMap order)."""
+    c = ClerkDesc()
+    c.type = type_
+    c.handle_virtual = handle_virtual
+    c.n_resp = len(resp)
+    for i, r in enumerate(resp):
+        c.resp[i] = r
+    c.n_axes = len(axes)
+    for i, (k, n, lo, hi) in enumerate(axes):
+        c.axes[i].kind, c.axes[i].n, c.axes[i].min, c.axes[i].max = k, n, lo, hi
+    if g_filter is not None:
+        c.filter_g_top, c.filter_g_low = g_filter
+    return c
+
+
+def tally_struct(clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
+    arr = (ClerkDesc * max(1, len(clerks)))(*clerks)
+    t = TallyDesc(len(clerks), C.cast(arr, C.POINTER(ClerkDesc)), batch_size, norm_clerk, norm_val)
+    return t, arr
+
+
+def point_source_struct(r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
+    s = PointSourceDesc()
+    for i in range(3):
+        s.r[i] = r[i]
+        s.dir[i] = dir[i]
+    s.isotropic = 1 if isotropic else 0
+    s.G = G
+    keep = None
+    if prob_g is not None:
+        keep = np.ascontiguousarray(prob_g, dtype=np.float64)
+        s.n_prob_g = len(keep)
+        s.prob_g = _p(keep, C.c_double)
+    else:
+        s.n_prob_g = 0
+        s.prob_g = C.cast(None, f64p)
+    return s, keep
