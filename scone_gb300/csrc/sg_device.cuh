@@ -1,0 +1,631 @@
+// sg_device.cuh -- device-side data layout and the particle-tracking hot path of libsconegpu.
+//
+// Everything in this header is templated on the working precision R:
+//   R = double : all-FP64 verification form.  Compiled with -fmad=false so every multiply and add is
+//                rounded separately, in SCONE's operation order; per-history results then match the
+//                CPU restatement exactly (collision counts, end-of-history RNG states, bin indices).
+//   R = float  : mixed form.  Cross sections, distances, sampling and direction arithmetic in FP32;
+//                positions (every level), the surface-coincidence tests, tally sums and k in FP64.
+//                Geometric tolerances are widened to the FP32 distance accuracy (see Tol<float>).
+//
+// Data layout in HBM (all flat, read-only during a launch, resident across cycles):
+//   surfaces  DSurf[n]           64 B records (type, bc, params, tolerance)
+//   universes DUni[n]            128 B records; pin radii, cell lists and the geometry graph are
+//                                separate int/double arrays indexed from the record
+//   MG data   [mat][G] SoA arrays of R, P0/prod as [mat][Gin][Gout]
+//   banks     SoA: r (3 x FP64), dir (3 x FP64), wgt, G, brood -- see sg_internal.h
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "sg_internal.h"
+
+namespace sg {
+
+// ------------------------------------------------------------------ constants
+__device__ __constant__ static const double D_INF = 9223372036854775808.0;   // 2**63 (universalVariables.f90:21)
+
+template <class R> struct Tol;
+// SCONE's values (universalVariables.f90:21-25, numPrecision.f90:25, transportOperatorST_class.f90:59,
+// genericProcedures.f90:1067 -- the last two are default-real literals).
+template <> struct Tol<double> {
+  static __device__ __forceinline__ double fp_rel() { return 1.0e-7; }
+  static __device__ __forceinline__ double st_void() { return (double)1.0E-12f; }
+  static __device__ __forceinline__ double rot() { return (double)1.0E-8f; }
+};
+// FP32 distances land a crossing within ~1e-6 relative of the surface, so the tie rule between
+// nesting levels is widened to 1e-5; surface tolerances and the cell-crossing nudge are scaled on
+// the host (surface records carry the tolerance of the form they were uploaded for).
+template <> struct Tol<float> {
+  static __device__ __forceinline__ float fp_rel() { return 1.0e-5f; }
+  static __device__ __forceinline__ float st_void() { return 1.0E-12f; }
+  static __device__ __forceinline__ float rot() { return 1.0E-4f; }
+};
+
+// ------------------------------------------------------------------ RNG (RandomNumbers/RNG_class.f90)
+static constexpr uint64_t RNG_G = 2806196910506780709ULL;
+static constexpr uint64_t RNG_MASK = 0x7FFFFFFFFFFFFFFFULL;
+static constexpr int64_t RNG_STRIDE = 152917;
+
+__device__ __forceinline__ uint64_t lcg_next(uint64_t s) {
+  s = (RNG_G * s) & RNG_MASK;
+  return (s + 1ULL) & RNG_MASK;
+}
+template <class R> __device__ __forceinline__ R rng_to_real(uint64_t s);
+// get: real(seed) * 2^-63 (RNG_class.f90:161)
+template <> __device__ __forceinline__ double rng_to_real<double>(uint64_t s) {
+  return __ll2double_rn((long long)s) * 0x1p-63;
+}
+// mixed form: the top 24 bits of the 63-bit state, made odd so that xi lies in (0,1) and -log(xi)
+// is finite; the LCG stream (and so every draw's position in it) is the same as in FP64.
+template <> __device__ __forceinline__ float rng_to_real<float>(uint64_t s) {
+  return (float)((uint32_t)(s >> 39) | 1u) * 0x1p-24f;
+}
+// skip (RNG_class.f90:251-304)
+__host__ __device__ inline uint64_t lcg_skip(uint64_t s, int64_t k_in) {
+  uint64_t k = (k_in >= 0) ? (uint64_t)k_in : (uint64_t)INT64_MAX - (uint64_t)(-k_in) + 1ULL;
+  k &= RNG_MASK;
+  uint64_t Gk = 1, Ck = 0, gsq = RNG_G, L = 1;
+  while (k > 0) {
+    if (k & 1ULL) {
+      Gk = (Gk * gsq) & RNG_MASK;
+      Ck = (Ck * gsq) & RNG_MASK;
+      Ck = (Ck + L) & RNG_MASK;
+    }
+    L = (L * (gsq + 1ULL)) & RNG_MASK;
+    gsq = (gsq * gsq) & RNG_MASK;
+    k >>= 1;
+  }
+  return (Gk * s + Ck) & RNG_MASK;
+}
+
+template <class R> struct Rng {
+  uint64_t s;
+  __device__ __forceinline__ R get() { s = lcg_next(s); return rng_to_real<R>(s); }
+};
+
+// ------------------------------------------------------------------ math helpers
+template <class R> __device__ __forceinline__ R dlog(R x);
+template <> __device__ __forceinline__ double dlog<double>(double x) { return log(x); }
+template <> __device__ __forceinline__ float dlog<float>(float x) { return logf(x); }
+template <class R> __device__ __forceinline__ R dsqrt(R x);
+template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sgn(double a, double b) { return copysign(fabs(a), b); }
+__device__ __forceinline__ float sgn(float a, float b) { return copysignf(fabsf(a), b); }
+// Component i of a 3-vector held in registers, by selects (a runtime index into a register array
+// would force the array into local memory).
+template <class T> __device__ __forceinline__ T at3(const T* a, int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
+
+// sin/cos of phi = 2*pi*xi (multiScatterMG_class.f90:208, pointSource_class.f90:221)
+template <class R> __device__ __forceinline__ void sincos_phi(R xi, R& s, R& c);
+template <> __device__ __forceinline__ void sincos_phi<double>(double xi, double& s, double& c) {
+  const double TWO_PI = 2.0 * 3.14159265358979323846264338327950288;
+  double phi = TWO_PI * xi;
+  sincos(phi, &s, &c);
+}
+template <> __device__ __forceinline__ void sincos_phi<float>(float xi, float& s, float& c) {
+  sincospif(2.0f * xi, &s, &c);
+}
+
+// gfortran NORM2 (scaled sum of squares) used by rotateVector's final normalisation
+__device__ __forceinline__ double norm2_scaled(double a0, double a1, double a2) {
+  double scale = 1.0, ssq = 0.0;
+  double v[3] = {a0, a1, a2};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0.0) {
+      double a = fabs(v[i]);
+      if (scale < a) { double t = scale / a; ssq = 1.0 + ssq * t * t; scale = a; }
+      else { double t = a / scale; ssq = ssq + t * t; }
+    }
+  }
+  return scale * sqrt(ssq);
+}
+
+// rotateVector (SharedModules/genericProcedures.f90:1047-1084)
+template <class R>
+__device__ __forceinline__ void rotate_vector(R& u, R& v, R& w, R mu, R sinPol, R cosPol) {
+  R A = dsqrt<R>(fmax(R(0), R(1) - mu * mu));
+  R B = dsqrt<R>(fmax(R(0), R(1) - w * w));
+  R n0, n1, n2;
+  if (B > Tol<R>::rot()) {
+    n0 = mu * u + A * (u * w * cosPol - v * sinPol) / B;
+    n1 = mu * v + A * (v * w * cosPol + u * sinPol) / B;
+    n2 = mu * w - A * B * cosPol;
+  } else {
+    B = dsqrt<R>(fmax(R(0), R(1) - v * v));
+    n0 = mu * u + A * (u * v * cosPol + w * sinPol) / B;
+    n1 = mu * v - A * B * cosPol;
+    n2 = mu * w + A * (v * w * cosPol - u * sinPol) / B;
+  }
+  if constexpr (sizeof(R) == 8) {
+    double n = norm2_scaled(n0, n1, n2);
+    u = n0 / n; v = n1 / n; w = n2 / n;
+  } else {
+    float inv = rsqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+    u = n0 * inv; v = n1 * inv; w = n2 * inv;
+  }
+}
+
+// ------------------------------------------------------------------ surfaces (Geometry/Surfaces)
+// distance, evaluate, going, halfspace, BCs.  Positions are FP64; the coincidence test `abs(c) < tol`
+// is always done on an FP64 c; the remaining distance arithmetic is in R.
+template <class R>
+__device__ __forceinline__ double surf_evaluate(const DSurf& s, const double r[3]) {
+  switch (s.type) {
+    case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
+      return at3(r, s.axis) - s.p[0];
+    case SG_SURF_PLANE:
+      return (r[0] * s.p[0] + r[1] * s.p[1] + r[2] * s.p[2]) - s.p[3];
+    case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {
+      double d0 = at3(r, s.pl0) - s.p[s.pl0], d1 = at3(r, s.pl1) - s.p[s.pl1];
+      return (d0 * d0 + d1 * d1) - s.p[3] * s.p[3];
+    }
+    case SG_SURF_SPHERE: {
+      double d0 = r[0] - s.p[0], d1 = r[1] - s.p[1], d2 = r[2] - s.p[2];
+      return (d0 * d0 + d1 * d1 + d2 * d2) - s.p[3] * s.p[3];
+    }
+    case SG_SURF_BOX: {
+      double m = fmax(fabs(r[0] - s.p[0]) - s.p[3], fabs(r[1] - s.p[1]) - s.p[4]);
+      return fmax(m, fabs(r[2] - s.p[2]) - s.p[5]);
+    }
+    default: {
+      double a = fabs(at3(r, s.pl0) - s.p[s.pl0]) - s.p[3 + s.pl0];
+      double b = fabs(at3(r, s.pl1) - s.p[s.pl1]) - s.p[3 + s.pl1];
+      return fmax(a, b);
+    }
+  }
+}
+
+// box/squareCylinder slab intersection (box_class.f90:168-237, squareCylinder_class.f90:212-270)
+template <class R>
+__device__ __forceinline__ R slab_distance(const DSurf& s, const double r[3], const R u[3], int nax,
+                                           int ax0, int ax1, int ax2) {
+  const R FP_MISS_TOL = (sizeof(R) == 8) ? R(1.0 + 10.0 * 2.220446049250313e-16) : R(1.0f + 10.0f * 1.1920929e-7f);
+  const R HUGE_R = (sizeof(R) == 8) ? R(1.7976931348623157e308) : R(3.4028234663852886e38f);
+  const R INF_R = R(D_INF);
+  R far = HUGE_R, near = -HUGE_R;
+  int axes[3] = {ax0, ax1, ax2};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (i < nax) {
+      int ax = axes[i];
+      R rb = R(at3(r, ax) - s.p[ax]);
+      R a_far = sgn(R(s.p[3 + ax]), at3(u, ax));
+      R a_near = -a_far;
+      R tn, tf;
+      if (at3(u, ax) != R(0)) { tn = (a_near - rb) / at3(u, ax); tf = (a_far - rb) / at3(u, ax); }
+      else {
+        tn = sgn(INF_R, a_near - rb); tf = sgn(INF_R, a_far - rb);
+        if (tn > tf) { R t = tn; tn = tf; tf = t; }
+      }
+      far = fmin(far, tf);
+      near = fmax(near, tn);
+    }
+  }
+  R d;
+  if (far <= near * FP_MISS_TOL) d = INF_R;
+  else if (fabs(surf_evaluate<R>(s, r)) < s.tol) d = (fabs(far) >= fabs(near)) ? far : near;
+  else d = (near <= R(0)) ? far : near;
+  if (d <= R(0) || d > INF_R) d = INF_R;
+  return d;
+}
+
+template <class R>
+__device__ __forceinline__ R surf_distance(const DSurf& s, const double r[3], const R u[3]) {
+  const R INF_R = R(D_INF);
+  switch (s.type) {
+    case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE: {   // aPlane_class.f90:157-181
+      double ra64 = s.p[0] - at3(r, s.axis);
+      R ua = at3(u, s.axis), d;
+      if (fabs(ra64) < s.tol) d = INF_R;
+      else if (ua != R(0)) d = R(ra64) / ua;
+      else d = INF_R;
+      if (d <= R(0) || d > INF_R) d = INF_R;
+      return d;
+    }
+    case SG_SURF_PLANE: {                                                // plane_class.f90:144-163
+      R k = u[0] * R(s.p[0]) + u[1] * R(s.p[1]) + u[2] * R(s.p[2]);
+      double c = surf_evaluate<R>(s, r);
+      R d;
+      if (k == R(0) || fabs(c) < s.tol) d = INF_R;
+      else { d = -R(c) / k; if (d <= R(0) || d > INF_R) d = INF_R; }
+      return d;
+    }
+    case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {           // cylinder_class.f90:231-270
+      double c = surf_evaluate<R>(s, r);
+      R k = R(at3(r, s.pl0) - s.p[s.pl0]) * at3(u, s.pl0) + R(at3(r, s.pl1) - s.p[s.pl1]) * at3(u, s.pl1);
+      R a = R(1) - at3(u, s.axis) * at3(u, s.axis);
+      R delta = k * k - a * R(c), d;
+      if (delta < R(0) || a == R(0)) d = INF_R;
+      else if (fabs(c) < s.tol) {
+        if (k >= R(0)) d = INF_R;
+        else { d = -k + dsqrt<R>(delta); d = d / a; }
+      } else if (c < 0.0) { d = -k + dsqrt<R>(delta); d = d / a; }
+      else { d = -k - dsqrt<R>(delta); d = d / a; if (d <= R(0)) d = INF_R; }
+      return fmin(d, INF_R);
+    }
+    case SG_SURF_SPHERE: {                                               // sphere_class.f90:152-183
+      double c = surf_evaluate<R>(s, r);
+      R k = R(r[0] - s.p[0]) * u[0] + R(r[1] - s.p[1]) * u[1] + R(r[2] - s.p[2]) * u[2];
+      R delta = k * k - R(c), d;
+      if (delta < R(0)) d = INF_R;
+      else if (fabs(c) < s.tol) { if (k >= R(0)) d = INF_R; else d = -k + dsqrt<R>(delta); }
+      else if (c < 0.0) d = -k + dsqrt<R>(delta);
+      else { d = -k - dsqrt<R>(delta); if (d <= R(0)) d = INF_R; }
+      return d;
+    }
+    case SG_SURF_BOX:
+      return slab_distance<R>(s, r, u, 3, 0, 1, 2);
+    default:
+      return slab_distance<R>(s, r, u, 2, s.pl0, s.pl1, 0);
+  }
+}
+
+template <class R>
+__device__ __forceinline__ bool surf_going(const DSurf& s, const double r[3], const R u[3]) {
+  switch (s.type) {
+    case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
+      return at3(u, s.axis) > R(0);
+    case SG_SURF_PLANE: {
+      R proj = u[0] * R(s.p[0]) + u[1] * R(s.p[1]) + u[2] * R(s.p[2]);
+      if (proj == R(0)) return surf_evaluate<R>(s, r) >= 0.0;
+      return proj > R(0);
+    }
+    case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL:
+      return (R(at3(r, s.pl0) - s.p[s.pl0]) * at3(u, s.pl0) + R(at3(r, s.pl1) - s.p[s.pl1]) * at3(u, s.pl1)) >= R(0);
+    case SG_SURF_SPHERE:
+      return (R(r[0] - s.p[0]) * u[0] + R(r[1] - s.p[1]) * u[1] + R(r[2] - s.p[2]) * u[2]) >= R(0);
+    default: {   // box (box_class.f90:253-281) and squareCylinder (:272-300)
+      int axes[3] = {0, 1, 2};
+      int nax = 3;
+      if (s.type != SG_SURF_BOX) { axes[0] = s.pl0; axes[1] = s.pl1; nax = 2; }
+      int maxCom = axes[0];
+      double best = -1.0e308;
+      double rlm = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if (i < nax) {
+          double rl = at3(r, axes[i]) - s.p[axes[i]];
+          double v = fabs(rl) - s.p[3 + axes[i]];
+          if (v > best) { best = v; maxCom = axes[i]; rlm = rl; }
+        }
+      }
+      R proj = at3(u, maxCom) * (R)sgn(1.0, rlm);
+      if (proj == R(0)) return surf_evaluate<R>(s, r) >= 0.0;
+      return proj > R(0);
+    }
+  }
+}
+
+template <class R>
+__device__ __forceinline__ bool surf_halfspace(const DSurf& s, const double r[3], const R u[3]) {
+  double c = surf_evaluate<R>(s, r);   // surface_inter.f90:363-378
+  bool hs = c > 0.0;
+  if (fabs(c) < s.tol) hs = surf_going<R>(s, r, u);
+  return hs;
+}
+
+// explicitBC (box_class.f90:380-420, squareCylinder_class.f90:430-472)
+template <class R>
+__device__ __forceinline__ void surf_explicit_bc(const DSurf& s, double r[3], R u[3]) {
+  if (s.type != SG_SURF_BOX && !(s.type >= SG_SURF_XSQCYL && s.type <= SG_SURF_ZSQCYL)) return;
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    bool active = (s.type == SG_SURF_BOX) || ax == s.pl0 || ax == s.pl1;
+    if (!active) continue;
+    double r0 = r[ax] - s.p[ax];
+    if (fabs(r0) <= s.p[3 + ax] * (1.0 - s.tol)) continue;
+    int b = (r0 < 0.0) ? s.bc[2 * ax] : s.bc[2 * ax + 1];
+    if (b == SG_BC_REFLECTIVE) u[ax] = -u[ax];
+    else if (b == SG_BC_PERIODIC) r[ax] = r[ax] - 2.0 * sgn(s.p[3 + ax], r0);
+  }
+}
+
+// transformBC (box_class.f90:430-487, squareCylinder_class.f90:482-544)
+template <class R>
+__device__ __forceinline__ void surf_transform_bc(const DSurf& s, double r[3], R u[3]) {
+  if (s.type != SG_SURF_BOX && !(s.type >= SG_SURF_XSQCYL && s.type <= SG_SURF_ZSQCYL)) return;
+  int Ri[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    bool active = (s.type == SG_SURF_BOX) || ax == s.pl0 || ax == s.pl1;
+    double a_bar = s.p[3 + ax] * (1.0 - s.tol);
+    Ri[ax] = active ? ((int)ceil(fabs(r[ax] - s.p[ax]) / a_bar)) / 2 : 0;
+  }
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    bool active = (s.type == SG_SURF_BOX) || ax == s.pl0 || ax == s.pl1;
+    if (!active) continue;
+    for (int t = 1; t <= Ri[ax] && t <= 64; ++t) {
+      double r0 = r[ax] - s.p[ax];
+      int b = (r0 < 0.0) ? s.bc[2 * ax] : s.bc[2 * ax + 1];
+      if (b == SG_BC_REFLECTIVE) {
+        double a0 = sgn(s.p[3 + ax], r0) + s.p[ax];
+        double d = r[ax] - a0;
+        r[ax] = r[ax] - 2.0 * d;
+        u[ax] = -u[ax];
+      } else if (b == SG_BC_PERIODIC) {
+        double d = sgn(s.p[3 + ax], r0);
+        r[ax] = r[ax] - 2.0 * d;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ geometry state of one particle
+// Levels are held in registers (MAXL is a compile-time bound >= the geometry's nesting); rotated
+// universes are not supported, so every level shares one direction.
+template <class R, int MAXL>
+struct Coords {
+  double r[MAXL][3];
+  R u[3];
+  int uni[MAXL];
+  int base[MAXL];    // graph location (0-based) of local cell 1 of the level's universe (uniRootID-1)
+  int local[MAXL];   // localID, 1-based
+  int nest;
+  int mat;
+  int uid;
+};
+
+struct DistCache {   // geometry_inter.f90:21-25
+  int lvl;
+};
+
+template <class R, int MAXL>
+struct Geom {
+  const DGeom& g;
+  __device__ __forceinline__ explicit Geom(const DGeom& gg) : g(gg) {}
+
+  // universe%findCell for the universe `u` at local position r
+  __device__ __forceinline__ int find_cell(int u, const double r[3], const R dir[3]) const {
+    const DUni& U = g.unis[u];
+    switch (U.type) {
+      case SG_UNI_ROOT:                                          // rootUniverse_class.f90:127-145
+        return surf_halfspace<R>(g.surfs[U.i[0]], r, dir) ? 2 : 1;
+      case SG_UNI_CELL: {                                        // cellUniverse_class.f90:203-246
+        int nc = U.i[1];
+        for (int c = 0; c < nc; ++c) {
+          int cell = g.uni_cells[U.i[0] + c];
+          bool isIt = false;
+          for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
+            int ss = g.cell_surf[k];
+            bool hs = surf_halfspace<R>(g.surfs[abs(ss) - 1], r, dir);
+            isIt = (hs == (ss > 0));
+            if (!isIt) break;
+          }
+          if (isIt) return c + 1;
+        }
+        return nc + 1;
+      }
+      case SG_UNI_PIN: {                                         // pinUniverse_class.f90:150-173
+        double rsq = r[0] * r[0] + r[1] * r[1];
+        double mul = ((double)(r[0] * (double)dir[0] + r[1] * (double)dir[1]) >= 0.0) ? -1.0 : 1.0;
+        int N = U.i[1];
+        for (int l = 1; l <= N; ++l)
+          if (rsq < g.pin_rsq[U.i[0] + l - 1] + mul * g.pin_tol[U.i[0] + l - 1]) return l;
+        return N + 1;
+      }
+      default: {                                                 // latUniverse_class.f90:270-312
+        int ijk[3];
+        bool out = false;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          ijk[i] = (int)floor((r[i] - U.d[3 + i]) / U.d[i]) + 1;
+          double r_bar = r[i] - U.d[3 + i] - ijk[i] * U.d[i] + 0.5 * U.d[i];
+          if (fabs(r_bar) > U.d[6 + i] && r_bar * (double)dir[i] > 0.0) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
+          if (ijk[i] <= 0 || ijk[i] > U.i[i]) out = true;
+        }
+        return out ? U.i[3] : ijk[0] + U.i[0] * (ijk[1] - 1 + U.i[1] * (ijk[2] - 1));
+      }
+    }
+  }
+
+  __device__ __forceinline__ static void get_ijk(int localID, const int* sizeN, int ijk[3]) {
+    int temp = localID - 1;                                      // latUniverse_class.f90:489-506
+    int base = temp / sizeN[0];
+    ijk[0] = temp - sizeN[0] * base + 1;
+    temp = base;
+    base = temp / sizeN[1];
+    ijk[1] = temp - sizeN[1] * base + 1;
+    ijk[2] = base + 1;
+  }
+
+  // pin annulus k: zCylinder at the origin (pinUniverse_class.f90:114-118)
+  __device__ __forceinline__ R pin_cyl(const DUni& U, int k, const double r[3], const R u[3]) const {
+    const R INF_R = R(D_INF);
+    double c = (r[0] * r[0] + r[1] * r[1]) - g.pin_rsq[U.i[0] + k];
+    R kk = R(r[0]) * u[0] + R(r[1]) * u[1];
+    R a = R(1) - u[2] * u[2];
+    R delta = kk * kk - a * R(c), d;
+    if (delta < R(0) || a == R(0)) d = INF_R;
+    else if (fabs(c) < g.pin_tol[U.i[0] + k]) {
+      if (kk >= R(0)) d = INF_R;
+      else { d = -kk + dsqrt<R>(delta); d = d / a; }
+    } else if (c < 0.0) { d = -kk + dsqrt<R>(delta); d = d / a; }
+    else { d = -kk - dsqrt<R>(delta); d = d / a; if (d <= R(0)) d = INF_R; }
+    return fmin(d, INF_R);
+  }
+
+  // universe%distance
+  __device__ __forceinline__ void uni_distance(int u, int localID, const double r[3], const R dir[3],
+                                               R& d, int& surfIdx) const {
+    const R INF_R = R(D_INF);
+    const DUni& U = g.unis[u];
+    switch (U.type) {
+      case SG_UNI_ROOT:                                          // rootUniverse_class.f90:152-162
+        surfIdx = U.i[0] + 1;
+        d = surf_distance<R>(g.surfs[U.i[0]], r, dir);
+        return;
+      case SG_UNI_CELL: {                                        // simpleCell_class.f90:120-141
+        int cell = g.uni_cells[U.i[0] + localID - 1];
+        d = INF_R; surfIdx = 0;
+        for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {
+          int ss = g.cell_surf[k];
+          R td = surf_distance<R>(g.surfs[abs(ss) - 1], r, dir);
+          if (td < d) { d = td; surfIdx = abs(ss); }
+        }
+        return;
+      }
+      case SG_UNI_PIN: {                                         // pinUniverse_class.f90:185-226
+        int N = U.i[1];
+        R d_out = (localID > N) ? INF_R : pin_cyl(U, localID - 1, r, dir);
+        R d_in = (localID == 1) ? INF_R : pin_cyl(U, localID - 2, r, dir);
+        if (d_in < d_out) { surfIdx = -1; d = d_in; } else { surfIdx = -2; d = d_out; }
+        return;
+      }
+      default: {                                                 // latUniverse_class.f90:319-373
+        if (localID == U.i[3]) {
+          surfIdx = -7;
+          d = surf_distance<R>(g.surfs[U.i[4]], r, dir);       // outline box
+          return;
+        }
+        int ijk[3];
+        get_ijk(localID, U.i, ijk);
+        d = INF_R;
+        int ax = 0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          double r_bar = r[i] - U.d[3 + i];
+          r_bar = r_bar - (ijk[i] - 0.5) * U.d[i];
+          R bound = sgn(R(U.d[i] * 0.5), dir[i]);
+          R td = (bound - R(r_bar)) / dir[i];
+          if (td < d) { d = td; ax = i; }
+        }
+        d = fmax(R(0), d);
+        d = fmin(INF_R, d);
+        R uax = (ax == 0) ? dir[0] : (ax == 1) ? dir[1] : dir[2];
+        int s = (ax + 1) * 2;
+        if (uax < R(0)) s -= 1;
+        surfIdx = -s;
+        return;
+      }
+    }
+  }
+
+  // universe%cellOffset (latUniverse_class.f90:394-414; zero for the others)
+  __device__ __forceinline__ void cell_offset(int u, int localID, double off[3]) const {
+    const DUni& U = g.unis[u];
+    off[0] = off[1] = off[2] = 0.0;
+    if (U.type == SG_UNI_LAT && U.i[5] != 0 && localID != U.i[3]) {
+      int ijk[3];
+      get_ijk(localID, U.i, ijk);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) off[i] = (ijk[i] - 0.5) * U.d[i] + U.d[3 + i];
+    }
+  }
+
+  // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow
+  __device__ __forceinline__ bool dive(Coords<R, MAXL>& c, int start) const {
+#pragma unroll
+    for (int i = 0; i < MAXL; ++i) {
+      if (i < start) continue;
+      int loc = c.base[i] + c.local[i] - 1;
+      int2 gf = g.graph[loc];
+      if (gf.x >= 0) { c.mat = gf.x; c.uid = gf.y; c.nest = i + 1; return true; }
+      if (i + 1 >= MAXL) break;
+      int nu = -gf.x - 1;
+      double off[3];
+      cell_offset(c.uni[i], c.local[i], off);
+      const DUni& N = g.unis[nu];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c.r[i + 1][k] = (c.r[i][k] - off[k]) - N.origin[k];
+      c.uni[i + 1] = nu;
+      c.base[i + 1] = gf.y - 1;
+      c.local[i + 1] = find_cell(nu, c.r[i + 1], c.u);
+    }
+    c.mat = SG_UNDEF_MAT;
+    c.nest = MAXL;
+    return false;
+  }
+
+  // geometryStd%placeCoord (geometryStd_class.f90:119-147): level-1 position is c.r[0] (global;
+  // the root universe carries no origin offset)
+  __device__ __forceinline__ bool place(Coords<R, MAXL>& c) const {
+    c.uni[0] = g.root;
+    c.base[0] = 0;
+    c.local[0] = find_cell(g.root, c.r[0], c.u);
+    return dive(c, 0);
+  }
+
+  // geometryStd%teleport (geometryStd_class.f90:492-514).  Level 1 holds the global position:
+  // the root universe has no origin offset (checked at upload).
+  __device__ __forceinline__ bool teleport(Coords<R, MAXL>& c, R dist) const {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c.r[0][k] = c.r[0][k] + (double)dist * (double)c.u[k];
+    bool ok = place(c);
+    if (c.mat == 0) {
+      surf_transform_bc<R>(g.surfs[g.border], c.r[0], c.u);
+      ok = place(c);
+    }
+    return ok;
+  }
+
+  // move_withCache / move_noCache (geometryStd_class.f90:214-352); fields absent (fieldDist = INF).
+  // Returns the event; maxDist is replaced by the distance moved.
+  __device__ __forceinline__ int move(Coords<R, MAXL>& c, R& maxDist, R cdist[MAXL], int csurf[MAXL],
+                                      DistCache& cache, bool useCache) const {
+    R dist = R(D_INF);
+    int surfIdx = 0, level = 0;
+    if (!useCache) cache.lvl = 0;
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) {
+      if (l < c.nest) {
+        if (cache.lvl < l + 1) {
+          uni_distance(c.uni[l], c.local[l], c.r[l], c.u, cdist[l], csurf[l]);
+          cache.lvl += 1;
+        }
+        R td = cdist[l];
+        if ((dist - td) >= dist * Tol<R>::fp_rel()) { dist = td; surfIdx = csurf[l]; level = l + 1; }
+      }
+    }
+    if (maxDist < dist) {                                         // collision inside the cell
+#pragma unroll
+      for (int l = 0; l < MAXL; ++l)
+        if (l < c.nest)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)maxDist * (double)c.u[k];
+      cache.lvl = 0;
+      return 1;   // COLL_EV
+    }
+    if (surfIdx == g.border + 1 && level == 1) {                  // domain boundary
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c.r[0][k] = c.r[0][k] + (double)dist * (double)c.u[k];
+      maxDist = dist;
+      cache.lvl = 0;
+      surf_explicit_bc<R>(g.surfs[g.border], c.r[0], c.u);
+      place(c);
+      return 2;   // BOUNDARY_EV
+    }
+    // crossing at `level`
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l)
+      if (l < level)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)dist * (double)c.u[k];
+    maxDist = dist;
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) if (l < level - 1) cdist[l] = cdist[l] - dist;
+    cache.lvl = level - 1;
+    c.nest = level;
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) {
+      if (l == level - 1) {
+        const DUni& U = g.unis[c.uni[l]];
+        if (U.type == SG_UNI_PIN) {                               // pinUniverse_class.f90:236-253
+          c.local[l] += (surfIdx == -1) ? -1 : 1;
+        } else {
+          if (U.type == SG_UNI_CELL) {                            // cellUniverse_class.f90:388-431
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)c.u[k] * g.nudge;
+          }
+          c.local[l] = find_cell(c.uni[l], c.r[l], c.u);
+        }
+      }
+    }
+    dive(c, level - 1);
+    return 3;   // CROSS_EV
+  }
+};
+
+}  // namespace sg

@@ -1,0 +1,1049 @@
+// sg_host.cu -- host implementation of the C ABI in include/scone_gpu.h.
+//
+// One handle owns one CUDA stream, the resident geometry / MG data / tally memory and two particle
+// banks sized by sg_config.max_bank.  Each eigenvalue cycle runs as: start-weight reduction ->
+// history-loop kernel -> brood-ordered site scatter -> end-weight reduction -> tally close ->
+// population control, with one host synchronisation (to learn the number of fission sites).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <functional>
+
+#include "sg_device.cuh"
+#include "sg_launch.h"
+#include "sg_support.h"
+
+using namespace sg;
+
+namespace {
+
+const double INF = 9223372036854775808.0;
+const double SURF_TOL = 1.0e-12;          // universalVariables.f90:23
+const double NUDGE = 1.0e-8;              // universalVariables.f90:25
+const double FP_REL_TOL = 1.0e-7;
+// mixed form: tolerances sized to FP32 distance accuracy (a crossing lands within ~1e-7 |d|)
+const double SURF_TOL_M = 4.0e-6;
+const double NUDGE_M = 1.0e-4;
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) return h->fail(SG_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+struct DArr {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = alloc(v.size() ? v.size() : 1);
+    if (e != cudaSuccess) return e;
+    if (v.empty()) return cudaSuccess;
+    e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct BankBufs {
+  DArr<double> r, dir, wgt, time;
+  DArr<int> G, brood;
+  cudaError_t alloc(size_t cap) {
+    cudaError_t e;
+    if ((e = r.alloc(3 * cap)) || (e = dir.alloc(3 * cap)) || (e = wgt.alloc(cap)) || (e = time.alloc(cap)) ||
+        (e = G.alloc(cap)) || (e = brood.alloc(cap)))
+      return e;
+    return cudaSuccess;
+  }
+  DBank view() { return DBank{r.p, dir.p, wgt.p, G.p, brood.p, time.p}; }
+  void free() { r.free(); dir.free(); wgt.free(); time.free(); G.free(); brood.free(); }
+};
+
+struct Admin {
+  std::vector<sg_clerk_desc> clerks;
+  std::vector<long long> addr;   // 1-based within the admin
+  long long N = 0;
+  long long off = 0;             // offset of bin 1 in the handle's tally arrays
+  int batchSize = 1, cycles = 0, batchN = 0;
+  long long normAddr = -1;
+  double normVal = 1.0;
+  int atch = -1;
+  long long keffAnalog = -1, keffImplicit = -1;   // 0-based admin-relative addresses
+  bool lastCycle() const { return (cycles + 1) % batchSize == 0; }
+};
+
+}  // namespace
+
+struct sg_handle_t {
+  sg_config cfg;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // geometry
+  bool hasGeom = false;
+  int maxl = 4;
+  double bounds[6];
+  DArr<DSurf> surfs64, surfsMx;
+  DArr<DUni> unis64, unisMx;
+  DArr<int> uniCells, cellPtr, cellSurf;
+  DArr<double> pinRsq, pinTol64, pinTolMx;
+  DArr<int2> graph;
+  DGeom g64{}, gMx{};
+
+  // MG data
+  bool hasMG = false;
+  bool anyFissile = false;
+  int nMat = 0, nG = 0;
+  DArr<double> mgD[9];
+  DArr<float> mgF[9];
+  DArr<int> fissile;
+  DMG<double> mg64{};
+  DMG<float> mgMx{};
+
+  // tallies
+  std::vector<Admin> admins;
+  long long totalBins = 0;
+  DArr<double> acc, bin, csum, csum2;
+
+  // banks and work buffers
+  int cap = 0;
+  BankBufs bank[2];
+  int cur = 0;                 // index of the "this cycle" bank
+  DArr<double> sR, sDir, sWgt, sTime;
+  DArr<int> sG, sBrood, sSeq, sCursor;
+  int regionCap = 0;
+  DArr<int> histN, start, scanTmp, flags, pos, kbuf;
+  DArr<unsigned long long> keys, sel;
+  DArr<unsigned int> hist16;
+  DArr<double> sumPart, scal;  // scal: 0 k_eff, 1 k_new, 2 start weight, 3 end weight, 4 k_end
+  DArr<int> totals;            // 0 sites total, 1 kept total, 2 dup total, 3 error
+  DArr<DCounters> ctr;
+  DArr<int> recColl;
+  DArr<unsigned long long> recRng;
+  int lastN = 0;
+
+  // point source
+  bool hasSource = false;
+  PointSourceArgs psrc{};
+  DArr<double> probG;
+
+  // eigen state
+  bool eigenReady = false;
+  int pop = 0;
+  unsigned long long master = 0;
+  double k = 1.0;
+
+  int fail(int code, const std::string& m) {
+    err = m;
+    return code;
+  }
+};
+
+namespace {
+
+int check_handle(sg_handle h) { return h ? SG_OK : SG_ERR_BAD_ARG; }
+
+unsigned long long rng_stride(unsigned long long s, long long n) { return lcg_skip(s, 152917LL * n); }
+
+// ------------------------------------------------------------------ geometry build
+int build_geometry(sg_handle h, const sg_geometry_desc* g) {
+  const int ns = g->n_surf, nu = g->n_uni;
+  if (ns <= 0 || nu <= 0 || g->root_uni < 0 || g->root_uni >= nu || g->border_surf < 0 || g->border_surf >= ns)
+    return h->fail(SG_ERR_BAD_ARG, "geometry: bad counts or root/border index");
+  std::vector<DSurf> s64(ns), sMx(ns);
+  auto fill_surf = [&](DSurf& s, int type, const double* par, bool mixed) -> bool {
+    std::memset(&s, 0, sizeof(s));
+    s.type = type;
+    for (int i = 0; i < SG_SURF_NPAR; ++i) s.p[i] = par[i];
+    s.axis = 2; s.pl0 = 0; s.pl1 = 1;
+    switch (type) {
+      case SG_SURF_XPLANE: s.axis = 0; break;
+      case SG_SURF_YPLANE: s.axis = 1; break;
+      case SG_SURF_ZPLANE: s.axis = 2; break;
+      case SG_SURF_XCYL: case SG_SURF_XSQCYL: s.axis = 0; s.pl0 = 1; s.pl1 = 2; break;
+      case SG_SURF_YCYL: case SG_SURF_YSQCYL: s.axis = 1; s.pl0 = 0; s.pl1 = 2; break;
+      case SG_SURF_ZCYL: case SG_SURF_ZSQCYL: s.axis = 2; s.pl0 = 0; s.pl1 = 1; break;
+      case SG_SURF_PLANE: case SG_SURF_SPHERE: case SG_SURF_BOX: break;
+      default: return false;
+    }
+    if (type == SG_SURF_PLANE) {   // plane_class.f90:78-84, gfortran NORM2 of coefficients 1-3
+      double scale = 1.0, ssq = 0.0;
+      for (int i = 0; i < 3; ++i)
+        if (par[i] != 0.0) {
+          double a = std::fabs(par[i]);
+          if (scale < a) { double t = scale / a; ssq = 1.0 + ssq * t * t; scale = a; }
+          else { double t = a / scale; ssq = ssq + t * t; }
+        }
+      double n = scale * std::sqrt(ssq);
+      for (int i = 0; i < 4; ++i) s.p[i] = par[i] / n;
+    }
+    const bool curved = type == SG_SURF_XCYL || type == SG_SURF_YCYL || type == SG_SURF_ZCYL || type == SG_SURF_SPHERE;
+    if (!mixed) s.tol = curved ? 2.0 * s.p[3] * SURF_TOL : SURF_TOL;   // cylinder :181, sphere :107
+    else {
+      double scale = 1.0;
+      if (type == SG_SURF_XPLANE || type == SG_SURF_YPLANE || type == SG_SURF_ZPLANE) scale = std::max(1.0, std::fabs(s.p[0]));
+      else if (type == SG_SURF_PLANE) scale = std::max(1.0, std::fabs(s.p[3]));
+      else if (!curved) for (int i = 0; i < 3; ++i) scale = std::max(scale, std::fabs(s.p[i]) + std::fabs(s.p[3 + i]));
+      s.tol = curved ? 2.0 * s.p[3] * SURF_TOL_M : SURF_TOL_M * scale;
+    }
+    return true;
+  };
+  for (int i = 0; i < ns; ++i) {
+    if (!fill_surf(s64[i], g->surf_type[i], g->surf_par + SG_SURF_NPAR * i, false) ||
+        !fill_surf(sMx[i], g->surf_type[i], g->surf_par + SG_SURF_NPAR * i, true))
+      return h->fail(SG_ERR_BAD_ARG, "geometry: unknown surface type");
+  }
+  for (int i = 0; i < 6; ++i) {
+    if (g->bc[i] < 0 || g->bc[i] > 2) return h->fail(SG_ERR_BAD_ARG, "geometry: bad boundary condition");
+    s64[g->border_surf].bc[i] = g->bc[i];
+    sMx[g->border_surf].bc[i] = g->bc[i];
+  }
+  // cells
+  std::vector<int> cptr(g->cell_ptr, g->cell_ptr + g->n_cell + 1);
+  std::vector<int> csurf(g->cell_surf, g->cell_surf + (g->n_cell ? g->cell_ptr[g->n_cell] : 0));
+  for (int v : csurf)
+    if (v == 0 || std::abs(v) > ns) return h->fail(SG_ERR_BAD_ARG, "geometry: bad cell surface index");
+  // universes
+  std::vector<DUni> u64(nu), uMx(nu);
+  std::vector<std::vector<int>> fills(nu);
+  std::vector<int> uniCells;
+  std::vector<double> rsq, tol64, tolMx;
+  for (int u = 0; u < nu; ++u) {
+    DUni U;
+    std::memset(&U, 0, sizeof(U));
+    U.type = g->uni_type[u];
+    for (int i = 0; i < 3; ++i) U.origin[i] = g->uni_origin[3 * u + i];
+    std::vector<int> ip(g->uni_ipar + g->uni_iptr[u], g->uni_ipar + g->uni_iptr[u + 1]);
+    std::vector<double> dp(g->uni_dpar + g->uni_dptr[u], g->uni_dpar + g->uni_dptr[u + 1]);
+    std::vector<int> f(g->uni_fill + g->uni_fptr[u], g->uni_fill + g->uni_fptr[u + 1]);
+    DUni Um = U;
+    switch (U.type) {
+      case SG_UNI_ROOT:                          // rootUniverse_class.f90:100-119: fills [inside, OUTSIDE]
+        if (ip.size() != 1 || f.size() != 1) return h->fail(SG_ERR_BAD_ARG, "root universe: ipar/fill");
+        if (U.origin[0] != 0.0 || U.origin[1] != 0.0 || U.origin[2] != 0.0)
+          return h->fail(SG_ERR_BAD_ARG, "root universe: origin offset is not supported");
+        U.i[0] = ip[0];
+        f.push_back(0);
+        break;
+      case SG_UNI_CELL:                          // cellUniverse_class.f90:145-151: + UNDEF, OVERLAP
+        if (ip.size() != f.size()) return h->fail(SG_ERR_BAD_ARG, "cell universe: cells/fills mismatch");
+        U.i[0] = (int)uniCells.size();
+        U.i[1] = (int)ip.size();
+        for (int c : ip) {
+          if (c < 0 || c >= g->n_cell) return h->fail(SG_ERR_BAD_ARG, "cell universe: bad cell index");
+          uniCells.push_back(c);
+        }
+        f.push_back(SG_UNDEF_MAT);
+        f.push_back(SG_OVERLAP_MAT);
+        break;
+      case SG_UNI_PIN: {                         // pinUniverse_class.f90:76-139
+        int N = (int)dp.size() + 1;
+        if ((int)f.size() != N) return h->fail(SG_ERR_BAD_ARG, "pin universe: radii/fills mismatch");
+        U.i[0] = (int)rsq.size();
+        U.i[1] = N;
+        for (int i = 0; i < N; ++i) {
+          double rad = (i < N - 1) ? dp[i] : INF * 1.1;
+          if (i < N - 1 && (rad <= 0.0 || (i > 0 && rad <= dp[i - 1])))
+            return h->fail(SG_ERR_BAD_ARG, "pin universe: radii must be positive and ascending");
+          rsq.push_back(rad * rad);
+          tol64.push_back(2.0 * rad * SURF_TOL);
+          tolMx.push_back(2.0 * rad * SURF_TOL_M);
+        }
+        break;
+      }
+      case SG_UNI_LAT: {                         // latUniverse_class.f90:113-260
+        if (ip.size() < 3 || dp.size() != 3) return h->fail(SG_ERR_BAD_ARG, "lattice: shape/pitch");
+        int sizeN[3] = {ip[0], ip[1], ip[2]};
+        double pitch[3] = {dp[0], dp[1], dp[2]};
+        if (sizeN[2] == 0) { sizeN[2] = 1; pitch[2] = 2.0 * INF; }
+        if (sizeN[0] <= 0 || sizeN[1] <= 0) return h->fail(SG_ERR_BAD_ARG, "lattice: zero shape");
+        int nloc = sizeN[0] * sizeN[1] * sizeN[2] + 1;
+        if ((int)f.size() != nloc) return h->fail(SG_ERR_BAD_ARG, "lattice: fills must be nx*ny*nz + 1");
+        for (int i = 0; i < 3; ++i) {
+          U.i[i] = sizeN[i];
+          U.d[i] = pitch[i];
+          U.d[3 + i] = -(sizeN[i] * 0.5 * pitch[i]);
+          U.d[6 + i] = pitch[i] * 0.5 - pitch[i] * SURF_TOL;
+        }
+        U.i[3] = nloc;
+        U.i[5] = (ip.size() > 3) ? (ip[3] != 0) : 1;
+        // outline box (latUniverse_class.f90:176-183) appended as an extra surface
+        double par[SG_SURF_NPAR] = {0, 0, 0, std::fabs(U.d[3]), std::fabs(U.d[4]), std::fabs(U.d[5])};
+        DSurf o64, oMx;
+        fill_surf(o64, SG_SURF_BOX, par, false);
+        fill_surf(oMx, SG_SURF_BOX, par, true);
+        U.i[4] = (int)s64.size();
+        s64.push_back(o64);
+        sMx.push_back(oMx);
+        break;
+      }
+      default:
+        return h->fail(SG_ERR_BAD_ARG, "geometry: unknown universe type");
+    }
+    Um = U;
+    if (U.type == SG_UNI_LAT)
+      for (int i = 0; i < 3; ++i) Um.d[6 + i] = U.d[i] * 0.5 - U.d[i] * SURF_TOL_M;
+    u64[u] = U;
+    uMx[u] = Um;
+    fills[u] = f;
+  }
+  // shrunk geomGraph (geomGraph_class.f90:172-232 layout; :309-345 unique IDs)
+  std::vector<int> base(nu, -1);
+  std::vector<int2> graph;
+  auto layout = [&](int u) {
+    base[u] = (int)graph.size() + 1;
+    for (int f : fills[u]) graph.push_back(make_int2(f, 0));
+  };
+  layout(g->root_uni);
+  for (size_t loc = 0; loc < graph.size(); ++loc) {
+    int f = graph[loc].x;
+    if (f < 0) {
+      int u = -f - 1;
+      if (u < 0 || u >= nu) return h->fail(SG_ERR_BAD_ARG, "geometry: fill names a missing universe");
+      if (base[u] < 0) layout(u);
+      graph[loc].y = base[u];
+    }
+  }
+  int cells = 0;
+  for (auto& e : graph) if (e.x > 0) e.y = ++cells;
+  // nesting depth
+  std::function<int(int, int)> depth = [&](int u, int d) -> int {
+    if (d > SG_MAX_NEST) return d;
+    int m = d;
+    for (int f : fills[u]) if (f < 0) m = std::max(m, depth(-f - 1, d + 1));
+    return m;
+  };
+  int dep = depth(g->root_uni, 1);
+  if (dep > 4) return h->fail(SG_ERR_BAD_ARG, "geometry: nesting deeper than 4 levels is not supported");
+  h->maxl = dep <= 2 ? 2 : 4;
+  // bounds (geometryStd_class.f90:186-205)
+  {
+    const DSurf& b = s64[g->border_surf];
+    for (int i = 0; i < 3; ++i) { h->bounds[i] = -INF; h->bounds[3 + i] = INF; }
+    if (b.type == SG_SURF_BOX) for (int i = 0; i < 3; ++i) { h->bounds[i] = b.p[i] - b.p[3 + i]; h->bounds[3 + i] = b.p[i] + b.p[3 + i]; }
+    else if (b.type >= SG_SURF_XSQCYL) { int pl[2] = {b.pl0, b.pl1}; for (int i : pl) { h->bounds[i] = b.p[i] - b.p[3 + i]; h->bounds[3 + i] = b.p[i] + b.p[3 + i]; } }
+    else if (b.type == SG_SURF_SPHERE) for (int i = 0; i < 3; ++i) { h->bounds[i] = b.p[i] - b.p[3]; h->bounds[3 + i] = b.p[i] + b.p[3]; }
+    else if (b.type >= SG_SURF_XCYL && b.type <= SG_SURF_ZCYL) { int pl[2] = {b.pl0, b.pl1}; for (int i : pl) { h->bounds[i] = b.p[i] - b.p[3]; h->bounds[3 + i] = b.p[i] + b.p[3]; } }
+    for (int i = 0; i < 3; ++i)
+      if (h->bounds[i] <= -INF && h->bounds[3 + i] >= INF) { h->bounds[i] = 0.0; h->bounds[3 + i] = 0.0; }
+  }
+  cudaStream_t st = h->stream;
+  CK(h->surfs64.upload(s64, st));
+  CK(h->surfsMx.upload(sMx, st));
+  CK(h->unis64.upload(u64, st));
+  CK(h->unisMx.upload(uMx, st));
+  CK(h->uniCells.upload(uniCells, st));
+  CK(h->cellPtr.upload(cptr, st));
+  CK(h->cellSurf.upload(csurf, st));
+  CK(h->pinRsq.upload(rsq, st));
+  CK(h->pinTol64.upload(tol64, st));
+  CK(h->pinTolMx.upload(tolMx, st));
+  CK(h->graph.upload(graph, st));
+  h->g64 = DGeom{h->surfs64.p, h->unis64.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
+                 h->pinTol64.p, h->graph.p, g->root_uni, g->border_surf, NUDGE};
+  h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
+                 h->pinTolMx.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M};
+  h->hasGeom = true;
+  // active materials for the majorant
+  return SG_OK;
+}
+
+std::vector<int> active_mats(sg_handle h, const std::vector<int2>& graph) {
+  std::vector<int> a;
+  for (auto& e : graph) if (e.x > 0 && e.x <= h->nMat) a.push_back(e.x);
+  std::sort(a.begin(), a.end());
+  a.erase(std::unique(a.begin(), a.end()), a.end());
+  return a;
+}
+
+int build_mg(sg_handle h, const sg_mg_desc* d) {
+  const int M = d->n_mat, nG = d->n_g;
+  if (M <= 0 || nG <= 0) return h->fail(SG_ERR_BAD_ARG, "mg: bad sizes");
+  if (!h->hasGeom) return h->fail(SG_ERR_STATE, "mg: upload the geometry first (majorant uses its materials)");
+  h->nMat = M;
+  h->nG = nG;
+  const size_t MG = (size_t)M * nG;
+  std::vector<double> total(MG), scatter(MG), capture(MG), fission(MG, 0), nuf(MG, 0), chi(MG, 0);
+  std::vector<double> P0(MG * nG), prod(MG * nG);
+  std::vector<int> fis(M);
+  h->anyFissile = false;
+  for (int m = 0; m < M; ++m) {
+    fis[m] = d->fissile[m] ? 1 : 0;
+    h->anyFissile |= fis[m] != 0;
+    for (size_t k = (size_t)m * nG * nG; k < (size_t)(m + 1) * nG * nG; ++k) { P0[k] = d->p0[k]; prod[k] = d->prod[k]; }
+    for (int gi = 0; gi < nG; ++gi) {
+      size_t k = (size_t)m * nG + gi;
+      double s = 0.0;                              // multiScatterMG: scatterXSs = sum(P0, 1)
+      for (int go = 0; go < nG; ++go) s = s + P0[k * nG + go];
+      scatter[k] = s;
+      capture[k] = d->capture[k];
+      if (fis[m]) { fission[k] = d->fission[k]; nuf[k] = d->nu[k] * d->fission[k]; }
+      total[k] = scatter[k] + capture[k];          // baseMgNeutronMaterial_class.f90:282-289
+      if (fis[m]) total[k] = total[k] + fission[k];
+      if (!(total[k] > 0.0)) return h->fail(SG_ERR_BAD_ARG, "mg: non-positive total cross section");
+    }
+    if (fis[m]) {                                  // fissionMG_class.f90:262-268
+      double S = 0.0;
+      for (int g = 0; g < nG; ++g) S = S + d->chi[(size_t)m * nG + g];
+      for (int g = 0; g < nG; ++g) {
+        double c = d->chi[(size_t)m * nG + g];
+        if (std::fabs(S - 1.0) > 0.01 * FP_REL_TOL) c = c / S;
+        chi[(size_t)m * nG + g] = c;
+      }
+    }
+  }
+  std::vector<int2> graph(h->graph.n);
+  CK(cudaMemcpy(graph.data(), h->graph.p, graph.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+  std::vector<int> act = active_mats(h, graph);
+  for (int a : act) if (a > M) return h->fail(SG_ERR_BAD_ARG, "mg: geometry uses a material beyond n_mat");
+  std::vector<double> maj(nG, 0.0);                // initMajorant (baseMgNeutronDatabase :458-503)
+  for (int g = 0; g < nG; ++g) {
+    double xs = 0.0;
+    for (int a : act) xs = std::max(xs, total[(size_t)(a - 1) * nG + g]);
+    maj[g] = xs * 1.0;
+  }
+  const std::vector<double>* src[9] = {&total, &scatter, &capture, &fission, &nuf, &chi, &P0, &prod, &maj};
+  cudaStream_t st = h->stream;
+  for (int i = 0; i < 9; ++i) {
+    CK(h->mgD[i].upload(*src[i], st));
+    std::vector<float> f(src[i]->begin(), src[i]->end());
+    CK(h->mgF[i].upload(f, st));
+  }
+  CK(h->fissile.upload(fis, st));
+  double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
+  h->mg64 = DMG<double>{M, nG, h->mgD[0].p, h->mgD[1].p, h->mgD[2].p, h->mgD[3].p, h->mgD[4].p, h->mgD[5].p,
+                        h->mgD[6].p, h->mgD[7].p, h->fissile.p, h->mgD[8].p, cxs};
+  h->mgMx = DMG<float>{M, nG, h->mgF[0].p, h->mgF[1].p, h->mgF[2].p, h->mgF[3].p, h->mgF[4].p, h->mgF[5].p,
+                       h->mgF[6].p, h->mgF[7].p, h->fissile.p, h->mgF[8].p, (float)cxs};
+  h->hasMG = true;
+  return SG_OK;
+}
+
+int alloc_work(sg_handle h) {
+  const size_t cap = (size_t)h->cap;
+  for (int b = 0; b < 2; ++b) CK(h->bank[b].alloc(cap));
+  h->regionCap = (int)((2 * cap + SITE_REGIONS - 1) / SITE_REGIONS) + 4096;
+  const size_t sc = (size_t)h->regionCap * SITE_REGIONS;
+  CK(h->sR.alloc(3 * sc)); CK(h->sDir.alloc(3 * sc)); CK(h->sWgt.alloc(sc)); CK(h->sTime.alloc(sc));
+  CK(h->sG.alloc(sc)); CK(h->sBrood.alloc(sc)); CK(h->sSeq.alloc(sc)); CK(h->sCursor.alloc(SITE_REGIONS));
+  CK(h->histN.alloc(cap + 1)); CK(h->start.alloc(cap + 1)); CK(h->scanTmp.alloc(scan_tmp_size((int)cap + 1) + 16));
+  CK(h->flags.alloc(cap + 1)); CK(h->pos.alloc(cap + 1)); CK(h->kbuf.alloc(4));
+  CK(h->keys.alloc(cap)); CK(h->sel.alloc(2)); CK(h->hist16.alloc(65536));
+  CK(h->sumPart.alloc(SUM_BLOCKS)); CK(h->scal.alloc(8)); CK(h->totals.alloc(8)); CK(h->ctr.alloc(1));
+  if (h->cfg.record_histories) { CK(h->recColl.alloc(cap)); CK(h->recRng.alloc(cap)); }
+  CK(cudaMemset(h->scal.p, 0, 8 * sizeof(double)));
+  return SG_OK;
+}
+
+DSites site_view(sg_handle h) {
+  return DSites{h->sR.p, h->sDir.p, h->sWgt.p, h->sG.p, h->sBrood.p, h->sSeq.p, h->sTime.p, h->sCursor.p, h->regionCap};
+}
+
+// clerks of admin `a` and its attachment flattened for one launch (attachment first)
+template <class R>
+int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long long& hi) {
+  std::vector<int> chain;
+  for (int x = a; x >= 0; x = h->admins[x].atch) {
+    if (chain.size() > 4) return h->fail(SG_ERR_BAD_ARG, "tally: attachment cycle");
+    chain.push_back(x);
+  }
+  std::reverse(chain.begin(), chain.end());
+  lo = 0; hi = 0;
+  bool first = true;
+  for (int x : chain) {
+    const Admin& A = h->admins[x];
+    if (A.N == 0) continue;
+    if (first) { lo = A.off; hi = A.off + A.N; first = false; }
+    lo = std::min(lo, A.off);
+    hi = std::max(hi, A.off + A.N);
+  }
+  t.n_clerks = 0;
+  t.keff_clerk = -1;
+  for (int x : chain) {
+    const Admin& A = h->admins[x];
+    for (size_t c = 0; c < A.clerks.size(); ++c) {
+      const sg_clerk_desc& d = A.clerks[c];
+      if (d.type == SG_CLERK_KEFF_ANALOG) continue;   // scored at cycle start/end only
+      if (t.n_clerks >= MAX_CLERKS) return h->fail(SG_ERR_BAD_ARG, "tally: too many clerks in one launch");
+      DClerk& K = t.clerks[t.n_clerks];
+      std::memset(&K, 0, sizeof(K));
+      K.type = d.type;
+      K.handle_virtual = d.handle_virtual;
+      K.width = d.n_resp > 0 ? d.n_resp : 1;
+      for (int i = 0; i < 4; ++i) K.resp[i] = d.resp[i];
+      K.n_axes = d.n_axes;
+      long long mul = 1;
+      for (int i = 0; i < d.n_axes; ++i) {
+        K.ax_kind[i] = d.axes[i].kind;
+        K.ax_n[i] = d.axes[i].n;
+        K.ax_min[i] = d.axes[i].min;
+        K.ax_step[i] = (d.axes[i].max - d.axes[i].min) / d.axes[i].n;
+        K.ax_inv_step[i] = 1.0 / K.ax_step[i];
+        K.multi[i] = mul;
+        mul *= d.axes[i].n;
+      }
+      K.g_top = d.filter_g_top;
+      K.g_low = d.filter_g_low;
+      K.acc_off = A.off + (A.addr[c] - 1) - lo;
+      if (d.type == SG_CLERK_KEFF_IMPLICIT) {
+        if (t.keff_clerk >= 0) return h->fail(SG_ERR_BAD_ARG, "tally: one k-implicit clerk per launch");
+        t.keff_clerk = t.n_clerks;
+      }
+      t.n_clerks++;
+    }
+  }
+  return SG_OK;
+}
+
+// The gen loop over `n` histories of bank `in` on the device; fission sites are written into bank
+// `out` in brood order.  Returns SG_OK and the number of sites.
+template <class R>
+int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long master, const double* d_k,
+               DBank out, int outcap, int* S_out, sg_cycle_stats* st, const DGeom& geom, const DMG<R>& mg) {
+  cudaStream_t s = h->stream;
+  TransportArgs<R> t;
+  std::memset(&t, 0, sizeof(t));
+  long long lo = 0, hi = 0;
+  int rc = build_clerks<R>(h, admin, t, lo, hi);
+  if (rc) return rc;
+  t.geom = geom;
+  t.mg = mg;
+  t.in = in;
+  t.n = n;
+  t.master = master;
+  t.k_eff = d_k;
+  t.acc = h->acc.p + lo;
+  t.acc_n = (int)(hi - lo);
+  size_t smem = (size_t)t.acc_n * sizeof(double);
+  t.use_smem = (t.acc_n > 0 && smem <= 64 * 1024) ? 1 : 0;
+  if (!t.use_smem) smem = 0;
+  t.sites = site_view(h);
+  t.hist_nsites = h->histN.p;
+  t.rec_coll = h->cfg.record_histories ? h->recColl.p : nullptr;
+  t.rec_rng = h->cfg.record_histories ? h->recRng.p : nullptr;
+  t.ctr = h->ctr.p;
+  t.use_cache = h->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
+  t.max_segments = 1000000;
+  CK(cudaMemsetAsync(h->ctr.p, 0, sizeof(DCounters), s));
+  CK(cudaMemsetAsync(h->sCursor.p, 0, SITE_REGIONS * sizeof(int), s));
+  CK(cudaMemsetAsync(h->histN.p, 0, (size_t)(n + 1) * sizeof(int), s));
+  CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), s));
+  CK(launch_transport<R>(t, h->maxl, h->cfg.transport == SG_TRANSPORT_DT, smem, s, nullptr));
+  CK(exclusive_scan(h->histN.p, n + 1, h->start.p, h->scanTmp.p, h->totals.p + 0, s));
+  CK(launch_site_scatter(site_view(h), h->start.p, out, outcap, h->totals.p + 3, s));
+  DCounters c;
+  int tot[8];
+  CK(cudaMemcpyAsync(&c, h->ctr.p, sizeof(c), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(tot, h->totals.p, sizeof(tot), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  h->lastN = n;
+  if (c.err_code) {
+    char m[160];
+    std::snprintf(m, sizeof(m), "transport: error %d raised in history %d", c.err_code, c.err_hist);
+    return h->fail(c.err_code, m);
+  }
+  if (tot[3] || tot[0] > outcap) return h->fail(SG_ERR_BANK_OVERFLOW, "transport: fission bank overflow");
+  *S_out = tot[0];
+  if (st) {
+    st->n_histories = n;
+    st->n_events = (int64_t)c.events;
+    st->n_collisions = (int64_t)c.collisions;
+    st->n_next = tot[0];
+  }
+  return SG_OK;
+}
+
+int gen_loop(sg_handle h, int admin, DBank in, int n, unsigned long long master, const double* d_k, DBank out,
+             int outcap, int* S, sg_cycle_stats* st) {
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
+  if (admin < 0 || admin >= (int)h->admins.size()) return h->fail(SG_ERR_BAD_ARG, "bad tally admin");
+  if (n < 0 || n > h->cap) return h->fail(SG_ERR_BANK_OVERFLOW, "bank larger than max_bank");
+  if (h->cfg.precision == SG_PREC_MIXED) return gen_loop_t<float>(h, admin, in, n, master, d_k, out, outcap, S, st, h->gMx, h->mgMx);
+  return gen_loop_t<double>(h, admin, in, n, master, d_k, out, outcap, S, st, h->g64, h->mg64);
+}
+
+// tallyAdmin%reportCycleStart: keffAnalog START_POP (keffAnalogClerk_class.f90:140-147)
+int cycle_start(sg_handle h, int admin, const double* d_w, double w) {
+  for (int x = admin; x >= 0; x = h->admins[x].atch) {
+    const Admin& A = h->admins[x];
+    if (A.keffAnalog >= 0) CK(add_scalar(h->acc.p + A.off + A.keffAnalog, d_w, w, h->stream));
+  }
+  return SG_OK;
+}
+
+// tallyAdmin%reportCycleEnd for the chain (attachment first); k of `kadmin` is written to k_out
+int cycle_end(sg_handle h, int admin, const double* d_endw, const double* d_kend, int kadmin, double* k_out) {
+  std::vector<int> chain;
+  for (int x = admin; x >= 0; x = h->admins[x].atch) chain.push_back(x);
+  std::reverse(chain.begin(), chain.end());
+  for (int x : chain) {
+    Admin& A = h->admins[x];
+    TallyCloseArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.acc = h->acc.p + A.off;
+    a.bin = h->bin.p + A.off;
+    a.csum = h->csum.p + A.off;
+    a.csum2 = h->csum2.p + A.off;
+    a.N = A.N;
+    a.last_cycle = A.lastCycle();
+    a.close_batch = (A.cycles + 1) % A.batchSize == 0;
+    a.keff_analog = A.keffAnalog;
+    a.keff_implicit = A.keffImplicit;
+    a.norm_addr = A.normAddr >= 1 ? A.normAddr - 1 : -1;
+    a.norm_val = A.normVal;
+    a.end_weight = d_endw;
+    a.k_end = d_kend;
+    int batchN = A.batchN + (a.close_batch ? 1 : 0);
+    a.batchN = batchN;
+    a.k_out = (x == kadmin) ? k_out : nullptr;
+    a.k_addr = A.keffImplicit >= 0 ? A.keffImplicit + 4 : (A.keffAnalog >= 0 ? A.keffAnalog + 2 : -1);
+    if (A.N > 0) CK(launch_tally_close(a, h->stream));
+    A.cycles += 1;
+    A.batchN = batchN;
+  }
+  return SG_OK;
+}
+
+// particleDungeon%normSize_Repr on the device: sites (sorted by brood) in `in`, result in `out`
+int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long master, DBank out, int n_hist) {
+  cudaStream_t s = h->stream;
+  if (S <= 0) return h->fail(SG_ERR_STATE, "normSize: empty fission bank");
+  int excess = S - totPop;
+  int heap = excess > 0 ? excess : (excess < 0 ? (-excess) % S : 0);
+  if (heap > 0) {
+    k_rn_keys<<<((S + 31) / 32 + 127) / 128, 128, 0, s>>>(master, S, h->keys.p);
+    CK(cudaGetLastError());
+    CK(radix_select(h->keys.p, S, heap, h->sel.p, h->kbuf.p, h->hist16.p, s));
+  }
+  if (excess > 0) {
+    CK(launch_flags(h->keys.p, S, h->sel.p, 1, h->flags.p, s));
+    CK(cudaMemsetAsync(h->flags.p + S, 0, sizeof(int), s));
+    CK(exclusive_scan(h->flags.p, S + 1, h->pos.p, h->scanTmp.p, h->totals.p + 1, s));
+    CK(launch_compact(in, S, h->flags.p, h->pos.p, out, s));
+    int kept = 0;
+    CK(cudaMemcpyAsync(&kept, h->totals.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (kept != totPop) return h->fail(SG_ERR_STATE, "normSize: normalisation failed (ties at the threshold)");
+  } else if (excess < 0) {
+    int n_copies = (-excess) / S;
+    if ((long long)(n_copies + 1) * S + heap > h->cap) return h->fail(SG_ERR_BANK_OVERFLOW, "normSize: bank overflow");
+    if (heap > 0) CK(launch_flags(h->keys.p, S, h->sel.p, 0, h->flags.p, s));
+    else CK(cudaMemsetAsync(h->flags.p, 0, (size_t)S * sizeof(int), s));
+    CK(cudaMemsetAsync(h->flags.p + S, 0, sizeof(int), s));
+    CK(exclusive_scan(h->flags.p, S + 1, h->pos.p, h->scanTmp.p, h->totals.p + 2, s));
+    CK(launch_replicate(in, S, h->flags.p, h->pos.p, h->start.p, n_copies, out, s));
+    (void)n_hist;
+  } else {
+    CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.dir, in.dir, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.wgt, in.wgt, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.time, in.time, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.G, in.G, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.brood, in.brood, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
+  }
+  return SG_OK;
+}
+
+int h2d_bank(sg_handle h, const sg_bank* b, int n, DBank d) {
+  cudaStream_t s = h->stream;
+  if (!b->r || !b->dir) return h->fail(SG_ERR_BAD_ARG, "bank: r and dir are required");
+  CK(cudaMemcpyAsync(d.r, b->r, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.dir, b->dir, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (b->wgt) CK(cudaMemcpyAsync(d.wgt, b->wgt, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  else {
+    std::vector<double> one(n, 1.0);
+    CK(cudaMemcpyAsync(d.wgt, one.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  if (b->G) CK(cudaMemcpyAsync(d.G, b->G, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  else return h->fail(SG_ERR_BAD_ARG, "bank: G is required for MG transport");
+  if (b->time) CK(cudaMemcpyAsync(d.time, b->time, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  else CK(cudaMemsetAsync(d.time, 0, sizeof(double) * n, s));
+  return SG_OK;
+}
+
+int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
+  cudaStream_t s = h->stream;
+  if (n <= 0) return SG_OK;
+  if (b->r) CK(cudaMemcpyAsync(b->r, d.r, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->dir) CK(cudaMemcpyAsync(b->dir, d.dir, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->wgt) CK(cudaMemcpyAsync(b->wgt, d.wgt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->G) CK(cudaMemcpyAsync(b->G, d.G, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  if (b->time) CK(cudaMemcpyAsync(b->time, d.time, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->brood_id) CK(cudaMemcpyAsync(b->brood_id, d.brood, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return SG_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int32_t sg_create(const sg_config* cfg, sg_handle* out) {
+  if (!cfg || !out) return SG_ERR_BAD_ARG;
+  *out = nullptr;
+  if (cfg->precision != SG_PREC_FP64 && cfg->precision != SG_PREC_MIXED) return SG_ERR_BAD_ARG;
+  if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_ST_NOCACHE) return SG_ERR_BAD_ARG;
+  if (cfg->max_bank <= 0) return SG_ERR_BAD_ARG;
+  sg_handle h = new sg_handle_t();
+  h->cfg = *cfg;
+  h->cap = cfg->max_bank;
+  if (cudaSetDevice(cfg->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return SG_ERR_CUDA;
+  }
+  int rc = alloc_work(h);
+  if (rc) { delete h; return rc; }
+  *out = h;
+  return SG_OK;
+}
+
+int32_t sg_destroy(sg_handle h) {
+  if (!h) return SG_ERR_BAD_ARG;
+  cudaStreamSynchronize(h->stream);
+  for (auto& b : h->bank) b.free();
+  h->surfs64.free(); h->surfsMx.free(); h->unis64.free(); h->unisMx.free(); h->uniCells.free();
+  h->cellPtr.free(); h->cellSurf.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
+  for (auto& a : h->mgD) a.free();
+  for (auto& a : h->mgF) a.free();
+  h->fissile.free(); h->acc.free(); h->bin.free(); h->csum.free(); h->csum2.free();
+  h->sR.free(); h->sDir.free(); h->sWgt.free(); h->sTime.free(); h->sG.free(); h->sBrood.free(); h->sSeq.free();
+  h->sCursor.free(); h->histN.free(); h->start.free(); h->scanTmp.free(); h->flags.free(); h->pos.free();
+  h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->sumPart.free(); h->scal.free();
+  h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return SG_OK;
+}
+
+int32_t sg_last_error(sg_handle h, char* buf, size_t len) {
+  if (!h || !buf || len == 0) return SG_ERR_BAD_ARG;
+  std::snprintf(buf, len, "%s", h->err.c_str());
+  return SG_OK;
+}
+
+int32_t sg_upload_geometry(sg_handle h, const sg_geometry_desc* g) {
+  if (!h || !g) return SG_ERR_BAD_ARG;
+  return build_geometry(h, g);
+}
+
+int32_t sg_upload_mg(sg_handle h, const sg_mg_desc* mg) {
+  if (!h || !mg) return SG_ERR_BAD_ARG;
+  return build_mg(h, mg);
+}
+
+int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out) {
+  if (!h || !t || !admin_out || t->n_clerks < 0) return SG_ERR_BAD_ARG;
+  Admin A;
+  long long loc = 1;
+  for (int i = 0; i < t->n_clerks; ++i) {
+    const sg_clerk_desc& d = t->clerks[i];
+    long long size;
+    if (d.type == SG_CLERK_KEFF_ANALOG) { size = 3; A.keffAnalog = loc - 1; }
+    else if (d.type == SG_CLERK_KEFF_IMPLICIT) { size = 5; A.keffImplicit = loc - 1; }
+    else if (d.type == SG_CLERK_COLLISION || d.type == SG_CLERK_TRACK) {
+      if (d.n_resp < 1 || d.n_resp > 4 || d.n_axes < 0 || d.n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "tally: bad clerk");
+      long long nb = 1;
+      for (int a = 0; a < d.n_axes; ++a) {
+        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_MATERIAL)
+          return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
+        if (d.axes[a].kind <= SG_AXIS_Z && !(d.axes[a].max > d.axes[a].min))
+          return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap needs max > min");
+        nb *= d.axes[a].n;
+      }
+      size = nb * d.n_resp;
+    } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown clerk type");
+    A.clerks.push_back(d);
+    A.addr.push_back(loc);
+    loc += size;
+  }
+  A.N = loc - 1;
+  A.batchSize = t->batch_size > 0 ? t->batch_size : 1;
+  if (t->norm_clerk >= 0) {
+    if (t->norm_clerk >= t->n_clerks) return h->fail(SG_ERR_BAD_ARG, "tally: bad norm clerk");
+    A.normAddr = A.addr[t->norm_clerk];
+    A.normVal = t->norm_val;
+  }
+  A.off = h->totalBins;
+  // grow the device score memory, keeping what earlier admins hold
+  long long newTotal = h->totalBins + A.N;
+  DArr<double>* arrs[4] = {&h->acc, &h->bin, &h->csum, &h->csum2};
+  for (DArr<double>* a : arrs) {
+    std::vector<double> old(h->totalBins);
+    if (h->totalBins) { cudaError_t e = cudaMemcpy(old.data(), a->p, h->totalBins * sizeof(double), cudaMemcpyDeviceToHost); if (e) return h->fail(SG_ERR_CUDA, "tally copy"); }
+    old.resize(newTotal > 0 ? newTotal : 1, 0.0);
+    CK(a->upload(old, h->stream));
+  }
+  h->totalBins = newTotal;
+  h->admins.push_back(A);
+  *admin_out = (int32_t)h->admins.size() - 1;
+  return SG_OK;
+}
+
+int32_t sg_attach_tally(sg_handle h, int32_t admin, int32_t atch) {
+  if (!h || admin < 0 || admin >= (int)h->admins.size() || atch < 0 || atch >= (int)h->admins.size() || admin == atch)
+    return SG_ERR_BAD_ARG;
+  h->admins[admin].atch = atch;
+  return SG_OK;
+}
+
+int32_t sg_set_point_source(sg_handle h, const sg_point_source_desc* src) {
+  if (!h || !src) return SG_ERR_BAD_ARG;
+  PointSourceArgs& p = h->psrc;
+  for (int i = 0; i < 3; ++i) { p.r[i] = src->r[i]; p.dir[i] = src->dir[i]; }
+  p.isotropic = src->isotropic;
+  p.G = src->G;
+  p.n_prob_g = src->n_prob_g;
+  if (src->n_prob_g > 0) {
+    std::vector<double> v(src->prob_g, src->prob_g + src->n_prob_g);
+    CK(h->probG.upload(v, h->stream));
+    p.prob_g = h->probG.p;
+  } else p.prob_g = nullptr;
+  h->hasSource = true;
+  return SG_OK;
+}
+
+int32_t sg_generate_source(sg_handle h, uint64_t master_state, int32_t n, sg_bank* out) {
+  if (!h || !out || n < 0 || n > h->cap) return SG_ERR_BAD_ARG;
+  if (!h->hasSource) return h->fail(SG_ERR_STATE, "no point source set");
+  PointSourceArgs a = h->psrc;
+  a.out = h->bank[h->cur].view();
+  a.n = n;
+  a.master = master_state;
+  if (n > 0) CK(launch_point_source(a, h->stream));
+  return d2h_bank(h, a.out, n, out);
+}
+
+int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t n, uint64_t master_state,
+                          double k_eff, sg_bank* next, int32_t next_cap, sg_cycle_stats* stats) {
+  if (!h || !in || n < 0 || n > h->cap) return SG_ERR_BAD_ARG;
+  DBank A = h->bank[0].view(), B = h->bank[1].view();
+  int rc = h2d_bank(h, in, n, A);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->scal.p + 0, &k_eff, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int S = 0;
+  sg_cycle_stats st{};
+  rc = gen_loop(h, admin, A, n, master_state, h->scal.p + 0, B, h->cap, &S, &st);
+  if (rc) return rc;
+  h->eigenReady = false;   // the resident banks were overwritten
+  if (next && S > 0) {
+    if (S > next_cap) return h->fail(SG_ERR_BANK_OVERFLOW, "next bank capacity too small");
+    rc = d2h_bank(h, B, S, next);
+    if (rc) return rc;
+  }
+  if (stats) {
+    *stats = st;
+    stats->k_eff = k_eff;
+    stats->k_new = k_eff;
+    double sw = 0, ew = 0;
+    if (in->wgt) for (int i = 0; i < n; ++i) sw += in->wgt[i]; else sw = n;
+    if (next && next->wgt) for (int i = 0; i < S && i < next_cap; ++i) ew += next->wgt[i];
+    stats->start_weight = sw;
+    stats->end_weight = ew;
+  }
+  return SG_OK;
+}
+
+int32_t sg_tally_cycle_start(sg_handle h, int32_t admin, double w) {
+  if (!h || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  return cycle_start(h, admin, nullptr, w);
+}
+
+int32_t sg_tally_cycle_end(sg_handle h, int32_t admin, double w, double k_end) {
+  if (!h || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  CK(cudaMemcpyAsync(h->scal.p + 3, &w, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->scal.p + 4, &k_end, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, -1, nullptr);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return SG_OK;
+}
+
+int32_t sg_tally_size(sg_handle h, int32_t admin, int64_t* n) {
+  if (!h || !n || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  *n = h->admins[admin].N;
+  return SG_OK;
+}
+
+int32_t sg_get_bins(sg_handle h, int32_t admin, double* bins, int64_t n) {
+  if (!h || !bins || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  const Admin& A = h->admins[admin];
+  if (n < A.N) return h->fail(SG_ERR_BAD_ARG, "get_bins: buffer smaller than the tally");
+  if (A.N == 0) return SG_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(bins, h->bin.p + A.off, A.N * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(bins + n, h->csum.p + A.off, A.N * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(bins + 2 * n, h->csum2.p + A.off, A.N * sizeof(double), cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+int32_t sg_get_keff(sg_handle h, int32_t admin, double* k, double* sd) {
+  if (!h || !k || !sd || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  const Admin& A = h->admins[admin];
+  long long addr = A.keffImplicit >= 0 ? A.keffImplicit + 4 : (A.keffAnalog >= 0 ? A.keffAnalog + 2 : -1);
+  if (addr < 0) return h->fail(SG_ERR_BAD_ARG, "admin has no k clerk");
+  double cs[2];
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&cs[0], h->csum.p + A.off + addr, sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&cs[1], h->csum2.p + A.off + addr, sizeof(double), cudaMemcpyDeviceToHost));
+  int N = A.batchN;                                  // scoreMemory%getResult (:537-573)
+  double mean = cs[0] / N;
+  double inv_N = 1.0 / N;
+  double inv_Nm1 = (N != 1) ? 1.0 / (N - 1) : 1.0;
+  double var = cs[1] * inv_N * inv_Nm1 - mean * mean * inv_Nm1;
+  *k = mean;
+  *sd = std::sqrt(var);
+  return SG_OK;
+}
+
+int32_t sg_eigen_init(sg_handle h, int32_t pop, uint64_t master_state, double k0) {
+  if (!h || pop <= 0 || pop > h->cap) return SG_ERR_BAD_ARG;
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
+  h->cur = 0;
+  CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), h->stream));
+  CK(launch_fission_source(h->g64, h->mg64, h->bank[0].view(), pop, master_state, h->bounds, h->maxl,
+                           h->totals.p + 3, h->stream));
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->totals.p + 3, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (e) return h->fail(e, "fission source: no fissile material found");
+  h->pop = pop;
+  h->master = rng_stride(master_state, pop);        // generateInitialState (:363-364)
+  h->k = k0;
+  double kk[2] = {k0, 1.0};                          // k used, and nextCycle%k_eff (dungeon default 1)
+  CK(cudaMemcpyAsync(h->scal.p + 0, &kk[0], sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->scal.p + 4, &kk[1], sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->eigenReady = true;
+  return SG_OK;
+}
+
+int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats* stats) {
+  if (!h || !h->eigenReady) return h ? h->fail(SG_ERR_STATE, "call sg_eigen_init first") : SG_ERR_BAD_ARG;
+  if (admin < 0 || admin >= (int)h->admins.size() || atch < 0 || atch >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  cudaStream_t s = h->stream;
+  DBank A = h->bank[h->cur].view(), B = h->bank[1 - h->cur].view();
+  const int n = h->pop;
+  CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, s));       // popWeight(thisCycle)
+  int rc = cycle_start(h, admin, h->scal.p + 2, 0.0);
+  if (rc) return rc;
+  int S = 0;
+  sg_cycle_stats st{};
+  rc = gen_loop(h, admin, A, n, h->master, h->scal.p + 0, B, h->cap, &S, &st);
+  if (rc) return rc;
+  h->master = rng_stride(h->master, (long long)h->pop + 1);              // :257
+  CK(deterministic_sum(B.wgt, S, h->sumPart.p, h->scal.p + 3, s));       // popWeight(nextCycle)
+  rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, atch, h->scal.p + 1);
+  if (rc) return rc;
+  rc = norm_size(h, B, S, h->pop, h->master, A, n);                      // :269, result in A
+  if (rc) return rc;
+  h->master = rng_stride(h->master, 1);                                  // :275
+  CK(cudaMemcpyAsync(h->scal.p + 0, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->scal.p + 4, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  double sc[5];
+  CK(cudaMemcpyAsync(sc, h->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  double kUsed = h->k;
+  h->k = sc[1];
+  if (stats) {
+    *stats = st;
+    stats->start_weight = sc[2];
+    stats->end_weight = sc[3];
+    stats->k_eff = kUsed;
+    stats->k_new = sc[1];
+  }
+  return SG_OK;
+}
+
+int32_t sg_eigen_state(sg_handle h, uint64_t* master, double* k) {
+  if (!h || !master || !k) return SG_ERR_BAD_ARG;
+  *master = h->master;
+  *k = h->k;
+  return SG_OK;
+}
+
+int32_t sg_eigen_get_bank(sg_handle h, sg_bank* out, int32_t cap, int32_t* pop) {
+  if (!h || !out || !pop) return SG_ERR_BAD_ARG;
+  *pop = h->pop;
+  return d2h_bank(h, h->bank[h->cur].view(), std::min(cap, h->pop), out);
+}
+
+int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* master_state, sg_cycle_stats* stats) {
+  if (!h || !master_state || n <= 0 || n > h->cap) return SG_ERR_BAD_ARG;
+  if (!h->hasSource) return h->fail(SG_ERR_STATE, "no point source set");
+  if (h->anyFissile) return h->fail(SG_ERR_BAD_ARG, "fixed-source runs with fissile materials are not supported");
+  cudaStream_t s = h->stream;
+  DBank A = h->bank[0].view(), B = h->bank[1].view();
+  PointSourceArgs a = h->psrc;                                           // fixedSource%generate
+  a.out = A;
+  a.n = n;
+  a.master = *master_state;
+  CK(launch_point_source(a, s));
+  unsigned long long m = rng_stride(*master_state, n);                   // :189
+  int rc = cycle_start(h, admin, nullptr, (double)n);
+  if (rc) return rc;
+  const double one = 1.0;
+  CK(cudaMemcpyAsync(h->scal.p + 0, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(h->scal.p + 4, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+  int S = 0;
+  sg_cycle_stats st{};
+  rc = gen_loop(h, admin, A, n, m, h->scal.p + 0, B, h->cap, &S, &st);
+  if (rc) return rc;
+  m = rng_stride(m, n);                                                  // :264
+  const double wn = (double)n;
+  CK(cudaMemcpyAsync(h->scal.p + 3, &wn, sizeof(double), cudaMemcpyHostToDevice, s));
+  rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, -1, nullptr);   // :267
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s));
+  h->eigenReady = false;
+  *master_state = m;
+  if (stats) {
+    *stats = st;
+    stats->start_weight = n;
+    stats->end_weight = n;
+    stats->k_eff = 1.0;
+    stats->k_new = 1.0;
+  }
+  return SG_OK;
+}
+
+int32_t sg_get_history_records(sg_handle h, int32_t* collisions, uint64_t* rng_end, int32_t n) {
+  if (!h || !h->cfg.record_histories) return h ? h->fail(SG_ERR_STATE, "record_histories is off") : SG_ERR_BAD_ARG;
+  int m = std::min(n, h->lastN);
+  if (m <= 0) return SG_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  if (collisions) CK(cudaMemcpy(collisions, h->recColl.p, sizeof(int) * m, cudaMemcpyDeviceToHost));
+  if (rng_end) CK(cudaMemcpy(rng_end, h->recRng.p, sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+int32_t sg_rng_draws(uint64_t* state, double* out, int32_t n) {
+  if (!state || (!out && n > 0)) return SG_ERR_BAD_ARG;
+  uint64_t s = *state;
+  for (int i = 0; i < n; ++i) {
+    s = (2806196910506780709ULL * s) & 0x7FFFFFFFFFFFFFFFULL;
+    s = (s + 1ULL) & 0x7FFFFFFFFFFFFFFFULL;
+    out[i] = (double)(int64_t)s * 0x1p-63;
+  }
+  *state = s;
+  return SG_OK;
+}
+
+uint64_t sg_rng_skip(uint64_t state, int64_t k) { return lcg_skip(state, k); }
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// sg_internal.h -- device data records shared by the kernels and the host side of libsconegpu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/scone_gpu.h"
+
+namespace sg {
+
+// One surface: 64-bit params as uploaded (plane coefficients normalised), tolerance of the
+// precision form the record was built for, boundary conditions (border surface only).
+struct DSurf {
+  int type;
+  int axis;        // aPlane axis / cylinder axis
+  int pl0, pl1;    // in-plane axes of cylinders and square cylinders
+  int bc[6];
+  int pad[2];
+  double p[SG_SURF_NPAR];
+  double tol;
+};
+
+// One universe.  i[] / d[] by type:
+//   ROOT: i0 border surface
+//   CELL: i0 first entry in uni_cells, i1 number of cells
+//   PIN : i0 first annulus in pin_rsq/pin_tol, i1 number of annuli (last one has radius 1.1*INF)
+//   LAT : i0..i2 sizeN, i3 outLocalID, i4 outline surface, i5 offset flag;
+//         d0..2 pitch, d3..5 corner, d6..8 a_bar (half pitch reduced by the surface tolerance)
+struct DUni {
+  int type;
+  int i[7];
+  double origin[3];
+  double d[9];
+};
+
+struct DGeom {
+  const DSurf* surfs;
+  const DUni* unis;
+  const int* uni_cells;
+  const int* cell_ptr;
+  const int* cell_surf;
+  const double* pin_rsq;
+  const double* pin_tol;
+  const int2* graph;    // geomGraph: x = matIdx (>= 0) or -(uniIdx), y = uniqueID or uniRootID (1-based)
+  int root;             // root universe (0-based)
+  int border;           // border surface (0-based)
+  double nudge;         // cellUniverse crossing nudge of the precision form
+};
+
+// MG macroscopic data in the working precision R ([mat][G], P0/prod [mat][Gin][Gout])
+template <class R>
+struct DMG {
+  int nMat, nG;
+  const R* total;
+  const R* scatter;
+  const R* capture;
+  const R* fission;
+  const R* nuFission;
+  const R* chi;
+  const R* P0;
+  const R* prod;
+  const int* fissile;
+  const R* majorant;
+  R collisionXS;
+};
+
+// One tally clerk as the kernels see it (all admins of a launch flattened; acc offsets global).
+struct DClerk {
+  int type;
+  int handle_virtual;
+  int width;
+  int resp[4];
+  int n_axes;
+  int ax_kind[3];
+  int ax_n[3];
+  int g_top, g_low;
+  int pad;
+  double ax_min[3];
+  double ax_step[3];
+  double ax_inv_step[3];
+  long long multi[3];
+  long long acc_off;     // offset (0-based) of this clerk's first bin in the launch's acc array
+};
+
+static constexpr int MAX_CLERKS = 8;
+
+// SoA particle bank in device memory
+struct DBank {
+  double* r;       // [n][3]
+  double* dir;     // [n][3]
+  double* wgt;
+  int* G;
+  int* brood;
+  double* time;
+};
+
+// Fission sites produced by one gen loop before they are ordered by brood ID.  The buffer is split
+// into NREG regions, each filled through its own atomic cursor, so the append rate is not limited
+// by one contended counter.
+static constexpr int SITE_REGIONS = 64;
+struct DSites {
+  double* r;
+  double* dir;
+  double* wgt;
+  int* G;
+  int* brood;
+  int* seq;
+  double* time;
+  int* cursor;          // [SITE_REGIONS]
+  int region_cap;
+};
+
+// Per-launch counters written by the transport kernel
+struct DCounters {
+  unsigned long long events;
+  unsigned long long collisions;
+  int work;             // next history to hand out
+  int err_code;         // first error (SG_ERR_*), 0 if none
+  int err_hist;         // history that raised it
+  int pad;
+};
+
+template <class R>
+struct TransportArgs {
+  DGeom geom;
+  DMG<R> mg;
+  DBank in;
+  int n;
+  unsigned long long master;
+  const double* k_eff;
+  DClerk clerks[MAX_CLERKS];
+  int n_clerks;
+  int keff_clerk;       // index of the keff-implicit clerk (accumulated in registers), -1 if none
+  double* acc;          // tally accumulators of the launch (global)
+  int acc_n;
+  int use_smem;         // accumulate map clerks in shared memory
+  DSites sites;
+  int* hist_nsites;     // [n] sites per history (0 when no fission)
+  int* rec_coll;        // [n] or null
+  unsigned long long* rec_rng;  // [n] or null
+  DCounters* ctr;
+  int use_cache;        // transportOperatorST cache flag
+  int max_segments;     // safety limit per history
+};
+
+}  // namespace sg

@@ -1,0 +1,20 @@
+// sg_launch.h -- host-callable launch wrappers of the kernels (one definition per translation unit).
+#pragma once
+#include "sg_internal.h"
+
+namespace sg {
+
+// persistent history-loop kernel; maxl is the compile-time nesting bound (2 or 4)
+template <class R>
+cudaError_t launch_transport(const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
+                             cudaStream_t s, int* grid_out);
+// occupancy-derived persistent grid size for a kernel configuration
+template <class R>
+int transport_grid(int maxl, bool dt, size_t smem);
+
+// fissionSource sampling on the device (fissionSource_class.f90:149-271), FP64 arithmetic
+cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank out, int n,
+                                  unsigned long long master, const double* bounds6, int maxl,
+                                  int* err, cudaStream_t s);
+
+}  // namespace sg

@@ -1,0 +1,396 @@
+// sg_transport.cuh -- the history loop kernel: the `gen:` loop of SCONE's physics packages with
+// transportOperatorST/DT, neutronMGstd collisions and tally reports fused into one persistent kernel.
+//
+// Execution model: a persistent grid (a multiple of the SM count); each thread carries one particle
+// history at a time and takes the next one as soon as its history ends, so a warp stays full until
+// the bank runs dry.  Warps take histories from a global counter in chunks of 32 (one atomic per
+// chunk).  Each loop iteration advances every live lane by one flight segment, so lanes diverge
+// only inside collision processing.  Map-based tallies are accumulated in a shared-memory copy of
+// the launch's score memory (SCONE's per-thread parallelBins, scoreMemory_class.f90:215-233,
+// become per-block bins) and flushed with FP64 atomics at the end; the k-implicit estimator is
+// accumulated in registers.
+#pragma once
+#include "sg_device.cuh"
+
+namespace sg {
+
+static constexpr unsigned FULL = 0xffffffffu;
+
+// fates (tallyCodes.f90:23-27)
+enum { FATE_NONE = 5000, FATE_ABS = 5001, FATE_LEAK = 5002 };
+// macro MTs (endfConstants.f90:116-130)
+enum { MT_TOTAL = -1, MT_DISAP = -2, MT_ESCATTER = -3, MT_IESCATTER = -4, MT_FISSION = -6,
+       MT_NUFISSION = -7, MT_ALLSCATTER = -20, MT_ABSORPTION = -21, MT_NONELASTIC = -22 };
+
+__device__ __forceinline__ void raise_error(DCounters* ctr, int code, int hist) {
+  if (atomicCAS(&ctr->err_code, 0, code) == 0) ctr->err_hist = hist;
+}
+
+template <class R, int MAXL, bool DT>
+struct Tracker {
+  const TransportArgs<R>& A;
+  const Geom<R, MAXL> geom;
+  const DMG<R>& mg;
+  double* acc;
+  R k_eff;
+
+  // particle state
+  Coords<R, MAXL> c;
+  R cdist[MAXL];
+  int csurf[MAXL];
+  DistCache cache;
+  Rng<R> rng;
+  R w, w0;
+  int G;
+  int collN;
+  int hist;
+  int nsites;
+  double time;
+  int segs;
+  // k-implicit accumulators (keffImplicitClerk bins IMP_PROD, SCATTER_PROD, IMP_ABS, ANA_LEAK)
+  double kprod, kscat, kabs, kleak;
+  unsigned long long nEv, nColl;
+
+  __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
+      : A(a), geom(a.geom), mg(a.mg), acc(accp) {
+    k_eff = (R)(*a.k_eff);
+    kprod = kscat = kabs = kleak = 0.0;
+    nEv = nColl = 0;
+  }
+
+  __device__ __forceinline__ R xs(const R* t, int mat, int g) const { return t[(mat - 1) * mg.nG + (g - 1)]; }
+
+  // neutronMacroXSs%get for the MG material (neutronXsPackages_class.f90:143-190)
+  __device__ __forceinline__ R macro(int mat, int g, int MT) const {
+    if (mat <= 0 || mat == SG_VOID_MAT) return R(0);
+    int k = (mat - 1) * mg.nG + (g - 1);
+    bool f = mg.fissile[mat - 1] != 0;
+    switch (MT) {
+      case MT_TOTAL: return mg.total[k];
+      case MT_DISAP: return mg.capture[k];
+      case MT_ESCATTER: return R(0);
+      case MT_NONELASTIC: return mg.scatter[k] + (f ? mg.fission[k] : R(0)) + mg.capture[k];
+      case MT_IESCATTER: return mg.scatter[k];
+      case MT_ALLSCATTER: return R(0) + mg.scatter[k];
+      case MT_FISSION: return f ? mg.fission[k] : R(0);
+      case MT_NUFISSION: return f ? mg.nuFission[k] : R(0);
+      case MT_ABSORPTION: return mg.capture[k] + (f ? mg.fission[k] : R(0));
+      default: return R(0);
+    }
+  }
+  __device__ __forceinline__ R response(int code, int mat, int g) const {
+    return code == SG_RESP_FLUX ? R(1) : macro(mat, g, code);
+  }
+
+  // multiMap of spaceMap / group / material axes (multiMap_class.f90:153-173, grid_class.f90:225-245)
+  __device__ __forceinline__ int map_bin(const DClerk& K, const double r[3], int g, int mat) const {
+    long long idx = 1;
+    for (int a = 0; a < K.n_axes; ++a) {
+      int b = 0;
+      int kind = K.ax_kind[a];
+      if (kind <= SG_AXIS_Z) {
+        double v = at3(r, kind - 1);
+        if constexpr (sizeof(R) == 8) b = (int)floor((v - K.ax_min[a]) / K.ax_step[a]) + 1;
+        else b = (int)floorf((float)(v - K.ax_min[a]) * (float)K.ax_inv_step[a]) + 1;
+        if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
+      } else if (kind == SG_AXIS_GROUP) {
+        b = (g >= 1 && g <= K.ax_n[a]) ? g : 0;
+      } else {
+        b = (mat >= 1 && mat <= K.ax_n[a]) ? mat : 0;
+      }
+      if (b == 0) return 0;
+      idx += (long long)(b - 1) * K.multi[a];
+    }
+    return (int)idx;
+  }
+
+  __device__ __forceinline__ void score(long long at, double v) { atomicAdd(acc + at, v); }
+
+  // tallyAdmin%reportInColl -> collisionClerk (collisionClerk_class.f90:192-242) and
+  // keffImplicitClerk (keffImplicitClerk_class.f90:180-227)
+  __device__ __forceinline__ void report_in_coll(bool virt, R trackXS) {
+    for (int k = 0; k < A.n_clerks; ++k) {
+      const DClerk& K = A.clerks[k];
+      if (K.type == SG_CLERK_COLLISION) {
+        if (!K.handle_virtual && virt) continue;
+        if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
+        int bin = map_bin(K, c.r[0], G, c.mat);
+        if (bin == 0) continue;
+        R flux = K.handle_virtual ? w / trackXS : w / xs(mg.total, c.mat, G);
+        long long at = K.acc_off + (long long)K.width * (bin - 1);
+        for (int i = 0; i < K.width; ++i) score(at + i, (double)(response(K.resp[i], c.mat, G) * flux));
+      } else if (K.type == SG_CLERK_KEFF_IMPLICIT) {
+        if (c.mat == SG_VOID_MAT) continue;
+        R flux = w / trackXS;
+        bool f = mg.fissile[c.mat - 1] != 0;
+        R nuF = f ? xs(mg.nuFission, c.mat, G) : R(0);
+        R absXS = xs(mg.capture, c.mat, G) + (f ? xs(mg.fission, c.mat, G) : R(0));
+        kprod += (double)(nuF * flux);
+        kabs += (double)(absXS * flux);
+      }
+    }
+  }
+  // trackClerk%reportPath (trackClerk_class.f90:185-232): pre-path position and material
+  __device__ __forceinline__ void report_path(const double rpre[3], int matPre, R L) {
+    for (int k = 0; k < A.n_clerks; ++k) {
+      const DClerk& K = A.clerks[k];
+      if (K.type != SG_CLERK_TRACK) continue;
+      if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
+      int bin = map_bin(K, rpre, G, matPre);
+      if (bin == 0) continue;
+      long long at = K.acc_off + (long long)K.width * (bin - 1);
+      for (int i = 0; i < K.width; ++i) score(at + i, (double)(response(K.resp[i], matPre, G) * w * L));
+    }
+  }
+
+  __device__ __forceinline__ void write_site(const R dir[3], int gout, R wgt) {
+    int region = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (SITE_REGIONS - 1);
+    int slot = atomicAdd(&A.sites.cursor[region], 1);
+    if (slot >= A.sites.region_cap) { raise_error(A.ctr, SG_ERR_BANK_OVERFLOW, hist); return; }
+    long long i = (long long)region * A.sites.region_cap + slot;
+    A.sites.r[3 * i + 0] = c.r[0][0];
+    A.sites.r[3 * i + 1] = c.r[0][1];
+    A.sites.r[3 * i + 2] = c.r[0][2];
+    A.sites.dir[3 * i + 0] = (double)dir[0];
+    A.sites.dir[3 * i + 1] = (double)dir[1];
+    A.sites.dir[3 * i + 2] = (double)dir[2];
+    A.sites.wgt[i] = (double)wgt;
+    A.sites.G[i] = gout;
+    A.sites.brood[i] = hist;
+    A.sites.seq[i] = nsites;
+    A.sites.time[i] = time;
+    nsites += 1;
+  }
+
+  // collisionProcessor%collide with neutronMGstd (collisionProcessor_inter.f90:114-195,
+  // neutronMGstd_class.f90:85-297).  Returns true if the particle died.
+  __device__ __forceinline__ bool collide(R trackXS) {
+    const int mat = c.mat;
+    (void)rng.get();                                     // alpha test, drawn even for alpha = 0
+    const int k = (mat - 1) * mg.nG + (G - 1);
+    const bool fiss = mg.fissile[mat - 1] != 0;
+    const R total = mg.total[k], inel = mg.scatter[k], capture = mg.capture[k];
+    const R rr = rng.get();
+    int C = 1;                                           // neutronMacroXSs%invert (:211-250)
+    R x = total * rr - R(0);
+    if (x > R(0)) C = C + 1;
+    x = x - inel;
+    if (x > R(0)) C = C + 1;
+    x = x - capture;
+    if (x > R(0)) C = C + 1;
+    report_in_coll(false, trackXS);
+    const R preCollW = w;
+    if (fiss) {                                          // implicit (:134-201)
+      R rand1 = rng.get();
+      R nuF = mg.nuFission[k];
+      int n = (int)(fabs((w * nuF) / (w0 * total * k_eff)) + rand1);
+      if (n >= 1) {
+        R sw = sgn(w0, w);
+        for (int s = 0; s < n; ++s) {                    // fissionMG%sampleOut (:183-206)
+          R mu = R(2) * rng.get() - R(1);
+          R sp, cp;
+          sincos_phi<R>(rng.get(), sp, cp);
+          R rem = rng.get();
+          int go = 1;
+          for (go = 1; go <= mg.nG; ++go) {
+            rem = rem - mg.chi[(mat - 1) * mg.nG + (go - 1)];
+            if (rem < R(0)) break;
+          }
+          if (go > mg.nG) { raise_error(A.ctr, SG_ERR_NAN, hist); go = mg.nG; }
+          R d[3] = {c.u[0], c.u[1], c.u[2]};
+          rotate_vector<R>(d[0], d[1], d[2], mu, sp, cp);
+          write_site(d, go, sw);
+        }
+      }
+    }
+    bool dead;
+    int MT;
+    if (C <= 2) {                                        // inelastic (:221-252), multiScatterMG%sampleOut
+      R rem = rng.get() * inel;
+      const R* row = mg.P0 + (long long)k * mg.nG;
+      int go;
+      for (go = 1; go <= mg.nG; ++go) {
+        rem = rem - row[go - 1];
+        if (rem < R(0)) break;
+      }
+      if (go > mg.nG) { raise_error(A.ctr, SG_ERR_NAN, hist); go = mg.nG; }
+      R mu = R(2) * rng.get() - R(1);
+      R sp, cp;
+      sincos_phi<R>(rng.get(), sp, cp);
+      R w_mul = mg.prod[(long long)k * mg.nG + (go - 1)];
+      G = go;
+      w = w * w_mul;
+      rotate_vector<R>(c.u[0], c.u[1], c.u[2], mu, sp, cp);
+      MT = MT_IESCATTER;
+      dead = false;
+    } else {                                             // capture / fission
+      MT = (C == 3) ? MT_DISAP : MT_FISSION;
+      dead = true;
+    }
+    collN += 1;
+    nColl += 1;
+    if (A.keff_clerk >= 0 && MT == MT_IESCATTER) {       // keffImplicit reportOutColl (:241-268)
+      R sc = fmax(w - preCollW, R(0));
+      if (sc > R(0)) kscat += (double)sc;
+    }
+    return dead;
+  }
+
+  __device__ __forceinline__ void start(int h) {
+    hist = h;
+    const int i = h - 1;
+    c.r[0][0] = A.in.r[3 * i + 0];
+    c.r[0][1] = A.in.r[3 * i + 1];
+    c.r[0][2] = A.in.r[3 * i + 2];
+    c.u[0] = (R)A.in.dir[3 * i + 0];
+    c.u[1] = (R)A.in.dir[3 * i + 1];
+    c.u[2] = (R)A.in.dir[3 * i + 2];
+    w = (R)A.in.wgt[i];
+    w0 = w;
+    G = A.in.G[i];
+    time = A.in.time ? A.in.time[i] : 0.0;
+    rng.s = lcg_skip(A.master, RNG_STRIDE * (long long)h);
+    collN = 0;
+    nsites = 0;
+    segs = 0;
+    cache.lvl = 0;
+    if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
+  }
+
+  __device__ __forceinline__ void finish() {
+    if (A.hist_nsites) A.hist_nsites[hist - 1] = nsites;
+    if (A.rec_coll) A.rec_coll[hist - 1] = collN;
+    if (A.rec_rng) A.rec_rng[hist - 1] = rng.s;
+  }
+
+  // One flight segment (and the collision that may end it).  Returns true when the history ended.
+  __device__ __forceinline__ bool step() {
+    const R INF_R = R(D_INF);
+    if (++segs > A.max_segments) { raise_error(A.ctr, SG_ERR_LOST, hist); return true; }
+    int mat = c.mat;
+    if constexpr (!DT) {
+      // surfaceTracking (transportOperatorST_class.f90:48-166)
+      const bool isVoid = (mat == SG_VOID_MAT);
+      const R sigTot = isVoid ? R(0) : xs(mg.total, mat, G);
+      const R sigmaTrack = isVoid ? mg.collisionXS : fmax(sigTot, mg.collisionXS);
+      R dist, invSig, sigT;
+      if (sigmaTrack < Tol<R>::st_void()) { dist = INF_R; invSig = INF_R; sigT = R(0); }
+      else { invSig = R(1) / sigmaTrack; dist = -dlog<R>(rng.get()) * invSig; sigT = sigTot; }
+      const double rpre[3] = {c.r[0][0], c.r[0][1], c.r[0][2]};
+      const int matPre = mat;
+      const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0);
+      time = time + (double)dist;
+      nEv += 1;
+      report_path(rpre, matPre, dist);
+      mat = c.mat;
+      if (mat == 0) { leak(); return true; }
+      if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
+        raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
+        return true;
+      }
+      if (ev == 1) {
+        if (rng.get() < sigT * invSig) {
+          cache.lvl = 0;
+          return collide(sigmaTrack) ? (absorbed(), true) : false;
+        }
+        report_in_coll(true, sigmaTrack);
+      }
+      return false;
+    } else {
+      // deltaTracking (transportOperatorDT_class.f90:47-131)
+      const R maj = fmax(mg.majorant[G - 1], mg.collisionXS);
+      const R majInv = R(1) / maj;
+      const R dist = -dlog<R>(rng.get()) * majInv;
+      if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return true; }
+      time = time + (double)dist;
+      nEv += 1;
+      mat = c.mat;
+      if (mat == 0) { leak(); return true; }
+      if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return false; }
+      if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
+        raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
+        return true;
+      }
+      const R sigT = xs(mg.total, mat, G);
+      if (rng.get() < sigT * majInv) return collide(maj) ? (absorbed(), true) : false;
+      report_in_coll(true, maj);
+      return false;
+    }
+  }
+
+  // reportHist for a leaked particle (keffImplicitClerk ANA_LEAK, :276-290)
+  __device__ __forceinline__ void leak() { if (A.keff_clerk >= 0) kleak += (double)w; }
+  __device__ __forceinline__ void absorbed() {}
+};
+
+template <class R, int MAXL, bool DT>
+__global__ void __launch_bounds__(128) k_transport(const __grid_constant__ TransportArgs<R> A) {
+  extern __shared__ double s_acc[];
+  const bool smem = A.use_smem != 0;
+  if (smem) {
+    for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) s_acc[i] = 0.0;
+    __syncthreads();
+  }
+  Tracker<R, MAXL, DT> T(A, smem ? s_acc : A.acc);
+  const int lane = threadIdx.x & 31;
+  bool alive = false, done = false;
+  int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
+
+  while (true) {
+    unsigned need = __ballot_sync(FULL, !alive && !done);
+    while (need) {
+      if (q_next >= q_end) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&A.ctr->work, 32);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= A.n) {
+          if (!alive) done = true;
+          break;
+        }
+        q_next = base;
+        q_end = min(base + 32, A.n);
+      }
+      const int avail = q_end - q_next;
+      const int rank = __popc(need & ((1u << lane) - 1u));
+      const bool mine = ((need >> lane) & 1u) && rank < avail;
+      if (mine) { T.start(q_next + rank + 1); alive = true; }
+      q_next += min(__popc(need), avail);
+      need &= ~__ballot_sync(FULL, mine);
+    }
+    if (__all_sync(FULL, !alive)) break;
+    if (alive) {
+      if (T.step()) { T.finish(); alive = false; }
+    }
+  }
+
+  // flush: keff registers (warp reduce) and the block's score memory
+  if (A.keff_clerk >= 0) {
+    double v[4] = {T.kprod, T.kscat, T.kabs, T.kleak};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(FULL, v[q], o);
+    if (lane == 0) {
+      long long off = A.clerks[A.keff_clerk].acc_off;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (v[q] != 0.0) atomicAdd(A.acc + off + q, v[q]);
+    }
+  }
+  unsigned long long ev = T.nEv, co = T.nColl;
+  for (int o = 16; o > 0; o >>= 1) {
+    ev += __shfl_down_sync(FULL, ev, o);
+    co += __shfl_down_sync(FULL, co, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&A.ctr->events, ev);
+    atomicAdd(&A.ctr->collisions, co);
+  }
+  if (smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) {
+      double v = s_acc[i];
+      if (v != 0.0) atomicAdd(A.acc + i, v);
+    }
+  }
+}
+
+}  // namespace sg

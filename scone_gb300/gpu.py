@@ -1,0 +1,202 @@
+"""Python face of libsconegpu (ctypes over the C ABI in include/scone_gpu.h).
+
+`TransportOperatorGPU` plays the role of SCONE's transportOperator + collisionOperator for a whole
+particle bank: it owns the resident geometry (geometryStd), MG nuclear data (baseMgNeutronDatabase)
+and tally admins (tallyAdmin / tallyClerk / scoreMemory) on the GPU.  There is no CPU fallback:
+constructing it without the compiled library or without a CUDA device raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+
+
+def library_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libsconegpu.so")
+
+
+def load(build=True):
+    """Load (building first if needed) libsconegpu.so; raises if it cannot be loaded."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if build:
+        from . import build as _b
+        _b.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libsconegpu.so is missing at {path}; run scone_gb300.build.build()")
+    L = C.CDLL(path)
+    vp, i32, i64, u64, f64, P = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.POINTER
+    sig = {
+        "sg_create": (i32, [P(abi.Config), P(vp)]), "sg_destroy": (i32, [vp]),
+        "sg_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "sg_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
+        "sg_upload_mg": (i32, [vp, P(abi.MGDesc)]),
+        "sg_upload_tally": (i32, [vp, P(abi.TallyDesc), P(i32)]),
+        "sg_attach_tally": (i32, [vp, i32, i32]),
+        "sg_set_point_source": (i32, [vp, P(abi.PointSourceDesc)]),
+        "sg_generate_source": (i32, [vp, u64, i32, P(abi.Bank)]),
+        "sg_transport_bank": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(abi.CycleStats)]),
+        "sg_tally_cycle_start": (i32, [vp, i32, f64]), "sg_tally_cycle_end": (i32, [vp, i32, f64, f64]),
+        "sg_tally_size": (i32, [vp, i32, P(i64)]), "sg_get_bins": (i32, [vp, i32, P(f64), i64]),
+        "sg_get_keff": (i32, [vp, i32, P(f64), P(f64)]),
+        "sg_eigen_init": (i32, [vp, i32, u64, f64]), "sg_eigen_cycle": (i32, [vp, i32, i32, P(abi.CycleStats)]),
+        "sg_eigen_state": (i32, [vp, P(u64), P(f64)]), "sg_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
+        "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
+        "sg_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
+        "sg_rng_draws": (i32, [P(u64), P(f64), i32]), "sg_rng_skip": (u64, [u64, i64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = res, args
+    _LIB = L
+    return L
+
+
+class SconeGpuError(RuntimeError):
+    pass
+
+
+class TransportOperatorGPU:
+    """A GPU transport operator for whole banks (the `gen:` loop of SCONE's physics packages)."""
+
+    def __init__(self, problem=None, precision=abi.PREC_FP64, transport=abi.TRANSPORT_ST, max_bank=1 << 20,
+                 device=0, record_histories=False):
+        self.L = load()
+        self.h = C.c_void_p()
+        self._keep = []
+        cfg = abi.Config(precision, transport, device, max_bank, 1 if record_histories else 0)
+        rc = self.L.sg_create(C.byref(cfg), C.byref(self.h))
+        if rc != 0:
+            raise SconeGpuError(f"sg_create failed with {rc} (is a CUDA device present?)")
+        self.max_bank = max_bank
+        if problem is not None:
+            self.upload_geometry(problem.geometry)
+            if problem.mg is not None:
+                self.upload_mg(problem.mg)
+            if problem.source:
+                self.set_point_source(**problem.source)
+
+    def _check(self, rc):
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            self.L.sg_last_error(self.h, buf, 512)
+            raise SconeGpuError(f"libsconegpu error {rc}: {buf.value.decode()}")
+        return rc
+
+    def close(self):
+        if self.h:
+            self.L.sg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_geometry(self, g):
+        s, keep = abi.geometry_struct(g)
+        self._keep.append(keep)
+        self._check(self.L.sg_upload_geometry(self.h, C.byref(s)))
+
+    def upload_mg(self, m):
+        s, keep = abi.mg_struct(m)
+        self._keep.append(keep)
+        self._check(self.L.sg_upload_mg(self.h, C.byref(s)))
+
+    def upload_tally(self, clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
+        t, arr = abi.tally_struct(clerks, batch_size, norm_clerk, norm_val)
+        self._keep.append(arr)
+        a = C.c_int32()
+        self._check(self.L.sg_upload_tally(self.h, C.byref(t), C.byref(a)))
+        return a.value
+
+    def attach_tally(self, admin, atch):
+        self._check(self.L.sg_attach_tally(self.h, admin, atch))
+
+    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
+        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g)
+        self._keep.append((s, keep))
+        self._check(self.L.sg_set_point_source(self.h, C.byref(s)))
+
+    def generate_source(self, master, n):
+        b = abi.HostBank(n)
+        self._check(self.L.sg_generate_source(self.h, C.c_uint64(master), n, C.byref(b.struct)))
+        return b
+
+    def transport_bank(self, admin, bank, master, k_eff=1.0, next_cap=None):
+        n = bank.n
+        cap = next_cap if next_cap is not None else max(4 * n, 16)
+        nxt = abi.HostBank(cap)
+        st = abi.CycleStats()
+        self._check(self.L.sg_transport_bank(self.h, admin, C.byref(bank.struct), n, C.c_uint64(master), k_eff,
+                                             C.byref(nxt.struct), cap, C.byref(st)))
+        return nxt, st
+
+    def tally_cycle_start(self, admin, w):
+        self._check(self.L.sg_tally_cycle_start(self.h, admin, w))
+
+    def tally_cycle_end(self, admin, w, k=1.0):
+        self._check(self.L.sg_tally_cycle_end(self.h, admin, w, k))
+
+    def bins(self, admin):
+        n = C.c_int64()
+        self._check(self.L.sg_tally_size(self.h, admin, C.byref(n)))
+        out = np.zeros(3 * max(n.value, 1))
+        self._check(self.L.sg_get_bins(self.h, admin, out.ctypes.data_as(C.POINTER(C.c_double)), n.value))
+        return out[:3 * n.value].reshape(3, n.value).T.copy()
+
+    def keff(self, admin):
+        k, s = C.c_double(), C.c_double()
+        self._check(self.L.sg_get_keff(self.h, admin, C.byref(k), C.byref(s)))
+        return k.value, s.value
+
+    def history_records(self, n):
+        c = np.zeros(n, np.int32)
+        r = np.zeros(n, np.uint64)
+        self._check(self.L.sg_get_history_records(self.h, c.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  r.ctypes.data_as(C.POINTER(C.c_uint64)), n))
+        return c, r
+
+    def eigen_init(self, pop, master, k0=1.0):
+        self._check(self.L.sg_eigen_init(self.h, pop, C.c_uint64(master), k0))
+
+    def eigen_cycle(self, admin, atch):
+        st = abi.CycleStats()
+        self._check(self.L.sg_eigen_cycle(self.h, admin, atch, C.byref(st)))
+        return st
+
+    def eigen_state(self):
+        m, k = C.c_uint64(), C.c_double()
+        self._check(self.L.sg_eigen_state(self.h, C.byref(m), C.byref(k)))
+        return m.value, k.value
+
+    def eigen_bank(self, cap):
+        b = abi.HostBank(cap)
+        pop = C.c_int32()
+        self._check(self.L.sg_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
+        return b, pop.value
+
+    def fixed_source_cycle(self, admin, n, master):
+        m = C.c_uint64(master)
+        st = abi.CycleStats()
+        self._check(self.L.sg_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        return m.value, st
+
+
+def rng_draws(state, n):
+    L = load()
+    s = C.c_uint64(state)
+    out = np.zeros(n)
+    L.sg_rng_draws(C.byref(s), out.ctypes.data_as(C.POINTER(C.c_double)), n)
+    return out, s.value
+
+
+def rng_skip(state, k):
+    return load().sg_rng_skip(C.c_uint64(state), C.c_int64(k))

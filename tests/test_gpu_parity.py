@@ -1,0 +1,149 @@
+"""GPU parity: libsconegpu against the CPU oracle (a restatement of SCONE's algorithm).
+
+All-FP64 form: bit-level agreement per history (number of real collisions and the RNG state at the
+end of every history, i.e. every draw in SCONE's order), identical fission banks, and tallies equal
+to round-off (scores are summed in a different order: relative tolerance 1e-10).
+Mixed form: statistical agreement with the FP64 form (k within 4 sigma, flux z-scores).
+"""
+import numpy as np
+import pytest
+
+from scone_gb300 import abi, problems
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5C3A84C9
+
+
+@pytest.fixture(scope="module")
+def gpu_mod():
+    from scone_gb300 import gpu
+    gpu.load()
+    return gpu
+
+
+def make_pair(gpu, orl, prob, transport=abi.TRANSPORT_ST, precision=abi.PREC_FP64, max_bank=1 << 18):
+    g = gpu.TransportOperatorGPU(prob, precision=precision, transport=transport, max_bank=max_bank,
+                                 record_histories=True)
+    o = orl.Oracle(prob, transport=transport)
+    return g, o
+
+
+def test_point_source_bank_bitexact(gpu_mod, oracle_mod):
+    p = problems.infinite_medium_2g()
+    g, o = make_pair(gpu_mod, oracle_mod, p)
+    bg = g.generate_source(SEED, 5000)
+    bo = o.generate_source(SEED, 5000)
+    for k in ("r", "dir", "G", "wgt"):
+        assert np.array_equal(bg[k], bo[k]), k
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
+def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport):
+    p = problems.infinite_medium_2g()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport)
+    n = 20000
+    bank = o.generate_source(SEED, n)
+    ag = g.upload_tally(p.tallies["flux"])
+    ao = o.upload_tally(p.tallies["flux"])
+    master = 987654321
+    _, sg = g.transport_bank(ag, bank, master)
+    _, so = o.transport_bank(ao, bank, master)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(rg, ro)
+    assert sg.n_events == so.n_events and sg.n_collisions == so.n_collisions
+    for t in (g, o):
+        t.tally_cycle_end(ag if t is g else ao, float(n))
+    bg, bo = g.bins(ag), o.bins(ao)
+    np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_lattice_fp64_bank_parity(gpu_mod, oracle_mod, transport):
+    p = problems.lattice_17x17_7g()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport)
+    n = 4000
+    o.eigen_init(n, SEED)
+    bank, pop = o.eigen_bank(n)
+    assert pop == n
+    ag = g.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+    ao = o.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+    master = 1122334455
+    ng, sg = g.transport_bank(ag, bank, master, k_eff=1.05)
+    no, so = o.transport_bank(ao, bank, master, k_eff=1.05)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(rg, ro)
+    assert sg.n_next == so.n_next > 0
+    m = so.n_next
+    for k in ("r", "dir", "G", "wgt", "brood_id"):
+        assert np.array_equal(ng[k][:m], no[k][:m]), k
+    g.tally_cycle_end(ag, float(m), 1.05)
+    o.tally_cycle_end(ao, float(m), 1.05)
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=1e-300)
+
+
+def _eigen(t, p, pop, n_in, n_act):
+    inact = t.upload_tally([])
+    act = t.upload_tally(p.tallies["mesh"])
+    ia = t.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+    aa = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+    t.attach_tally(inact, ia)
+    t.attach_tally(act, aa)
+    t.eigen_init(pop, SEED)
+    ks = []
+    for _ in range(n_in):
+        ks.append(t.eigen_cycle(inact, ia).k_new)
+    for _ in range(n_act):
+        ks.append(t.eigen_cycle(act, aa).k_new)
+    return np.array(ks), t.keff(aa), t.bins(act)
+
+
+def test_lattice_eigen_fp64_cycles(gpu_mod, oracle_mod):
+    p = problems.lattice_17x17_7g()
+    g, o = make_pair(gpu_mod, oracle_mod, p)
+    kg, keg, bg = _eigen(g, p, 3000, 3, 3)
+    ko, keo, bo = _eigen(o, p, 3000, 3, 3)
+    np.testing.assert_allclose(kg, ko, rtol=1e-10)
+    mg, _ = g.eigen_state()
+    mo, _ = o.eigen_state()
+    assert mg == mo
+    bgk, _ = g.eigen_bank(3000)
+    bok, _ = o.eigen_bank(3000)
+    np.testing.assert_allclose(bgk["r"], bok["r"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(bg, bo, rtol=1e-8, atol=1e-300)
+
+
+def test_lattice_mixed_vs_fp64_statistics(gpu_mod):
+    p = problems.lattice_17x17_7g()
+    res = {}
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, max_bank=1 << 19)
+        ks, (k, sd), bins = _eigen(t, p, 100000, 5, 10)
+        res[prec] = (k, sd, bins)
+    k64, s64, b64 = res[abi.PREC_FP64]
+    k32, s32, b32 = res[abi.PREC_MIXED]
+    assert abs(k64 - k32) < 4.0 * np.hypot(s64, s32), (k64, s64, k32, s32)
+    n = 10
+    m64, m32 = b64[:, 1] / n, b32[:, 1] / n
+    v64 = (b64[:, 2] / n - m64 ** 2) / (n - 1)
+    v32 = (b32[:, 2] / n - m32 ** 2) / (n - 1)
+    ok = (v64 + v32) > 0
+    z = (m64[ok] - m32[ok]) / np.sqrt(v64[ok] + v32[ok])
+    assert abs(z.mean()) < 0.2 and z.std() < 1.3, (z.mean(), z.std())
+
+
+def test_fixed_source_device_cycle_matches_oracle(gpu_mod, oracle_mod):
+    p = problems.infinite_medium_2g()
+    g, o = make_pair(gpu_mod, oracle_mod, p)
+    ag = g.upload_tally(p.tallies["flux"])
+    ao = o.upload_tally(p.tallies["flux"])
+    mg = mo = 4242
+    for _ in range(3):
+        mg, _ = g.fixed_source_cycle(ag, 10000, mg)
+        mo, _ = o.fixed_source_cycle(ao, 10000, mo)
+    assert mg == mo
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10)
