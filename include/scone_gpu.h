@@ -198,6 +198,9 @@ typedef struct sg_cycle_stats {
   double  end_weight;           /* popWeight of the produced bank    */
   double  k_eff;                /* k used for this cycle              */
   double  k_new;                /* k estimate after the cycle (eigen device cycles) */
+  double  transport_ms;         /* history-loop kernel time, CUDA events on the handle's stream */
+  double  cycle_ms;             /* whole call, CUDA events on the handle's stream */
+  int64_t n_kernels;            /* kernels launched by the call */
 } sg_cycle_stats;
 
 typedef struct sg_handle_t* sg_handle;

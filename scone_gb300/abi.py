@@ -96,7 +96,8 @@ class CycleStats(C.Structure):
     _fields_ = [
         ("n_histories", C.c_int64), ("n_events", C.c_int64), ("n_collisions", C.c_int64),
         ("n_next", C.c_int64), ("start_weight", C.c_double), ("end_weight", C.c_double),
-        ("k_eff", C.c_double), ("k_new", C.c_double),
+        ("k_eff", C.c_double), ("k_new", C.c_double), ("transport_ms", C.c_double),
+        ("cycle_ms", C.c_double), ("n_kernels", C.c_int64),
     ]
 
 

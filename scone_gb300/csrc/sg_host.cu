@@ -135,6 +135,9 @@ struct sg_handle_t {
   DArr<int> recColl;
   DArr<unsigned long long> recRng;
   int lastN = 0;
+  long long launches = 0;      // kernels launched since the last reset (cycle stats)
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float lastTransportMs = 0.f;
 
   // point source
   bool hasSource = false;
@@ -542,14 +545,18 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   CK(cudaMemsetAsync(h->sCursor.p, 0, SITE_REGIONS * sizeof(int), s));
   CK(cudaMemsetAsync(h->histN.p, 0, (size_t)(n + 1) * sizeof(int), s));
   CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), s));
+  CK(cudaEventRecord(h->ev[0], s));
   CK(launch_transport<R>(t, h->maxl, h->cfg.transport == SG_TRANSPORT_DT, smem, s, nullptr));
+  CK(cudaEventRecord(h->ev[1], s));
   CK(exclusive_scan(h->histN.p, n + 1, h->start.p, h->scanTmp.p, h->totals.p + 0, s));
   CK(launch_site_scatter(site_view(h), h->start.p, out, outcap, h->totals.p + 3, s));
+  h->launches += 5;
   DCounters c;
   int tot[8];
   CK(cudaMemcpyAsync(&c, h->ctr.p, sizeof(c), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(tot, h->totals.p, sizeof(tot), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  CK(cudaEventElapsedTime(&h->lastTransportMs, h->ev[0], h->ev[1]));
   h->lastN = n;
   if (c.err_code) {
     char m[160];
@@ -563,6 +570,7 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
     st->n_events = (int64_t)c.events;
     st->n_collisions = (int64_t)c.collisions;
     st->n_next = tot[0];
+    st->transport_ms = h->lastTransportMs;
   }
   return SG_OK;
 }
@@ -580,7 +588,7 @@ int gen_loop(sg_handle h, int admin, DBank in, int n, unsigned long long master,
 int cycle_start(sg_handle h, int admin, const double* d_w, double w) {
   for (int x = admin; x >= 0; x = h->admins[x].atch) {
     const Admin& A = h->admins[x];
-    if (A.keffAnalog >= 0) CK(add_scalar(h->acc.p + A.off + A.keffAnalog, d_w, w, h->stream));
+    if (A.keffAnalog >= 0) { CK(add_scalar(h->acc.p + A.off + A.keffAnalog, d_w, w, h->stream)); h->launches += 1; }
   }
   return SG_OK;
 }
@@ -611,7 +619,7 @@ int cycle_end(sg_handle h, int admin, const double* d_endw, const double* d_kend
     a.batchN = batchN;
     a.k_out = (x == kadmin) ? k_out : nullptr;
     a.k_addr = A.keffImplicit >= 0 ? A.keffImplicit + 4 : (A.keffAnalog >= 0 ? A.keffAnalog + 2 : -1);
-    if (A.N > 0) CK(launch_tally_close(a, h->stream));
+    if (A.N > 0) { CK(launch_tally_close(a, h->stream)); h->launches += 1; }
     A.cycles += 1;
     A.batchN = batchN;
   }
@@ -628,12 +636,14 @@ int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long maste
     k_rn_keys<<<((S + 31) / 32 + 127) / 128, 128, 0, s>>>(master, S, h->keys.p);
     CK(cudaGetLastError());
     CK(radix_select(h->keys.p, S, heap, h->sel.p, h->kbuf.p, h->hist16.p, s));
+    h->launches += 9;
   }
   if (excess > 0) {
     CK(launch_flags(h->keys.p, S, h->sel.p, 1, h->flags.p, s));
     CK(cudaMemsetAsync(h->flags.p + S, 0, sizeof(int), s));
     CK(exclusive_scan(h->flags.p, S + 1, h->pos.p, h->scanTmp.p, h->totals.p + 1, s));
     CK(launch_compact(in, S, h->flags.p, h->pos.p, out, s));
+    h->launches += 5;
     int kept = 0;
     CK(cudaMemcpyAsync(&kept, h->totals.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -646,6 +656,7 @@ int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long maste
     CK(cudaMemsetAsync(h->flags.p + S, 0, sizeof(int), s));
     CK(exclusive_scan(h->flags.p, S + 1, h->pos.p, h->scanTmp.p, h->totals.p + 2, s));
     CK(launch_replicate(in, S, h->flags.p, h->pos.p, h->start.p, n_copies, out, s));
+    h->launches += (heap > 0 ? 5 : 4);
     (void)n_hist;
   } else {
     CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
@@ -709,6 +720,8 @@ int32_t sg_create(const sg_config* cfg, sg_handle* out) {
   }
   int rc = alloc_work(h);
   if (rc) { delete h; return rc; }
+  for (auto& e : h->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) { delete h; return SG_ERR_CUDA; }
   *out = h;
   return SG_OK;
 }
@@ -726,6 +739,7 @@ int32_t sg_destroy(sg_handle h) {
   h->sCursor.free(); h->histN.free(); h->start.free(); h->scanTmp.free(); h->flags.free(); h->pos.free();
   h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->sumPart.free(); h->scal.free();
   h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
+  for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(h->stream);
   delete h;
   return SG_OK;
@@ -833,6 +847,8 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
                           double k_eff, sg_bank* next, int32_t next_cap, sg_cycle_stats* stats) {
   if (!h || !in || n < 0 || n > h->cap) return SG_ERR_BAD_ARG;
   DBank A = h->bank[0].view(), B = h->bank[1].view();
+  h->launches = 0;
+  CK(cudaEventRecord(h->ev[2], h->stream));
   int rc = h2d_bank(h, in, n, A);
   if (rc) return rc;
   CK(cudaMemcpyAsync(h->scal.p + 0, &k_eff, sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -846,8 +862,14 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
     rc = d2h_bank(h, B, S, next);
     if (rc) return rc;
   }
+  CK(cudaEventRecord(h->ev[3], h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  float cyc = 0.f;
+  CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
   if (stats) {
     *stats = st;
+    stats->cycle_ms = cyc;
+    stats->n_kernels = h->launches;
     stats->k_eff = k_eff;
     stats->k_new = k_eff;
     double sw = 0, ew = 0;
@@ -939,7 +961,10 @@ int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
   cudaStream_t s = h->stream;
   DBank A = h->bank[h->cur].view(), B = h->bank[1 - h->cur].view();
   const int n = h->pop;
+  h->launches = 0;
+  CK(cudaEventRecord(h->ev[2], s));
   CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, s));       // popWeight(thisCycle)
+  h->launches += 2;
   int rc = cycle_start(h, admin, h->scal.p + 2, 0.0);
   if (rc) return rc;
   int S = 0;
@@ -948,6 +973,7 @@ int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
   if (rc) return rc;
   h->master = rng_stride(h->master, (long long)h->pop + 1);              // :257
   CK(deterministic_sum(B.wgt, S, h->sumPart.p, h->scal.p + 3, s));       // popWeight(nextCycle)
+  h->launches += 2;
   rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, atch, h->scal.p + 1);
   if (rc) return rc;
   rc = norm_size(h, B, S, h->pop, h->master, A, n);                      // :269, result in A
@@ -957,7 +983,10 @@ int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
   CK(cudaMemcpyAsync(h->scal.p + 4, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
   double sc[5];
   CK(cudaMemcpyAsync(sc, h->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev[3], s));
   CK(cudaStreamSynchronize(s));
+  float cyc = 0.f;
+  CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
   double kUsed = h->k;
   h->k = sc[1];
   if (stats) {
@@ -966,6 +995,8 @@ int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
     stats->end_weight = sc[3];
     stats->k_eff = kUsed;
     stats->k_new = sc[1];
+    stats->cycle_ms = cyc;
+    stats->n_kernels = h->launches;
   }
   return SG_OK;
 }
@@ -989,7 +1020,10 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
   if (h->anyFissile) return h->fail(SG_ERR_BAD_ARG, "fixed-source runs with fissile materials are not supported");
   cudaStream_t s = h->stream;
   DBank A = h->bank[0].view(), B = h->bank[1].view();
+  h->launches = 0;
+  CK(cudaEventRecord(h->ev[2], s));
   PointSourceArgs a = h->psrc;                                           // fixedSource%generate
+  h->launches += 1;
   a.out = A;
   a.n = n;
   a.master = *master_state;
@@ -1009,7 +1043,10 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
   CK(cudaMemcpyAsync(h->scal.p + 3, &wn, sizeof(double), cudaMemcpyHostToDevice, s));
   rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, -1, nullptr);   // :267
   if (rc) return rc;
+  CK(cudaEventRecord(h->ev[3], s));
   CK(cudaStreamSynchronize(s));
+  float cyc = 0.f;
+  CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
   h->eigenReady = false;
   *master_state = m;
   if (stats) {
@@ -1018,6 +1055,8 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
     stats->end_weight = n;
     stats->k_eff = 1.0;
     stats->k_new = 1.0;
+    stats->cycle_ms = cyc;
+    stats->n_kernels = h->launches;
   }
   return SG_OK;
 }
