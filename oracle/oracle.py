@@ -61,7 +61,8 @@ def lib():
             "or_rotate_vector": (i32, [P(f64), f64, f64, P(f64)]),
             "or_scoremem_new": (i32, [i64, i32, P(vp)]), "or_scoremem_free": (i32, [vp]),
             "or_scoremem_score": (i32, [vp, f64, i64]), "or_scoremem_accumulate": (i32, [vp, f64, i64]),
-            "or_scoremem_close": (i32, [vp, f64]), "or_scoremem_result": (i32, [vp, i64, i32, P(f64), P(f64)]),
+            "or_scoremem_close": (i32, [vp, f64]), "or_scoremem_reduce": (i32, [vp]),
+            "or_scoremem_closebin": (i32, [vp, f64, i64]), "or_scoremem_closecycle": (i32, [vp, f64]), "or_scoremem_result": (i32, [vp, i64, i32, P(f64), P(f64)]),
             "or_timed_gen_loop": (i64, [vp, i32, P(abi.Bank), i32, u64, f64, i32, P(i64)]),
         }
         for name, (res, args) in sig.items():
@@ -304,6 +305,15 @@ class ScoreMemory:
 
     def close_cycle(self, f=1.0):
         self.L.or_scoremem_close(self.h, f)
+
+    def reduce_bins(self):
+        self.L.or_scoremem_reduce(self.h)
+
+    def close_bin(self, f, idx):
+        self.L.or_scoremem_closebin(self.h, f, idx)
+
+    def close_cycle_only(self, f):
+        self.L.or_scoremem_closecycle(self.h, f)
 
     def result(self, idx, samples=-1):
         m, s = C.c_double(), C.c_double()

@@ -883,8 +883,15 @@ struct ScoreMemory {
       batchN += 1;
     }
   }
+  void closeBin(double normFactor, int64_t idx) {                          // :356-375
+    double res = bin[idx - 1] * normFactor;
+    csum[idx - 1] = csum[idx - 1] + res;
+    csum2[idx - 1] = csum2[idx - 1] + res * res;
+    bin[idx - 1] = 0.0;
+  }
   double getScore(int64_t idx) const { return (idx <= 0 || idx > N) ? 0.0 : bin[idx - 1]; }  // :597-608
   void getResult(double& mean, double& STD, int64_t idx, int samples = -1) const {          // :537-573
+    if (idx < 1 || idx > N) { mean = 0.0; STD = 0.0; return; }
     int n = samples > 0 ? samples : batchN;
     mean = csum[idx - 1] / n;
     double inv_N = 1.0 / n;
@@ -1641,6 +1648,9 @@ int32_t or_scoremem_new(int64_t n, int32_t batch, or_handle* out) {
 int32_t or_scoremem_free(or_handle h) { delete reinterpret_cast<orc::ScoreMemory*>(h); return SG_OK; }
 int32_t or_scoremem_score(or_handle h, double s, int64_t idx) { reinterpret_cast<orc::ScoreMemory*>(h)->score(s, idx); return SG_OK; }
 int32_t or_scoremem_accumulate(or_handle h, double s, int64_t idx) { reinterpret_cast<orc::ScoreMemory*>(h)->accumulate(s, idx); return SG_OK; }
+int32_t or_scoremem_reduce(or_handle h) { reinterpret_cast<orc::ScoreMemory*>(h)->reduceBins(); return SG_OK; }
+int32_t or_scoremem_closebin(or_handle h, double f, int64_t idx) { reinterpret_cast<orc::ScoreMemory*>(h)->closeBin(f, idx); return SG_OK; }
+int32_t or_scoremem_closecycle(or_handle h, double f) { reinterpret_cast<orc::ScoreMemory*>(h)->closeCycle(f); return SG_OK; }
 int32_t or_scoremem_close(or_handle h, double f) {
   orc::ScoreMemory* m = reinterpret_cast<orc::ScoreMemory*>(h); m->reduceBins(); m->closeCycle(f); return SG_OK;
 }

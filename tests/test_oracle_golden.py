@@ -1,0 +1,357 @@
+"""Pins the CPU oracle to SCONE: the known answers of SCONE's own unit and integration tests
+(cited per test) and a Python big-integer evaluation of its RNG (tests/golden/make_golden.py)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from scone_gb300 import abi, problems
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scone_golden.json")))
+SURF_TOL = 1.0e-12
+INF = 2.0 ** 63
+SQRT2 = math.sqrt(2.0)
+
+
+# ---------------------------------------------------------------- RNG (RandomNumbers/RNG_class.f90)
+def test_rng_draws_match_bigint_recurrence(oracle_mod):
+    g = GOLD["rng"]
+    xs, s = oracle_mod.rng_draws(g["seed"], 1000)
+    assert np.array_equal(xs[:64], np.array(g["draws"]))
+    assert str(s) == g["state_1000"]
+
+
+def test_rng_skip_matches_bigint(oracle_mod):
+    g = GOLD["rng"]
+    for k, v in g["skip"].items():
+        assert str(oracle_mod.rng_skip(g["seed"], int(k))) == v, k
+    for k, v in g["skip_negative"].items():
+        assert str(oracle_mod.rng_skip(g["seed"], int(k))) == v, k
+
+
+def test_rng_skip_forward_backward_scone(oracle_mod):
+    # RandomNumbers/Tests/RNG_test.f90:36-70
+    seed = 0x5C3A84C9
+    first, _ = oracle_mod.rng_draws(seed, 1)
+    N = 13456757
+    seq, s_end = oracle_mod.rng_draws(seed, N + 1)
+    s2 = oracle_mod.rng_skip(seed, N)
+    r2_end, s2 = oracle_mod.rng_draws(s2, 1)
+    assert r2_end[0] == seq[N]          # the (N+1)-th draw: r_end after N draws following the first
+    back = oracle_mod.rng_skip(s2, -(N + 1))
+    r2_start, _ = oracle_mod.rng_draws(back, 1)
+    assert r2_start[0] == first[0]
+
+
+def test_rng_pow_of_gsq_table_is_successive_squares():
+    # RNG_class.f90:53-59 documents the table as g^(2^j) mod 2^63
+    G, M = 2806196910506780709, (1 << 63) - 1
+    g = G
+    for j, v in enumerate(GOLD["pow_of_gsq"][:60]):
+        g = (g * g) & M
+        assert g == int(v), j
+
+
+# ---------------------------------------------------------------- scoreMemory (Tallies/Tests/scoreMemory_test.f90:92-200)
+def test_score_memory_golden(oracle_mod):
+    A, M = 2469, 65521
+    seed = 9294
+    rnd = []
+    for _ in range(200):
+        seed = (A * seed) % M
+        rnd.append(seed / float(M))
+    rnd = np.array(rnd)
+    scores = 2.0 + np.sin(math.pi * rnd - math.pi / 2)
+    ints = (rnd * 100).astype(np.int32)
+    mem = oracle_mod.ScoreMemory(7, 1)
+    for i in range(10):
+        for j in range(20 * i, 20 * i + 20):
+            mem.score(float(scores[j]), 1)
+            mem.score(float(ints[j]), 2)
+            mem.score(float(ints[j]), 3)
+            mem.accumulate(float(scores[j]), 4)
+            mem.accumulate(float(ints[j]), 5)
+            mem.accumulate(float(ints[j]), 6)
+        mem.reduce_bins()
+        mem.close_bin(1.2, 3)
+        mem.close_cycle_only(0.7)
+    tol = 1e-9
+    m, s = mem.result(1)
+    assert abs(m - 26.401471259728442) < tol and abs(s - 0.645969443981583) < tol
+    m, s = mem.result(2)
+    assert abs(m - 623.0) < tol and abs(s - 27.982494527829360) < tol
+    m, s = mem.result(3)
+    assert abs(m - 1068.0) < tol and abs(s - 47.969990619136050) < tol
+    m, s = mem.result(4, 200)
+    assert abs(m - 1.885819375694888) < tol and abs(s - 0.049102082638055) < tol
+    m, s = mem.result(5, 200)
+    assert abs(m - 44.5) < tol and abs(s - 2.015580019267494) < tol
+    m, s = mem.result(7)
+    assert m == 0.0 and s == 0.0
+    m, s = mem.result(-7)
+    assert m == 0.0 and s == 0.0
+
+
+# ---------------------------------------------------------------- surfaces (Geometry/Surfaces/Tests)
+def _unit(v):
+    v = np.array(v, float)
+    return v / np.linalg.norm(v)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_cylinder_distance_and_halfspace(oracle_mod, axis):
+    # cylinder_test.f90:200-340 -- origin (2,2,2), radius 2, x/y/z cylinders
+    typ = [abi.XCYL, abi.YCYL, abi.ZCYL][axis]
+    par = [2.0, 2.0, 2.0, 2.0]
+    a = axis
+    p1, p2 = [(1, 2), (0, 2), (0, 1)][axis]
+    ev = lambda r, u: oracle_mod.surf_eval(typ, par, r, u)
+    tol = 1e-7
+    # halfspace
+    r = np.full(3, 2.0); r[p1] = 0.0
+    u = np.zeros(3); u[p1] = 1.0; u[a] = 1.0; u = _unit(u)
+    assert not ev(r, u)["halfspace"]
+    assert not ev(r - SURF_TOL * u, u)["halfspace"]
+    assert ev(r - SQRT2 * 1.00001 * SURF_TOL * u, u)["halfspace"]
+    assert ev(r - 2.0 * u, u)["halfspace"]
+    assert not ev(r + 2.0 * u, u)["halfspace"]
+    ut = np.zeros(3); ut[p2] = 1.0; ut[a] = 1.0
+    assert ev(r, _unit(ut))["halfspace"]
+    # distance outside
+    r = np.full(3, 2.0); r[p1] = -1.0
+    u = np.zeros(3); u[a] = 1.0; u[p1] = 1.0; u = _unit(u)
+    assert abs(ev(r, u)["distance"] - SQRT2) < tol * SQRT2
+    u = np.zeros(3); u[a] = 1.0; u[p1] = math.sqrt(3.0) / 2; u[p2] = 0.5; u = _unit(u)
+    ref = 1.275200556 * SQRT2
+    assert abs(ev(r, u)["distance"] - ref) < tol * ref
+    u = np.zeros(3); u[a] = 1.0e20; u[p1] = 1.0; u = _unit(u)
+    assert ev(r, u)["distance"] == INF
+    # at the surface
+    r = np.full(3, 2.0); r[p1] = 0.0
+    u = np.zeros(3); u[a] = 1.0; u[p1] = 1.0; u = _unit(u)
+    assert abs(ev(r, u)["distance"] - 4 * SQRT2) < tol * 4 * SQRT2
+    assert ev(r, -u)["distance"] == INF
+    # outside within tolerance
+    r = np.full(3, 2.0); r[p1] = -0.5 * SURF_TOL
+    ref = (4.0 + 0.5 * SURF_TOL) * SQRT2
+    assert abs(ev(r, u)["distance"] - ref) < tol * ref
+    # inside
+    r = np.full(3, 2.0); r[p1] = 1.0
+    assert abs(ev(r, u)["distance"] - 3 * SQRT2) < tol * 3 * SQRT2
+    assert abs(ev(r, -u)["distance"] - SQRT2) < tol * SQRT2
+
+
+BOX = [1.0, 2.0, 1.0, 1.0, 2.0, 3.0]   # box_test.f90:12 origin (1 2 1) halfwidth (1 2 3)
+
+
+def test_box_distance(oracle_mod):
+    # box_test.f90:testDistance
+    ev = lambda r, u: oracle_mod.surf_eval(abi.BOX, BOX, r, u)["distance"]
+    tol = 1e-7
+    r = [-2.0, 0.001, 1.0]
+    assert abs(ev(r, [1, 0, 0]) - 2.0) < tol * 2
+    assert ev(r, [-1, 0, 0]) == INF
+    assert ev(r, _unit([1, -0.002, 1])) == INF
+    assert abs(ev(r, _unit([1, 0, 1])) - 2 * SQRT2) < tol * 2 * SQRT2
+    assert ev([-2.7, -0.3, 1.0 / 3.0], _unit([2.7, 0.3, 3.0 + 2.0 / 3.0])) == INF
+    assert ev([-2.0, 0.0, 1.0], [1, 0, 0]) == INF
+    r = [1.0, 2.0, -2.0]
+    assert abs(ev(r, [0, 0, 1]) - 6.0) < tol * 6
+    assert ev(r, [0, 0, -1]) == INF
+    assert abs(ev([1.0, 2.0, -2.0 - 0.5 * SURF_TOL], [0, 0, 1]) - (6.0 + 0.5 * SURF_TOL)) < tol * 6
+    u = _unit([0, 1, 1])
+    assert abs(ev([1.0, 2.0, -1.0], u) - 2 * SQRT2) < tol * 2 * SQRT2
+    assert abs(ev([1.0, 2.0, -1.0], -u) - SQRT2) < tol * SQRT2
+
+
+def test_box_boundary_conditions(oracle_mod):
+    # box_test.f90:testBC -- BC (vacuum, reflective, periodic, periodic, reflective, reflective)
+    bc = [0, 1, 2, 2, 1, 1]
+    f = lambda r, u, t=False: oracle_mod.surf_bc(abi.BOX, BOX, bc, r, u, transform=t)
+    r, u = f([0.0, 1.0, -1.0], [1, 0, 0])
+    assert np.allclose(r, [0, 1, -1]) and np.allclose(u, [1, 0, 0])
+    r, u = f([1.0, 1.0, -2.0], [0, 0, -1])
+    assert np.allclose(r, [1, 1, -2]) and np.allclose(u, [0, 0, 1])
+    r, u = f([1.0, 0.0, -1.0], [0, -1, 0])
+    assert np.allclose(r, [1, 4, -1]) and np.allclose(u, [0, -1, 0])
+    r, u = f([2.0, 0.0, 4.0], _unit([1, -1, 1]))
+    assert np.allclose(r, [2, 4, 4], atol=1e-6) and np.allclose(u, _unit([-1, -1, -1]), atol=1e-6)
+    r, u = f([4.5, -10.0, 4.0], _unit([1, 1, 1]), True)
+    assert np.allclose(r, [-0.5, 2.0, 4.0], atol=1e-6) and np.allclose(u, _unit([-1, 1, -1]), atol=1e-6)
+    r, u = f([2.0, 0.0, 4.0], _unit([1, -1, 1]), True)
+    assert np.allclose(r, [2, 4, 4], atol=1e-6) and np.allclose(u, _unit([-1, -1, -1]), atol=1e-6)
+
+
+def test_aplane_and_sphere(oracle_mod):
+    # aPlane_test / sphere_test behaviour: distance along the axis, tolerance band, parallel miss
+    ev = lambda t, p, r, u: oracle_mod.surf_eval(t, p, r, u)
+    assert abs(ev(abi.XPLANE, [3.0], [1.0, 0, 0], [1, 0, 0])["distance"] - 2.0) < 1e-12
+    assert ev(abi.XPLANE, [3.0], [1.0, 0, 0], [-1, 0, 0])["distance"] == INF
+    assert ev(abi.XPLANE, [3.0], [3.0 - 0.5 * SURF_TOL, 0, 0], [1, 0, 0])["distance"] == INF
+    assert ev(abi.XPLANE, [3.0], [1.0, 0, 0], [0, 1, 0])["distance"] == INF
+    s = ev(abi.SPHERE, [0, 0, 0, 2.0], [0.0, 0, 0], [1, 0, 0])
+    assert abs(s["distance"] - 2.0) < 1e-12 and not s["halfspace"]
+    s = ev(abi.SPHERE, [0, 0, 0, 2.0], [-4.0, 0, 0], [1, 0, 0])
+    assert abs(s["distance"] - 2.0) < 1e-12 and s["halfspace"]
+    assert ev(abi.SPHERE, [0, 0, 0, 2.0], [-4.0, 3.0, 0], [1, 0, 0])["distance"] == INF
+
+
+def test_rotate_vector_properties(oracle_mod):
+    # rotateVector (genericProcedures.f90:1047-1084): result is unit and at cosine mu to the input
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        d = _unit(rng.normal(size=3))
+        mu = rng.uniform(-1, 1)
+        phi = rng.uniform(0, 2 * math.pi)
+        out = oracle_mod.rotate_vector(d, mu, phi)
+        assert abs(np.linalg.norm(out) - 1.0) < 1e-14
+        assert abs(out @ d - mu) < 1e-12
+    out = oracle_mod.rotate_vector([0.0, 0.0, 1.0], 0.3, 1.1)       # the |w| ~ 1 branch
+    assert abs(out[2] - 0.3) < 1e-12
+
+
+# ---------------------------------------------------------------- geometryStd (Geometry/Tests/geometryStd_iTest.f90:44-250)
+def test_geometry_std_lattice_itest(oracle_mod):
+    g, mats = problems.scone_test_lat()
+    o = oracle_mod.Oracle()
+    o.upload_geometry(g)
+    tol = 1e-7
+    assert o.what_is_at([0, 0, 0])[0] == mats["water"]
+    assert o.what_is_at([0.63, -0.09, 0.0], [0, -1, 0])[0] == mats["mox43"]
+    o.coords_init([0.1, 0.1, 0.0], [0, 0, 1])
+    o.coords_place()
+    for lvl, ref in ((0, [0.1, 0.1, 0.0]), (1, [0.1, 0.1, 0.0]), (2, [0.1 - 0.63, 0.1 - 0.63, 0.0])):
+        r, u, _ = o.coords_get(lvl)
+        assert np.allclose(r, ref, atol=tol) and np.allclose(u, [0, 0, 1])
+    # unique IDs of the shrunk graph (slicePlot 'uniqueID' pixels 5,5 and 1,1)
+    assert o.what_is_at([-0.63, -0.63, 0.0])[1] == 2
+    assert o.what_is_at([-0.63 - 0.6, -0.63 - 0.6, 0.0])[1] == 3
+    assert np.allclose(o.bounds(), [-1.26, -1.26, 0, 1.26, 1.26, 0], atol=tol)
+    u = _unit([-1, -2, 0])
+    o.coords_init([0, 0, 0], u)
+    o.coords_move(3, 3.0)                                  # teleport
+    r, uu, info = o.coords_get(0)
+    assert np.allclose(r, [-1.1783592, -0.1632816, 0], atol=tol)
+    assert np.allclose(uu, _unit([1, -2, 0]), atol=tol) and info["mat"] == mats["water"]
+    o.coords_init([0, 0, 0], [0, -1, 0])                   # geometry moveGlobal
+    d, ev = o.coords_move(2, 1.0)
+    r, _, info = o.coords_get(0)
+    assert ev == 1 and np.allclose(r, [0, -1, 0], atol=tol) and abs(d - 1.0) < tol
+    d, ev = o.coords_move(2, 1.0)
+    r, _, info = o.coords_get(0)
+    assert ev == 2 and np.allclose(r, [0, 1.26, 0], atol=tol) and abs(d - 0.26) < tol
+    o.coords_init([-0.63, -0.63, 0.0], [0, -1, 0])         # move (no cache)
+    o.coords_place()
+    for maxd, ev_ref, r_ref, d_ref in ((1.0, 3, [-0.63, -1.13, 0], 0.5), (1.0, 2, [-0.63, 1.26, 0], 0.13),
+                                       (0.08, 1, [-0.63, 1.18, 0], 0.08)):
+        d, ev = o.coords_move(0, maxd)
+        r, _, info = o.coords_get(0)
+        assert ev == ev_ref and np.allclose(r, r_ref, atol=tol) and abs(d - d_ref) < tol
+        assert info["mat"] == mats["water"]
+
+
+def _lattice_uni1_geometry():
+    # latUniverse_test.f90:18-29 uni1: pitch (1 2 3), shape (3 2 2) (fills replaced by materials)
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0, 0, 0, 50.0, 50.0, 50.0)
+    lat = gb.lattice_universe((3, 2, 2), (1.0, 2.0, 3.0), list(range(1, 13)), 13)
+    gb.root_universe(box, problems.uni_fill(lat), bc=[0] * 6)
+    return gb.arrays()
+
+
+def test_lattice_universe_enter_and_distance(oracle_mod):
+    # latUniverse_test.f90:112-260
+    o = oracle_mod.Oracle()
+    o.upload_geometry(_lattice_uni1_geometry())
+    for r, u, loc in (([1.0, 1.0, 0.5], [0, 0, 1], 12), ([1.6, 0.5, 0.5], [0, 0, 1], 13),
+                      ([-0.5, 0.0, 0.0], _unit([-1, 1, -1]), 4)):
+        o.coords_init(r, u)
+        o.coords_place()
+        assert o.coords_get(1)[2]["local"] == loc
+    o.coords_init([0.0, 0.1, 0.5], [0.0, -0.0, 1.0])
+    o.coords_place()
+    d, ev = o.coords_move(0, 100.0)
+    assert ev == 3 and abs(d - 2.5) < 2.5e-7
+    eps = 0.5 * SURF_TOL
+    o.coords_init([-1.0, 0.0 - eps, -0.5], _unit([1, 1, 0]))
+    o.coords_place()
+    assert o.coords_get(1)[2]["local"] == 4
+    d, ev = o.coords_move(0, 100.0)
+    assert abs(d - SQRT2 * 0.5) < 1e-7
+
+
+# ---------------------------------------------------------------- MG data (baseMgNeutronDatabase_iTest.f90:44-130)
+def _mg_from_gold(names):
+    mats = [GOLD[n] for n in names]
+    nG = mats[0]["numberOfGroups"]
+    P0 = np.array([np.array(m["P0"]).reshape(nG, nG) for m in mats])       # rows = incident group
+    prod = np.array([np.array(m["scatteringMultiplicity"]).reshape(nG, nG) for m in mats])
+    cap = np.array([m["capture"] for m in mats])
+    fis = np.array([m.get("fission", [0.0] * nG) for m in mats])
+    nu = np.array([m.get("nu", [0.0] * nG) for m in mats])
+    chi = np.array([m.get("chi", [0.0] * nG) for m in mats])
+    d = problems.mg_data(nG, cap, P0, capture=cap, fission=fis, nu=nu, chi=chi, prod=prod)
+    return d
+
+
+def test_mg_database_itest_values(oracle_mod):
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0, 0, 0, 1.0, 1.0, 1.0)
+    gb.root_universe(box, 1, bc=[1] * 6)                     # only material 1 active (activate([1]))
+    o = oracle_mod.Oracle()
+    o.upload_geometry(gb.arrays())
+    o.upload_mg(_mg_from_gold(["mgMat1", "mgMat2"]))
+    tol = 1e-6
+    assert abs(o.mg_info(1, 1)["total"] - 2.1) < tol       # getTrackingXS(MATERIAL_XS), G = 1
+    assert abs(o.mg_info(2, 1)["total"] - 3.1) < tol       # getTotalMatXS(mat 2), G = 1
+    assert abs(o.mg_info(1, 3)["total"] - 6.0) < tol
+    assert abs(o.mg_info(1, 1)["majorant"] - 2.1) < tol
+    m2 = o.mg_info(2, 1)
+    assert abs(m2["scatter"] - 1.1) < tol and abs(m2["capture"] - 1.0) < tol
+    assert abs(m2["fission"] - 1.0) < tol and abs(m2["nu_fission"] - 2.3) < tol
+    m1 = o.mg_info(1, 4)
+    assert abs(m1["total"] - 7.1) < tol and abs(m1["scatter"] - 3.1) < tol and abs(m1["capture"] - 4.0) < tol
+    assert m1["fission"] == 0.0 and m1["nu_fission"] == 0.0
+
+
+# ---------------------------------------------------------------- whole-cycle sanity of the restatement
+def test_infinite_medium_flux_matches_analytic(oracle_mod):
+    """2-group infinite medium, collision estimator: phi_1 = 1/(St1 - S11), phi_2 = phi_1 S12/(St2 - S22)."""
+    p = problems.infinite_medium_2g()
+    o = oracle_mod.Oracle(p)
+    adm = o.upload_tally(p.tallies["flux"])
+    m = 2024
+    nb, n = 20, 5000
+    for _ in range(nb):
+        m, _ = o.fixed_source_cycle(adm, n, m)
+    b = o.bins(adm)
+    mean = b[:, 1] / nb / n
+    sd = np.sqrt((b[:, 2] / nb - (b[:, 1] / nb) ** 2) / (nb - 1)) / n
+    st = p.meta["sigma_t"]
+    P0 = p.mg["p0"][0]
+    phi1 = 1.0 / (st[0] - P0[0, 0])
+    phi2 = phi1 * P0[0, 1] / (st[1] - P0[1, 1])
+    assert abs(mean[0] - phi1) < 4 * sd[0] and abs(mean[1] - phi2) < 4 * sd[1]
+
+
+def test_lattice_eigen_st_dt_agree(oracle_mod):
+    """ST and DT are different estimators of the same k (SCONE's two transport operators)."""
+    p = problems.lattice_17x17_7g()
+    res = []
+    for tr in (abi.TRANSPORT_ST, abi.TRANSPORT_DT):
+        o = oracle_mod.Oracle(p, transport=tr)
+        inact, act = o.upload_tally([]), o.upload_tally([])
+        ia = o.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+        aa = o.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        o.attach_tally(inact, ia)
+        o.attach_tally(act, aa)
+        o.eigen_init(4000, 99)
+        for _ in range(4):
+            o.eigen_cycle(inact, ia)
+        for _ in range(8):
+            o.eigen_cycle(act, aa)
+        res.append(o.keff(aa))
+    (k1, s1), (k2, s2) = res
+    assert abs(k1 - k2) < 4 * math.hypot(s1, s2)
