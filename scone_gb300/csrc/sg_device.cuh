@@ -148,38 +148,58 @@ __device__ __forceinline__ void rotate_vector(R& u, R& v, R& w, R mu, R sinPol, 
 }
 
 // ------------------------------------------------------------------ surfaces (Geometry/Surfaces)
-// distance, evaluate, going, halfspace, BCs.  Positions are FP64; the coincidence test `abs(c) < tol`
-// is always done on an FP64 c; the remaining distance arithmetic is in R.
-template <class R>
-__device__ __forceinline__ double surf_evaluate(const DSurf& s, const double r[3]) {
+// Position type T: double for the root level (global coordinates) and for every level in the FP64
+// form; R (float) for levels below the root in the mixed form, where parameters come from the FP32
+// copies.  The coincidence test `abs(c) < tol` is evaluated in T.
+template <class T> __device__ __forceinline__ T SP(const DSurf& s, int i);
+template <> __device__ __forceinline__ double SP<double>(const DSurf& s, int i) { return s.p[i]; }
+template <> __device__ __forceinline__ float SP<float>(const DSurf& s, int i) { return s.pf[i]; }
+template <class T> __device__ __forceinline__ T STOL(const DSurf& s);
+template <> __device__ __forceinline__ double STOL<double>(const DSurf& s) { return s.tol; }
+template <> __device__ __forceinline__ float STOL<float>(const DSurf& s) { return s.tolf; }
+template <class T> __device__ __forceinline__ T UD(const DUni& u, int i);
+template <> __device__ __forceinline__ double UD<double>(const DUni& u, int i) { return u.d[i]; }
+template <> __device__ __forceinline__ float UD<float>(const DUni& u, int i) { return u.f[i]; }
+template <class T> __device__ __forceinline__ T UO(const DUni& u, int i);
+template <> __device__ __forceinline__ double UO<double>(const DUni& u, int i) { return u.origin[i]; }
+template <> __device__ __forceinline__ float UO<float>(const DUni& u, int i) { return u.originf[i]; }
+template <class T> __device__ __forceinline__ T PIN_RSQ(const DGeom& g, int k);
+template <> __device__ __forceinline__ double PIN_RSQ<double>(const DGeom& g, int k) { return g.pin_rsq[k]; }
+template <> __device__ __forceinline__ float PIN_RSQ<float>(const DGeom& g, int k) { return g.pin_rsqf[k]; }
+template <class T> __device__ __forceinline__ T PIN_TOL(const DGeom& g, int k);
+template <> __device__ __forceinline__ double PIN_TOL<double>(const DGeom& g, int k) { return g.pin_tol[k]; }
+template <> __device__ __forceinline__ float PIN_TOL<float>(const DGeom& g, int k) { return g.pin_tolf[k]; }
+
+template <class T>
+__device__ __forceinline__ T surf_evaluate(const DSurf& s, const T r[3]) {
   switch (s.type) {
     case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
-      return at3(r, s.axis) - s.p[0];
+      return at3(r, s.axis) - SP<T>(s, 0);                                       // aPlane_class.f90:139
     case SG_SURF_PLANE:
-      return (r[0] * s.p[0] + r[1] * s.p[1] + r[2] * s.p[2]) - s.p[3];
-    case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {
-      double d0 = at3(r, s.pl0) - s.p[s.pl0], d1 = at3(r, s.pl1) - s.p[s.pl1];
-      return (d0 * d0 + d1 * d1) - s.p[3] * s.p[3];
+      return (r[0] * SP<T>(s, 0) + r[1] * SP<T>(s, 1) + r[2] * SP<T>(s, 2)) - SP<T>(s, 3);   // plane :125
+    case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {                   // cylinder_class.f90:222
+      T d0 = at3(r, s.pl0) - SP<T>(s, s.pl0), d1 = at3(r, s.pl1) - SP<T>(s, s.pl1);
+      return (d0 * d0 + d1 * d1) - SP<T>(s, 3) * SP<T>(s, 3);
     }
-    case SG_SURF_SPHERE: {
-      double d0 = r[0] - s.p[0], d1 = r[1] - s.p[1], d2 = r[2] - s.p[2];
-      return (d0 * d0 + d1 * d1 + d2 * d2) - s.p[3] * s.p[3];
+    case SG_SURF_SPHERE: {                                                        // sphere_class.f90:143
+      T d0 = r[0] - SP<T>(s, 0), d1 = r[1] - SP<T>(s, 1), d2 = r[2] - SP<T>(s, 2);
+      return (d0 * d0 + d1 * d1 + d2 * d2) - SP<T>(s, 3) * SP<T>(s, 3);
     }
-    case SG_SURF_BOX: {
-      double m = fmax(fabs(r[0] - s.p[0]) - s.p[3], fabs(r[1] - s.p[1]) - s.p[4]);
-      return fmax(m, fabs(r[2] - s.p[2]) - s.p[5]);
+    case SG_SURF_BOX: {                                                           // box_class.f90:134-143
+      T m = fmax(fabs(r[0] - SP<T>(s, 0)) - SP<T>(s, 3), fabs(r[1] - SP<T>(s, 1)) - SP<T>(s, 4));
+      return fmax(m, fabs(r[2] - SP<T>(s, 2)) - SP<T>(s, 5));
     }
-    default: {
-      double a = fabs(at3(r, s.pl0) - s.p[s.pl0]) - s.p[3 + s.pl0];
-      double b = fabs(at3(r, s.pl1) - s.p[s.pl1]) - s.p[3 + s.pl1];
+    default: {                                                                    // squareCylinder evaluate
+      T a = fabs(at3(r, s.pl0) - SP<T>(s, s.pl0)) - SP<T>(s, 3 + s.pl0);
+      T b = fabs(at3(r, s.pl1) - SP<T>(s, s.pl1)) - SP<T>(s, 3 + s.pl1);
       return fmax(a, b);
     }
   }
 }
 
 // box/squareCylinder slab intersection (box_class.f90:168-237, squareCylinder_class.f90:212-270)
-template <class R>
-__device__ __forceinline__ R slab_distance(const DSurf& s, const double r[3], const R u[3], int nax,
+template <class R, class T>
+__device__ __forceinline__ R slab_distance(const DSurf& s, const T r[3], const R u[3], int nax,
                                            int ax0, int ax1, int ax2) {
   const R FP_MISS_TOL = (sizeof(R) == 8) ? R(1.0 + 10.0 * 2.220446049250313e-16) : R(1.0f + 10.0f * 1.1920929e-7f);
   const R HUGE_R = (sizeof(R) == 8) ? R(1.7976931348623157e308) : R(3.4028234663852886e38f);
@@ -190,11 +210,12 @@ __device__ __forceinline__ R slab_distance(const DSurf& s, const double r[3], co
   for (int i = 0; i < 3; ++i) {
     if (i < nax) {
       int ax = axes[i];
-      R rb = R(at3(r, ax) - s.p[ax]);
-      R a_far = sgn(R(s.p[3 + ax]), at3(u, ax));
+      R rb = R(at3(r, ax) - SP<T>(s, ax));
+      R ua = at3(u, ax);
+      R a_far = sgn(R(SP<T>(s, 3 + ax)), ua);
       R a_near = -a_far;
       R tn, tf;
-      if (at3(u, ax) != R(0)) { tn = (a_near - rb) / at3(u, ax); tf = (a_far - rb) / at3(u, ax); }
+      if (ua != R(0)) { tn = (a_near - rb) / ua; tf = (a_far - rb) / ua; }
       else {
         tn = sgn(INF_R, a_near - rb); tf = sgn(INF_R, a_far - rb);
         if (tn > tf) { R t = tn; tn = tf; tf = t; }
@@ -205,108 +226,108 @@ __device__ __forceinline__ R slab_distance(const DSurf& s, const double r[3], co
   }
   R d;
   if (far <= near * FP_MISS_TOL) d = INF_R;
-  else if (fabs(surf_evaluate<R>(s, r)) < s.tol) d = (fabs(far) >= fabs(near)) ? far : near;
+  else if (fabs(surf_evaluate<T>(s, r)) < STOL<T>(s)) d = (fabs(far) >= fabs(near)) ? far : near;
   else d = (near <= R(0)) ? far : near;
   if (d <= R(0) || d > INF_R) d = INF_R;
   return d;
 }
 
-template <class R>
-__device__ __forceinline__ R surf_distance(const DSurf& s, const double r[3], const R u[3]) {
+template <class R, class T>
+__device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R u[3]) {
   const R INF_R = R(D_INF);
   switch (s.type) {
     case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE: {   // aPlane_class.f90:157-181
-      double ra64 = s.p[0] - at3(r, s.axis);
+      T ra = SP<T>(s, 0) - at3(r, s.axis);
       R ua = at3(u, s.axis), d;
-      if (fabs(ra64) < s.tol) d = INF_R;
-      else if (ua != R(0)) d = R(ra64) / ua;
+      if (fabs(ra) < STOL<T>(s)) d = INF_R;
+      else if (ua != R(0)) d = R(ra) / ua;
       else d = INF_R;
       if (d <= R(0) || d > INF_R) d = INF_R;
       return d;
     }
     case SG_SURF_PLANE: {                                                // plane_class.f90:144-163
-      R k = u[0] * R(s.p[0]) + u[1] * R(s.p[1]) + u[2] * R(s.p[2]);
-      double c = surf_evaluate<R>(s, r);
+      R k = u[0] * R(SP<T>(s, 0)) + u[1] * R(SP<T>(s, 1)) + u[2] * R(SP<T>(s, 2));
+      T c = surf_evaluate<T>(s, r);
       R d;
-      if (k == R(0) || fabs(c) < s.tol) d = INF_R;
+      if (k == R(0) || fabs(c) < STOL<T>(s)) d = INF_R;
       else { d = -R(c) / k; if (d <= R(0) || d > INF_R) d = INF_R; }
       return d;
     }
     case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL: {           // cylinder_class.f90:231-270
-      double c = surf_evaluate<R>(s, r);
-      R k = R(at3(r, s.pl0) - s.p[s.pl0]) * at3(u, s.pl0) + R(at3(r, s.pl1) - s.p[s.pl1]) * at3(u, s.pl1);
+      T c = surf_evaluate<T>(s, r);
+      R k = R(at3(r, s.pl0) - SP<T>(s, s.pl0)) * at3(u, s.pl0) + R(at3(r, s.pl1) - SP<T>(s, s.pl1)) * at3(u, s.pl1);
       R a = R(1) - at3(u, s.axis) * at3(u, s.axis);
       R delta = k * k - a * R(c), d;
       if (delta < R(0) || a == R(0)) d = INF_R;
-      else if (fabs(c) < s.tol) {
+      else if (fabs(c) < STOL<T>(s)) {
         if (k >= R(0)) d = INF_R;
         else { d = -k + dsqrt<R>(delta); d = d / a; }
-      } else if (c < 0.0) { d = -k + dsqrt<R>(delta); d = d / a; }
+      } else if (c < T(0)) { d = -k + dsqrt<R>(delta); d = d / a; }
       else { d = -k - dsqrt<R>(delta); d = d / a; if (d <= R(0)) d = INF_R; }
       return fmin(d, INF_R);
     }
     case SG_SURF_SPHERE: {                                               // sphere_class.f90:152-183
-      double c = surf_evaluate<R>(s, r);
-      R k = R(r[0] - s.p[0]) * u[0] + R(r[1] - s.p[1]) * u[1] + R(r[2] - s.p[2]) * u[2];
+      T c = surf_evaluate<T>(s, r);
+      R k = R(r[0] - SP<T>(s, 0)) * u[0] + R(r[1] - SP<T>(s, 1)) * u[1] + R(r[2] - SP<T>(s, 2)) * u[2];
       R delta = k * k - R(c), d;
       if (delta < R(0)) d = INF_R;
-      else if (fabs(c) < s.tol) { if (k >= R(0)) d = INF_R; else d = -k + dsqrt<R>(delta); }
-      else if (c < 0.0) d = -k + dsqrt<R>(delta);
+      else if (fabs(c) < STOL<T>(s)) { if (k >= R(0)) d = INF_R; else d = -k + dsqrt<R>(delta); }
+      else if (c < T(0)) d = -k + dsqrt<R>(delta);
       else { d = -k - dsqrt<R>(delta); if (d <= R(0)) d = INF_R; }
       return d;
     }
     case SG_SURF_BOX:
-      return slab_distance<R>(s, r, u, 3, 0, 1, 2);
+      return slab_distance<R, T>(s, r, u, 3, 0, 1, 2);
     default:
-      return slab_distance<R>(s, r, u, 2, s.pl0, s.pl1, 0);
+      return slab_distance<R, T>(s, r, u, 2, s.pl0, s.pl1, 0);
   }
 }
 
-template <class R>
-__device__ __forceinline__ bool surf_going(const DSurf& s, const double r[3], const R u[3]) {
+template <class R, class T>
+__device__ __forceinline__ bool surf_going(const DSurf& s, const T r[3], const R u[3]) {
   switch (s.type) {
     case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE:
       return at3(u, s.axis) > R(0);
     case SG_SURF_PLANE: {
-      R proj = u[0] * R(s.p[0]) + u[1] * R(s.p[1]) + u[2] * R(s.p[2]);
-      if (proj == R(0)) return surf_evaluate<R>(s, r) >= 0.0;
+      R proj = u[0] * R(SP<T>(s, 0)) + u[1] * R(SP<T>(s, 1)) + u[2] * R(SP<T>(s, 2));
+      if (proj == R(0)) return surf_evaluate<T>(s, r) >= T(0);
       return proj > R(0);
     }
     case SG_SURF_XCYL: case SG_SURF_YCYL: case SG_SURF_ZCYL:
-      return (R(at3(r, s.pl0) - s.p[s.pl0]) * at3(u, s.pl0) + R(at3(r, s.pl1) - s.p[s.pl1]) * at3(u, s.pl1)) >= R(0);
+      return (R(at3(r, s.pl0) - SP<T>(s, s.pl0)) * at3(u, s.pl0) + R(at3(r, s.pl1) - SP<T>(s, s.pl1)) * at3(u, s.pl1)) >= R(0);
     case SG_SURF_SPHERE:
-      return (R(r[0] - s.p[0]) * u[0] + R(r[1] - s.p[1]) * u[1] + R(r[2] - s.p[2]) * u[2]) >= R(0);
+      return (R(r[0] - SP<T>(s, 0)) * u[0] + R(r[1] - SP<T>(s, 1)) * u[1] + R(r[2] - SP<T>(s, 2)) * u[2]) >= R(0);
     default: {   // box (box_class.f90:253-281) and squareCylinder (:272-300)
       int axes[3] = {0, 1, 2};
       int nax = 3;
       if (s.type != SG_SURF_BOX) { axes[0] = s.pl0; axes[1] = s.pl1; nax = 2; }
       int maxCom = axes[0];
-      double best = -1.0e308;
-      double rlm = 0.0;
+      T best = T(-1.0e30);
+      T rlm = T(0);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         if (i < nax) {
-          double rl = at3(r, axes[i]) - s.p[axes[i]];
-          double v = fabs(rl) - s.p[3 + axes[i]];
-          if (v > best) { best = v; maxCom = axes[i]; rlm = rl; }
+          T rl = at3(r, axes[i]) - SP<T>(s, axes[i]);
+          T v = fabs(rl) - SP<T>(s, 3 + axes[i]);
+          if (i == 0 || v > best) { best = v; maxCom = axes[i]; rlm = rl; }
         }
       }
-      R proj = at3(u, maxCom) * (R)sgn(1.0, rlm);
-      if (proj == R(0)) return surf_evaluate<R>(s, r) >= 0.0;
+      R proj = at3(u, maxCom) * (R)sgn(T(1), rlm);
+      if (proj == R(0)) return surf_evaluate<T>(s, r) >= T(0);
       return proj > R(0);
     }
   }
 }
 
-template <class R>
-__device__ __forceinline__ bool surf_halfspace(const DSurf& s, const double r[3], const R u[3]) {
-  double c = surf_evaluate<R>(s, r);   // surface_inter.f90:363-378
-  bool hs = c > 0.0;
-  if (fabs(c) < s.tol) hs = surf_going<R>(s, r, u);
+template <class R, class T>
+__device__ __forceinline__ bool surf_halfspace(const DSurf& s, const T r[3], const R u[3]) {
+  T c = surf_evaluate<T>(s, r);   // surface_inter.f90:363-378
+  bool hs = c > T(0);
+  if (fabs(c) < STOL<T>(s)) hs = surf_going<R, T>(s, r, u);
   return hs;
 }
 
-// explicitBC (box_class.f90:380-420, squareCylinder_class.f90:430-472)
+// explicitBC (box_class.f90:380-420, squareCylinder_class.f90:430-472); root level, FP64 positions
 template <class R>
 __device__ __forceinline__ void surf_explicit_bc(const DSurf& s, double r[3], R u[3]) {
   if (s.type != SG_SURF_BOX && !(s.type >= SG_SURF_XSQCYL && s.type <= SG_SURF_ZSQCYL)) return;
@@ -322,7 +343,7 @@ __device__ __forceinline__ void surf_explicit_bc(const DSurf& s, double r[3], R 
   }
 }
 
-// transformBC (box_class.f90:430-487, squareCylinder_class.f90:482-544)
+// transformBC (box_class.f90:430-487, squareCylinder_class.f90:482-544); root level, FP64 positions
 template <class R>
 __device__ __forceinline__ void surf_transform_bc(const DSurf& s, double r[3], R u[3]) {
   if (s.type != SG_SURF_BOX && !(s.type >= SG_SURF_XSQCYL && s.type <= SG_SURF_ZSQCYL)) return;
@@ -354,11 +375,14 @@ __device__ __forceinline__ void surf_transform_bc(const DSurf& s, double r[3], R
 }
 
 // ------------------------------------------------------------------ geometry state of one particle
-// Levels are held in registers (MAXL is a compile-time bound >= the geometry's nesting); rotated
-// universes are not supported, so every level shares one direction.
+// Level 1 (the root universe, global coordinates) is held in FP64; the levels below in R: FP64 in the
+// verification form, FP32 local coordinates in the mixed form.  Levels live in registers (MAXL is a
+// compile-time bound >= the geometry's nesting); rotated universes are not supported, so every level
+// shares one direction.
 template <class R, int MAXL>
 struct Coords {
-  double r[MAXL][3];
+  double r0[3];
+  R rl[MAXL > 1 ? MAXL - 1 : 1][3];
   R u[3];
   int uni[MAXL];
   int base[MAXL];    // graph location (0-based) of local cell 1 of the level's universe (uniRootID-1)
@@ -378,11 +402,12 @@ struct Geom {
   __device__ __forceinline__ explicit Geom(const DGeom& gg) : g(gg) {}
 
   // universe%findCell for the universe `u` at local position r
-  __device__ __forceinline__ int find_cell(int u, const double r[3], const R dir[3]) const {
+  template <class T>
+  __device__ __forceinline__ int find_cell(int u, const T r[3], const R dir[3]) const {
     const DUni& U = g.unis[u];
     switch (U.type) {
       case SG_UNI_ROOT:                                          // rootUniverse_class.f90:127-145
-        return surf_halfspace<R>(g.surfs[U.i[0]], r, dir) ? 2 : 1;
+        return surf_halfspace<R, T>(g.surfs[U.i[0]], r, dir) ? 2 : 1;
       case SG_UNI_CELL: {                                        // cellUniverse_class.f90:203-246
         int nc = U.i[1];
         for (int c = 0; c < nc; ++c) {
@@ -390,7 +415,7 @@ struct Geom {
           bool isIt = false;
           for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
             int ss = g.cell_surf[k];
-            bool hs = surf_halfspace<R>(g.surfs[abs(ss) - 1], r, dir);
+            bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir);
             isIt = (hs == (ss > 0));
             if (!isIt) break;
           }
@@ -399,11 +424,11 @@ struct Geom {
         return nc + 1;
       }
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:150-173
-        double rsq = r[0] * r[0] + r[1] * r[1];
-        double mul = ((double)(r[0] * (double)dir[0] + r[1] * (double)dir[1]) >= 0.0) ? -1.0 : 1.0;
+        T rsq = r[0] * r[0] + r[1] * r[1];
+        T mul = ((T)(r[0] * (T)dir[0] + r[1] * (T)dir[1]) >= T(0)) ? T(-1) : T(1);
         int N = U.i[1];
         for (int l = 1; l <= N; ++l)
-          if (rsq < g.pin_rsq[U.i[0] + l - 1] + mul * g.pin_tol[U.i[0] + l - 1]) return l;
+          if (rsq < PIN_RSQ<T>(g, U.i[0] + l - 1) + mul * PIN_TOL<T>(g, U.i[0] + l - 1)) return l;
         return N + 1;
       }
       default: {                                                 // latUniverse_class.f90:270-312
@@ -411,9 +436,10 @@ struct Geom {
         bool out = false;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          ijk[i] = (int)floor((r[i] - U.d[3 + i]) / U.d[i]) + 1;
-          double r_bar = r[i] - U.d[3 + i] - ijk[i] * U.d[i] + 0.5 * U.d[i];
-          if (fabs(r_bar) > U.d[6 + i] && r_bar * (double)dir[i] > 0.0) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
+          const T pitch = UD<T>(U, i), corner = UD<T>(U, 3 + i);
+          ijk[i] = (int)floor((r[i] - corner) / pitch) + 1;
+          T r_bar = r[i] - corner - ijk[i] * pitch + T(0.5) * pitch;
+          if (fabs(r_bar) > UD<T>(U, 6 + i) && r_bar * (T)dir[i] > T(0)) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
           if (ijk[i] <= 0 || ijk[i] > U.i[i]) out = true;
         }
         return out ? U.i[3] : ijk[0] + U.i[0] * (ijk[1] - 1 + U.i[1] * (ijk[2] - 1));
@@ -432,52 +458,54 @@ struct Geom {
   }
 
   // pin annulus k: zCylinder at the origin (pinUniverse_class.f90:114-118)
-  __device__ __forceinline__ R pin_cyl(const DUni& U, int k, const double r[3], const R u[3]) const {
+  template <class T>
+  __device__ __forceinline__ R pin_cyl(const DUni& U, int k, const T r[3], const R u[3]) const {
     const R INF_R = R(D_INF);
-    double c = (r[0] * r[0] + r[1] * r[1]) - g.pin_rsq[U.i[0] + k];
+    T c = (r[0] * r[0] + r[1] * r[1]) - PIN_RSQ<T>(g, U.i[0] + k);
     R kk = R(r[0]) * u[0] + R(r[1]) * u[1];
     R a = R(1) - u[2] * u[2];
     R delta = kk * kk - a * R(c), d;
     if (delta < R(0) || a == R(0)) d = INF_R;
-    else if (fabs(c) < g.pin_tol[U.i[0] + k]) {
+    else if (fabs(c) < PIN_TOL<T>(g, U.i[0] + k)) {
       if (kk >= R(0)) d = INF_R;
       else { d = -kk + dsqrt<R>(delta); d = d / a; }
-    } else if (c < 0.0) { d = -kk + dsqrt<R>(delta); d = d / a; }
+    } else if (c < T(0)) { d = -kk + dsqrt<R>(delta); d = d / a; }
     else { d = -kk - dsqrt<R>(delta); d = d / a; if (d <= R(0)) d = INF_R; }
     return fmin(d, INF_R);
   }
 
   // universe%distance
-  __device__ __forceinline__ void uni_distance(int u, int localID, const double r[3], const R dir[3],
+  template <class T>
+  __device__ __forceinline__ void uni_distance(int u, int localID, const T r[3], const R dir[3],
                                                R& d, int& surfIdx) const {
     const R INF_R = R(D_INF);
     const DUni& U = g.unis[u];
     switch (U.type) {
       case SG_UNI_ROOT:                                          // rootUniverse_class.f90:152-162
         surfIdx = U.i[0] + 1;
-        d = surf_distance<R>(g.surfs[U.i[0]], r, dir);
+        d = surf_distance<R, T>(g.surfs[U.i[0]], r, dir);
         return;
       case SG_UNI_CELL: {                                        // simpleCell_class.f90:120-141
         int cell = g.uni_cells[U.i[0] + localID - 1];
         d = INF_R; surfIdx = 0;
         for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {
           int ss = g.cell_surf[k];
-          R td = surf_distance<R>(g.surfs[abs(ss) - 1], r, dir);
+          R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir);
           if (td < d) { d = td; surfIdx = abs(ss); }
         }
         return;
       }
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:185-226
         int N = U.i[1];
-        R d_out = (localID > N) ? INF_R : pin_cyl(U, localID - 1, r, dir);
-        R d_in = (localID == 1) ? INF_R : pin_cyl(U, localID - 2, r, dir);
+        R d_out = (localID > N) ? INF_R : pin_cyl<T>(U, localID - 1, r, dir);
+        R d_in = (localID == 1) ? INF_R : pin_cyl<T>(U, localID - 2, r, dir);
         if (d_in < d_out) { surfIdx = -1; d = d_in; } else { surfIdx = -2; d = d_out; }
         return;
       }
       default: {                                                 // latUniverse_class.f90:319-373
         if (localID == U.i[3]) {
           surfIdx = -7;
-          d = surf_distance<R>(g.surfs[U.i[4]], r, dir);       // outline box
+          d = surf_distance<R, T>(g.surfs[U.i[4]], r, dir);     // outline box
           return;
         }
         int ijk[3];
@@ -486,9 +514,10 @@ struct Geom {
         int ax = 0;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          double r_bar = r[i] - U.d[3 + i];
-          r_bar = r_bar - (ijk[i] - 0.5) * U.d[i];
-          R bound = sgn(R(U.d[i] * 0.5), dir[i]);
+          const T pitch = UD<T>(U, i);
+          T r_bar = r[i] - UD<T>(U, 3 + i);
+          r_bar = r_bar - (ijk[i] - T(0.5)) * pitch;
+          R bound = sgn(R(pitch * T(0.5)), dir[i]);
           R td = (bound - R(r_bar)) / dir[i];
           if (td < d) { d = td; ax = i; }
         }
@@ -504,15 +533,22 @@ struct Geom {
   }
 
   // universe%cellOffset (latUniverse_class.f90:394-414; zero for the others)
-  __device__ __forceinline__ void cell_offset(int u, int localID, double off[3]) const {
+  template <class T>
+  __device__ __forceinline__ void cell_offset(int u, int localID, T off[3]) const {
     const DUni& U = g.unis[u];
-    off[0] = off[1] = off[2] = 0.0;
+    off[0] = off[1] = off[2] = T(0);
     if (U.type == SG_UNI_LAT && U.i[5] != 0 && localID != U.i[3]) {
       int ijk[3];
       get_ijk(localID, U.i, ijk);
 #pragma unroll
-      for (int i = 0; i < 3; ++i) off[i] = (ijk[i] - 0.5) * U.d[i] + U.d[3 + i];
+      for (int i = 0; i < 3; ++i) off[i] = (ijk[i] - T(0.5)) * UD<T>(U, i) + UD<T>(U, 3 + i);
     }
+  }
+
+  // level-l distance (root level in FP64 positions, lower levels in R)
+  __device__ __forceinline__ void level_distance(const Coords<R, MAXL>& c, int l, R& d, int& s) const {
+    if (l == 0) uni_distance<double>(c.uni[0], c.local[0], c.r0, c.u, d, s);
+    else uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], c.u, d, s);
   }
 
   // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow
@@ -525,40 +561,57 @@ struct Geom {
       if (gf.x >= 0) { c.mat = gf.x; c.uid = gf.y; c.nest = i + 1; return true; }
       if (i + 1 >= MAXL) break;
       int nu = -gf.x - 1;
-      double off[3];
-      cell_offset(c.uni[i], c.local[i], off);
       const DUni& N = g.unis[nu];
+      if (i == 0) {
+        double off[3];
+        cell_offset<double>(c.uni[0], c.local[0], off);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) c.r[i + 1][k] = (c.r[i][k] - off[k]) - N.origin[k];
+        for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+      } else {
+        R off[3];
+        cell_offset<R>(c.uni[i], c.local[i], off);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c.rl[i][k] = (c.rl[i > 0 ? i - 1 : 0][k] - off[k]) - UO<R>(N, k);
+      }
       c.uni[i + 1] = nu;
       c.base[i + 1] = gf.y - 1;
-      c.local[i + 1] = find_cell(nu, c.r[i + 1], c.u);
+      c.local[i + 1] = find_cell<R>(nu, c.rl[i], c.u);
     }
     c.mat = SG_UNDEF_MAT;
     c.nest = MAXL;
     return false;
   }
 
-  // geometryStd%placeCoord (geometryStd_class.f90:119-147): level-1 position is c.r[0] (global;
+  // geometryStd%placeCoord (geometryStd_class.f90:119-147): level-1 position is c.r0 (global;
   // the root universe carries no origin offset)
   __device__ __forceinline__ bool place(Coords<R, MAXL>& c) const {
     c.uni[0] = g.root;
     c.base[0] = 0;
-    c.local[0] = find_cell(g.root, c.r[0], c.u);
+    c.local[0] = find_cell<double>(g.root, c.r0, c.u);
     return dive(c, 0);
   }
 
-  // geometryStd%teleport (geometryStd_class.f90:492-514).  Level 1 holds the global position:
-  // the root universe has no origin offset (checked at upload).
+  // geometryStd%teleport (geometryStd_class.f90:492-514)
   __device__ __forceinline__ bool teleport(Coords<R, MAXL>& c, R dist) const {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c.r[0][k] = c.r[0][k] + (double)dist * (double)c.u[k];
+    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)dist * (double)c.u[k];
     bool ok = place(c);
     if (c.mat == 0) {
-      surf_transform_bc<R>(g.surfs[g.border], c.r[0], c.u);
+      surf_transform_bc<R>(g.surfs[g.border], c.r0, c.u);
       ok = place(c);
     }
     return ok;
+  }
+
+  // moveLocal over levels 1..n (coord_class.f90:346-356)
+  __device__ __forceinline__ void move_levels(Coords<R, MAXL>& c, int n, R d) const {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)d * (double)c.u[k];
+#pragma unroll
+    for (int l = 1; l < MAXL; ++l)
+      if (l < n)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c.rl[l - 1][k] = c.rl[l - 1][k] + d * c.u[k];
   }
 
   // move_withCache / move_noCache (geometryStd_class.f90:214-352); fields absent (fieldDist = INF).
@@ -572,7 +625,7 @@ struct Geom {
     for (int l = 0; l < MAXL; ++l) {
       if (l < c.nest) {
         if (cache.lvl < l + 1) {
-          uni_distance(c.uni[l], c.local[l], c.r[l], c.u, cdist[l], csurf[l]);
+          level_distance(c, l, cdist[l], csurf[l]);
           cache.lvl += 1;
         }
         R td = cdist[l];
@@ -580,29 +633,21 @@ struct Geom {
       }
     }
     if (maxDist < dist) {                                         // collision inside the cell
-#pragma unroll
-      for (int l = 0; l < MAXL; ++l)
-        if (l < c.nest)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)maxDist * (double)c.u[k];
+      move_levels(c, c.nest, maxDist);
       cache.lvl = 0;
       return 1;   // COLL_EV
     }
     if (surfIdx == g.border + 1 && level == 1) {                  // domain boundary
 #pragma unroll
-      for (int k = 0; k < 3; ++k) c.r[0][k] = c.r[0][k] + (double)dist * (double)c.u[k];
+      for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)dist * (double)c.u[k];
       maxDist = dist;
       cache.lvl = 0;
-      surf_explicit_bc<R>(g.surfs[g.border], c.r[0], c.u);
+      surf_explicit_bc<R>(g.surfs[g.border], c.r0, c.u);
       place(c);
       return 2;   // BOUNDARY_EV
     }
     // crossing at `level`
-#pragma unroll
-    for (int l = 0; l < MAXL; ++l)
-      if (l < level)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)dist * (double)c.u[k];
+    move_levels(c, level, dist);
     maxDist = dist;
 #pragma unroll
     for (int l = 0; l < MAXL; ++l) if (l < level - 1) cdist[l] = cdist[l] - dist;
@@ -614,12 +659,19 @@ struct Geom {
         const DUni& U = g.unis[c.uni[l]];
         if (U.type == SG_UNI_PIN) {                               // pinUniverse_class.f90:236-253
           c.local[l] += (surfIdx == -1) ? -1 : 1;
-        } else {
+        } else if (l == 0) {
           if (U.type == SG_UNI_CELL) {                            // cellUniverse_class.f90:388-431
 #pragma unroll
-            for (int k = 0; k < 3; ++k) c.r[l][k] = c.r[l][k] + (double)c.u[k] * g.nudge;
+            for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)c.u[k] * g.nudge;
           }
-          c.local[l] = find_cell(c.uni[l], c.r[l], c.u);
+          c.local[0] = find_cell<double>(c.uni[0], c.r0, c.u);
+        } else {
+          R* rr = c.rl[l > 0 ? l - 1 : 0];
+          if (U.type == SG_UNI_CELL) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) rr[k] = rr[k] + c.u[k] * (R)g.nudge;
+          }
+          c.local[l] = find_cell<R>(c.uni[l], rr, c.u);
         }
       }
     }

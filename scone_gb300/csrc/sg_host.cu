@@ -101,6 +101,7 @@ struct sg_handle_t {
   DArr<DUni> unis64, unisMx;
   DArr<int> uniCells, cellPtr, cellSurf;
   DArr<double> pinRsq, pinTol64, pinTolMx;
+  DArr<float> pinRsqF, pinTolF;
   DArr<int2> graph;
   DGeom g64{}, gMx{};
 
@@ -203,6 +204,8 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
       else if (!curved) for (int i = 0; i < 3; ++i) scale = std::max(scale, std::fabs(s.p[i]) + std::fabs(s.p[3 + i]));
       s.tol = curved ? 2.0 * s.p[3] * SURF_TOL_M : SURF_TOL_M * scale;
     }
+    for (int i = 0; i < SG_SURF_NPAR; ++i) s.pf[i] = (float)s.p[i];
+    s.tolf = (float)s.tol;
     return true;
   };
   for (int i = 0; i < ns; ++i) {
@@ -300,6 +303,8 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
     Um = U;
     if (U.type == SG_UNI_LAT)
       for (int i = 0; i < 3; ++i) Um.d[6 + i] = U.d[i] * 0.5 - U.d[i] * SURF_TOL_M;
+    for (int i = 0; i < 3; ++i) { U.originf[i] = (float)U.origin[i]; Um.originf[i] = (float)Um.origin[i]; }
+    for (int i = 0; i < 9; ++i) { U.f[i] = (float)U.d[i]; Um.f[i] = (float)Um.d[i]; }
     u64[u] = U;
     uMx[u] = Um;
     fills[u] = f;
@@ -355,11 +360,18 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   CK(h->pinRsq.upload(rsq, st));
   CK(h->pinTol64.upload(tol64, st));
   CK(h->pinTolMx.upload(tolMx, st));
+  {
+    std::vector<float> rf(rsq.size()), tf(tolMx.size());
+    for (size_t i = 0; i < rsq.size(); ++i) rf[i] = (float)std::min(rsq[i], 1.0e38);
+    for (size_t i = 0; i < tolMx.size(); ++i) tf[i] = (float)std::min(tolMx[i], 1.0e38);
+    CK(h->pinRsqF.upload(rf, st));
+    CK(h->pinTolF.upload(tf, st));
+  }
   CK(h->graph.upload(graph, st));
   h->g64 = DGeom{h->surfs64.p, h->unis64.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTol64.p, h->graph.p, g->root_uni, g->border_surf, NUDGE};
+                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE};
   h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTolMx.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M};
+                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M};
   h->hasGeom = true;
   // active materials for the majorant
   return SG_OK;
@@ -496,6 +508,8 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
         K.ax_min[i] = d.axes[i].min;
         K.ax_step[i] = (d.axes[i].max - d.axes[i].min) / d.axes[i].n;
         K.ax_inv_step[i] = 1.0 / K.ax_step[i];
+        K.ax_minf[i] = (float)K.ax_min[i];
+        K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
         K.multi[i] = mul;
         mul *= d.axes[i].n;
       }
@@ -732,6 +746,7 @@ int32_t sg_destroy(sg_handle h) {
   for (auto& b : h->bank) b.free();
   h->surfs64.free(); h->surfsMx.free(); h->unis64.free(); h->unisMx.free(); h->uniCells.free();
   h->cellPtr.free(); h->cellSurf.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
+  h->pinRsqF.free(); h->pinTolF.free();
   for (auto& a : h->mgD) a.free();
   for (auto& a : h->mgF) a.free();
   h->fissile.free(); h->acc.free(); h->bin.free(); h->csum.free(); h->csum2.free();

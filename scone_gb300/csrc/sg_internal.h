@@ -8,6 +8,8 @@ namespace sg {
 
 // One surface: 64-bit params as uploaded (plane coefficients normalised), tolerance of the
 // precision form the record was built for, boundary conditions (border surface only).
+// The FP32 copies (pf, tolf) serve the mixed form at nesting levels below the root, where positions
+// are local FP32 coordinates.
 struct DSurf {
   int type;
   int axis;        // aPlane axis / cylinder axis
@@ -16,6 +18,9 @@ struct DSurf {
   int pad[2];
   double p[SG_SURF_NPAR];
   double tol;
+  float pf[SG_SURF_NPAR];
+  float tolf;
+  float padf;
 };
 
 // One universe.  i[] / d[] by type:
@@ -29,6 +34,8 @@ struct DUni {
   int i[7];
   double origin[3];
   double d[9];
+  float originf[3];
+  float f[9];      // FP32 copy of d
 };
 
 struct DGeom {
@@ -39,6 +46,8 @@ struct DGeom {
   const int* cell_surf;
   const double* pin_rsq;
   const double* pin_tol;
+  const float* pin_rsqf;  // FP32 copies (mixed form)
+  const float* pin_tolf;
   const int2* graph;    // geomGraph: x = matIdx (>= 0) or -(uniIdx), y = uniqueID or uniRootID (1-based)
   int root;             // root universe (0-based)
   int border;           // border surface (0-based)
@@ -76,6 +85,8 @@ struct DClerk {
   double ax_min[3];
   double ax_step[3];
   double ax_inv_step[3];
+  float ax_minf[3];
+  float ax_inv_stepf[3];
   long long multi[3];
   long long acc_off;     // offset (0-based) of this clerk's first bin in the launch's acc array
 };

@@ -26,10 +26,10 @@ __global__ void __launch_bounds__(128) k_fission_source(const __grid_constant__ 
   for (int att = 0; att < 10000; ++att) {
     double x0 = rng.get(), x1 = rng.get(), x2 = rng.get();
     Coords<double, MAXL> c;
-    c.r[0][0] = (a.bounds[3] - a.bounds[0]) * x0 + a.bounds[0];
-    c.r[0][1] = (a.bounds[4] - a.bounds[1]) * x1 + a.bounds[1];
-    c.r[0][2] = (a.bounds[5] - a.bounds[2]) * x2 + a.bounds[2];
-    const double rs[3] = {c.r[0][0], c.r[0][1], c.r[0][2]};
+    c.r0[0] = (a.bounds[3] - a.bounds[0]) * x0 + a.bounds[0];
+    c.r0[1] = (a.bounds[4] - a.bounds[1]) * x1 + a.bounds[1];
+    c.r0[2] = (a.bounds[5] - a.bounds[2]) * x2 + a.bounds[2];
+    const double rs[3] = {c.r0[0], c.r0[1], c.r0[2]};
     c.u[0] = 1.0; c.u[1] = 0.0; c.u[2] = 0.0;
     geom.place(c);
     const int mat = c.mat;

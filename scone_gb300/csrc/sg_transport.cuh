@@ -45,16 +45,17 @@ struct Tracker {
   int collN;
   int hist;
   int nsites;
-  double time;
+  R time;            // particle time (MG speed 1: path length); FP32 in the mixed form
   int segs;
-  // k-implicit accumulators (keffImplicitClerk bins IMP_PROD, SCATTER_PROD, IMP_ABS, ANA_LEAK)
-  double kprod, kscat, kabs, kleak;
+  // k-implicit per-thread partial sums (keffImplicitClerk bins IMP_PROD, SCATTER_PROD, IMP_ABS,
+  // ANA_LEAK), in R; the batch sums they are added to are FP64
+  R kprod, kscat, kabs, kleak;
   unsigned long long nEv, nColl;
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
       : A(a), geom(a.geom), mg(a.mg), acc(accp) {
     k_eff = (R)(*a.k_eff);
-    kprod = kscat = kabs = kleak = 0.0;
+    kprod = kscat = kabs = kleak = R(0);
     nEv = nColl = 0;
   }
 
@@ -91,7 +92,7 @@ struct Tracker {
       if (kind <= SG_AXIS_Z) {
         double v = at3(r, kind - 1);
         if constexpr (sizeof(R) == 8) b = (int)floor((v - K.ax_min[a]) / K.ax_step[a]) + 1;
-        else b = (int)floorf((float)(v - K.ax_min[a]) * (float)K.ax_inv_step[a]) + 1;
+        else b = (int)floorf(((float)v - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;
         if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
       } else if (kind == SG_AXIS_GROUP) {
         b = (g >= 1 && g <= K.ax_n[a]) ? g : 0;
@@ -114,7 +115,7 @@ struct Tracker {
       if (K.type == SG_CLERK_COLLISION) {
         if (!K.handle_virtual && virt) continue;
         if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
-        int bin = map_bin(K, c.r[0], G, c.mat);
+        int bin = map_bin(K, c.r0, G, c.mat);
         if (bin == 0) continue;
         R flux = K.handle_virtual ? w / trackXS : w / xs(mg.total, c.mat, G);
         long long at = K.acc_off + (long long)K.width * (bin - 1);
@@ -125,8 +126,8 @@ struct Tracker {
         bool f = mg.fissile[c.mat - 1] != 0;
         R nuF = f ? xs(mg.nuFission, c.mat, G) : R(0);
         R absXS = xs(mg.capture, c.mat, G) + (f ? xs(mg.fission, c.mat, G) : R(0));
-        kprod += (double)(nuF * flux);
-        kabs += (double)(absXS * flux);
+        kprod += nuF * flux;
+        kabs += absXS * flux;
       }
     }
   }
@@ -148,9 +149,9 @@ struct Tracker {
     int slot = atomicAdd(&A.sites.cursor[region], 1);
     if (slot >= A.sites.region_cap) { raise_error(A.ctr, SG_ERR_BANK_OVERFLOW, hist); return; }
     long long i = (long long)region * A.sites.region_cap + slot;
-    A.sites.r[3 * i + 0] = c.r[0][0];
-    A.sites.r[3 * i + 1] = c.r[0][1];
-    A.sites.r[3 * i + 2] = c.r[0][2];
+    A.sites.r[3 * i + 0] = c.r0[0];
+    A.sites.r[3 * i + 1] = c.r0[1];
+    A.sites.r[3 * i + 2] = c.r0[2];
     A.sites.dir[3 * i + 0] = (double)dir[0];
     A.sites.dir[3 * i + 1] = (double)dir[1];
     A.sites.dir[3 * i + 2] = (double)dir[2];
@@ -158,7 +159,7 @@ struct Tracker {
     A.sites.G[i] = gout;
     A.sites.brood[i] = hist;
     A.sites.seq[i] = nsites;
-    A.sites.time[i] = time;
+    A.sites.time[i] = (double)time;
     nsites += 1;
   }
 
@@ -231,7 +232,7 @@ struct Tracker {
     nColl += 1;
     if (A.keff_clerk >= 0 && MT == MT_IESCATTER) {       // keffImplicit reportOutColl (:241-268)
       R sc = fmax(w - preCollW, R(0));
-      if (sc > R(0)) kscat += (double)sc;
+      if (sc > R(0)) kscat += sc;
     }
     return dead;
   }
@@ -239,16 +240,16 @@ struct Tracker {
   __device__ __forceinline__ void start(int h) {
     hist = h;
     const int i = h - 1;
-    c.r[0][0] = A.in.r[3 * i + 0];
-    c.r[0][1] = A.in.r[3 * i + 1];
-    c.r[0][2] = A.in.r[3 * i + 2];
+    c.r0[0] = A.in.r[3 * i + 0];
+    c.r0[1] = A.in.r[3 * i + 1];
+    c.r0[2] = A.in.r[3 * i + 2];
     c.u[0] = (R)A.in.dir[3 * i + 0];
     c.u[1] = (R)A.in.dir[3 * i + 1];
     c.u[2] = (R)A.in.dir[3 * i + 2];
     w = (R)A.in.wgt[i];
     w0 = w;
     G = A.in.G[i];
-    time = A.in.time ? A.in.time[i] : 0.0;
+    time = (R)A.in.time[i];
     rng.s = lcg_skip(A.master, RNG_STRIDE * (long long)h);
     collN = 0;
     nsites = 0;
@@ -276,10 +277,10 @@ struct Tracker {
       R dist, invSig, sigT;
       if (sigmaTrack < Tol<R>::st_void()) { dist = INF_R; invSig = INF_R; sigT = R(0); }
       else { invSig = R(1) / sigmaTrack; dist = -dlog<R>(rng.get()) * invSig; sigT = sigTot; }
-      const double rpre[3] = {c.r[0][0], c.r[0][1], c.r[0][2]};
+      const double rpre[3] = {c.r0[0], c.r0[1], c.r0[2]};
       const int matPre = mat;
       const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0);
-      time = time + (double)dist;
+      time = time + dist;
       nEv += 1;
       report_path(rpre, matPre, dist);
       mat = c.mat;
@@ -302,7 +303,7 @@ struct Tracker {
       const R majInv = R(1) / maj;
       const R dist = -dlog<R>(rng.get()) * majInv;
       if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return true; }
-      time = time + (double)dist;
+      time = time + dist;
       nEv += 1;
       mat = c.mat;
       if (mat == 0) { leak(); return true; }
@@ -319,7 +320,7 @@ struct Tracker {
   }
 
   // reportHist for a leaked particle (keffImplicitClerk ANA_LEAK, :276-290)
-  __device__ __forceinline__ void leak() { if (A.keff_clerk >= 0) kleak += (double)w; }
+  __device__ __forceinline__ void leak() { if (A.keff_clerk >= 0) kleak += w; }
   __device__ __forceinline__ void absorbed() {}
 };
 
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
 
   // flush: keff registers (warp reduce) and the block's score memory
   if (A.keff_clerk >= 0) {
-    double v[4] = {T.kprod, T.kscat, T.kabs, T.kleak};
+    double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
 #pragma unroll
     for (int q = 0; q < 4; ++q)
       for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(FULL, v[q], o);
