@@ -42,8 +42,9 @@ def args_():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--pop", type=int, default=1_000_000)
-    ap.add_argument("--transport", default="st", choices=["st", "dt"])
+    ap.add_argument("--transport", default="st", choices=["st", "dt", "st-nocache"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--form", default="history", choices=["event", "history"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile", action="store_true", help="a short run for ncu captures")
@@ -219,9 +220,10 @@ def main():
     from scone_gb300 import gpu
 
     prec = abi.PREC_MIXED if a.precision == "mixed" else abi.PREC_FP64
-    tr = abi.TRANSPORT_ST if a.transport == "st" else abi.TRANSPORT_DT
+    tr = {"st": abi.TRANSPORT_ST, "dt": abi.TRANSPORT_DT, "st-nocache": abi.TRANSPORT_ST_NOCACHE}[a.transport]
     cap = int(2.5 * a.pop) + 4096
-    t = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=cap, device=local)
+    form = abi.FORM_EVENT if a.form == "event" else abi.FORM_HISTORY
+    t = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=cap, device=local, form=form)
     inact, ia, act, aa = lattice_setup(t, p)
     # replicas: rank r uses the master stream strided by r * pop (SCONE's getOffset sharding)
     master0 = gpu.rng_skip(SEED, 152917 * rank * a.pop)
@@ -314,7 +316,8 @@ def main():
     if tr_info and tr_info.get("bytes_per_event"):
         traffic = tr_info["bytes_per_event"] * ev_per_launch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "peak_source": peak_kind, "kernel": "k_transport (history loop)",
+            "traffic": traffic, "peak_source": peak_kind, "kernel": ("event loop: k_ev_start + k_ev_transit + k_ev_collide + k_ev_transit<tail>"
+                       if a.form == "event" else "k_transport (history loop)"),
             "bytes_per_event": bpe, "events_per_launch": ev_per_launch, "launch_ms": launch_ms}
 
     cpu = None
@@ -339,7 +342,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": "lattice_17x17_7g_eigen", "particles_per_cycle": a.pop, "groups": 7,
                    "lattice": "17x17 pins r=0.54 cm pitch=1.26 cm, reflective box", "transport": a.transport.upper(),
-                   "precision": a.precision, "step": "one active eigenvalue cycle (gen loop + site order + "
+                   "precision": a.precision, "form": a.form, "step": "one active eigenvalue cycle (gen loop + site order + "
                    "tally close + normSize_Repr + k feedback)", "tally": "17x17x7 mesh flux + implicit k",
                    "l2": "per-step working set exceeds L2 (bank 72 MB in, ~80 MB sites, 72 MB ordered, 72 MB normalised)",
                    "parallelism": f"replicas{world}"},

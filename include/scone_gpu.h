@@ -79,6 +79,10 @@ extern "C" {
 #define SG_PREC_FP64       0      /* all-FP64 verification mode                                  */
 #define SG_PREC_MIXED      1      /* FP32 XS/distances/sampling, FP64 positions and tally sums   */
 
+/* execution forms of the gen loop */
+#define SG_FORM_EVENT      0      /* event-based: transit / collision kernels over compacted queues */
+#define SG_FORM_HISTORY    1      /* one persistent history-loop kernel                          */
+
 /* transport operators (transportOperatorFactory_func.f90:48-60) */
 #define SG_TRANSPORT_ST    1      /* transportOperatorST, distance cache on                      */
 #define SG_TRANSPORT_DT    2      /* transportOperatorDT                                         */
@@ -176,6 +180,7 @@ typedef struct sg_config {
   int32_t device;               /* CUDA device ordinal           */
   int32_t max_bank;             /* capacity of each device bank (particles) */
   int32_t record_histories;     /* 1: keep per-history collision counts and end RNG states */
+  int32_t form;                 /* SG_FORM_EVENT (default) or SG_FORM_HISTORY */
 } sg_config;
 
 /* A particle bank as SoA host arrays of SCONE's particleStateData (particle_class.f90:50-65).

@@ -20,6 +20,8 @@ UNI_ROOT, UNI_CELL, UNI_PIN, UNI_LAT = 1, 2, 3, 4
 BC_VACUUM, BC_REFLECTIVE, BC_PERIODIC = 0, 1, 2
 # precision forms
 PREC_FP64, PREC_MIXED = 0, 1
+# execution forms
+FORM_EVENT, FORM_HISTORY = 0, 1
 # transport operators
 TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE = 1, 2, 3
 # clerks
@@ -82,7 +84,7 @@ class PointSourceDesc(C.Structure):
 class Config(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("transport", C.c_int32), ("device", C.c_int32),
-        ("max_bank", C.c_int32), ("record_histories", C.c_int32),
+        ("max_bank", C.c_int32), ("record_histories", C.c_int32), ("form", C.c_int32),
     ]
 
 

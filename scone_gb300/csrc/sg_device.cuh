@@ -545,10 +545,28 @@ struct Geom {
     }
   }
 
+  // Mixed form: the level-2 coordinates are re-derived from the FP64 level-1 position instead of
+  // being accumulated separately in FP32, so both levels see one position wherever their surfaces
+  // coincide (a lattice filling the root box).  The FP64 form accumulates every level as SCONE does.
+  __device__ __forceinline__ void sync_level2(Coords<R, MAXL>& c) const {
+    if constexpr (sizeof(R) == 4 && MAXL > 1) {
+      if (c.nest > 1) {
+        double off[3];
+        cell_offset<double>(c.uni[0], c.local[0], off);
+        const DUni& N = g.unis[c.uni[1]];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+      }
+    }
+  }
+
   // level-l distance (root level in FP64 positions, lower levels in R)
-  __device__ __forceinline__ void level_distance(const Coords<R, MAXL>& c, int l, R& d, int& s) const {
+  __device__ __forceinline__ void level_distance(Coords<R, MAXL>& c, int l, R& d, int& s) const {
     if (l == 0) uni_distance<double>(c.uni[0], c.local[0], c.r0, c.u, d, s);
-    else uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], c.u, d, s);
+    else {
+      if (l == 1) sync_level2(c);
+      uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], c.u, d, s);
+    }
   }
 
   // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow
@@ -629,7 +647,9 @@ struct Geom {
           cache.lvl += 1;
         }
         R td = cdist[l];
-        if ((dist - td) >= dist * Tol<R>::fp_rel()) { dist = td; surfIdx = csurf[l]; level = l + 1; }
+        // geometryStd_class.f90:655,710 tie rule; the mixed form adds an absolute term of a few FP32
+        // ulps of the geometry size so coincident surfaces at different levels resolve to the upper one
+        if ((dist - td) >= dist * Tol<R>::fp_rel() + R(g.tie_abs)) { dist = td; surfIdx = csurf[l]; level = l + 1; }
       }
     }
     if (maxDist < dist) {                                         // collision inside the cell
@@ -666,6 +686,7 @@ struct Geom {
           }
           c.local[0] = find_cell<double>(c.uni[0], c.r0, c.u);
         } else {
+          if (l == 1) sync_level2(c);
           R* rr = c.rl[l > 0 ? l - 1 : 0];
           if (U.type == SG_UNI_CELL) {
 #pragma unroll

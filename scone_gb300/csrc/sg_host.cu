@@ -135,6 +135,11 @@ struct sg_handle_t {
   DArr<DCounters> ctr;
   DArr<int> recColl;
   DArr<unsigned long long> recRng;
+  // event form: particle state (sized for FP64 and 4 levels), queues and their counters
+  DArr<double> pR0, pRl, pU, pW, pW0, pTime, pTrack;
+  DArr<int> pGeo, pInts, qT0, qT1, qC, qCtr;
+  DArr<unsigned long long> pRng;
+  int evIterations = 0;
   int lastN = 0;
   long long launches = 0;      // kernels launched since the last reset (cycle stats)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -368,10 +373,14 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
     CK(h->pinTolF.upload(tf, st));
   }
   CK(h->graph.upload(graph, st));
+  // mixed-form tie tolerance: 16 FP32 ulps of the largest root coordinate
+  double scale = 1.0;
+  for (int i = 0; i < 6; ++i) scale = std::max(scale, std::fabs(h->bounds[i]));
+  const double tie_abs = 16.0 * scale * 0x1p-23;
   h->g64 = DGeom{h->surfs64.p, h->unis64.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE};
+                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0};
   h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M};
+                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs};
   h->hasGeom = true;
   // active materials for the majorant
   return SG_OK;
@@ -460,8 +469,31 @@ int alloc_work(sg_handle h) {
   CK(h->keys.alloc(cap)); CK(h->sel.alloc(2)); CK(h->hist16.alloc(65536));
   CK(h->sumPart.alloc(SUM_BLOCKS)); CK(h->scal.alloc(8)); CK(h->totals.alloc(8)); CK(h->ctr.alloc(1));
   if (h->cfg.record_histories) { CK(h->recColl.alloc(cap)); CK(h->recRng.alloc(cap)); }
+  if (h->cfg.form == SG_FORM_EVENT) {
+    CK(h->pR0.alloc(3 * cap)); CK(h->pRl.alloc(9 * cap)); CK(h->pU.alloc(3 * cap));
+    CK(h->pW.alloc(cap)); CK(h->pW0.alloc(cap)); CK(h->pTime.alloc(cap)); CK(h->pTrack.alloc(cap));
+    CK(h->pGeo.alloc(15 * cap)); CK(h->pInts.alloc(5 * cap)); CK(h->pRng.alloc(cap));
+    CK(h->qT0.alloc(cap)); CK(h->qT1.alloc(cap)); CK(h->qC.alloc(cap)); CK(h->qCtr.alloc(8));
+  }
   CK(cudaMemset(h->scal.p, 0, 8 * sizeof(double)));
   return SG_OK;
+}
+
+template <class R>
+DPart<R> part_view(sg_handle h) {
+  DPart<R> p;
+  p.r0 = h->pR0.p;
+  p.rl = reinterpret_cast<R*>(h->pRl.p);
+  p.u = reinterpret_cast<R*>(h->pU.p);
+  p.geo = h->pGeo.p;
+  p.rng = h->pRng.p;
+  p.w = reinterpret_cast<R*>(h->pW.p);
+  p.w0 = reinterpret_cast<R*>(h->pW0.p);
+  p.time = reinterpret_cast<R*>(h->pTime.p);
+  p.trackXS = reinterpret_cast<R*>(h->pTrack.p);
+  p.ints = h->pInts.p;
+  p.cap = h->cap;
+  return p;
 }
 
 DSites site_view(sg_handle h) {
@@ -560,11 +592,49 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   CK(cudaMemsetAsync(h->histN.p, 0, (size_t)(n + 1) * sizeof(int), s));
   CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), s));
   CK(cudaEventRecord(h->ev[0], s));
-  CK(launch_transport<R>(t, h->maxl, h->cfg.transport == SG_TRANSPORT_DT, smem, s, nullptr));
+  const bool dt = h->cfg.transport == SG_TRANSPORT_DT;
+  if (h->cfg.form == SG_FORM_HISTORY) {
+    CK(launch_transport<R>(t, h->maxl, dt, smem, s, nullptr));
+    h->launches += 1;
+  } else {
+    // event form: start, then transit / collide rounds over compacted queues, then the tail
+    t.use_smem = 0;
+    t.part = part_view<R>(h);
+    int* qc = h->qCtr.p;              // [0] transit count A, [1] transit count B, [2] collision count, [3] work
+    int* qT[2] = {h->qT0.p, h->qT1.p};
+    CK(cudaMemsetAsync(qc, 0, 8 * sizeof(int), s));
+    t.q = DQueues{nullptr, nullptr, qT[0], qc + 0, qc + 3};
+    CK(launch_kind<R>(K_EV_START, t, h->maxl, dt, 0, s, nullptr));
+    int cur = 0, it = 0;
+    const int tail = std::max(4096, n / 64);
+    const int CHUNK = 4;
+    h->launches += 1;
+    while (true) {
+      for (int k = 0; k < CHUNK; ++k, ++it) {
+        CK(cudaMemsetAsync(qc + 2, 0, 2 * sizeof(int), s));
+        t.q = DQueues{qT[cur], qc + cur, h->qC.p, qc + 2, qc + 3};
+        CK(launch_kind<R>(K_EV_TRANSIT, t, h->maxl, dt, 0, s, nullptr));
+        CK(cudaMemsetAsync(qc + (1 - cur), 0, sizeof(int), s));
+        t.q = DQueues{h->qC.p, qc + 2, qT[1 - cur], qc + (1 - cur), qc + 3};
+        CK(launch_kind<R>(K_EV_COLLIDE, t, h->maxl, dt, 0, s, nullptr));
+        cur = 1 - cur;
+        h->launches += 2;
+      }
+      int left = 0;
+      CK(cudaMemcpyAsync(&left, qc + cur, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (left <= tail || it > 4096) break;
+    }
+    CK(cudaMemsetAsync(qc + 3, 0, sizeof(int), s));
+    t.q = DQueues{qT[cur], qc + cur, nullptr, nullptr, qc + 3};
+    CK(launch_kind<R>(K_EV_TAIL, t, h->maxl, dt, 0, s, nullptr));
+    h->launches += 1;
+    h->evIterations = it;
+  }
   CK(cudaEventRecord(h->ev[1], s));
   CK(exclusive_scan(h->histN.p, n + 1, h->start.p, h->scanTmp.p, h->totals.p + 0, s));
   CK(launch_site_scatter(site_view(h), h->start.p, out, outcap, h->totals.p + 3, s));
-  h->launches += 5;
+  h->launches += 4;
   DCounters c;
   int tot[8];
   CK(cudaMemcpyAsync(&c, h->ctr.p, sizeof(c), cudaMemcpyDeviceToHost, s));
@@ -725,6 +795,7 @@ int32_t sg_create(const sg_config* cfg, sg_handle* out) {
   if (cfg->precision != SG_PREC_FP64 && cfg->precision != SG_PREC_MIXED) return SG_ERR_BAD_ARG;
   if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_ST_NOCACHE) return SG_ERR_BAD_ARG;
   if (cfg->max_bank <= 0) return SG_ERR_BAD_ARG;
+  if (cfg->form != SG_FORM_EVENT && cfg->form != SG_FORM_HISTORY) return SG_ERR_BAD_ARG;
   sg_handle h = new sg_handle_t();
   h->cfg = *cfg;
   h->cap = cfg->max_bank;
@@ -754,6 +825,8 @@ int32_t sg_destroy(sg_handle h) {
   h->sCursor.free(); h->histN.free(); h->start.free(); h->scanTmp.free(); h->flags.free(); h->pos.free();
   h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->sumPart.free(); h->scal.free();
   h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
+  h->pR0.free(); h->pRl.free(); h->pU.free(); h->pW.free(); h->pW0.free(); h->pTime.free(); h->pTrack.free();
+  h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(h->stream);
   delete h;

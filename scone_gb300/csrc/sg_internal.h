@@ -52,6 +52,7 @@ struct DGeom {
   int root;             // root universe (0-based)
   int border;           // border surface (0-based)
   double nudge;         // cellUniverse crossing nudge of the precision form
+  double tie_abs;       // absolute part of the tie rule between nesting levels (0 in the FP64 form)
 };
 
 // MG macroscopic data in the working precision R ([mat][G], P0/prod [mat][Gin][Gout])
@@ -129,6 +130,31 @@ struct DCounters {
   int pad;
 };
 
+// Particle state between the event kernels, component-major SoA of capacity `cap` (slot = bank index).
+template <class R>
+struct DPart {
+  double* r0;      // [3][cap]  level-1 (global) position
+  R* rl;           // [3*(MAXL-1)][cap] local positions below the root
+  R* u;            // [3][cap]
+  int* geo;        // [3*MAXL+3][cap] universe, graph base, local ID per level; nesting, material, unique ID
+  unsigned long long* rng;
+  R* w;
+  R* w0;
+  R* time;
+  R* trackXS;
+  int* ints;       // [5][cap] G, collisionN, history, sites written, segments
+  int cap;
+};
+
+// Work queues of the event form: slots of particles awaiting transit or collision.
+struct DQueues {
+  const int* in;
+  const int* n_in;
+  int* out;
+  int* n_out;
+  int* work;       // next entry of `in` to hand out (persistent kernels)
+};
+
 template <class R>
 struct TransportArgs {
   DGeom geom;
@@ -150,6 +176,8 @@ struct TransportArgs {
   DCounters* ctr;
   int use_cache;        // transportOperatorST cache flag
   int max_segments;     // safety limit per history
+  DPart<R> part;        // event form: particle state
+  DQueues q;            // event form: queues of the launch
 };
 
 }  // namespace sg

@@ -4,13 +4,17 @@
 
 namespace sg {
 
+// kernel kinds of the history loop and of the event form
+enum { K_HISTORY = 0, K_EV_START = 1, K_EV_TRANSIT = 2, K_EV_COLLIDE = 3, K_EV_TAIL = 4, K_KINDS = 5 };
+
+template <class R>
+cudaError_t launch_kind(int kind, const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
+                        cudaStream_t s, int* grid_out);
+
 // persistent history-loop kernel; maxl is the compile-time nesting bound (2 or 4)
 template <class R>
 cudaError_t launch_transport(const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
                              cudaStream_t s, int* grid_out);
-// occupancy-derived persistent grid size for a kernel configuration
-template <class R>
-int transport_grid(int maxl, bool dt, size_t smem);
 
 // fissionSource sampling on the device (fissionSource_class.f90:149-271), FP64 arithmetic
 cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank out, int n,

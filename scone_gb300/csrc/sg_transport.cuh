@@ -15,6 +15,7 @@
 namespace sg {
 
 static constexpr unsigned FULL = 0xffffffffu;
+enum { SEG_MORE = 0, SEG_END = 1, SEG_COLLIDE = 2 };
 
 // fates (tallyCodes.f90:23-27)
 enum { FATE_NONE = 5000, FATE_ABS = 5001, FATE_LEAK = 5002 };
@@ -47,6 +48,7 @@ struct Tracker {
   int nsites;
   R time;            // particle time (MG speed 1: path length); FP32 in the mixed form
   int segs;
+  R trackXS;         // tracking XS of the segment that ended in a real collision
   // k-implicit per-thread partial sums (keffImplicitClerk bins IMP_PROD, SCATTER_PROD, IMP_ABS,
   // ANA_LEAK), in R; the batch sums they are added to are FP64
   R kprod, kscat, kabs, kleak;
@@ -264,10 +266,12 @@ struct Tracker {
     if (A.rec_rng) A.rec_rng[hist - 1] = rng.s;
   }
 
-  // One flight segment (and the collision that may end it).  Returns true when the history ended.
-  __device__ __forceinline__ bool step() {
+  // One flight segment of surfaceTracking / deltaTracking.  Returns SEG_MORE (keep tracking),
+  // SEG_END (the history ended: leak or error) or SEG_COLLIDE (a real collision; trackXS holds the
+  // tracking cross section the collision estimators use).
+  __device__ __forceinline__ int segment() {
     const R INF_R = R(D_INF);
-    if (++segs > A.max_segments) { raise_error(A.ctr, SG_ERR_LOST, hist); return true; }
+    if (++segs > A.max_segments) { raise_error(A.ctr, SG_ERR_LOST, hist); return SEG_END; }
     int mat = c.mat;
     if constexpr (!DT) {
       // surfaceTracking (transportOperatorST_class.f90:48-166)
@@ -284,45 +288,149 @@ struct Tracker {
       nEv += 1;
       report_path(rpre, matPre, dist);
       mat = c.mat;
-      if (mat == 0) { leak(); return true; }
+      if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
-        return true;
+        return SEG_END;
       }
       if (ev == 1) {
         if (rng.get() < sigT * invSig) {
           cache.lvl = 0;
-          return collide(sigmaTrack) ? (absorbed(), true) : false;
+          trackXS = sigmaTrack;
+          return SEG_COLLIDE;
         }
         report_in_coll(true, sigmaTrack);
       }
-      return false;
+      return SEG_MORE;
     } else {
       // deltaTracking (transportOperatorDT_class.f90:47-131)
       const R maj = fmax(mg.majorant[G - 1], mg.collisionXS);
       const R majInv = R(1) / maj;
       const R dist = -dlog<R>(rng.get()) * majInv;
-      if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return true; }
+      if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return SEG_END; }
       time = time + dist;
       nEv += 1;
       mat = c.mat;
-      if (mat == 0) { leak(); return true; }
-      if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return false; }
+      if (mat == 0) { leak(); return SEG_END; }
+      if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return SEG_MORE; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
-        return true;
+        return SEG_END;
       }
       const R sigT = xs(mg.total, mat, G);
-      if (rng.get() < sigT * majInv) return collide(maj) ? (absorbed(), true) : false;
+      if (rng.get() < sigT * majInv) { trackXS = maj; return SEG_COLLIDE; }
       report_in_coll(true, maj);
-      return false;
+      return SEG_MORE;
     }
+  }
+
+  // One segment and, when it ends in a real collision, the collision.  True when the history ended.
+  __device__ __forceinline__ bool step() {
+    const int e = segment();
+    if (e == SEG_COLLIDE) return collide(trackXS);
+    return e == SEG_END;
+  }
+
+  // ---- particle state held in device memory between the event kernels (component-major SoA)
+  __device__ __forceinline__ void store(const DPart<R>& P, int i) const {
+    const long long cap = P.cap;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { P.r0[k * cap + i] = c.r0[k]; P.u[k * cap + i] = c.u[k]; }
+#pragma unroll
+    for (int l = 0; l < MAXL - 1; ++l)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) P.rl[(l * 3 + k) * cap + i] = c.rl[l][k];
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) {
+      P.geo[(3 * l + 0) * cap + i] = c.uni[l];
+      P.geo[(3 * l + 1) * cap + i] = c.base[l];
+      P.geo[(3 * l + 2) * cap + i] = c.local[l];
+    }
+    P.geo[(3 * MAXL + 0) * cap + i] = c.nest;
+    P.geo[(3 * MAXL + 1) * cap + i] = c.mat;
+    P.geo[(3 * MAXL + 2) * cap + i] = c.uid;
+    P.rng[i] = rng.s;
+    P.w[i] = w;
+    P.w0[i] = w0;
+    P.time[i] = time;
+    P.trackXS[i] = trackXS;
+    P.ints[0 * cap + i] = G;
+    P.ints[1 * cap + i] = collN;
+    P.ints[2 * cap + i] = hist;
+    P.ints[3 * cap + i] = nsites;
+    P.ints[4 * cap + i] = segs;
+  }
+  __device__ __forceinline__ void load(const DPart<R>& P, int i) {
+    const long long cap = P.cap;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { c.r0[k] = P.r0[k * cap + i]; c.u[k] = P.u[k * cap + i]; }
+#pragma unroll
+    for (int l = 0; l < MAXL - 1; ++l)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c.rl[l][k] = P.rl[(l * 3 + k) * cap + i];
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) {
+      c.uni[l] = P.geo[(3 * l + 0) * cap + i];
+      c.base[l] = P.geo[(3 * l + 1) * cap + i];
+      c.local[l] = P.geo[(3 * l + 2) * cap + i];
+    }
+    c.nest = P.geo[(3 * MAXL + 0) * cap + i];
+    c.mat = P.geo[(3 * MAXL + 1) * cap + i];
+    c.uid = P.geo[(3 * MAXL + 2) * cap + i];
+    rng.s = P.rng[i];
+    w = P.w[i];
+    w0 = P.w0[i];
+    time = P.time[i];
+    trackXS = P.trackXS[i];
+    G = P.ints[0 * cap + i];
+    collN = P.ints[1 * cap + i];
+    hist = P.ints[2 * cap + i];
+    nsites = P.ints[3 * cap + i];
+    segs = P.ints[4 * cap + i];
+    cache.lvl = 0;
   }
 
   // reportHist for a leaked particle (keffImplicitClerk ANA_LEAK, :276-290)
   __device__ __forceinline__ void leak() { if (A.keff_clerk >= 0) kleak += w; }
   __device__ __forceinline__ void absorbed() {}
 };
+
+
+// k-implicit partial sums and event counters of a warp, reduced and added to global memory
+template <class R, int MAXL, bool DT>
+__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, DT>& T, const TransportArgs<R>& A, int lane) {
+  if (A.keff_clerk >= 0) {
+    double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(FULL, v[q], o);
+    if (lane == 0) {
+      long long off = A.clerks[A.keff_clerk].acc_off;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) if (v[q] != 0.0) atomicAdd(A.acc + off + q, v[q]);
+    }
+  }
+  unsigned long long ev = T.nEv, co = T.nColl;
+  for (int o = 16; o > 0; o >>= 1) {
+    ev += __shfl_down_sync(FULL, ev, o);
+    co += __shfl_down_sync(FULL, co, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&A.ctr->events, ev);
+    atomicAdd(&A.ctr->collisions, co);
+  }
+}
+
+// warp-aggregated append to a queue counter: one atomic per warp for the lanes that are active
+__device__ __forceinline__ int warp_append(int* counter) {
+  const unsigned m = __activemask();
+  const int leader = __ffs(m) - 1;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + __popc(m & ((1u << lane) - 1u));
+}
 
 template <class R, int MAXL, bool DT>
 __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ TransportArgs<R> A) {
@@ -364,27 +472,7 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
     }
   }
 
-  // flush: keff registers (warp reduce) and the block's score memory
-  if (A.keff_clerk >= 0) {
-    double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(FULL, v[q], o);
-    if (lane == 0) {
-      long long off = A.clerks[A.keff_clerk].acc_off;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) if (v[q] != 0.0) atomicAdd(A.acc + off + q, v[q]);
-    }
-  }
-  unsigned long long ev = T.nEv, co = T.nColl;
-  for (int o = 16; o > 0; o >>= 1) {
-    ev += __shfl_down_sync(FULL, ev, o);
-    co += __shfl_down_sync(FULL, co, o);
-  }
-  if (lane == 0) {
-    atomicAdd(&A.ctr->events, ev);
-    atomicAdd(&A.ctr->collisions, co);
-  }
+  flush_counters(T, A, lane);
   if (smem) {
     __syncthreads();
     for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) {
@@ -392,6 +480,101 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
       if (v != 0.0) atomicAdd(A.acc + i, v);
     }
   }
+}
+
+
+// ================================================================== event form
+// Histories are started once (k_ev_start), then alternate between the transit kernel (flight
+// segments until a real collision, surface crossings and path/virtual-collision tallies included)
+// and the collision kernel (neutronMGstd physics), each over a compacted queue of particle slots.
+// Every warp in a launch therefore runs one kind of event.  The last few percent of histories are
+// finished by the tail kernel (the history loop over the remaining queue).  Per-history RNG streams
+// make the results independent of this scheduling.
+
+template <class R, int MAXL, bool DT>
+__global__ void __launch_bounds__(128) k_ev_start(const __grid_constant__ TransportArgs<R> A) {
+  Tracker<R, MAXL, DT> T(A, A.acc);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T.start(i + 1);
+    T.store(A.part, i);
+    A.q.out[i] = i;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.q.n_out = A.n;
+}
+
+// TAIL = false: stop at a real collision and queue the particle for k_ev_collide.
+// TAIL = true : run each particle to the end of its history (collisions included).
+template <class R, int MAXL, bool DT, bool TAIL>
+__global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ TransportArgs<R> A) {
+  Tracker<R, MAXL, DT> T(A, A.acc);
+  const int lane = threadIdx.x & 31;
+  const int nIn = *A.q.n_in;
+  bool alive = false, done = false;
+  int slot = -1;
+  int q_next = 0, q_end = 0;
+  while (true) {
+    unsigned need = __ballot_sync(FULL, !alive && !done);
+    while (need) {
+      if (q_next >= q_end) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(A.q.work, 32);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= nIn) {
+          if (!alive) done = true;
+          break;
+        }
+        q_next = base;
+        q_end = min(base + 32, nIn);
+      }
+      const int avail = q_end - q_next;
+      const int rank = __popc(need & ((1u << lane) - 1u));
+      const bool mine = ((need >> lane) & 1u) && rank < avail;
+      if (mine) {
+        slot = A.q.in[q_next + rank];
+        T.load(A.part, slot);
+        alive = true;
+      }
+      q_next += min(__popc(need), avail);
+      need &= ~__ballot_sync(FULL, mine);
+    }
+    if (__all_sync(FULL, !alive)) break;
+    if (alive) {
+      if constexpr (TAIL) {
+        if (T.step()) { T.finish(); alive = false; }
+      } else {
+        const int e = T.segment();
+        if (e == SEG_END) { T.finish(); alive = false; }
+        else if (e == SEG_COLLIDE) {
+          T.store(A.part, slot);
+          A.q.out[warp_append(A.q.n_out)] = slot;
+          alive = false;
+        }
+      }
+    }
+  }
+  flush_counters(T, A, lane);
+}
+
+template <class R, int MAXL, bool DT>
+__global__ void __launch_bounds__(128) k_ev_collide(const __grid_constant__ TransportArgs<R> A) {
+  Tracker<R, MAXL, DT> T(A, A.acc);
+  const int nIn = *A.q.n_in;
+  const int stride = gridDim.x * blockDim.x;
+  const int first = blockIdx.x * blockDim.x + threadIdx.x;
+  const int rounds = (nIn + stride - 1) / stride;      // uniform trip count keeps warps convergent
+  for (int r = 0; r < rounds; ++r) {
+    const int idx = first + r * stride;
+    if (idx < nIn) {
+      const int slot = A.q.in[idx];
+      T.load(A.part, slot);
+      if (T.collide(T.trackXS)) T.finish();
+      else {
+        T.store(A.part, slot);
+        A.q.out[warp_append(A.q.n_out)] = slot;
+      }
+    }
+  }
+  flush_counters(T, A, threadIdx.x & 31);
 }
 
 }  // namespace sg

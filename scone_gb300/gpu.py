@@ -66,11 +66,11 @@ class TransportOperatorGPU:
     """A GPU transport operator for whole banks (the `gen:` loop of SCONE's physics packages)."""
 
     def __init__(self, problem=None, precision=abi.PREC_FP64, transport=abi.TRANSPORT_ST, max_bank=1 << 20,
-                 device=0, record_histories=False):
+                 device=0, record_histories=False, form=abi.FORM_EVENT):
         self.L = load()
         self.h = C.c_void_p()
         self._keep = []
-        cfg = abi.Config(precision, transport, device, max_bank, 1 if record_histories else 0)
+        cfg = abi.Config(precision, transport, device, max_bank, 1 if record_histories else 0, form)
         rc = self.L.sg_create(C.byref(cfg), C.byref(self.h))
         if rc != 0:
             raise SconeGpuError(f"sg_create failed with {rc} (is a CUDA device present?)")

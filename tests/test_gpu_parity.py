@@ -22,9 +22,13 @@ def gpu_mod():
     return gpu
 
 
-def make_pair(gpu, orl, prob, transport=abi.TRANSPORT_ST, precision=abi.PREC_FP64, max_bank=1 << 18):
+FORMS = [abi.FORM_EVENT, abi.FORM_HISTORY]
+
+
+def make_pair(gpu, orl, prob, transport=abi.TRANSPORT_ST, precision=abi.PREC_FP64, max_bank=1 << 18,
+              form=abi.FORM_EVENT):
     g = gpu.TransportOperatorGPU(prob, precision=precision, transport=transport, max_bank=max_bank,
-                                 record_histories=True)
+                                 record_histories=True, form=form)
     o = orl.Oracle(prob, transport=transport)
     return g, o
 
@@ -40,10 +44,11 @@ def test_point_source_bank_bitexact(gpu_mod, oracle_mod):
     np.testing.assert_allclose(bg["dir"], bo["dir"], rtol=0, atol=1e-15)
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
-def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport):
+def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
     p = problems.infinite_medium_2g()
-    g, o = make_pair(gpu_mod, oracle_mod, p, transport)
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
     n = 20000
     bank = o.generate_source(SEED, n)
     ag = g.upload_tally(p.tallies["flux"])
@@ -62,10 +67,11 @@ def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport):
     np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=0)
 
 
-@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
-def test_lattice_fp64_bank_parity(gpu_mod, oracle_mod, transport):
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
+def test_lattice_fp64_bank_parity(gpu_mod, oracle_mod, transport, form):
     p = problems.lattice_17x17_7g()
-    g, o = make_pair(gpu_mod, oracle_mod, p, transport)
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
     n = 4000
     o.eigen_init(n, SEED)
     bank, pop = o.eigen_bank(n)
@@ -107,9 +113,10 @@ def _eigen(t, p, pop, n_in, n_act):
     return np.array(ks), t.keff(aa), t.bins(act)
 
 
-def test_lattice_eigen_fp64_cycles(gpu_mod, oracle_mod):
+@pytest.mark.parametrize("form", FORMS)
+def test_lattice_eigen_fp64_cycles(gpu_mod, oracle_mod, form):
     p = problems.lattice_17x17_7g()
-    g, o = make_pair(gpu_mod, oracle_mod, p)
+    g, o = make_pair(gpu_mod, oracle_mod, p, form=form)
     kg, keg, bg = _eigen(g, p, 3000, 3, 3)
     ko, keo, bo = _eigen(o, p, 3000, 3, 3)
     np.testing.assert_allclose(kg, ko, rtol=1e-10)
@@ -122,11 +129,14 @@ def test_lattice_eigen_fp64_cycles(gpu_mod, oracle_mod):
     np.testing.assert_allclose(bg, bo, rtol=1e-8, atol=1e-300)
 
 
-def test_lattice_mixed_vs_fp64_statistics(gpu_mod):
+@pytest.mark.parametrize("form,transport", [(abi.FORM_EVENT, abi.TRANSPORT_ST), (abi.FORM_HISTORY, abi.TRANSPORT_ST),
+                                            (abi.FORM_HISTORY, abi.TRANSPORT_ST_NOCACHE),
+                                            (abi.FORM_HISTORY, abi.TRANSPORT_DT)])
+def test_lattice_mixed_vs_fp64_statistics(gpu_mod, form, transport):
     p = problems.lattice_17x17_7g()
     res = {}
     for prec in (abi.PREC_FP64, abi.PREC_MIXED):
-        t = gpu_mod.TransportOperatorGPU(p, precision=prec, max_bank=1 << 19)
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, max_bank=1 << 19, form=form, transport=transport)
         ks, (k, sd), bins = _eigen(t, p, 100000, 5, 10)
         res[prec] = (k, sd, bins)
     k64, s64, b64 = res[abi.PREC_FP64]
@@ -141,9 +151,10 @@ def test_lattice_mixed_vs_fp64_statistics(gpu_mod):
     assert abs(z.mean()) < 0.2 and z.std() < 1.3, (z.mean(), z.std())
 
 
-def test_fixed_source_device_cycle_matches_oracle(gpu_mod, oracle_mod):
+@pytest.mark.parametrize("form", FORMS)
+def test_fixed_source_device_cycle_matches_oracle(gpu_mod, oracle_mod, form):
     p = problems.infinite_medium_2g()
-    g, o = make_pair(gpu_mod, oracle_mod, p)
+    g, o = make_pair(gpu_mod, oracle_mod, p, form=form)
     ag = g.upload_tally(p.tallies["flux"])
     ao = o.upload_tally(p.tallies["flux"])
     mg = mo = 4242
