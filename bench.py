@@ -42,7 +42,8 @@ def args_():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--pop", type=int, default=1_000_000)
-    ap.add_argument("--transport", default="st", choices=["st", "dt", "st-nocache"])
+    ap.add_argument("--transport", default="dt", choices=["st", "dt", "st-nocache"])
+    ap.add_argument("--no-alt", action="store_true", help="skip the second transport operator measurement")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--form", default="history", choices=["event", "history"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -130,12 +131,12 @@ def lattice_setup(t, p):
     return inact, ia, act, aa
 
 
-def cpu_rate(p, pop_bank, threads, target_s=10.0, max_hist=2_000_000):
+def cpu_rate(p, pop_bank, threads, target_s=10.0, max_hist=2_000_000, transport=None):
     """Histories/s of the oracle's OpenMP gen loop on the host cores over a bounded sample: the
     bank is transported repeatedly (fresh RNG streams) until about target_s seconds have passed."""
     from oracle import oracle
     from scone_gb300 import abi
-    o = oracle.Oracle(p, transport=abi.TRANSPORT_ST)
+    o = oracle.Oracle(p, transport=abi.TRANSPORT_ST if transport is None else transport)
     adm = o.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
     n = min(max_hist, len(pop_bank["wgt"]))
     bank = abi.HostBank(n, {k: v[:n] for k, v in pop_bank.items()})
@@ -165,7 +166,8 @@ def reference_arm(a, p):
     from oracle import oracle
     from scone_gb300 import abi
     threads = os.cpu_count() or 1
-    o = oracle.Oracle(p, transport=abi.TRANSPORT_ST)
+    tr = {"st": abi.TRANSPORT_ST, "dt": abi.TRANSPORT_DT, "st-nocache": abi.TRANSPORT_ST_NOCACHE}[a.transport]
+    o = oracle.Oracle(p, transport=tr)
     o.eigen_init(a.pop, SEED)
     bank, pop = o.eigen_bank(a.pop)
     bd = host_bank_dict(bank, pop)
@@ -188,7 +190,7 @@ def reference_arm(a, p):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "events_per_s": ev / tot,
         "config": {"workload": "lattice_17x17_7g_eigen", "particles_per_cycle": n, "groups": 7,
-                   "lattice": "17x17 pins r=0.54 pitch=1.26", "transport": "ST",
+                   "lattice": "17x17 pins r=0.54 pitch=1.26", "transport": a.transport.upper(),
                    "reference": "C++ restatement of SCONE's algorithm (oracle/); SCONE is Fortran and no "
                                 "Fortran compiler exists here"},
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
@@ -289,6 +291,27 @@ def main():
                "h2d_bytes_per_step": pop * (24 + 24 + 8 + 4 + 8),
                "d2h_bytes_per_step": int(d2h / a.steps), "ms_per_step": 1e3 * we / a.steps}
 
+    # the other transport operator of config 1 ("surface tracking vs delta tracking"), same K steps
+    alt = None
+    if not a.no_alt and world == 1:
+        tr2 = abi.TRANSPORT_ST if tr == abi.TRANSPORT_DT else abi.TRANSPORT_DT
+        t2 = gpu.TransportOperatorGPU(p, precision=prec, transport=tr2, max_bank=cap, device=local, form=form)
+        i2, ia2, a2, aa2 = lattice_setup(t2, p)
+        t2.eigen_init(a.pop, master0)
+        for _ in range(warm):
+            t2.eigen_cycle(i2, ia2)
+        c2 = e2 = h2 = 0.0
+        k2 = None
+        for _ in range(a.steps):
+            st = t2.eigen_cycle(a2, aa2)
+            c2 += st.cycle_ms
+            e2 += st.n_events
+            h2 += st.n_histories
+            k2 = st.k_new
+        alt = {"transport": "ST" if tr2 == abi.TRANSPORT_ST else "DT", "value": h2 / (c2 / 1e3),
+               "unit": "histories/s", "events_per_s": e2 / (c2 / 1e3), "ms_per_step": c2 / a.steps, "k_eff": k2}
+        t2.close()
+
     # max over ranks of the device time; histories summed over ranks
     sec = cyc_ms / 1e3
     if pg:
@@ -326,7 +349,7 @@ def main():
             bank, pop = t.eigen_bank(min(a.pop, 400000))
             bd = host_bank_dict(bank, min(pop, 400000))
             threads = os.cpu_count() or 1
-            rate, erate, n, dt = cpu_rate(p, bd, threads)
+            rate, erate, n, dt = cpu_rate(p, bd, threads, transport=tr)
             cpu = {"value": rate, "unit": "histories/s", "cores": threads, "kind": "port",
                    "sample": f"{n} histories (lattice bank of {min(pop, 400000)} transported repeatedly), "
                              f"{dt:.1f} s, OpenMP over histories",
@@ -348,6 +371,7 @@ def main():
                    "parallelism": f"replicas{world}"},
         "events_per_s": events / sec, "k_eff": ks[-1], "wall_ms_per_step": 1e3 * wall / a.steps,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "other_transport": alt,
     }
     print(json.dumps(line), flush=True)
     if pg:
