@@ -278,6 +278,26 @@ int32_t sg_eigen_get_bank(sg_handle h, sg_bank* out, int32_t cap, int32_t* pop);
 int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* master_state,
                               sg_cycle_stats* stats);
 
+/* ---------------------------------------------------------------- gen loop without allocation */
+
+/* No counterpart in SCONE.  The gen loop of sg_transport_bank for callers that cannot allocate
+ * device memory when a cycle runs: code recorded into a CUDA graph (a plain cudaMalloc is not
+ * allowed during stream capture), programs whose device memory belongs to another allocator or
+ * pool, real-time sections that must stay out of the driver's allocator.  The banks are the
+ * caller's device arrays (dev_in: r, dir, wgt, G, time; dev_next: every array, capacity next_cap);
+ * the handle must already hold the geometry, data and tallies.  It calls no cudaMalloc/cudaFree:
+ * its scratch (site staging, per-history counts, scan sums, counters, k) is one static device array
+ * of 3 MiB that every GPU loading the library holds until exit, which limits a call to
+ * SG_NOALLOC_MAX_HISTORIES histories and SG_NOALLOC_MAX_SITES fission sites (larger n is rejected
+ * with SG_ERR_BAD_ARG).  The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  All calls share the array: calls that overlap on the GPU race.
+ * Returns the number of sites written in *n_next; results are those of sg_transport_bank. */
+#define SG_NOALLOC_MAX_HISTORIES 16384
+#define SG_NOALLOC_MAX_SITES     32768
+int32_t sg_transport_bank_noalloc(sg_handle h, int32_t admin, const sg_bank* dev_in, int32_t n,
+                                  uint64_t master_state, double k_eff, sg_bank* dev_next,
+                                  int32_t next_cap, int32_t* n_next);
+
 /* ---------------------------------------------------------------- verification records */
 
 /* Per-history records of the last gen loop (needs cfg.record_histories): number of real

@@ -21,6 +21,7 @@ UNITS = {
     "sg_tr_mixed.cu": [],
     "sg_support.cu": ["-fmad=false"],
     "sg_host.cu": ["-fmad=false"],
+    "sg_noalloc.cu": ["-fmad=false"],
 }
 
 

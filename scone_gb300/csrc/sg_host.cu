@@ -15,6 +15,7 @@
 #include "sg_device.cuh"
 #include "sg_launch.h"
 #include "sg_support.h"
+#include "sg_noalloc.h"
 
 using namespace sg;
 
@@ -785,6 +786,36 @@ int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
 }
 
 }  // namespace
+
+// Bridge for sg_transport_bank_noalloc (sg_noalloc.cu): the launch arguments that do not depend on
+// the call.  Reads the handle only; allocates nothing.
+int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<double>* t64, TransportArgs<float>* t32,
+                     long long* lo) {
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
+  if (admin < 0 || admin >= (int)h->admins.size()) return h->fail(SG_ERR_BAD_ARG, "bad tally admin");
+  v->stream = h->stream;
+  v->precision = h->cfg.precision;
+  v->transport = h->cfg.transport;
+  v->maxl = h->maxl;
+  v->err = &h->err;
+  std::memset(t64, 0, sizeof(*t64));
+  std::memset(t32, 0, sizeof(*t32));
+  long long hi = 0;
+  int rc = build_clerks<double>(h, admin, *t64, *lo, hi);
+  if (rc) return rc;
+  rc = build_clerks<float>(h, admin, *t32, *lo, hi);
+  if (rc) return rc;
+  t64->geom = h->g64;
+  t64->mg = h->mg64;
+  t32->geom = h->gMx;
+  t32->mg = h->mgMx;
+  t64->acc = h->acc.p + *lo;
+  t32->acc = h->acc.p + *lo;
+  t64->acc_n = t32->acc_n = (int)(hi - *lo);
+  t64->use_cache = t32->use_cache = h->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
+  t64->max_segments = t32->max_segments = 1000000;
+  return SG_OK;
+}
 
 // ====================================================================== C ABI
 extern "C" {

@@ -50,6 +50,7 @@ def load(build=True):
         "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
         "sg_rng_draws": (i32, [P(u64), P(f64), i32]), "sg_rng_skip": (u64, [u64, i64]),
+        "sg_transport_bank_noalloc": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(i32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
