@@ -281,9 +281,9 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
 /* ---------------------------------------------------------------- gen loop without allocation */
 
 /* No counterpart in SCONE.  The gen loop of sg_transport_bank for callers that cannot allocate
- * device memory when a cycle runs: code recorded into a CUDA graph (a plain cudaMalloc is not
- * allowed during stream capture), programs whose device memory belongs to another allocator or
- * pool, real-time sections that must stay out of the driver's allocator.  The banks are the
+ * device memory when a cycle runs: programs whose device memory belongs to another allocator or
+ * to a pool reserved up front (cudaMalloc would go around it or fail once the pool holds the GPU),
+ * and real-time sections that must stay out of the driver's allocator, whose calls can block.  The banks are the
  * caller's device arrays (dev_in: r, dir, wgt, G, time; dev_next: every array, capacity next_cap);
  * the handle must already hold the geometry, data and tallies.  It calls no cudaMalloc/cudaFree:
  * its scratch (site staging, per-history counts, scan sums, counters, k) is one static device array

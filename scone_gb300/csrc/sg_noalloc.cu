@@ -1,10 +1,10 @@
 // sg_noalloc.cu -- sg_transport_bank_noalloc: the gen loop for callers that cannot allocate device
 // memory.
 //
-// Some callers cannot call cudaMalloc at the point where they run a cycle: code recorded into a
-// CUDA graph (a plain cudaMalloc is not allowed during stream capture), host programs whose device
-// memory is owned by another allocator or pool, and real-time sections that must not enter the
-// driver's allocator.  For them this entry point runs the history-loop kernel on banks the caller
+// Some callers cannot call cudaMalloc at the point where they run a cycle: host programs whose
+// device memory is owned by another allocator or by a pool reserved up front (a cudaMalloc would
+// bypass it, or fail once the pool holds the GPU's memory), and real-time sections that must not
+// enter the driver's allocator, whose calls can block.  For them this entry point runs the history-loop kernel on banks the caller
 // already holds in device memory and keeps all of its per-call scratch (fission-site staging,
 // per-history site counts, scan partial sums, counters, k) in one file-scope static __device__
 // array.  The handle (geometry, nuclear data, tallies) must have been set up beforehand.

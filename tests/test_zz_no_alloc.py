@@ -1,7 +1,8 @@
 """sg_transport_bank_noalloc: the gen loop for callers that cannot allocate device memory.
 
-Callers recording a CUDA graph, callers whose device memory belongs to another allocator and
-real-time sections cannot call cudaMalloc while a cycle runs.  This entry point keeps its scratch in
+Callers whose device memory belongs to another allocator or to a pool reserved up front, and
+real-time sections that must not block in the driver's allocator, cannot call cudaMalloc while a
+cycle runs.  This entry point keeps its scratch in
 a static device array and works on banks the caller already holds on the device.  The test checks
 that two calls in a row (the second one sees the first call's leftovers in the shared scratch) give
 the fission bank of the allocating entry point, sg_transport_bank, within the parity tolerances.
