@@ -93,6 +93,8 @@ extern "C" {
 #define SG_CLERK_TRACK          2 /* trackClerk_class.f90                                        */
 #define SG_CLERK_KEFF_ANALOG    3 /* keffAnalogClerk_class.f90  (3 bins)                         */
 #define SG_CLERK_KEFF_IMPLICIT  4 /* keffImplicitClerk_class.f90 (5 bins)                        */
+#define SG_CLERK_SURFACE_CURRENT 5 /* no SCONE counterpart: weight crossing planes normal to an axis,
+                                      bins [plane][map bin][direction -,+] (direction fastest)     */
 
 /* tally map axes (Tallies/TallyMaps) */
 #define SG_AXIS_X          1      /* spaceMap axis x, lin grid                                   */
@@ -100,6 +102,8 @@ extern "C" {
 #define SG_AXIS_Z          3
 #define SG_AXIS_GROUP      4      /* MG group axis (no SCONE counterpart: energyMap maps MG to 0) */
 #define SG_AXIS_MATERIAL   5      /* materialMap over 1..n                                       */
+#define SG_AXIS_ENERGY     6      /* energyMap, log grid over [min,max] (energyMap_class.f90:278-293,
+                                     grid_class.f90:76-90,164-166); MG particles map to 0        */
 
 /* tally responses: 0 = fluxResponse, otherwise a macroResponse MT (endfConstants.f90:116-130) */
 #define SG_RESP_FLUX       0
@@ -140,6 +144,29 @@ typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN =
   double         avg_dist;      /* `avgDist`; <= 0 means none   */
 } sg_mg_desc;
 
+/* Continuous-energy neutron data: the part of aceNeutronDatabase / aceNeutronNuclide /
+ * ceNeutronMaterial the tracking cycle reads (aceNeutronNuclide_class.f90:44-51,342-453,
+ * aceNeutronDatabase_class.f90:346-808,1330-1621, ceNeutronMaterial_class.f90:338-455).
+ * Nuclides are non-fissile with elastic scattering isotropic in the CM frame and no inelastic
+ * channels (the ESZ-block data of an ACE card: energy grid, total, elastic, absorption). */
+typedef struct sg_ce_desc {
+  int32_t        n_nuc;
+  const int64_t* nuc_ptr;       /* [n_nuc+1] offsets of each nuclide's points in e / xs           */
+  const double*  e;             /* energy grids [MeV], ascending per nuclide                      */
+  const double*  xs;            /* [point][4] mainData order: total, elastic, inelastic, capture [b] */
+  const double*  A;             /* [n_nuc] mass ratio AW (neutron masses)                         */
+  const double*  kT;            /* [n_nuc] nuclide temperature kT [MeV]                           */
+  int32_t        n_mat;
+  const int32_t* mat_ptr;       /* [n_mat+1] into mat_nuc / mat_dens                              */
+  const int32_t* mat_nuc;       /* 0-based nuclide index, in composition order                    */
+  const double*  mat_dens;      /* atom density [1/(barn cm)]                                     */
+  int32_t        majorant;      /* 1: unionised majorant grid (aceNeutronDatabase `majorant`, default) */
+  double         min_e, max_e;  /* neutronCEstd minEnergy / maxEnergy (1e-11, 20)                 */
+  double         thresh_e;      /* neutronCEstd energyThreshold (400)                              */
+  double         thresh_a;      /* neutronCEstd massThreshold (1)                                  */
+  double         avg_dist;      /* `avgDist`; <= 0 means none                                     */
+} sg_ce_desc;
+
 typedef struct sg_axis_desc {
   int32_t kind;                 /* SG_AXIS_*                    */
   int32_t n;                    /* number of bins               */
@@ -155,6 +182,9 @@ typedef struct sg_clerk_desc {
   sg_axis_desc axes[3];
   int32_t      filter_g_top;    /* energyFilter for MG: pass if g_top <= G <= g_low; 0 = no filter */
   int32_t      filter_g_low;
+  int32_t      current_axis;    /* SG_CLERK_SURFACE_CURRENT: SG_AXIS_X/Y/Z normal of the planes */
+  int32_t      n_planes;        /* SG_CLERK_SURFACE_CURRENT: 1..8 plane positions          */
+  double       planes[8];
 } sg_clerk_desc;
 
 typedef struct sg_tally_desc {  /* tallyAdmin_class.f90:162-255 */
@@ -172,6 +202,7 @@ typedef struct sg_point_source_desc {  /* pointSource_class.f90:189-270, MG */
   int32_t G;                    /* used when n_prob_g == 0       */
   int32_t n_prob_g;
   const double* prob_g;         /* [n_prob_g]                    */
+  double  E;                    /* CE source energy [MeV] (pointSource `E`), ignored for MG */
 } sg_point_source_desc;
 
 typedef struct sg_config {
@@ -192,6 +223,7 @@ typedef struct sg_bank {
   int32_t* G;                   /* [n]    */
   double*  time;                /* [n]    */
   int32_t* brood_id;            /* [n]    */
+  double*  E;                   /* [n] CE energy [MeV]; NULL for MG problems */
 } sg_bank;
 
 typedef struct sg_cycle_stats {
@@ -224,6 +256,9 @@ int32_t sg_last_error(sg_handle h, char* buf, size_t len);
 int32_t sg_upload_geometry(sg_handle h, const sg_geometry_desc* g);
 /* baseMgNeutronDatabase%init + activate/initMajorant: baseMgNeutronDatabase_class.f90:340-503 */
 int32_t sg_upload_mg(sg_handle h, const sg_mg_desc* mg);
+/* aceNeutronDatabase%init + activate/initMajorant (aceNeutronDatabase_class.f90:873-1163,1291-1323): the
+ * handle becomes a continuous-energy problem (replaces sg_upload_mg; banks carry E, not G). */
+int32_t sg_upload_ce(sg_handle h, const sg_ce_desc* ce);
 /* tallyAdmin%init: tallyAdmin_class.f90:162-255; returns an admin id */
 int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out);
 /* tallyAdmin%push: tallyAdmin_class.f90 (attachment receives every report first) */

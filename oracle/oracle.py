@@ -64,6 +64,11 @@ def lib():
             "or_scoremem_close": (i32, [vp, f64]), "or_scoremem_reduce": (i32, [vp]),
             "or_scoremem_closebin": (i32, [vp, f64, i64]), "or_scoremem_closecycle": (i32, [vp, f64]), "or_scoremem_result": (i32, [vp, i64, i32, P(f64), P(f64)]),
             "or_timed_gen_loop": (i64, [vp, i32, P(abi.Bank), i32, u64, f64, i32, P(i64)]),
+            "or_upload_ce": (i32, [vp, P(abi.CEDesc)]),
+            "or_ce_micro": (i32, [vp, i32, f64, P(f64)]), "or_ce_mat_total": (i32, [vp, i32, f64, P(f64)]),
+            "or_ce_majorant": (i32, [vp, f64, P(f64)]), "or_ce_union_size": (i32, [vp, P(i64)]),
+            "or_asymptotic_scatter": (i32, [f64, f64, f64, P(f64)]),
+            "or_target_velocity": (i32, [f64, P(f64), f64, f64, P(u64), P(f64)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -89,6 +94,8 @@ class Oracle:
             self.upload_geometry(problem.geometry)
             if problem.mg is not None:
                 self.upload_mg(problem.mg)
+            if getattr(problem, "ce", None) is not None:
+                self.upload_ce(problem.ce)
             if problem.source:
                 self.set_point_source(**problem.source)
 
@@ -120,6 +127,31 @@ class Oracle:
         self._keep.append(keep)
         self._check(self.L.or_upload_mg(self.h, C.byref(s)))
 
+    def upload_ce(self, d):
+        s, keep = abi.ce_struct(d)
+        self._keep.append(keep)
+        self._check(self.L.or_upload_ce(self.h, C.byref(s)))
+
+    def ce_micro(self, nuc, E):
+        out = np.zeros(4)
+        self._check(self.L.or_ce_micro(self.h, nuc, E, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def ce_mat_total(self, mat, E):
+        v = C.c_double()
+        self._check(self.L.or_ce_mat_total(self.h, mat, E, C.byref(v)))
+        return v.value
+
+    def ce_majorant(self, E):
+        v = C.c_double()
+        self._check(self.L.or_ce_majorant(self.h, E, C.byref(v)))
+        return v.value
+
+    def ce_union_size(self):
+        n = C.c_int64()
+        self._check(self.L.or_ce_union_size(self.h, C.byref(n)))
+        return n.value
+
     def upload_tally(self, clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
         t, arr = abi.tally_struct(clerks, batch_size, norm_clerk, norm_val)
         self._keep.append(arr)
@@ -130,8 +162,8 @@ class Oracle:
     def attach_tally(self, admin, atch):
         self._check(self.L.or_attach_tally(self.h, admin, atch))
 
-    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
-        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g)
+    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None, E=0.0):
+        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g, E)
         self._keep.append((s, keep))
         self._check(self.L.or_set_point_source(self.h, C.byref(s)))
 
@@ -325,3 +357,17 @@ class ScoreMemory:
             self.L.or_scoremem_free(self.h)
         except Exception:
             pass
+
+
+def asymptotic_scatter(E, mu, A):
+    out = np.zeros(2)
+    lib().or_asymptotic_scatter(E, mu, A, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out[0], out[1]
+
+
+def target_velocity(E, d, A, kT, state):
+    d, dp = _d(d)
+    s = C.c_uint64(state)
+    v = np.zeros(3)
+    lib().or_target_velocity(E, dp, A, kT, C.byref(s), v.ctypes.data_as(C.POINTER(C.c_double)))
+    return v, s.value

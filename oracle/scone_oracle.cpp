@@ -853,6 +853,208 @@ struct MGData {
   double T(int m, int g) const { return total[(size_t)(m - 1) * nG + (g - 1)]; }
 };
 
+// ---------------------------------------------------------------- continuous-energy data
+// genericProcedures.f90:132-166 binaryFloorIdxClosed_Real: 1-based floor index of v in a(1:N);
+// v == a(N) gives N-1; <= 0 when v is outside [a(1), a(N)] or the search does not end in 70 steps.
+static int binaryFloorIdx(const double* a, int N, double v) {
+  int bottom = 1, top = N;
+  if (v < a[bottom - 1] || v > a[top - 1]) return -1;
+  for (int i = 1; i <= 70; ++i) {
+    int idx = (top + bottom) / 2;
+    if (bottom == idx) return idx;
+    if (a[idx - 1] <= v) bottom = idx;
+    else top = idx;
+  }
+  return -2;
+}
+
+static const double neutronMass = 939.56542194;     // universalVariables.f90:90
+static const double lightSpeed = 2.99792458e10;     // universalVariables.f90:91
+static const double SQRT_PI = std::sqrt(PI);        // numPrecision.f90:24
+static const double MAJ_NUDGE = 1.0e-06;            // aceNeutronDatabase_class.f90:1345
+
+// aceNeutronNuclide (aceNeutronNuclide_class.f90:44-51,116): eGrid and mainData(TOTAL, ESCATTER,
+// IESCATTER, CAPTURE) of a non-fissile nuclide
+struct CENuclide {
+  std::vector<double> e;
+  std::vector<double> d;   // [N][4]
+  int N = 0;
+  double A = 1.0, kT = 0.0;
+  // search (:342-359): floor index (1-based) and interpolation factor
+  bool search(double E, int& idx, double& f) const {
+    idx = binaryFloorIdx(e.data(), N, E);
+    if (idx <= 0) return false;
+    double E_top = e[idx], E_low = e[idx - 1];
+    f = (E - E_low) / (E_top - E_low);
+    return true;
+  }
+  // totalXS / microXSs (:374-453): xs(idx+1)*f + (1-f)*xs(idx)
+  double interp(int idx, double f, int k) const { return d[(size_t)idx * 4 + k] * f + (1.0 - f) * d[(size_t)(idx - 1) * 4 + k]; }
+};
+
+struct CEMaterial {
+  std::vector<int> nuc;      // 0-based
+  std::vector<double> dens;
+};
+
+struct CEData {
+  std::vector<CENuclide> nucs;
+  std::vector<CEMaterial> mats;
+  double eBounds[2] = {0, 0};
+  bool hasMajorant = true;
+  std::vector<double> eGridUnion, majorant;
+  std::vector<int> activeMat;   // 1-based
+  double minE = 1.0e-11, maxE = 20.0, threshE = 400.0, threshA = 1.0, collisionXS = 0.0;
+
+  int build(const sg_ce_desc* d, std::string& err) {
+    nucs.assign(d->n_nuc, CENuclide());
+    for (int i = 0; i < d->n_nuc; ++i) {
+      CENuclide& n = nucs[i];
+      int64_t a = d->nuc_ptr[i], b = d->nuc_ptr[i + 1];
+      n.N = (int)(b - a);
+      if (n.N < 2) { err = "nuclide grid needs >= 2 points"; return -1; }
+      n.e.assign(d->e + a, d->e + b);
+      n.d.assign(d->xs + 4 * a, d->xs + 4 * b);
+      n.A = d->A[i]; n.kT = d->kT[i];
+    }
+    mats.assign(d->n_mat, CEMaterial());
+    for (int m = 0; m < d->n_mat; ++m)
+      for (int k = d->mat_ptr[m]; k < d->mat_ptr[m + 1]; ++k) {
+        mats[m].nuc.push_back(d->mat_nuc[k]);
+        mats[m].dens.push_back(d->mat_dens[k]);
+      }
+    // energy bounds over all nuclides (aceNeutronDatabase_class.f90:1043-1052)
+    eBounds[0] = nucs[0].e[0]; eBounds[1] = nucs[0].e[nucs[0].N - 1];
+    for (size_t i = 1; i < nucs.size(); ++i) {
+      eBounds[0] = std::max(eBounds[0], nucs[i].e[0]);
+      eBounds[1] = std::min(eBounds[1], nucs[i].e[nucs[i].N - 1]);
+    }
+    hasMajorant = d->majorant != 0;
+    minE = d->min_e; maxE = d->max_e; threshE = d->thresh_e; threshA = d->thresh_a;
+    collisionXS = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
+    return 0;
+  }
+
+  // updateTotalNucXS (aceNeutronDatabase_class.f90:702-727) without URR / S(a,b)
+  bool nucTotal(int n, double E, double& xs) const {
+    int idx; double f;
+    if (!nucs[n].search(E, idx, f)) return false;
+    xs = nucs[n].interp(idx, f, 0);
+    return true;
+  }
+  // updateTotalMatXS (:517-570): sum over the composition in order, times densityFactor 1
+  bool matTotal(int m, double E, double& total) const {
+    const CEMaterial& M = mats[m - 1];
+    total = 0.0;
+    for (size_t i = 0; i < M.nuc.size(); ++i) {
+      double s;
+      if (!nucTotal(M.nuc[i], E, s)) return false;
+      total = total + M.dens[i] * s;
+    }
+    total = total * 1.0;
+    return true;
+  }
+  // updateMajorantXS (:346-394)
+  bool majorantXS(double E, double& xs) const {
+    if (hasMajorant) {
+      int idx = binaryFloorIdx(eGridUnion.data(), (int)eGridUnion.size(), E);
+      if (idx <= 0) return false;
+      double E_top = eGridUnion[idx], E_low = eGridUnion[idx - 1];
+      double f = (E - E_low) / (E_top - E_low);
+      xs = majorant[idx] * f + (1.0 - f) * majorant[idx - 1];
+      return true;
+    }
+    xs = 0.0;
+    for (int m : activeMat) {
+      double t;
+      if (!matTotal(m, E, t)) return false;
+      xs = std::max(xs, t);
+    }
+    return true;
+  }
+  // initMajorant (:1330-1621) without URR / S(a,b) / TMS.  The merge loop adds each nuclide's grid
+  // points in ascending order until its first point outside eBounds (that nuclide then stops
+  // contributing); the temporary grid starts filled with eBounds(2); duplicates are removed.
+  void initMajorant(const std::vector<int>& act) {
+    activeMat = act;
+    std::vector<int> nucSet;
+    for (int m : act) for (int n : mats[m - 1].nuc)
+      if (std::find(nucSet.begin(), nucSet.end(), n) == nucSet.end()) nucSet.push_back(n);
+    std::vector<double> g;
+    for (int n : nucSet) {
+      const CENuclide& N = nucs[n];
+      for (int i = 0; i < N.N; ++i) {
+        if (N.e[i] < eBounds[0] || N.e[i] > eBounds[1]) break;
+        g.push_back(N.e[i]);
+      }
+    }
+    g.push_back(eBounds[1]);
+    std::sort(g.begin(), g.end());
+    eGridUnion.clear();
+    for (double x : g) if (eGridUnion.empty() || x != eGridUnion.back()) eGridUnion.push_back(x);
+    majorant.assign(eGridUnion.size(), 0.0);
+    for (size_t i = 0; i < eGridUnion.size(); ++i) {
+      double E = eGridUnion[i];
+      if (E < eBounds[0]) E = eBounds[0];
+      if (E > eBounds[1]) E = eBounds[1];
+      double maj = 0.0;
+      for (int m : act) {
+        double t = 0.0;
+        matTotal(m, E, t);
+        t = t * 1.0;                                     // rho = densityFactor = 1
+        maj = std::max(maj, t);
+      }
+      majorant[i] = maj * (1.0 + MAJ_NUDGE);
+    }
+  }
+};
+
+// scatteringKernels_func.f90:281-334 (Gamma(3/2) and Gamma(2) samples of X)
+template <class RNGT>
+static double sample_x2expx2(RNGT& rand) {
+  double r1 = rand.get(), r2 = rand.get(), r3 = rand.get();
+  double cosine = std::cos(0.5 * PI * r1);
+  double beta = cosine * cosine;
+  double gamma05 = -std::log(r2) * beta;
+  double sample = -std::log(r3) + gamma05;
+  return std::sqrt(sample);
+}
+template <class RNGT>
+static double sample_x3expx2(RNGT& rand) {
+  double r1 = rand.get(), r2 = rand.get();
+  double sample = -std::log(r1) - std::log(r2);
+  return std::sqrt(sample);
+}
+// targetVelocity_constXS + sample_targetVelocity (scatteringKernels_func.f90:101-139,340-380)
+template <class RNGT>
+static void targetVelocity_constXS(double E, const double dir[3], double A, double kT, RNGT& rand, double V_t[3]) {
+  double Y = std::sqrt(A * E / kT);
+  double alpha = 2.0 / (Y * SQRT_PI + 2.0);
+  double X, mu;
+  while (true) {
+    double r1 = rand.get(), r2 = rand.get(), r3 = rand.get();
+    if (r1 > alpha) X = sample_x2expx2(rand);
+    else X = sample_x3expx2(rand);
+    mu = 2.0 * r2 - 1.0;
+    double rel_v = std::sqrt(Y * Y + X * X - 2.0 * X * Y * mu);
+    double P_acc = rel_v / (Y + X);
+    if (P_acc > r3) break;
+  }
+  double r1 = rand.get();
+  double phi = 2.0 * PI * r1;
+  rotateVector(dir, mu, phi, V_t);
+  double s = X * std::sqrt(kT / A);
+  for (int i = 0; i < 3; ++i) V_t[i] = V_t[i] * s;
+}
+// asymptoticScatter (scatteringKernels_func.f90:38-58)
+static void asymptoticScatter(double& E, double& mu, double A) {
+  double E_in = E;
+  double inv_Ap1 = 1.0 / (A + 1.0);
+  E = (1.0 + A * A + 2 * A * mu) * E_in * inv_Ap1 * inv_Ap1;
+  mu = (A * mu + 1) * std::sqrt(E_in / E) * inv_Ap1;
+  if (mu > 1.0) mu = 1.0;
+}
+
 // ---------------------------------------------------------------- scoreMemory (Tallies/scoreMemory_class.f90)
 struct ScoreMemory {
   std::vector<double> bin, csum, csum2;
@@ -903,13 +1105,15 @@ struct ScoreMemory {
 
 // ---------------------------------------------------------------- particle (ParticleObjects/particle_class.f90)
 struct PState {   // particleState subset carried by the banks
-  double wgt = 0, r[3] = {0, 0, 0}, dir[3] = {0, 0, 0}, time = 0;
+  double wgt = 0, r[3] = {0, 0, 0}, dir[3] = {0, 0, 0}, time = 0, E = 0;
   int G = 0, broodID = 0, matIdx = -1;
 };
 
 struct Particle {
   CoordList coords;
   int G = 1;
+  double E = 0.0;         // CE energy [MeV]
+  bool isMG = true;
   double w = 1.0, w0 = 1.0, time = 0.0;
   bool isDead = false;
   int fate = NO_FATE;
@@ -920,6 +1124,7 @@ struct Particle {
   // prePath snapshot used by track clerks
   double prePathR[3] = {0, 0, 0};
   int prePathMat = 0, prePathG = 1;
+  double prePathE = 0.0;
   int matIdx() const { return coords.matIdx; }
 };
 
@@ -934,6 +1139,7 @@ struct Clerk {
   int64_t size() const {
     if (d.type == SG_CLERK_KEFF_ANALOG) return 3;
     if (d.type == SG_CLERK_KEFF_IMPLICIT) return 5;
+    if (d.type == SG_CLERK_SURFACE_CURRENT) return (int64_t)d.n_planes * nbins * 2;
     return (int64_t)width * nbins;
   }
 };
@@ -949,6 +1155,8 @@ struct TallyAdmin {
 struct Oracle {
   Geometry geom;
   MGData mg;
+  CEData ce;
+  bool isCE = false;
   std::vector<TallyAdmin> admins;
   int transport = SG_TRANSPORT_ST;
   std::string err;
@@ -970,7 +1178,7 @@ struct Oracle {
   int64_t nEvents = 0, nColl = 0;
 
   // ----- clerk evaluation helpers (Tallies/TallyMaps, TallyFilters, TallyResponses)
-  int mapState(const Clerk& c, const double r[3], int G, int mat) const {
+  int mapState(const Clerk& c, const double r[3], int G, int mat, double E = 0.0, bool isMG = true) const {
     if (c.d.n_axes == 0) return 1;
     int64_t idx = 1;
     for (int a = 0; a < c.d.n_axes; ++a) {
@@ -984,6 +1192,12 @@ struct Oracle {
         b = (G >= 1 && G <= ax.n) ? G : 0;
       } else if (ax.kind == SG_AXIS_MATERIAL) {
         b = (mat >= 1 && mat <= ax.n) ? mat : 0;
+      } else if (ax.kind == SG_AXIS_ENERGY) {                     // energyMap (energyMap_class.f90:278-293)
+        if (isMG) b = 0;
+        else {
+          b = (int)std::floor(std::log(E / ax.min) / c.step[a]) + 1;   // grid%search log (grid_class.f90:164-166)
+          if (b < 1 || b >= ax.n + 1) b = 0;
+        }
       }
       if (b == 0) return 0;                                       // multiMap (multiMap_class.f90:153-173)
       idx = idx + (int64_t)(b - 1) * c.multi[a];
@@ -1009,8 +1223,33 @@ struct Oracle {
       default: return 0.0;
     }
   }
-  double response(int code, int mat, int G) const {
+  // ceNeutronMaterial%getMacroXSs -> updateMacroXSs (aceNeutronDatabase_class.f90:577-640) and
+  // neutronMacroXSs%get (neutronXsPackages_class.f90:115-190) for a non-fissile CE material
+  double macroXSce(int mat, double E, int MT) const {
+    if (mat <= 0 || mat == VOID_MAT) return 0.0;
+    const CEMaterial& M = ce.mats[mat - 1];
+    double x[4] = {0.0, 0.0, 0.0, 0.0};
+    for (size_t i = 0; i < M.nuc.size(); ++i) {
+      const CENuclide& N = ce.nucs[M.nuc[i]];
+      int idx; double f;
+      if (!N.search(E, idx, f)) return 0.0;
+      double dens = M.dens[i] * 1.0;
+      for (int k = 0; k < 4; ++k) x[k] = x[k] + dens * N.interp(idx, f, k);
+    }
+    switch (MT) {
+      case macroTotal: return x[0];
+      case macroDisappearance: return x[3];
+      case macroEscatter: return x[1];
+      case macroNonElastic: return x[2] + 0.0 + x[3];
+      case macroIEscatter: return x[2];
+      case macroAllScatter: return x[1] + x[2];
+      case macroAbsorbtion: return 0.0 + x[3];
+      default: return 0.0;
+    }
+  }
+  double response(int code, int mat, int G, double E = 0.0) const {
     if (code == SG_RESP_FLUX) return 1.0;
+    if (isCE) return macroXSce(mat, E, code);
     return macroXS(mat, G, code);                                // macroResponse_class.f90:141-172
   }
   bool filterPass(const Clerk& c, int G) const {                 // energyFilter_class.f90:109-127 (MG)
@@ -1027,11 +1266,14 @@ struct Oracle {
       if (c.d.type == SG_CLERK_COLLISION) {                      // collisionClerk_class.f90:192-242
         if (!c.d.handle_virtual && virt) continue;
         if (!filterPass(c, p.G)) continue;
-        int bin = mapState(c, p.coords.lvl[0].r, p.G, p.matIdx());
+        int bin = mapState(c, p.coords.lvl[0].r, p.G, p.matIdx(), p.E, p.isMG);
         if (bin == 0) continue;
-        double flux = c.d.handle_virtual ? p.w / trackXS : p.w / mg.T(p.matIdx(), p.G);
+        double flux;
+        if (c.d.handle_virtual) flux = p.w / trackXS;
+        else if (isCE) { double t = 0.0; ce.matTotal(p.matIdx(), p.E, t); flux = p.w / t; }
+        else flux = p.w / mg.T(p.matIdx(), p.G);
         int64_t addr = c.addr + (int64_t)c.width * (bin - 1) - 1;
-        for (int i = 0; i < c.width; ++i) A.mem.score(response(c.d.resp[i], p.matIdx(), p.G) * flux, addr + i + 1);
+        for (int i = 0; i < c.width; ++i) A.mem.score(response(c.d.resp[i], p.matIdx(), p.G, p.E) * flux, addr + i + 1);
       } else if (c.d.type == SG_CLERK_KEFF_IMPLICIT) {           // keffImplicitClerk_class.f90:180-227
         if (p.matIdx() == VOID_MAT) continue;
         double flux = p.w / trackXS;
@@ -1064,11 +1306,39 @@ struct Oracle {
     for (Clerk& c : A.clerks) {
       if (c.d.type == SG_CLERK_TRACK) {                          // trackClerk_class.f90:185-232
         if (!filterPass(c, p.prePathG)) continue;
-        int bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat);
+        int bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathE, p.isMG);
         if (bin == 0) continue;
         int64_t addr = c.addr + (int64_t)c.width * (bin - 1) - 1;
         for (int i = 0; i < c.width; ++i)
-          A.mem.score(response(c.d.resp[i], p.prePathMat, p.G) * p.w * L, addr + i + 1);
+          A.mem.score(response(c.d.resp[i], p.prePathMat, p.G, p.E) * p.w * L, addr + i + 1);
+      }
+    }
+  }
+  // Surface-current clerk (no SCONE counterpart): for every flight from x0 to x1 (global
+  // coordinates), each tally plane the flight crosses scores the weight in the bin of the
+  // pre-flight state and the crossing direction.  A plane is crossed when x0 and x1 lie on
+  // different sides of it (side: coordinate < plane); a leaking flight crosses every plane ahead of
+  // x0 in its direction of flight.
+  void reportCurrent(int a, Particle& p, const double x0[3], const double x1[3], const double u0[3], bool leaked) {
+    if (a < 0) return;
+    TallyAdmin& A = admins[a];
+    reportCurrent(A.atch, p, x0, x1, u0, leaked);
+    for (Clerk& c : A.clerks) {
+      if (c.d.type != SG_CLERK_SURFACE_CURRENT) continue;
+      int ax = c.d.current_axis - SG_AXIS_X;
+      double a0 = x0[ax], a1 = x1[ax], u = u0[ax];
+      int bin = 0;
+      for (int k = 0; k < c.d.n_planes; ++k) {
+        double pl = c.d.planes[k];
+        bool crossed;
+        if (leaked) crossed = (u > 0.0) ? (a0 < pl) : (u < 0.0 && a0 >= pl);
+        else crossed = (a0 < pl) != (a1 < pl);
+        if (!crossed) continue;
+        if (bin == 0) bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathE, p.isMG);
+        if (bin == 0) return;
+        int dirBin = (leaked ? u > 0.0 : a1 > a0) ? 1 : 0;
+        int64_t idx = ((int64_t)k * c.nbins + (bin - 1)) * 2 + dirBin;
+        A.mem.score(p.w, c.addr + idx);
       }
     }
   }
@@ -1122,13 +1392,34 @@ struct Oracle {
   // ----- transport (TransportOperator)
   double trackingXS_material(Particle& p) {          // getTrackingXS(MATERIAL_XS) (baseMgNeutronDatabase :95-133)
     int m = p.matIdx();
+    if (isCE) {                                      // ceNeutronDatabase_inter.f90:331-415
+      if (m == VOID_MAT) return std::max(0.0, ce.collisionXS);
+      return std::max(trackMatXS(p), ce.collisionXS);
+    }
     if (m == VOID_MAT) return mg.collisionXS;
     return std::max(mg.T(m, p.G), mg.collisionXS);
   }
   double trackMatXS(Particle& p) {                   // getTrackMatXS (:137-160)
     int m = p.matIdx();
     if (m == VOID_MAT) return 0.0;
+    if (isCE) {                                      // ceNeutronDatabase_inter.f90:384-415
+      double t = 0.0;
+      if (!ce.matTotal(m, p.E, t)) { err = "energy outside the nuclide data"; p.isDead = true; }
+      return t + 0.0;
+    }
     return mg.T(m, p.G);
+  }
+  double majorantXS(Particle& p) {                   // getTrackingXS(MAJORANT_XS)
+    if (isCE) {
+      double x = 0.0;
+      if (!ce.majorantXS(p.E, x)) { err = "energy outside the majorant grid"; p.isDead = true; }
+      return std::max(x + 0.0, ce.collisionXS);
+    }
+    return std::max(mg.majorant[p.G - 1], mg.collisionXS);
+  }
+  double speed(const Particle& p) const {            // particle_class.f90:481-503
+    if (p.isMG) return 1.0;
+    return std::sqrt(2.0 * p.E / neutronMass) * lightSpeed;
   }
 
   // surfaceTracking (transportOperatorST_class.f90:48-166); returns tracking XS cache value
@@ -1144,14 +1435,17 @@ struct Oracle {
         dist = -std::log(p.rng.get()) * invSigmaTrack;
         sigmaT = trackMatXS(p);
       }
-      // MG speed = 1 (particle_class.f90:481-503); timeMax = 0 -> no ageing
+      if (p.isDead) break;
+      double spd = speed(p);                         // timeMax = 0 -> no ageing
       for (int i = 0; i < 3; ++i) p.prePathR[i] = p.coords.lvl[0].r[i];
-      p.prePathMat = p.matIdx(); p.prePathG = p.G;
+      p.prePathMat = p.matIdx(); p.prePathG = p.G; p.prePathE = p.E;
+      double u0[3] = {p.coords.lvl[0].dir[0], p.coords.lvl[0].dir[1], p.coords.lvl[0].dir[2]};
       int event;
       geom.move(p.coords, dist, event, useCache ? &cache : nullptr);
-      p.time = p.time + dist / 1.0;
+      p.time = p.time + dist / spd;
       nEvents++;
       reportPath(admin, p, dist);
+      reportCurrent(admin, p, p.prePathR, p.coords.lvl[0].r, u0, p.matIdx() == OUTSIDE_MAT);
       if (p.matIdx() == OUTSIDE_MAT) { p.isDead = true; p.fate = LEAK_FATE; }
       else if (p.matIdx() == UNDEF_MAT) { err = "Particle is in undefined material"; p.isDead = true; }
       else if (p.matIdx() == OVERLAP_MAT) { err = "Particle is in overlapping cells"; p.isDead = true; }
@@ -1165,19 +1459,28 @@ struct Oracle {
 
   // deltaTracking (transportOperatorDT_class.f90:47-131)
   void deltaTracking(Particle& p, int admin, double& trackXS) {
-    double maj = std::max(mg.majorant[p.G - 1], mg.collisionXS);   // getTrackingXS(MAJORANT_XS)
+    double maj = majorantXS(p);
+    if (p.isDead) return;
     trackXS = maj;
     double majorant_inv = 1.0 / maj;
     while (true) {
       double distance = -std::log(p.rng.get()) * majorant_inv;
+      double spd = speed(p);
+      double x0[3] = {p.coords.lvl[0].r[0], p.coords.lvl[0].r[1], p.coords.lvl[0].r[2]};
+      double u0[3] = {p.coords.lvl[0].dir[0], p.coords.lvl[0].dir[1], p.coords.lvl[0].dir[2]};
+      int m0 = p.matIdx();
       geom.teleport(p.coords, distance);
-      p.time = p.time + distance / 1.0;
+      p.time = p.time + distance / spd;
       nEvents++;
       int m = p.matIdx();
+      for (int i = 0; i < 3; ++i) p.prePathR[i] = x0[i];
+      p.prePathMat = m0; p.prePathG = p.G; p.prePathE = p.E;
+      reportCurrent(admin, p, x0, p.coords.lvl[0].r, u0, m == OUTSIDE_MAT);
       if (m == OUTSIDE_MAT) { p.fate = LEAK_FATE; p.isDead = true; break; }
       if (m == VOID_MAT) { reportInColl(admin, p, true, trackXS); continue; }
       if (m == UNDEF_MAT || m == OVERLAP_MAT) { err = "Particle is in undefined/overlap material"; p.isDead = true; break; }
       double sigmaT = trackMatXS(p);
+      if (p.isDead) break;
       if (p.rng.get() < sigmaT * majorant_inv) break;
       else reportInColl(admin, p, true, trackXS);
     }
@@ -1258,6 +1561,91 @@ struct Oracle {
     if (p.isDead) { p.fate = ABS_FATE; reportHist(admin, p); }
   }
 
+  // collisionProcessor%collide with neutronCEstd (collisionProcessor_inter.f90:114-195,
+  // neutronCEstd_class.f90:157-588) for non-fissile nuclides with CM-isotropic elastic scattering
+  void collideCE(Particle& p, int admin, double trackXS) {
+    const int matIdx = p.matIdx();
+    // sampleCollision (:157-214)
+    double denom = trackMatXS(p);
+    double probAlpha = 0.0 / denom;                      // getAlphaAbsorption = 0 (alpha = 0)
+    (void)(p.rng.get() < probAlpha);
+    const CEMaterial& M = ce.mats[matIdx - 1];
+    // ceNeutronMaterial%sampleNuclide (ceNeutronMaterial_class.f90:338-455), TMS off
+    double trackMat = 0.0;
+    ce.matTotal(matIdx, p.E, trackMat);
+    double xi = trackMat * p.rng.get();
+    int nucIdx = -1;
+    for (size_t i = 0; i < M.nuc.size(); ++i) {
+      double tot = 0.0;
+      ce.nucTotal(M.nuc[i], p.E, tot);
+      xi = xi - tot * (M.dens[i] * 1.0);
+      if (xi < 0.0) { nucIdx = M.nuc[i]; break; }
+    }
+    if (nucIdx < 0) { err = "Nuclide sampling loop failed to terminate"; p.isDead = true; return; }
+    const CENuclide& N = ce.nucs[nucIdx];
+    int idx = 1; double f = 0.0;
+    N.search(p.E, idx, f);
+    double micro[4];
+    for (int k = 0; k < 4; ++k) micro[k] = N.interp(idx, f, k);
+    // neutronMicroXSs%invert (neutronXsPackages_class.f90:273-310): no fission data
+    double r = p.rng.get();
+    int C = 1;
+    double xs = micro[0] * r - micro[1];
+    if (xs > 0.0) C = C + 1;
+    xs = xs - micro[2];
+    if (xs > 0.0) C = C + 1;
+    xs = xs - micro[3];
+    if (xs > 0.0) C = C + 1;
+    reportInColl(admin, p, false, trackXS);
+    p.preCollWgt = p.w;
+    // implicit (:220-311): non-fissile nuclide, no sites
+    int MT;
+    if (C == 1) {                                        // elastic (:340-384)
+      MT = 2;                                            // N_N_elastic
+      double A = N.A, kT = N.kT;
+      bool isFixed = (p.E > kT * ce.threshE) && (A > ce.threshA);
+      if (isFixed) {                                     // scatterFromFixed (:460-491)
+        double mu = 2.0 * p.rng.get() - 1.0;             // elasticNeutronScatter%sampleOut (:168-195)
+        double phi = p.rng.get() * TWO_PI;
+        double E_out = p.E;
+        asymptoticScatter(E_out, mu, A);
+        p.coords.rotate(mu, phi);
+        p.E = E_out;
+      } else {                                           // scatterFromMoving (:495-585)
+        double dir_pre[3] = {p.coords.lvl[0].dir[0], p.coords.lvl[0].dir[1], p.coords.lvl[0].dir[2]};
+        double sE = std::sqrt(p.E);
+        double V_n[3], V_t[3], V_cm[3];
+        for (int i = 0; i < 3; ++i) V_n[i] = dir_pre[i] * sE;
+        targetVelocity_constXS(p.E, dir_pre, A, kT, p.rng, V_t);
+        for (int i = 0; i < 3; ++i) V_cm[i] = (V_n[i] + V_t[i] * A) / (A + 1);
+        for (int i = 0; i < 3; ++i) V_n[i] = V_n[i] - V_cm[i];
+        double U_n = norm2_3(V_n);
+        for (int i = 0; i < 3; ++i) V_n[i] = V_n[i] / U_n;
+        double mu = 2.0 * p.rng.get() - 1.0;
+        double phi = p.rng.get() * TWO_PI;
+        double rv[3];
+        rotateVector(V_n, mu, phi, rv);
+        for (int i = 0; i < 3; ++i) V_n[i] = rv[i] * U_n;
+        for (int i = 0; i < 3; ++i) V_n[i] = V_n[i] + V_cm[i];
+        U_n = norm2_3(V_n);
+        double dir_post[3];
+        for (int i = 0; i < 3; ++i) dir_post[i] = V_n[i] / U_n;
+        p.E = U_n * U_n;
+        p.coords.assignDirection(dir_post);
+      }
+    } else if (C == 2) {
+      err = "inelastic scattering is not supported by the CE data"; p.isDead = true; return;
+    } else {                                             // capture / fission: kill
+      MT = (C == 3) ? 101 : 18;
+      p.isDead = true;
+    }
+    if (p.E < ce.minE) p.isDead = true;                  // cutoffs (:434-444)
+    p.collisionN += 1;
+    nColl++;
+    reportOutColl(admin, p, MT);
+    if (p.isDead) { p.fate = ABS_FATE; reportHist(admin, p); }
+  }
+
   // one history: copy from the bank, place, history loop (eigenPhysicsPackage_class.f90:211-246)
   void runHistory(const PState& st, int n, uint64_t master, double k, int admin,
                   std::vector<PState>* sites, int32_t* recC, uint64_t* recR) {
@@ -1268,6 +1656,7 @@ struct Oracle {
     p.coords.takeAboveGeom();
     for (int i = 0; i < 3; ++i) { p.coords.lvl[0].r[i] = st.r[i]; p.coords.lvl[0].dir[i] = st.dir[i]; }
     p.G = st.G; p.time = st.time; p.fate = NO_FATE; p.collisionN = 0; p.isDead = false;
+    p.E = st.E; p.isMG = !isCE;
     p.broodID = n;
     geom.placeCoord(p.coords);
     p.k_eff = k;
@@ -1277,7 +1666,8 @@ struct Oracle {
       if (transport == SG_TRANSPORT_DT) deltaTracking(p, admin, trackXS);
       else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_ST);
       if (p.isDead) { reportHist(admin, p); break; }
-      collide(p, admin, trackXS, sites);
+      if (isCE) collideCE(p, admin, trackXS);
+      else collide(p, admin, trackXS, sites);
       if (p.isDead) break;
     }
     if (recC) *recC = p.collisionN;
@@ -1316,6 +1706,7 @@ struct Oracle {
       s.G = g;
     } else s.G = src.G;
     s.time = 0.0; s.wgt = 1.0;
+    s.E = src.E;
     return s;
   }
 
@@ -1410,6 +1801,7 @@ static void bankToStates(const sg_bank* b, int n, std::vector<orc::PState>& v) {
     s.G = b->G ? b->G[i] : 1;
     s.time = b->time ? b->time[i] : 0.0;
     s.broodID = b->brood_id ? b->brood_id[i] : 0;
+    s.E = b->E ? b->E[i] : 0.0;
   }
 }
 static void statesToBank(const std::vector<orc::PState>& v, sg_bank* b, int cap) {
@@ -1421,6 +1813,7 @@ static void statesToBank(const std::vector<orc::PState>& v, sg_bank* b, int cap)
     if (b->G) b->G[i] = s.G;
     if (b->time) b->time[i] = s.time;
     if (b->brood_id) b->brood_id[i] = s.broodID;
+    if (b->E) b->E[i] = s.E;
   }
 }
 
@@ -1449,6 +1842,43 @@ int32_t or_upload_mg(or_handle h, const sg_mg_desc* d) {
   o->mg.initMajorant(act);
   return SG_OK;
 }
+int32_t or_upload_ce(or_handle h, const sg_ce_desc* d) {
+  Oracle* o = O(h);
+  if (o->ce.build(d, o->err) != 0) return SG_ERR_BAD_ARG;
+  std::vector<int> act;
+  for (int f : o->geom.graphIdx) if (f > 0 && f <= (int)o->ce.mats.size()) act.push_back(f);
+  std::sort(act.begin(), act.end());
+  act.erase(std::unique(act.begin(), act.end()), act.end());
+  if (o->ce.hasMajorant) o->ce.initMajorant(act);
+  else o->ce.activeMat = act;
+  o->isCE = true;
+  return SG_OK;
+}
+// CE probes: nuclide microscopic XSs [total elastic inelastic capture], material total, majorant
+int32_t or_ce_micro(or_handle h, int32_t nuc, double E, double* out) {
+  const orc::CENuclide& N = O(h)->ce.nucs[nuc];
+  int idx; double f;
+  if (!N.search(E, idx, f)) return SG_ERR_BAD_ARG;
+  for (int k = 0; k < 4; ++k) out[k] = N.interp(idx, f, k);
+  return SG_OK;
+}
+int32_t or_ce_mat_total(or_handle h, int32_t mat, double E, double* out) {
+  return O(h)->ce.matTotal(mat, E, *out) ? SG_OK : SG_ERR_BAD_ARG;
+}
+int32_t or_ce_majorant(or_handle h, double E, double* out) {
+  return O(h)->ce.majorantXS(E, *out) ? SG_OK : SG_ERR_BAD_ARG;
+}
+int32_t or_ce_union_size(or_handle h, int64_t* n) { *n = (int64_t)O(h)->ce.eGridUnion.size(); return SG_OK; }
+int32_t or_asymptotic_scatter(double E, double mu, double A, double* out) {
+  orc::asymptoticScatter(E, mu, A); out[0] = E; out[1] = mu; return SG_OK;
+}
+int32_t or_target_velocity(double E, const double* dir, double A, double kT, uint64_t* state, double* V_t) {
+  orc::RNG r; r.s = *state;
+  orc::targetVelocity_constXS(E, dir, A, kT, r, V_t);
+  *state = r.s;
+  return SG_OK;
+}
+
 int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
   Oracle* o = O(h);
   orc::TallyAdmin A;
@@ -1460,6 +1890,7 @@ int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
     for (int a = 0; a < c.d.n_axes; ++a) {
       c.multi[a] = mul; mul *= c.d.axes[a].n;
       if (c.d.axes[a].kind <= SG_AXIS_Z) c.step[a] = (c.d.axes[a].max - c.d.axes[a].min) / c.d.axes[a].n;
+      if (c.d.axes[a].kind == SG_AXIS_ENERGY) c.step[a] = std::log(c.d.axes[a].max / c.d.axes[a].min) / c.d.axes[a].n;
     }
     c.nbins = mul;
     c.addr = memLoc;

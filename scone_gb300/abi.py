@@ -26,8 +26,9 @@ FORM_EVENT, FORM_HISTORY = 0, 1
 TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE = 1, 2, 3
 # clerks
 CLERK_COLLISION, CLERK_TRACK, CLERK_KEFF_ANALOG, CLERK_KEFF_IMPLICIT = 1, 2, 3, 4
+CLERK_SURFACE_CURRENT = 5
 # map axes
-AXIS_X, AXIS_Y, AXIS_Z, AXIS_GROUP, AXIS_MATERIAL = 1, 2, 3, 4, 5
+AXIS_X, AXIS_Y, AXIS_Z, AXIS_GROUP, AXIS_MATERIAL, AXIS_ENERGY = 1, 2, 3, 4, 5, 6
 # responses (macro MTs from SharedModules/endfConstants.f90:116-130)
 RESP_FLUX = 0
 MACRO_TOTAL, MACRO_CAPTURE, MACRO_FISSION, MACRO_NUFISSION, MACRO_ABSORPTION = -1, -2, -6, -7, -21
@@ -64,6 +65,7 @@ class ClerkDesc(C.Structure):
         ("type", C.c_int32), ("handle_virtual", C.c_int32), ("n_resp", C.c_int32),
         ("resp", C.c_int32 * 4), ("n_axes", C.c_int32), ("axes", AxisDesc * 3),
         ("filter_g_top", C.c_int32), ("filter_g_low", C.c_int32),
+        ("current_axis", C.c_int32), ("n_planes", C.c_int32), ("planes", C.c_double * 8),
     ]
 
 
@@ -77,7 +79,7 @@ class TallyDesc(C.Structure):
 class PointSourceDesc(C.Structure):
     _fields_ = [
         ("r", C.c_double * 3), ("dir", C.c_double * 3), ("isotropic", C.c_int32),
-        ("G", C.c_int32), ("n_prob_g", C.c_int32), ("prob_g", f64p),
+        ("G", C.c_int32), ("n_prob_g", C.c_int32), ("prob_g", f64p), ("E", C.c_double),
     ]
 
 
@@ -91,6 +93,16 @@ class Config(C.Structure):
 class Bank(C.Structure):
     _fields_ = [
         ("wgt", f64p), ("r", f64p), ("dir", f64p), ("G", i32p), ("time", f64p), ("brood_id", i32p),
+        ("E", f64p),
+    ]
+
+
+class CEDesc(C.Structure):
+    _fields_ = [
+        ("n_nuc", C.c_int32), ("nuc_ptr", C.POINTER(C.c_int64)), ("e", f64p), ("xs", f64p),
+        ("A", f64p), ("kT", f64p), ("n_mat", C.c_int32), ("mat_ptr", i32p), ("mat_nuc", i32p),
+        ("mat_dens", f64p), ("majorant", C.c_int32), ("min_e", C.c_double), ("max_e", C.c_double),
+        ("thresh_e", C.c_double), ("thresh_a", C.c_double), ("avg_dist", C.c_double),
     ]
 
 
@@ -116,15 +128,19 @@ class HostBank:
             arrays = dict(
                 wgt=np.ones(n, np.float64), r=np.zeros((n, 3), np.float64),
                 dir=np.zeros((n, 3), np.float64), G=np.ones(n, np.int32),
-                time=np.zeros(n, np.float64), brood_id=np.zeros(n, np.int32))
+                time=np.zeros(n, np.float64), brood_id=np.zeros(n, np.int32),
+                E=np.zeros(n, np.float64))
         self.a = arrays
-        for k in ("wgt", "r", "dir", "time"):
+        if "E" not in self.a:
+            self.a["E"] = np.zeros(self.n, np.float64)
+        for k in ("wgt", "r", "dir", "time", "E"):
             self.a[k] = np.ascontiguousarray(self.a[k], dtype=np.float64)
         for k in ("G", "brood_id"):
             self.a[k] = np.ascontiguousarray(self.a[k], dtype=np.int32)
         self.struct = Bank(_p(self.a["wgt"], C.c_double), _p(self.a["r"], C.c_double),
                            _p(self.a["dir"], C.c_double), _p(self.a["G"], C.c_int32),
-                           _p(self.a["time"], C.c_double), _p(self.a["brood_id"], C.c_int32))
+                           _p(self.a["time"], C.c_double), _p(self.a["brood_id"], C.c_int32),
+                           _p(self.a["E"], C.c_double))
 
     def __getitem__(self, k):
         return self.a[k]
@@ -188,8 +204,10 @@ def mg_struct(m):
     return s, keep
 
 
-def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None):
-    """Describe one tally clerk; axes = [(kind, n, min, max), ...] (multiMap order)."""
+def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None, current_axis=0, planes=()):
+    """Describe one tally clerk; axes = [(kind, n, min, max), ...] (multiMap order).
+
+    Surface-current clerks take the normal axis (AXIS_X/Y/Z) and up to 8 plane positions."""
     c = ClerkDesc()
     c.type = type_
     c.handle_virtual = handle_virtual
@@ -201,6 +219,10 @@ def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None):
         c.axes[i].kind, c.axes[i].n, c.axes[i].min, c.axes[i].max = k, n, lo, hi
     if g_filter is not None:
         c.filter_g_top, c.filter_g_low = g_filter
+    c.current_axis = current_axis
+    c.n_planes = len(planes)
+    for i, x in enumerate(planes):
+        c.planes[i] = x
     return c
 
 
@@ -210,8 +232,9 @@ def tally_struct(clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
     return t, arr
 
 
-def point_source_struct(r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
+def point_source_struct(r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None, E=0.0):
     s = PointSourceDesc()
+    s.E = E
     for i in range(3):
         s.r[i] = r[i]
         s.dir[i] = dir[i]
@@ -225,4 +248,33 @@ def point_source_struct(r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None
     else:
         s.n_prob_g = 0
         s.prob_g = C.cast(None, f64p)
+    return s, keep
+
+
+def ce_struct(d):
+    """Build a CEDesc from a dict (see problems.ce_data)."""
+    keep = {}
+
+    def arr(name, dt, ct):
+        a = np.ascontiguousarray(d[name], dtype=dt)
+        keep[name] = a
+        return _p(a, ct)
+
+    s = CEDesc()
+    s.n_nuc = len(d["A"])
+    s.nuc_ptr = arr("nuc_ptr", np.int64, C.c_int64)
+    s.e = arr("e", np.float64, C.c_double)
+    s.xs = arr("xs", np.float64, C.c_double)
+    s.A = arr("A", np.float64, C.c_double)
+    s.kT = arr("kT", np.float64, C.c_double)
+    s.n_mat = len(d["mat_ptr"]) - 1
+    s.mat_ptr = arr("mat_ptr", np.int32, C.c_int32)
+    s.mat_nuc = arr("mat_nuc", np.int32, C.c_int32)
+    s.mat_dens = arr("mat_dens", np.float64, C.c_double)
+    s.majorant = int(d.get("majorant", 1))
+    s.min_e = float(d.get("min_e", 1.0e-11))
+    s.max_e = float(d.get("max_e", 20.0))
+    s.thresh_e = float(d.get("thresh_e", 400.0))
+    s.thresh_a = float(d.get("thresh_a", 1.0))
+    s.avg_dist = float(d.get("avg_dist", 0.0))
     return s, keep

@@ -19,6 +19,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "sg_tr_fp64.cu": ["-fmad=false"],
     "sg_tr_mixed.cu": [],
+    "sg_tr_ce_fp64.cu": ["-fmad=false"],
+    "sg_tr_ce_mixed.cu": [],
     "sg_support.cu": ["-fmad=false"],
     "sg_host.cu": ["-fmad=false"],
     "sg_noalloc.cu": ["-fmad=false"],

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 #include <functional>
+#include <type_traits>
 
 #include "sg_device.cuh"
 #include "sg_launch.h"
@@ -61,7 +62,7 @@ struct DArr {
 };
 
 struct BankBufs {
-  DArr<double> r, dir, wgt, time;
+  DArr<double> r, dir, wgt, time, E;
   DArr<int> G, brood;
   cudaError_t alloc(size_t cap) {
     cudaError_t e;
@@ -70,8 +71,8 @@ struct BankBufs {
       return e;
     return cudaSuccess;
   }
-  DBank view() { return DBank{r.p, dir.p, wgt.p, G.p, brood.p, time.p}; }
-  void free() { r.free(); dir.free(); wgt.free(); time.free(); G.free(); brood.free(); }
+  DBank view() { return DBank{r.p, dir.p, wgt.p, G.p, brood.p, time.p, E.p}; }
+  void free() { r.free(); dir.free(); wgt.free(); time.free(); G.free(); brood.free(); E.free(); }
 };
 
 struct Admin {
@@ -116,6 +117,17 @@ struct sg_handle_t {
   DMG<double> mg64{};
   DMG<float> mgMx{};
 
+  // continuous-energy data
+  bool hasCE = false;
+  DArr<double> ceE, ceUE;
+  DArr<double> ceXs64, ceA64, ceKT64, ceDens64, ceMaj64;
+  DArr<float> ceXsF, ceAF, ceKTF, ceDensF, ceMajF;
+  DArr<long long> ceOff;
+  DArr<int2> ceHash, ceUHash;
+  DArr<int> ceMatPtr, ceMatNuc, ceAct;
+  DCE<double> ce64{};
+  DCE<float> ceMx{};
+
   // tallies
   std::vector<Admin> admins;
   long long totalBins = 0;
@@ -139,6 +151,7 @@ struct sg_handle_t {
   // event form: particle state (sized for FP64 and 4 levels), queues and their counters
   DArr<double> pR0, pRl, pU, pW, pW0, pTime, pTrack;
   DArr<int> pGeo, pInts, qT0, qT1, qC, qCtr;
+  DArr<double> pE;
   DArr<unsigned long long> pRng;
   int evIterations = 0;
   int lastN = 0;
@@ -458,6 +471,182 @@ int build_mg(sg_handle h, const sg_mg_desc* d) {
   return SG_OK;
 }
 
+// ------------------------------------------------------------------ continuous-energy data
+// Floor index with the reference's rule (genericProcedures.f90:132-166): the largest i with
+// e[i] <= x, n-2 for x = e[n-1]; -1 outside [e[0], e[n-1]].
+int floor_index(const double* e, int n, double x) {
+  if (!(x >= e[0] && x <= e[n - 1])) return -1;
+  if (x == e[n - 1]) return n - 2;
+  return (int)(std::upper_bound(e, e + n, x) - e) - 1;
+}
+
+// Hash brackets over [logMin, logMin + nBins / invStep]: bin b gets (lo, hi) with
+// e[lo] <= E < e[hi] for every E whose FP32-computed bin is b (edges widened by 1e-4 relative).
+std::vector<int2> hash_brackets(const double* e, int n, int nBins, float logMin, float invStep) {
+  std::vector<int2> h(nBins);
+  const double step = 1.0 / (double)invStep;
+  for (int b = 0; b < nBins; ++b) {
+    const double lo_e = std::exp((double)logMin + b * step) * (1.0 - 1.0e-4);
+    const double hi_e = std::exp((double)logMin + (b + 1) * step) * (1.0 + 1.0e-4);
+    int lo = (b == 0 || lo_e <= e[0]) ? 0 : std::max(0, floor_index(e, n, std::min(lo_e, e[n - 1])));
+    int hi = (b == nBins - 1 || hi_e >= e[n - 1]) ? n - 1 : floor_index(e, n, hi_e) + 1;
+    hi = std::min(std::max(hi, lo + 1), n - 1);
+    h[b] = make_int2(lo, hi);
+  }
+  return h;
+}
+
+// aceNeutronDatabase%init/activate/initMajorant (aceNeutronDatabase_class.f90:873-1163,1291-1621)
+// for non-fissile nuclides without URR or S(a,b) tables.
+int build_ce(sg_handle h, const sg_ce_desc* d) {
+  if (!h->hasGeom) return h->fail(SG_ERR_STATE, "ce: upload the geometry first (majorant uses its materials)");
+  if (h->hasMG) return h->fail(SG_ERR_STATE, "ce: the handle already holds MG data");
+  const int nN = d->n_nuc, nM = d->n_mat;
+  if (nN <= 0 || nM <= 0 || !d->nuc_ptr || !d->e || !d->xs || !d->A || !d->kT || !d->mat_ptr || !d->mat_nuc || !d->mat_dens)
+    return h->fail(SG_ERR_BAD_ARG, "ce: bad sizes or missing arrays");
+  if (!(d->min_e >= 0.0) || !(d->max_e > d->min_e) || !(d->thresh_e >= 0.0) || !(d->thresh_a >= 0.0))
+    return h->fail(SG_ERR_BAD_ARG, "ce: bad neutronCEstd settings");
+  const long long nP = d->nuc_ptr[nN];
+  std::vector<long long> off(d->nuc_ptr, d->nuc_ptr + nN + 1);
+  for (int i = 0; i < nN; ++i) {
+    if (off[i + 1] - off[i] < 2) return h->fail(SG_ERR_BAD_ARG, "ce: a nuclide grid needs at least 2 points");
+    if (off[i + 1] - off[i] > 0x7fffffff) return h->fail(SG_ERR_BAD_ARG, "ce: nuclide grid too large");
+    for (long long j = off[i]; j < off[i + 1]; ++j) {
+      if (j > off[i] && !(d->e[j] >= d->e[j - 1])) return h->fail(SG_ERR_BAD_ARG, "ce: energy grid not ascending");
+      if (d->xs[4 * j + 2] != 0.0) return h->fail(SG_ERR_BAD_ARG, "ce: inelastic channels are not supported");
+    }
+    if (!(d->A[i] > 0.0) || !(d->kT[i] > 0.0)) return h->fail(SG_ERR_BAD_ARG, "ce: A and kT must be positive");
+  }
+  for (int m = 0; m < nM; ++m)
+    for (int k = d->mat_ptr[m]; k < d->mat_ptr[m + 1]; ++k)
+      if (d->mat_nuc[k] < 0 || d->mat_nuc[k] >= nN) return h->fail(SG_ERR_BAD_ARG, "ce: bad nuclide index");
+  std::vector<int2> graph(h->graph.n);
+  CK(cudaMemcpy(graph.data(), h->graph.p, graph.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+  std::vector<int> act;
+  for (auto& e : graph) if (e.x > 0) act.push_back(e.x);
+  std::sort(act.begin(), act.end());
+  act.erase(std::unique(act.begin(), act.end()), act.end());
+  for (int a : act)
+    if (a > nM || d->mat_ptr[a] == d->mat_ptr[a - 1]) return h->fail(SG_ERR_BAD_ARG, "ce: geometry uses an undefined or empty material");
+  // energy bounds over all nuclides (:1043-1052)
+  double eb0 = d->e[off[0]], eb1 = d->e[off[1] - 1];
+  double gmin = eb0, gmax = eb1;
+  for (int i = 1; i < nN; ++i) {
+    eb0 = std::max(eb0, d->e[off[i]]);
+    eb1 = std::min(eb1, d->e[off[i + 1] - 1]);
+    gmin = std::min(gmin, d->e[off[i]]);
+    gmax = std::max(gmax, d->e[off[i + 1] - 1]);
+  }
+  if (!(gmin > 0.0)) return h->fail(SG_ERR_BAD_ARG, "ce: energies must be positive");
+  auto nuc_total = [&](int n, double E, double& xs) -> bool {   // updateTotalNucXS
+    const double* e = d->e + off[n];
+    int i = floor_index(e, (int)(off[n + 1] - off[n]), E);
+    if (i < 0) return false;
+    double f = (E - e[i]) / (e[i + 1] - e[i]);
+    const double* x = d->xs + 4 * (off[n] + i);
+    xs = x[4] * f + (1.0 - f) * x[0];
+    return true;
+  };
+  // unionised majorant (:1375-1621): every active nuclide's grid points up to its first point
+  // outside the bounds, plus eBounds(2); sorted and de-duplicated; value = max over the active
+  // materials of their total at that energy, nudged up by 1e-6
+  std::vector<double> ue, umaj;
+  if (d->majorant) {
+    std::vector<int> nucs;
+    for (int a : act)
+      for (int k = d->mat_ptr[a - 1]; k < d->mat_ptr[a]; ++k) nucs.push_back(d->mat_nuc[k]);
+    std::sort(nucs.begin(), nucs.end());
+    nucs.erase(std::unique(nucs.begin(), nucs.end()), nucs.end());
+    for (int n : nucs)
+      for (long long j = off[n]; j < off[n + 1]; ++j) {
+        if (d->e[j] < eb0 || d->e[j] > eb1) break;
+        ue.push_back(d->e[j]);
+      }
+    ue.push_back(eb1);
+    std::sort(ue.begin(), ue.end());
+    ue.erase(std::unique(ue.begin(), ue.end()), ue.end());
+    if (ue.size() < 2) return h->fail(SG_ERR_BAD_ARG, "ce: the union energy grid has fewer than 2 points");
+    umaj.resize(ue.size());
+    for (size_t i = 0; i < ue.size(); ++i) {
+      double E = std::min(std::max(ue[i], eb0), eb1);
+      double maj = 0.0;
+      for (int a : act) {
+        double t = 0.0;
+        for (int k = d->mat_ptr[a - 1]; k < d->mat_ptr[a]; ++k) {
+          double s = 0.0;
+          nuc_total(d->mat_nuc[k], E, s);
+          t = t + d->mat_dens[k] * s;
+        }
+        maj = std::max(maj, t * 1.0);
+      }
+      umaj[i] = maj * (1.0 + 1.0e-6);
+    }
+  }
+  // hash brackets: nuclides share one log range; the union grid has its own
+  const int nHash = 8192;
+  const float hLogMin = (float)std::log(gmin);
+  const float hInvStep = (float)(nHash / (std::log(gmax) - std::log(gmin)));
+  std::vector<int2> hash((size_t)nN * nHash);
+  for (int n = 0; n < nN; ++n) {
+    auto hb = hash_brackets(d->e + off[n], (int)(off[n + 1] - off[n]), nHash, hLogMin, hInvStep);
+    std::copy(hb.begin(), hb.end(), hash.begin() + (size_t)n * nHash);
+  }
+  int nUHash = 0;
+  float uLogMin = 0.f, uInvStep = 0.f;
+  std::vector<int2> uhash;
+  if (d->majorant) {
+    nUHash = (int)std::min<size_t>(1u << 18, std::max<size_t>(1024, ue.size() / 4));
+    uLogMin = (float)std::log(ue.front());
+    uInvStep = (float)(nUHash / (std::log(ue.back()) - std::log(ue.front())));
+    uhash = hash_brackets(ue.data(), (int)ue.size(), nUHash, uLogMin, uInvStep);
+  }
+  // uploads
+  cudaStream_t st = h->stream;
+  std::vector<double> e(d->e, d->e + nP), xs(d->xs, d->xs + 4 * nP), A(d->A, d->A + nN), kT(d->kT, d->kT + nN);
+  std::vector<int> mp(d->mat_ptr, d->mat_ptr + nM + 1), mn(d->mat_nuc, d->mat_nuc + d->mat_ptr[nM]);
+  std::vector<double> dens(d->mat_dens, d->mat_dens + d->mat_ptr[nM]);
+  CK(h->ceE.upload(e, st));
+  CK(h->ceXs64.upload(xs, st));
+  CK(h->ceA64.upload(A, st));
+  CK(h->ceKT64.upload(kT, st));
+  CK(h->ceDens64.upload(dens, st));
+  CK(h->ceXsF.upload(std::vector<float>(xs.begin(), xs.end()), st));
+  CK(h->ceAF.upload(std::vector<float>(A.begin(), A.end()), st));
+  CK(h->ceKTF.upload(std::vector<float>(kT.begin(), kT.end()), st));
+  CK(h->ceDensF.upload(std::vector<float>(dens.begin(), dens.end()), st));
+  CK(h->ceOff.upload(off, st));
+  CK(h->ceHash.upload(hash, st));
+  CK(h->ceMatPtr.upload(mp, st));
+  CK(h->ceMatNuc.upload(mn, st));
+  CK(h->ceAct.upload(act, st));
+  CK(h->ceUE.upload(ue, st));
+  CK(h->ceMaj64.upload(umaj, st));
+  CK(h->ceMajF.upload(std::vector<float>(umaj.begin(), umaj.end()), st));
+  CK(h->ceUHash.upload(uhash, st));
+  const double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
+  auto fill = [&](auto& D, auto xsP, auto aP, auto ktP, auto densP, auto majP) {
+    using RR = std::remove_reference_t<decltype(*xsP)>;
+    D.nNuc = nN; D.nMat = nM;
+    D.e = h->ceE.p; D.xs = xsP; D.off = h->ceOff.p; D.hash = h->ceHash.p; D.nHash = nHash;
+    D.hLogMin = hLogMin; D.hInvStep = hInvStep;
+    D.A = aP; D.kT = ktP; D.matPtr = h->ceMatPtr.p; D.matNuc = h->ceMatNuc.p; D.matDens = densP;
+    D.hasMajorant = d->majorant ? 1 : 0;
+    D.ue = h->ceUE.p; D.umaj = majP; D.uhash = h->ceUHash.p; D.nU = (int)ue.size(); D.nUHash = nUHash;
+    D.uLogMin = uLogMin; D.uInvStep = uInvStep;
+    D.act = h->ceAct.p; D.nAct = (int)act.size();
+    D.minE = d->min_e; D.threshE = (RR)d->thresh_e; D.threshA = (RR)d->thresh_a; D.collisionXS = (RR)cxs;
+  };
+  fill(h->ce64, (const double*)h->ceXs64.p, (const double*)h->ceA64.p, (const double*)h->ceKT64.p,
+       (const double*)h->ceDens64.p, (const double*)h->ceMaj64.p);
+  fill(h->ceMx, (const float*)h->ceXsF.p, (const float*)h->ceAF.p, (const float*)h->ceKTF.p,
+       (const float*)h->ceDensF.p, (const float*)h->ceMajF.p);
+  // banks carry energies
+  for (int b = 0; b < 2; ++b) CK(h->bank[b].E.alloc(h->cap));
+  if (h->cfg.form == SG_FORM_EVENT) CK(h->pE.alloc(h->cap));
+  h->hasCE = true;
+  return SG_OK;
+}
+
 int alloc_work(sg_handle h) {
   const size_t cap = (size_t)h->cap;
   for (int b = 0; b < 2; ++b) CK(h->bank[b].alloc(cap));
@@ -493,6 +682,7 @@ DPart<R> part_view(sg_handle h) {
   p.time = reinterpret_cast<R*>(h->pTime.p);
   p.trackXS = reinterpret_cast<R*>(h->pTrack.p);
   p.ints = h->pInts.p;
+  p.E = h->pE.p;
   p.cap = h->cap;
   return p;
 }
@@ -521,6 +711,7 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
   }
   t.n_clerks = 0;
   t.keff_clerk = -1;
+  t.has_current = 0;
   for (int x : chain) {
     const Admin& A = h->admins[x];
     for (size_t c = 0; c < A.clerks.size(); ++c) {
@@ -539,7 +730,9 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
         K.ax_kind[i] = d.axes[i].kind;
         K.ax_n[i] = d.axes[i].n;
         K.ax_min[i] = d.axes[i].min;
-        K.ax_step[i] = (d.axes[i].max - d.axes[i].min) / d.axes[i].n;
+        if (d.axes[i].kind == SG_AXIS_ENERGY)          // grid log step (grid_class.f90:76-90)
+          K.ax_step[i] = std::log(d.axes[i].max / d.axes[i].min) / d.axes[i].n;
+        else K.ax_step[i] = (d.axes[i].max - d.axes[i].min) / d.axes[i].n;
         K.ax_inv_step[i] = 1.0 / K.ax_step[i];
         K.ax_minf[i] = (float)K.ax_min[i];
         K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
@@ -549,6 +742,13 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
       K.g_top = d.filter_g_top;
       K.g_low = d.filter_g_low;
       K.acc_off = A.off + (A.addr[c] - 1) - lo;
+      K.nbins = mul;
+      if (d.type == SG_CLERK_SURFACE_CURRENT) {
+        K.cur_axis = d.current_axis - SG_AXIS_X;
+        K.n_planes = d.n_planes;
+        for (int q = 0; q < d.n_planes; ++q) K.planes[q] = d.planes[q];
+        t.has_current = 1;
+      }
       if (d.type == SG_CLERK_KEFF_IMPLICIT) {
         if (t.keff_clerk >= 0) return h->fail(SG_ERR_BAD_ARG, "tally: one k-implicit clerk per launch");
         t.keff_clerk = t.n_clerks;
@@ -563,7 +763,8 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
 // `out` in brood order.  Returns SG_OK and the number of sites.
 template <class R>
 int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long master, const double* d_k,
-               DBank out, int outcap, int* S_out, sg_cycle_stats* st, const DGeom& geom, const DMG<R>& mg) {
+               DBank out, int outcap, int* S_out, sg_cycle_stats* st, const DGeom& geom, const DMG<R>& mg,
+               const DCE<R>& ce) {
   cudaStream_t s = h->stream;
   TransportArgs<R> t;
   std::memset(&t, 0, sizeof(t));
@@ -572,6 +773,7 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   if (rc) return rc;
   t.geom = geom;
   t.mg = mg;
+  t.ce = ce;
   t.in = in;
   t.n = n;
   t.master = master;
@@ -594,8 +796,11 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), s));
   CK(cudaEventRecord(h->ev[0], s));
   const bool dt = h->cfg.transport == SG_TRANSPORT_DT;
+  auto launch_kind = [&](int kind, const TransportArgs<R>& a, int maxl, bool dtt, size_t sm, cudaStream_t ss, int* g) {
+    return h->hasCE ? launch_kind_ce<R>(kind, a, maxl, dtt, sm, ss, g) : sg::launch_kind<R>(kind, a, maxl, dtt, sm, ss, g);
+  };
   if (h->cfg.form == SG_FORM_HISTORY) {
-    CK(launch_transport<R>(t, h->maxl, dt, smem, s, nullptr));
+    CK(launch_kind(K_HISTORY, t, h->maxl, dt, smem, s, nullptr));
     h->launches += 1;
   } else {
     // event form: start, then transit / collide rounds over compacted queues, then the tail
@@ -605,7 +810,7 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
     int* qT[2] = {h->qT0.p, h->qT1.p};
     CK(cudaMemsetAsync(qc, 0, 8 * sizeof(int), s));
     t.q = DQueues{nullptr, nullptr, qT[0], qc + 0, qc + 3};
-    CK(launch_kind<R>(K_EV_START, t, h->maxl, dt, 0, s, nullptr));
+    CK(launch_kind(K_EV_START, t, h->maxl, dt, 0, s, nullptr));
     int cur = 0, it = 0;
     const int tail = std::max(4096, n / 64);
     const int CHUNK = 4;
@@ -614,10 +819,10 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
       for (int k = 0; k < CHUNK; ++k, ++it) {
         CK(cudaMemsetAsync(qc + 2, 0, 2 * sizeof(int), s));
         t.q = DQueues{qT[cur], qc + cur, h->qC.p, qc + 2, qc + 3};
-        CK(launch_kind<R>(K_EV_TRANSIT, t, h->maxl, dt, 0, s, nullptr));
+        CK(launch_kind(K_EV_TRANSIT, t, h->maxl, dt, 0, s, nullptr));
         CK(cudaMemsetAsync(qc + (1 - cur), 0, sizeof(int), s));
         t.q = DQueues{h->qC.p, qc + 2, qT[1 - cur], qc + (1 - cur), qc + 3};
-        CK(launch_kind<R>(K_EV_COLLIDE, t, h->maxl, dt, 0, s, nullptr));
+        CK(launch_kind(K_EV_COLLIDE, t, h->maxl, dt, 0, s, nullptr));
         cur = 1 - cur;
         h->launches += 2;
       }
@@ -628,7 +833,7 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
     }
     CK(cudaMemsetAsync(qc + 3, 0, sizeof(int), s));
     t.q = DQueues{qT[cur], qc + cur, nullptr, nullptr, qc + 3};
-    CK(launch_kind<R>(K_EV_TAIL, t, h->maxl, dt, 0, s, nullptr));
+    CK(launch_kind(K_EV_TAIL, t, h->maxl, dt, 0, s, nullptr));
     h->launches += 1;
     h->evIterations = it;
   }
@@ -662,11 +867,19 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
 
 int gen_loop(sg_handle h, int admin, DBank in, int n, unsigned long long master, const double* d_k, DBank out,
              int outcap, int* S, sg_cycle_stats* st) {
-  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
+  if (!h->hasGeom || !(h->hasMG || h->hasCE)) return h->fail(SG_ERR_STATE, "upload geometry and nuclear data first");
   if (admin < 0 || admin >= (int)h->admins.size()) return h->fail(SG_ERR_BAD_ARG, "bad tally admin");
   if (n < 0 || n > h->cap) return h->fail(SG_ERR_BANK_OVERFLOW, "bank larger than max_bank");
-  if (h->cfg.precision == SG_PREC_MIXED) return gen_loop_t<float>(h, admin, in, n, master, d_k, out, outcap, S, st, h->gMx, h->mgMx);
-  return gen_loop_t<double>(h, admin, in, n, master, d_k, out, outcap, S, st, h->g64, h->mg64);
+  if (h->hasCE) {
+    for (int x = admin; x >= 0; x = h->admins[x].atch)
+      for (const auto& d : h->admins[x].clerks) {
+        if (d.type == SG_CLERK_KEFF_IMPLICIT) return h->fail(SG_ERR_BAD_ARG, "tally: k-implicit clerks need fissile MG data");
+        if (d.filter_g_top > 0) return h->fail(SG_ERR_BAD_ARG, "tally: group filters apply to MG problems only");
+      }
+  }
+  if (h->cfg.precision == SG_PREC_MIXED)
+    return gen_loop_t<float>(h, admin, in, n, master, d_k, out, outcap, S, st, h->gMx, h->mgMx, h->ceMx);
+  return gen_loop_t<double>(h, admin, in, n, master, d_k, out, outcap, S, st, h->g64, h->mg64, h->ce64);
 }
 
 // tallyAdmin%reportCycleStart: keffAnalog START_POP (keffAnalogClerk_class.f90:140-147)
@@ -765,7 +978,12 @@ int h2d_bank(sg_handle h, const sg_bank* b, int n, DBank d) {
     CK(cudaMemcpyAsync(d.wgt, one.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
   }
-  if (b->G) CK(cudaMemcpyAsync(d.G, b->G, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  if (h->hasCE) {
+    if (!b->E) return h->fail(SG_ERR_BAD_ARG, "bank: E is required for CE transport");
+    CK(cudaMemcpyAsync(d.E, b->E, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    if (b->G) CK(cudaMemcpyAsync(d.G, b->G, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    else CK(cudaMemsetAsync(d.G, 0, sizeof(int) * n, s));
+  } else if (b->G) CK(cudaMemcpyAsync(d.G, b->G, sizeof(int) * n, cudaMemcpyHostToDevice, s));
   else return h->fail(SG_ERR_BAD_ARG, "bank: G is required for MG transport");
   if (b->time) CK(cudaMemcpyAsync(d.time, b->time, sizeof(double) * n, cudaMemcpyHostToDevice, s));
   else CK(cudaMemsetAsync(d.time, 0, sizeof(double) * n, s));
@@ -781,6 +999,7 @@ int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
   if (b->G) CK(cudaMemcpyAsync(b->G, d.G, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
   if (b->time) CK(cudaMemcpyAsync(b->time, d.time, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   if (b->brood_id) CK(cudaMemcpyAsync(b->brood_id, d.brood, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  if (b->E && d.E) CK(cudaMemcpyAsync(b->E, d.E, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   return SG_OK;
 }
@@ -858,6 +1077,10 @@ int32_t sg_destroy(sg_handle h) {
   h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
   h->pR0.free(); h->pRl.free(); h->pU.free(); h->pW.free(); h->pW0.free(); h->pTime.free(); h->pTrack.free();
   h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();
+  h->ceE.free(); h->ceUE.free(); h->ceXs64.free(); h->ceA64.free(); h->ceKT64.free(); h->ceDens64.free();
+  h->ceMaj64.free(); h->ceXsF.free(); h->ceAF.free(); h->ceKTF.free(); h->ceDensF.free(); h->ceMajF.free();
+  h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
+  h->pE.free();
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(h->stream);
   delete h;
@@ -877,7 +1100,13 @@ int32_t sg_upload_geometry(sg_handle h, const sg_geometry_desc* g) {
 
 int32_t sg_upload_mg(sg_handle h, const sg_mg_desc* mg) {
   if (!h || !mg) return SG_ERR_BAD_ARG;
+  if (h->hasCE) return h->fail(SG_ERR_STATE, "mg: the handle already holds CE data");
   return build_mg(h, mg);
+}
+
+int32_t sg_upload_ce(sg_handle h, const sg_ce_desc* ce) {
+  if (!h || !ce) return SG_ERR_BAD_ARG;
+  return build_ce(h, ce);
 }
 
 int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out) {
@@ -889,17 +1118,22 @@ int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out)
     long long size;
     if (d.type == SG_CLERK_KEFF_ANALOG) { size = 3; A.keffAnalog = loc - 1; }
     else if (d.type == SG_CLERK_KEFF_IMPLICIT) { size = 5; A.keffImplicit = loc - 1; }
-    else if (d.type == SG_CLERK_COLLISION || d.type == SG_CLERK_TRACK) {
-      if (d.n_resp < 1 || d.n_resp > 4 || d.n_axes < 0 || d.n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "tally: bad clerk");
+    else if (d.type == SG_CLERK_COLLISION || d.type == SG_CLERK_TRACK || d.type == SG_CLERK_SURFACE_CURRENT) {
+      const bool cur = d.type == SG_CLERK_SURFACE_CURRENT;
+      if ((!cur && (d.n_resp < 1 || d.n_resp > 4)) || d.n_axes < 0 || d.n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "tally: bad clerk");
+      if (cur && (d.current_axis < SG_AXIS_X || d.current_axis > SG_AXIS_Z || d.n_planes < 1 || d.n_planes > 8))
+        return h->fail(SG_ERR_BAD_ARG, "tally: surface-current clerk needs an axis and 1-8 planes");
       long long nb = 1;
       for (int a = 0; a < d.n_axes; ++a) {
-        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_MATERIAL)
+        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_ENERGY)
           return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
         if (d.axes[a].kind <= SG_AXIS_Z && !(d.axes[a].max > d.axes[a].min))
           return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap needs max > min");
+        if (d.axes[a].kind == SG_AXIS_ENERGY && !(d.axes[a].min > 0.0 && d.axes[a].max > d.axes[a].min))
+          return h->fail(SG_ERR_BAD_ARG, "tally: log energy grid needs 0 < min < max");
         nb *= d.axes[a].n;
       }
-      size = nb * d.n_resp;
+      size = cur ? nb * d.n_planes * 2 : nb * d.n_resp;
     } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown clerk type");
     A.clerks.push_back(d);
     A.addr.push_back(loc);
@@ -941,6 +1175,8 @@ int32_t sg_set_point_source(sg_handle h, const sg_point_source_desc* src) {
   for (int i = 0; i < 3; ++i) { p.r[i] = src->r[i]; p.dir[i] = src->dir[i]; }
   p.isotropic = src->isotropic;
   p.G = src->G;
+  p.E = src->E;
+  if (h->hasCE && !(src->E > 0.0)) return h->fail(SG_ERR_BAD_ARG, "point source: CE problems need E > 0");
   p.n_prob_g = src->n_prob_g;
   if (src->n_prob_g > 0) {
     std::vector<double> v(src->prob_g, src->prob_g + src->n_prob_g);
@@ -1054,7 +1290,7 @@ int32_t sg_get_keff(sg_handle h, int32_t admin, double* k, double* sd) {
 
 int32_t sg_eigen_init(sg_handle h, int32_t pop, uint64_t master_state, double k0) {
   if (!h || pop <= 0 || pop > h->cap) return SG_ERR_BAD_ARG;
-  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "eigenvalue runs need geometry and fissile MG data");
   h->cur = 0;
   CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), h->stream));
   CK(launch_fission_source(h->g64, h->mg64, h->bank[0].view(), pop, master_state, h->bounds, h->maxl,

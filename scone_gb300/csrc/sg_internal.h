@@ -72,6 +72,40 @@ struct DMG {
   R collisionXS;
 };
 
+// Continuous-energy neutron data (aceNeutronNuclide mainData / eGrid, ceNeutronMaterial composition,
+// aceNeutronDatabase unionised majorant).  Energy grids stay FP64 in both forms (the floor index is
+// the reference's exactly); cross sections, densities, masses and temperatures are in R.
+// Grid searches start from a hash over log(E): bin b of a nuclide (or of the union grid) holds the
+// bracket (lo, hi) of grid indices that contains every energy of that bin, widened by a margin
+// so that the FP32 log used to pick the bin cannot miss; a short binary search finishes it.
+template <class R>
+struct DCE {
+  int nNuc, nMat;
+  const double* e;          // all nuclide grids, concatenated
+  const R* xs;              // [point][4] total, elastic, inelastic, capture
+  const long long* off;     // [nNuc+1] first point of each nuclide
+  const int2* hash;         // [nNuc][nHash] nuclide-relative brackets
+  int nHash;
+  float hLogMin, hInvStep;  // bin = floor((log E - hLogMin) * hInvStep), clamped
+  const R* A;               // [nNuc] mass ratio
+  const R* kT;              // [nNuc] nuclide temperature [MeV]
+  const int* matPtr;        // [nMat+1]
+  const int* matNuc;        // 0-based nuclide indices in composition order
+  const R* matDens;         // atom densities
+  // unionised majorant (aceNeutronDatabase%majorant) or the active materials (on-the-fly majorant)
+  int hasMajorant;
+  const double* ue;         // union grid
+  const R* umaj;            // majorant values on it
+  const int2* uhash;
+  int nU, nUHash;
+  float uLogMin, uInvStep;
+  const int* act;           // active materials (1-based), for the on-the-fly majorant
+  int nAct;
+  double minE;              // neutronCEstd minEnergy cut-off
+  R threshE, threshA;       // free-gas thresholds
+  R collisionXS;
+};
+
 // One tally clerk as the kernels see it (all admins of a launch flattened; acc offsets global).
 struct DClerk {
   int type;
@@ -90,6 +124,10 @@ struct DClerk {
   float ax_inv_stepf[3];
   long long multi[3];
   long long acc_off;     // offset (0-based) of this clerk's first bin in the launch's acc array
+  long long nbins;       // map bins (surface-current clerks: per plane and direction)
+  int cur_axis;          // surface-current clerk: 0..2 normal of the planes
+  int n_planes;
+  double planes[8];
 };
 
 static constexpr int MAX_CLERKS = 8;
@@ -102,6 +140,7 @@ struct DBank {
   int* G;
   int* brood;
   double* time;
+  double* E;       // CE energy (null for MG)
 };
 
 // Fission sites produced by one gen loop before they are ordered by brood ID.  The buffer is split
@@ -143,6 +182,7 @@ struct DPart {
   R* time;
   R* trackXS;
   int* ints;       // [5][cap] G, collisionN, history, sites written, segments
+  double* E;       // [cap] CE energy
   int cap;
 };
 
@@ -159,6 +199,7 @@ template <class R>
 struct TransportArgs {
   DGeom geom;
   DMG<R> mg;
+  DCE<R> ce;
   DBank in;
   int n;
   unsigned long long master;
@@ -166,6 +207,7 @@ struct TransportArgs {
   DClerk clerks[MAX_CLERKS];
   int n_clerks;
   int keff_clerk;       // index of the keff-implicit clerk (accumulated in registers), -1 if none
+  int has_current;      // a surface-current clerk is present
   double* acc;          // tally accumulators of the launch (global)
   int acc_n;
   int use_smem;         // accumulate map clerks in shared memory

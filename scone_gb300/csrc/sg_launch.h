@@ -16,6 +16,11 @@ template <class R>
 cudaError_t launch_transport(const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
                              cudaStream_t s, int* grid_out);
 
+// the same kernels for continuous-energy data (neutronCEstd physics); defined in sg_tr_ce_*.cu
+template <class R>
+cudaError_t launch_kind_ce(int kind, const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
+                           cudaStream_t s, int* grid_out);
+
 // fissionSource sampling on the device (fissionSource_class.f90:149-271), FP64 arithmetic
 cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank out, int n,
                                   unsigned long long master, const double* bounds6, int maxl,

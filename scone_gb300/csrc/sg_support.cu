@@ -35,6 +35,7 @@ __global__ void k_point_source(PointSourceArgs a) {
   a.out.G[i] = g;
   a.out.brood[i] = 0;
   a.out.time[i] = 0.0;
+  if (a.out.E) a.out.E[i] = a.E;                                  // pointSource `E` (CE)
 }
 
 cudaError_t launch_point_source(const PointSourceArgs& a, cudaStream_t s) {

@@ -11,6 +11,7 @@ struct PointSourceArgs {
   int G;
   int n_prob_g;
   const double* prob_g;   // device
+  double E;               // CE source energy (written when out.E is set)
   DBank out;
   int n;
   unsigned long long master;

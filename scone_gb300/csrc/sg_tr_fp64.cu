@@ -9,13 +9,13 @@ namespace sg {
 template <>
 cudaError_t launch_kind<double>(int kind, const TransportArgs<double>& a, int maxl, bool dt, size_t smem,
                              cudaStream_t s, int* grid_out) {
-  return launch_kind_impl<double>(kind, a, maxl, dt, smem, s, grid_out);
+  return launch_kind_impl<double, false>(kind, a, maxl, dt, smem, s, grid_out);
 }
 
 template <>
 cudaError_t launch_transport<double>(const TransportArgs<double>& a, int maxl, bool dt, size_t smem,
                                   cudaStream_t s, int* grid_out) {
-  return launch_kind_impl<double>(K_HISTORY, a, maxl, dt, smem, s, grid_out);
+  return launch_kind_impl<double, false>(K_HISTORY, a, maxl, dt, smem, s, grid_out);
 }
 
 cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank out, int n,

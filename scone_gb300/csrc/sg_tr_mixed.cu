@@ -8,13 +8,13 @@ namespace sg {
 template <>
 cudaError_t launch_kind<float>(int kind, const TransportArgs<float>& a, int maxl, bool dt, size_t smem,
                              cudaStream_t s, int* grid_out) {
-  return launch_kind_impl<float>(kind, a, maxl, dt, smem, s, grid_out);
+  return launch_kind_impl<float, false>(kind, a, maxl, dt, smem, s, grid_out);
 }
 
 template <>
 cudaError_t launch_transport<float>(const TransportArgs<float>& a, int maxl, bool dt, size_t smem,
                                   cudaStream_t s, int* grid_out) {
-  return launch_kind_impl<float>(K_HISTORY, a, maxl, dt, smem, s, grid_out);
+  return launch_kind_impl<float, false>(K_HISTORY, a, maxl, dt, smem, s, grid_out);
 }
 
 }  // namespace sg

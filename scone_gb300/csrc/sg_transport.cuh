@@ -1,6 +1,10 @@
 // sg_transport.cuh -- the history loop kernel: the `gen:` loop of SCONE's physics packages with
 // transportOperatorST/DT, neutronMGstd collisions and tally reports fused into one persistent kernel.
 //
+// The same tracker serves multigroup (neutronMGstd, baseMgNeutronDatabase) and continuous-energy
+// (neutronCEstd, aceNeutronDatabase) problems: template parameter CE selects the nuclear data and
+// collision physics; geometry, transport operators and tallies are shared.
+//
 // Execution model: a persistent grid (a multiple of the SM count); each thread carries one particle
 // history at a time and takes the next one as soon as its history ends, so a warp stays full until
 // the bank runs dry.  Warps take histories from a global counter in chunks of 32 (one atomic per
@@ -11,6 +15,7 @@
 // accumulated in registers.
 #pragma once
 #include "sg_device.cuh"
+#include "sg_ce.cuh"
 
 namespace sg {
 
@@ -27,11 +32,12 @@ __device__ __forceinline__ void raise_error(DCounters* ctr, int code, int hist) 
   if (atomicCAS(&ctr->err_code, 0, code) == 0) ctr->err_hist = hist;
 }
 
-template <class R, int MAXL, bool DT>
+template <class R, int MAXL, bool DT, bool CE>
 struct Tracker {
   const TransportArgs<R>& A;
   const Geom<R, MAXL> geom;
   const DMG<R>& mg;
+  const DCE<R>& ce;
   double* acc;
   R k_eff;
 
@@ -49,13 +55,21 @@ struct Tracker {
   R time;            // particle time (MG speed 1: path length); FP32 in the mixed form
   int segs;
   R trackXS;         // tracking XS of the segment that ended in a real collision
+  // CE state: energy, and the cross sections cached for it (invalidated when E changes)
+  double E;
+  CEPoint ep;
+  R ceTot;           // total XS of material ceTotMat at E
+  int ceTotMat;      // -1: none cached
+  R ceMaj;           // majorant at E
+  bool ceMajOK;
+  R invSpeed;        // 1 / speed at E
   // k-implicit per-thread partial sums (keffImplicitClerk bins IMP_PROD, SCATTER_PROD, IMP_ABS,
   // ANA_LEAK), in R; the batch sums they are added to are FP64
   R kprod, kscat, kabs, kleak;
   unsigned long long nEv, nColl;
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
-      : A(a), geom(a.geom), mg(a.mg), acc(accp) {
+      : A(a), geom(a.geom), mg(a.mg), ce(a.ce), acc(accp) {
     k_eff = (R)(*a.k_eff);
     kprod = kscat = kabs = kleak = R(0);
     nEv = nColl = 0;
@@ -81,12 +95,33 @@ struct Tracker {
       default: return R(0);
     }
   }
+  // neutronMacroXSs%get for a CE material at the particle's energy
+  __device__ __forceinline__ R macro_ce(int mat, int MT) const {
+    if (mat <= 0 || mat == SG_VOID_MAT) return R(0);
+    R x[4];
+    if (!ce_mat_macro<R>(ce, mat, ep, x)) return R(0);
+    switch (MT) {
+      case MT_TOTAL: return x[0];
+      case MT_DISAP: return x[3];
+      case MT_ESCATTER: return x[1];
+      case MT_NONELASTIC: return x[2] + R(0) + x[3];
+      case MT_IESCATTER: return x[2];
+      case MT_ALLSCATTER: return x[1] + x[2];
+      case MT_ABSORPTION: return R(0) + x[3];
+      default: return R(0);
+    }
+  }
   __device__ __forceinline__ R response(int code, int mat, int g) const {
-    return code == SG_RESP_FLUX ? R(1) : macro(mat, g, code);
+    if (code == SG_RESP_FLUX) return R(1);
+    if constexpr (CE) return macro_ce(mat, code);
+    else return macro(mat, g, code);
   }
 
   // multiMap of spaceMap / group / material axes (multiMap_class.f90:153-173, grid_class.f90:225-245)
   __device__ __forceinline__ int map_bin(const DClerk& K, const double r[3], int g, int mat) const {
+    return map_bin_e(K, r, g, mat, E);
+  }
+  __device__ __forceinline__ int map_bin_e(const DClerk& K, const double r[3], int g, int mat, double En) const {
     long long idx = 1;
     for (int a = 0; a < K.n_axes; ++a) {
       int b = 0;
@@ -97,7 +132,12 @@ struct Tracker {
         else b = (int)floorf(((float)v - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;
         if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
       } else if (kind == SG_AXIS_GROUP) {
-        b = (g >= 1 && g <= K.ax_n[a]) ? g : 0;
+        b = (CE ? 0 : ((g >= 1 && g <= K.ax_n[a]) ? g : 0));
+      } else if (kind == SG_AXIS_ENERGY) {            // energyMap log grid (grid_class.f90:164-166)
+        if constexpr (!CE) b = 0;
+        else if constexpr (sizeof(R) == 8) b = (int)floor(log(En / K.ax_min[a]) / K.ax_step[a]) + 1;
+        else b = (int)floorf(__logf((float)(En / K.ax_min[a])) * K.ax_inv_stepf[a]) + 1;
+        if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
       } else {
         b = (mat >= 1 && mat <= K.ax_n[a]) ? mat : 0;
       }
@@ -119,10 +159,14 @@ struct Tracker {
         if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
         int bin = map_bin(K, c.r0, G, c.mat);
         if (bin == 0) continue;
-        R flux = K.handle_virtual ? w / trackXS : w / xs(mg.total, c.mat, G);
+        R flux;
+        if (K.handle_virtual) flux = w / trackXS;
+        else if constexpr (CE) flux = w / ce_total(c.mat);
+        else flux = w / xs(mg.total, c.mat, G);
         long long at = K.acc_off + (long long)K.width * (bin - 1);
         for (int i = 0; i < K.width; ++i) score(at + i, (double)(response(K.resp[i], c.mat, G) * flux));
       } else if (K.type == SG_CLERK_KEFF_IMPLICIT) {
+        if constexpr (CE) continue;                    // rejected for CE problems at upload
         if (c.mat == SG_VOID_MAT) continue;
         R flux = w / trackXS;
         bool f = mg.fissile[c.mat - 1] != 0;
@@ -144,6 +188,139 @@ struct Tracker {
       long long at = K.acc_off + (long long)K.width * (bin - 1);
       for (int i = 0; i < K.width; ++i) score(at + i, (double)(response(K.resp[i], matPre, G) * w * L));
     }
+  }
+
+  // Surface-current clerk (no SCONE counterpart): each tally plane crossed by the flight from rpre
+  // to the current position scores the weight in [plane][bin of the pre-flight state][direction].
+  // Side of a plane: coordinate < plane.  A leaking flight crosses every plane ahead of rpre.
+  __device__ __forceinline__ void report_current(const double rpre[3], int matPre, const R u0[3], bool leaked) {
+    for (int k = 0; k < A.n_clerks; ++k) {
+      const DClerk& K = A.clerks[k];
+      if (K.type != SG_CLERK_SURFACE_CURRENT) continue;
+      const double a0 = at3(rpre, K.cur_axis), a1 = at3(c.r0, K.cur_axis);
+      const R u = at3(u0, K.cur_axis);
+      int bin = -1;
+      for (int q = 0; q < K.n_planes; ++q) {
+        const double pl = K.planes[q];
+        const bool crossed = leaked ? ((u > R(0)) ? (a0 < pl) : (u < R(0) && a0 >= pl)) : ((a0 < pl) != (a1 < pl));
+        if (!crossed) continue;
+        if (bin < 0) bin = map_bin(K, rpre, G, matPre);
+        if (bin == 0) break;
+        const int dirBin = (leaked ? (u > R(0)) : (a1 > a0)) ? 1 : 0;
+        score(K.acc_off + ((long long)q * K.nbins + (bin - 1)) * 2 + dirBin, (double)w);
+      }
+    }
+  }
+
+  // ---- CE cross sections at the particle's energy (cached until E changes)
+  __device__ __forceinline__ void set_energy(double En) {
+    E = En;
+    ep = ce_point<R>(ce, En);
+    ceTotMat = -1;
+    ceMajOK = false;
+    // particle_class.f90:481-503: speed = sqrt(2E/m) c
+    invSpeed = (R)(1.0 / (sqrt(2.0 * En / 939.56542194) * 2.99792458e10));
+  }
+  __device__ __forceinline__ R ce_total(int mat) {
+    if (mat != ceTotMat) {
+      if (!ce_mat_total<R>(ce, mat, ep, ceTot)) { raise_error(A.ctr, SG_ERR_NAN, hist); ceTot = R(1); }
+      ceTotMat = mat;
+    }
+    return ceTot;
+  }
+  __device__ __forceinline__ R ce_major() {
+    if (!ceMajOK) {
+      if (!ce_majorant<R>(ce, ep, ceMaj)) { raise_error(A.ctr, SG_ERR_NAN, hist); ceMaj = R(1); }
+      ceMajOK = true;
+    }
+    return ceMaj;
+  }
+
+  // collisionProcessor%collide with neutronCEstd (collisionProcessor_inter.f90:114-195,
+  // neutronCEstd_class.f90:157-588) for non-fissile nuclides with CM-isotropic elastic scattering.
+  // Returns true if the particle died.
+  __device__ __forceinline__ bool collide_ce(R trackXS) {
+    const int mat = c.mat;
+    const R total = ce_total(mat);
+    (void)rng.get();                                     // alpha test (alpha = 0), always drawn
+    // sampleNuclide (ceNeutronMaterial_class.f90:338-455), TMS off
+    R xi = total * rng.get();
+    int nuc = -1;
+    long long gi = -1;
+    R f = R(0);
+    const int k0 = ce.matPtr[mat - 1], k1 = ce.matPtr[mat];
+    for (int k = k0; k < k1; ++k) {
+      const int n = ce.matNuc[k];
+      gi = ce_nuc_search<R>(ce, n, ep, f);
+      const R tot = ce_interp<R>(ce.xs, gi, f, 0);
+      xi = xi - tot * ce.matDens[k];
+      if (xi < R(0) || k == k1 - 1) { nuc = n; break; }
+    }
+    // microXSs (aceNeutronNuclide_class.f90:419-453) and neutronMicroXSs%invert (:273-310)
+    const R mt = ce_interp<R>(ce.xs, gi, f, 0), mel = ce_interp<R>(ce.xs, gi, f, 1);
+    const R min_ = ce_interp<R>(ce.xs, gi, f, 2), mcap = ce_interp<R>(ce.xs, gi, f, 3);
+    const R rr = rng.get();
+    int C = 1;
+    R x = mt * rr - mel;
+    if (x > R(0)) C = C + 1;
+    x = x - min_;
+    if (x > R(0)) C = C + 1;
+    x = x - mcap;
+    if (x > R(0)) C = C + 1;
+    report_in_coll(false, trackXS);
+    bool dead;
+    if (C == 1) {                                        // elastic (:340-384)
+      const R Anuc = ce.A[nuc], kT = ce.kT[nuc];
+      const bool isFixed = ((R)E > kT * ce.threshE) && (Anuc > ce.threshA);
+      double Eout;
+      if (isFixed) {                                     // scatterFromFixed + asymptoticScatter
+        R mu = R(2) * rng.get() - R(1);
+        R sp, cp;
+        sincos_phi<R>(rng.get(), sp, cp);
+        const double Ad = (double)Anuc, mud = (double)mu;
+        const double inv_Ap1 = 1.0 / (Ad + 1.0);
+        Eout = (1.0 + Ad * Ad + 2 * Ad * mud) * E * inv_Ap1 * inv_Ap1;
+        R muL = (R)((Ad * mud + 1) * sqrt(E / Eout) * inv_Ap1);
+        if (muL > R(1)) muL = R(1);
+        rotate_vector<R>(c.u[0], c.u[1], c.u[2], muL, sp, cp);
+      } else {                                           // scatterFromMoving (:495-585)
+        const R d0 = c.u[0], d1 = c.u[1], d2 = c.u[2];
+        const R sE = (R)sqrt(E);
+        R Vn[3] = {d0 * sE, d1 * sE, d2 * sE};
+        R Vt[3], Vcm[3];
+        bool bad = false;
+        target_velocity<R>((R)E, d0, d1, d2, Anuc, kT, rng, Vt, &bad);
+        if (bad) raise_error(A.ctr, SG_ERR_TIMEOUT, hist);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Vcm[i] = (Vn[i] + Vt[i] * Anuc) / (Anuc + R(1));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Vn[i] = Vn[i] - Vcm[i];
+        R Un = norm3<R>(Vn[0], Vn[1], Vn[2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Vn[i] = Vn[i] / Un;
+        const R mu = R(2) * rng.get() - R(1);
+        R sp, cp;
+        sincos_phi<R>(rng.get(), sp, cp);
+        rotate_vector<R>(Vn[0], Vn[1], Vn[2], mu, sp, cp);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Vn[i] = Vn[i] * Un + Vcm[i];
+        Un = norm3<R>(Vn[0], Vn[1], Vn[2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) c.u[i] = Vn[i] / Un;
+        Eout = (double)(Un * Un);
+      }
+      set_energy(Eout);
+      dead = false;
+    } else if (C == 2) {                                 // no inelastic channels in the data
+      raise_error(A.ctr, SG_ERR_BAD_ARG, hist);
+      dead = true;
+    } else {
+      dead = true;                                       // capture / fission
+    }
+    if (E < ce.minE) dead = true;                        // cutoffs (:434-444)
+    collN += 1;
+    nColl += 1;
+    return dead;
   }
 
   __device__ __forceinline__ void write_site(const R dir[3], int gout, R wgt) {
@@ -168,6 +345,7 @@ struct Tracker {
   // collisionProcessor%collide with neutronMGstd (collisionProcessor_inter.f90:114-195,
   // neutronMGstd_class.f90:85-297).  Returns true if the particle died.
   __device__ __forceinline__ bool collide(R trackXS) {
+    if constexpr (CE) return collide_ce(trackXS);
     const int mat = c.mat;
     (void)rng.get();                                     // alpha test, drawn even for alpha = 0
     const int k = (mat - 1) * mg.nG + (G - 1);
@@ -250,7 +428,8 @@ struct Tracker {
     c.u[2] = (R)A.in.dir[3 * i + 2];
     w = (R)A.in.wgt[i];
     w0 = w;
-    G = A.in.G[i];
+    G = CE ? 0 : A.in.G[i];
+    if constexpr (CE) set_energy(A.in.E[i]);
     time = (R)A.in.time[i];
     rng.s = lcg_skip(A.master, RNG_STRIDE * (long long)h);
     collN = 0;
@@ -276,18 +455,27 @@ struct Tracker {
     if constexpr (!DT) {
       // surfaceTracking (transportOperatorST_class.f90:48-166)
       const bool isVoid = (mat == SG_VOID_MAT);
-      const R sigTot = isVoid ? R(0) : xs(mg.total, mat, G);
-      const R sigmaTrack = isVoid ? mg.collisionXS : fmax(sigTot, mg.collisionXS);
+      R sigTot, sigmaTrack;
+      if constexpr (CE) {
+        sigTot = isVoid ? R(0) : ce_total(mat);
+        sigmaTrack = isVoid ? fmax(R(0), ce.collisionXS) : fmax(sigTot, ce.collisionXS);
+      } else {
+        sigTot = isVoid ? R(0) : xs(mg.total, mat, G);
+        sigmaTrack = isVoid ? mg.collisionXS : fmax(sigTot, mg.collisionXS);
+      }
       R dist, invSig, sigT;
       if (sigmaTrack < Tol<R>::st_void()) { dist = INF_R; invSig = INF_R; sigT = R(0); }
       else { invSig = R(1) / sigmaTrack; dist = -dlog<R>(rng.get()) * invSig; sigT = sigTot; }
       const double rpre[3] = {c.r0[0], c.r0[1], c.r0[2]};
+      const R u0[3] = {c.u[0], c.u[1], c.u[2]};
       const int matPre = mat;
       const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0);
-      time = time + dist;
+      if constexpr (CE) time = time + dist * invSpeed;
+      else time = time + dist;
       nEv += 1;
       report_path(rpre, matPre, dist);
       mat = c.mat;
+      if (A.has_current) report_current(rpre, matPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
@@ -304,20 +492,33 @@ struct Tracker {
       return SEG_MORE;
     } else {
       // deltaTracking (transportOperatorDT_class.f90:47-131)
-      const R maj = fmax(mg.majorant[G - 1], mg.collisionXS);
+      R maj;
+      if constexpr (CE) maj = fmax(ce_major(), ce.collisionXS);
+      else maj = fmax(mg.majorant[G - 1], mg.collisionXS);
       const R majInv = R(1) / maj;
       const R dist = -dlog<R>(rng.get()) * majInv;
+      double rpre[3];
+      R u0[3];
+      if (A.has_current) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) { rpre[i] = c.r0[i]; u0[i] = c.u[i]; }
+      }
+      const int matPre = mat;
       if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return SEG_END; }
-      time = time + dist;
+      if constexpr (CE) time = time + dist * invSpeed;
+      else time = time + dist;
       nEv += 1;
       mat = c.mat;
+      if (A.has_current) report_current(rpre, matPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return SEG_MORE; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
         return SEG_END;
       }
-      const R sigT = xs(mg.total, mat, G);
+      R sigT;
+      if constexpr (CE) sigT = ce_total(mat);
+      else sigT = xs(mg.total, mat, G);
       if (rng.get() < sigT * majInv) { trackXS = maj; return SEG_COLLIDE; }
       report_in_coll(true, maj);
       return SEG_MORE;
@@ -359,6 +560,7 @@ struct Tracker {
     P.ints[2 * cap + i] = hist;
     P.ints[3 * cap + i] = nsites;
     P.ints[4 * cap + i] = segs;
+    if constexpr (CE) P.E[i] = E;
   }
   __device__ __forceinline__ void load(const DPart<R>& P, int i) {
     const long long cap = P.cap;
@@ -388,6 +590,7 @@ struct Tracker {
     nsites = P.ints[3 * cap + i];
     segs = P.ints[4 * cap + i];
     cache.lvl = 0;
+    if constexpr (CE) set_energy(P.E[i]);
   }
 
   // reportHist for a leaked particle (keffImplicitClerk ANA_LEAK, :276-290)
@@ -397,8 +600,8 @@ struct Tracker {
 
 
 // k-implicit partial sums and event counters of a warp, reduced and added to global memory
-template <class R, int MAXL, bool DT>
-__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, DT>& T, const TransportArgs<R>& A, int lane) {
+template <class R, int MAXL, bool DT, bool CE>
+__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, DT, CE>& T, const TransportArgs<R>& A, int lane) {
   if (A.keff_clerk >= 0) {
     double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
 #pragma unroll
@@ -432,7 +635,7 @@ __device__ __forceinline__ int warp_append(int* counter) {
   return base + __popc(m & ((1u << lane) - 1u));
 }
 
-template <class R, int MAXL, bool DT>
+template <class R, int MAXL, bool DT, bool CE>
 __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ TransportArgs<R> A) {
   extern __shared__ double s_acc[];
   const bool smem = A.use_smem != 0;
@@ -440,7 +643,7 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
     for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) s_acc[i] = 0.0;
     __syncthreads();
   }
-  Tracker<R, MAXL, DT> T(A, smem ? s_acc : A.acc);
+  Tracker<R, MAXL, DT, CE> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
   bool alive = false, done = false;
   int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
@@ -491,9 +694,9 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
 // finished by the tail kernel (the history loop over the remaining queue).  Per-history RNG streams
 // make the results independent of this scheduling.
 
-template <class R, int MAXL, bool DT>
+template <class R, int MAXL, bool DT, bool CE>
 __global__ void __launch_bounds__(128) k_ev_start(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT> T(A, A.acc);
+  Tracker<R, MAXL, DT, CE> T(A, A.acc);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
     T.start(i + 1);
     T.store(A.part, i);
@@ -504,9 +707,9 @@ __global__ void __launch_bounds__(128) k_ev_start(const __grid_constant__ Transp
 
 // TAIL = false: stop at a real collision and queue the particle for k_ev_collide.
 // TAIL = true : run each particle to the end of its history (collisions included).
-template <class R, int MAXL, bool DT, bool TAIL>
+template <class R, int MAXL, bool DT, bool CE, bool TAIL>
 __global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT> T(A, A.acc);
+  Tracker<R, MAXL, DT, CE> T(A, A.acc);
   const int lane = threadIdx.x & 31;
   const int nIn = *A.q.n_in;
   bool alive = false, done = false;
@@ -555,9 +758,9 @@ __global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ Tran
   flush_counters(T, A, lane);
 }
 
-template <class R, int MAXL, bool DT>
+template <class R, int MAXL, bool DT, bool CE>
 __global__ void __launch_bounds__(128) k_ev_collide(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT> T(A, A.acc);
+  Tracker<R, MAXL, DT, CE> T(A, A.acc);
   const int nIn = *A.q.n_in;
   const int stride = gridDim.x * blockDim.x;
   const int first = blockIdx.x * blockDim.x + threadIdx.x;

@@ -37,6 +37,7 @@ def load(build=True):
         "sg_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
         "sg_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
         "sg_upload_mg": (i32, [vp, P(abi.MGDesc)]),
+        "sg_upload_ce": (i32, [vp, P(abi.CEDesc)]),
         "sg_upload_tally": (i32, [vp, P(abi.TallyDesc), P(i32)]),
         "sg_attach_tally": (i32, [vp, i32, i32]),
         "sg_set_point_source": (i32, [vp, P(abi.PointSourceDesc)]),
@@ -80,6 +81,8 @@ class TransportOperatorGPU:
             self.upload_geometry(problem.geometry)
             if problem.mg is not None:
                 self.upload_mg(problem.mg)
+            if getattr(problem, "ce", None) is not None:
+                self.upload_ce(problem.ce)
             if problem.source:
                 self.set_point_source(**problem.source)
 
@@ -111,6 +114,11 @@ class TransportOperatorGPU:
         self._keep.append(keep)
         self._check(self.L.sg_upload_mg(self.h, C.byref(s)))
 
+    def upload_ce(self, d):
+        s, keep = abi.ce_struct(d)
+        self._keep.append(keep)
+        self._check(self.L.sg_upload_ce(self.h, C.byref(s)))
+
     def upload_tally(self, clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
         t, arr = abi.tally_struct(clerks, batch_size, norm_clerk, norm_val)
         self._keep.append(arr)
@@ -121,8 +129,8 @@ class TransportOperatorGPU:
     def attach_tally(self, admin, atch):
         self._check(self.L.sg_attach_tally(self.h, admin, atch))
 
-    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None):
-        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g)
+    def set_point_source(self, r, G=1, dir=(1.0, 0.0, 0.0), isotropic=True, prob_g=None, E=0.0):
+        s, keep = abi.point_source_struct(r, G, dir, isotropic, prob_g, E)
         self._keep.append((s, keep))
         self._check(self.L.sg_set_point_source(self.h, C.byref(s)))
 

@@ -9,6 +9,8 @@ transport hot path); they produce the same geometry tables that SCONE's `geometr
 Workloads (all synthetic, seeded with numpy default_rng):
   * ``infinite_medium_2g``  -- 2-group infinite homogeneous medium, point source (fixed source).
   * ``lattice_17x17_7g``    -- 17x17 pin lattice, 7 groups, k-eigenvalue.
+  * ``ce_slab_3layer``      -- continuous-energy 3-layer slab (5/20/5 cm), 10 synthetic nuclides,
+                               fixed source, log-energy surface-current tally.
 """
 import numpy as np
 
@@ -123,9 +125,10 @@ def mg_data(n_g, total, scatter_matrix, capture=None, fission=None, nu=None, chi
 class Problem:
     """Geometry + data + tallies + source of one transport problem."""
 
-    def __init__(self, geometry, mg, name="", source=None, tallies=None, eigen=False, meta=None):
+    def __init__(self, geometry, mg, name="", source=None, tallies=None, eigen=False, meta=None, ce=None):
         self.geometry = geometry
         self.mg = mg
+        self.ce = ce
         self.name = name
         self.source = source or {}
         self.tallies = tallies or {}
@@ -237,3 +240,121 @@ def scone_test_lat():
     lat = gb.lattice_universe((2, 2, 0), (1.26, 1.26, 0.0), fills, water)
     gb.root_universe(sq_bound, uni_fill(lat), bc=[1, 1, 2, 2, 0, 0])
     return gb.arrays(), dict(water=water, mox43=mox43, uox=uox)
+
+
+# ----------------------------------------------------------------------------- CE data
+KT_293K = 2.53e-8          # kT at 293.6 K [MeV]
+
+
+def synthetic_nuclide(rng, n_points, A, kT=KT_293K, e_min=1.0e-11, e_max=20.0):
+    """One synthetic non-fissile nuclide on a log-spaced grid of n_points over [e_min, e_max] MeV.
+
+    elastic = potential scattering + a_el E^-1/2 + Lorentzian (single-level Breit-Wigner shaped)
+    peaks; capture = a_c E^-1/2 + the capture part of the same peaks (with the sqrt(E0/E) factor);
+    total = elastic + capture; no inelastic channel.  20-200 peaks at log-uniform energies in
+    [10 eV, 100 keV] with relative widths in [5e-4, 5e-3], heights 3-1000 b and elastic
+    fractions in [0.6, 0.99]."""
+    e = np.geomspace(e_min, e_max, n_points)
+    e[0], e[-1] = e_min, e_max
+    s_pot = rng.uniform(2.0, 20.0)
+    a_el = rng.uniform(0.0, 1.0e-3)
+    a_c = rng.uniform(1.0e-5, 2.0e-3)
+    n_peaks = int(rng.integers(20, 201))
+    e0 = 10.0 ** rng.uniform(-5.0, -1.0, n_peaks)
+    width = e0 * 10.0 ** rng.uniform(-3.3, -2.3, n_peaks)
+    height = 10.0 ** rng.uniform(0.5, 3.0, n_peaks)
+    gn = rng.uniform(0.6, 0.99, n_peaks)
+    inv_sqrt = 1.0 / np.sqrt(e)
+    el = s_pot + a_el * inv_sqrt
+    cap = a_c * inv_sqrt
+    for k in range(n_peaks):
+        lor = 1.0 / (1.0 + (2.0 * (e - e0[k]) / width[k]) ** 2)
+        el = el + height[k] * gn[k] * lor
+        cap = cap + height[k] * (1.0 - gn[k]) * np.sqrt(e0[k]) * inv_sqrt * lor
+    xs = np.zeros((n_points, 4))
+    xs[:, 0] = el + cap
+    xs[:, 1] = el
+    xs[:, 3] = cap
+    return dict(e=e, xs=xs, A=float(A), kT=float(kT))
+
+
+def ce_data(nuclides, materials, **settings):
+    """Assemble an sg_ce_desc dict: nuclides = [dict(e, xs, A, kT)], materials = [[(nuc, dens)]]."""
+    nuc_ptr = np.zeros(len(nuclides) + 1, np.int64)
+    for i, n in enumerate(nuclides):
+        nuc_ptr[i + 1] = nuc_ptr[i] + len(n["e"])
+    mat_ptr = np.zeros(len(materials) + 1, np.int32)
+    for i, m in enumerate(materials):
+        mat_ptr[i + 1] = mat_ptr[i] + len(m)
+    d = dict(
+        nuc_ptr=nuc_ptr,
+        e=np.concatenate([n["e"] for n in nuclides]).astype(np.float64),
+        xs=np.concatenate([n["xs"] for n in nuclides]).astype(np.float64).reshape(-1, 4),
+        A=np.array([n["A"] for n in nuclides], np.float64),
+        kT=np.array([n["kT"] for n in nuclides], np.float64),
+        mat_ptr=mat_ptr,
+        mat_nuc=np.array([k for m in materials for k, _ in m], np.int32),
+        mat_dens=np.array([x for m in materials for _, x in m], np.float64))
+    d.update(settings)
+    return d
+
+
+def ce_slab_3layer(seed=23, n_nuc=10, points=(20000, 100000), scale=1.0, source_E=2.0):
+    """Continuous-energy fixed-source 3-layer slab: x in [0,5], [5,25], [25,30] cm (xPlane cells of a
+    cellUniverse), vacuum in x, reflective in y and z; 10 synthetic nuclides with log grids of
+    U{2e4..1e5} points over [1e-11, 20] MeV and masses A ~ U[1, 60] (nuclide 4 has A = 1, which
+    always scatters from a moving target), kT = 2.53e-8 MeV; isotropic 2 MeV point source at the
+    slab centre.  Tallies: 200-bin log-energy current through the planes x = 0, 5, 25, 30, and a
+    collision-estimator flux per material and 200 log-energy bins.
+
+    ``scale`` < 1 shrinks the grids (a cheaper case with the same structure for the tests)."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(points[0], points[1] + 1, n_nuc)
+    sizes = np.maximum(64, (sizes * scale).astype(int))
+    A = rng.uniform(1.0, 60.0, n_nuc)
+    A[4] = 1.0
+    nucs = [synthetic_nuclide(rng, int(sizes[i]), A[i]) for i in range(n_nuc)]
+    dens = lambda: float(rng.uniform(0.004, 0.03))
+    materials = [
+        [(0, dens()), (1, dens()), (2, dens()), (3, dens())],
+        [(2, dens()), (3, dens()), (4, dens()), (5, dens()), (6, dens()), (7, dens())],
+        [(6, dens()), (7, dens()), (8, dens()), (9, dens())],
+    ]
+    ce = ce_data(nucs, materials)
+    gb = GeometryBuilder()
+    box = gb.surface(abi.BOX, 15.0, 0.0, 0.0, 15.0, 50.0, 50.0)
+    p5 = gb.surface(abi.XPLANE, 5.0)
+    p25 = gb.surface(abi.XPLANE, 25.0)
+    c1 = gb.cell([-(p5 + 1)])
+    c2 = gb.cell([p5 + 1, -(p25 + 1)])
+    c3 = gb.cell([p25 + 1])
+    slab = gb.cell_universe([c1, c2, c3], [1, 2, 3])
+    bc = [abi.BC_VACUUM, abi.BC_VACUUM] + [abi.BC_REFLECTIVE] * 4
+    gb.root_universe(box, uni_fill(slab), bc=bc)
+    e_axis = (abi.AXIS_ENERGY, 200, 1.0e-11, 20.0)
+    tallies = dict(
+        current=[abi.clerk(abi.CLERK_SURFACE_CURRENT, axes=[e_axis], current_axis=abi.AXIS_X,
+                           planes=(0.0, 5.0, 25.0, 30.0))],
+        flux=[abi.clerk(abi.CLERK_COLLISION, axes=[e_axis, (abi.AXIS_MATERIAL, 3, 0.0, 0.0)])])
+    return Problem(gb.arrays(), None, name="ce_slab_3layer", eigen=False, ce=ce,
+                   source=dict(r=(15.0, 0.0, 0.0), E=source_E), tallies=tallies,
+                   meta=dict(seed=seed, grid_points=[int(x) for x in sizes], A=A.tolist()))
+
+
+def ce_infinite_medium(A=1.0, sigma_s=20.0, sigma_c=0.1, dens=0.05, kT=KT_293K, n_points=4000,
+                       source_E=None):
+    """One nuclide with constant elastic and capture cross sections in an all-reflective box: the
+    collision-density spectrum approaches the Maxwellian flux E exp(-E/kT) when the source starts
+    near thermal energies (free-gas scattering for A = 1)."""
+    e = np.geomspace(1.0e-11, 20.0, n_points)
+    e[0], e[-1] = 1.0e-11, 20.0
+    xs = np.zeros((n_points, 4))
+    xs[:, 1] = sigma_s
+    xs[:, 3] = sigma_c
+    xs[:, 0] = sigma_s + sigma_c
+    ce = ce_data([dict(e=e, xs=xs, A=A, kT=kT)], [[(0, dens)]])
+    gb = GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 100.0, 100.0, 100.0)
+    gb.root_universe(box, 1, bc=[abi.BC_REFLECTIVE] * 6)
+    return Problem(gb.arrays(), None, name="ce_infinite_medium", ce=ce,
+                   source=dict(r=(0.0, 0.0, 0.0), E=kT if source_E is None else source_E))

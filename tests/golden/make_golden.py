@@ -5,7 +5,10 @@ Contents
                147-168, 251-304) evaluated with Python integers, independent of the C++ code;
   pow_of_gsq   the 63-entry table of RandomNumbers/RNG_class.f90:61-123, parsed from the file;
   mgMat1/2     the 4-group data of IntegrationTestFiles/mgMat1 and mgMat2 (used by
-               NuclearData/mgNeutronData/baseMgNeutron/Tests/baseMgNeutronDatabase_iTest.f90).
+               NuclearData/mgNeutronData/baseMgNeutron/Tests/baseMgNeutronDatabase_iTest.f90);
+  h1_ace       the ESZ block (energy grid, total, absorption, elastic) and AW/TZ of the 1001.03c
+               table in IntegrationTestFiles/1001JEF311.ace, the H-1 data that
+               NuclearData/ceNeutronData/aceDatabase/Tests/aceNeutronDatabase_iTest.f90 reads.
 
 Run from the repository root with the SCONE sources at $SCONE_REF (default /root/reference); the
 committed JSON is what the tests read, so the sources are only needed to regenerate it.
@@ -60,6 +63,27 @@ def parse_mg(path):
     return d
 
 
+def parse_ace_esz(path, first_line):
+    """ESZ block of the ACE table starting at 1-based line `first_line` (aceCard_class.f90:262-301):
+    header line (ZAID AW TZ date), comment, 4 lines of IZ/AW pairs, NXS(16), JXS(32), then XSS."""
+    lines = open(path).read().splitlines()[first_line - 1:]
+    zaid, aw, tz = lines[0].split()[:3]
+    ints = " ".join(lines[6:12]).split()
+    nxs = [int(x) for x in ints[:16]]
+    jxs = [int(x) for x in ints[16:48]]
+    nes = nxs[2]
+    need = jxs[0] - 1 + 4 * nes
+    xss = []
+    for ln in lines[12:]:
+        xss.extend(float(x) for x in ln.split())
+        if len(xss) >= need:
+            break
+    p = jxs[0] - 1
+    blk = lambda k: xss[p + k * nes: p + (k + 1) * nes]
+    return dict(zaid=zaid, aw=float(aw), tz=float(tz), e=blk(0), total=blk(1), absorption=blk(2),
+                elastic=blk(3))
+
+
 def main():
     seed = 0x5C3A84C9
     xs, st = lcg_draws(seed, 1000)
@@ -74,9 +98,12 @@ def main():
         gold["pow_of_gsq"] = [str(v) for v in parse_table(tbl)]
         gold["mgMat1"] = parse_mg(os.path.join(REF, "IntegrationTestFiles", "mgMat1"))
         gold["mgMat2"] = parse_mg(os.path.join(REF, "IntegrationTestFiles", "mgMat2"))
+        lib = open(os.path.join(REF, "IntegrationTestFiles", "testLib")).read()
+        line = int(re.search(r"1001\.03c;\s*(\d+);", lib).group(1))
+        gold["h1_ace"] = parse_ace_esz(os.path.join(REF, "IntegrationTestFiles", "1001JEF311.ace"), line)
     elif os.path.exists(OUT):
         old = json.load(open(OUT))
-        for k in ("pow_of_gsq", "mgMat1", "mgMat2"):
+        for k in ("pow_of_gsq", "mgMat1", "mgMat2", "h1_ace"):
             gold[k] = old[k]
     with open(OUT, "w") as f:
         json.dump(gold, f, indent=1)
