@@ -13,6 +13,17 @@ k feedback, all resident on the device.
   roofline  the history-loop kernel: algorithmic bytes (128 B per event, mixed form) / kernel time
   cpu_baseline  the CPU restatement of SCONE (oracle/) on the host cores, bounded sample
 
+Beside the lattice line, the same JSON line carries the uneven batch (4096 independent fixed-source
+problems of 1-16 groups, spheres and multi-slabs, 1e3-1e6 histories each, 5.9e8 histories in all):
+
+  batched   histories/s of the batched form (every cycle of every problem in one persistent launch,
+            one CUDA graph), mixed precision, delta tracking, launch shape from the autotuner
+  plain     histories/s of the plain form over the same batch: one problem per launch sequence
+            (sg_fixed_source_cycle per cycle), event-based and history-loop kernels
+  tally error  per-bin relative errors of the batched mixed form against the all-FP64 batched form
+  serving   Poisson arrivals of requests drawn from the batch (plus 5 % lattice eigenvalue
+            requests), continuous batching: p50/p99 latency, achieved and offered histories/s
+
 `--impl reference` times SCONE's algorithm on the host cores instead (the oracle restatement: SCONE
 itself is Fortran and cannot be built here), on the same workload and metric.
 Multi-GPU (torchrun): independent replicas, one per rank, each with its own RNG offset (the path
@@ -49,6 +60,12 @@ def args_():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile", action="store_true", help="a short run for ncu captures")
+    ap.add_argument("--batch-problems", type=int, default=4096, help="problems of the uneven batch")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched / plain / served measurements")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain one-problem-per-launch forms")
+    ap.add_argument("--no-fp64-batch", action="store_true", help="skip the all-FP64 batched reference run")
+    ap.add_argument("--serve-seconds", type=float, default=15.0)
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -199,6 +216,124 @@ def reference_arm(a, p):
         "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
+
+
+def batched_section(a, local):
+    """The uneven batch: batched form vs the plain forms, tally error vs all-FP64, and serving."""
+    import numpy as np
+    from scone_gb300 import abi, gpu, problems, serve
+    out = {"workload": f"batched_uneven_{a.batch_problems}", "precision": "mixed", "transport": "DT"}
+    batch = problems.batched_uneven(n_problems=a.batch_problems)
+    total = int(sum(pop * c for _, pop, c, _ in batch))
+    out["histories_per_step"] = total
+    out["problems"] = len(batch)
+
+    def load(prec):
+        B = gpu.BatchGPU(precision=prec, transport=abi.TRANSPORT_DT, device=local, max_problems=2 * len(batch),
+                         arena_bytes=4 << 30, max_work_items=1 << 21)
+        return B, [B.add(p, pop, c, m) for p, pop, c, m in batch]
+
+    B, slots = load(abi.PREC_MIXED)
+    # autotuner on a stratified sample (every 8th problem), then the full batch
+    t0 = time.perf_counter()
+    out["tuning"] = B.autotune(slots[::8])
+    out["autotune_s"] = time.perf_counter() - t0
+    B.run(slots)                                                       # warm-up
+    for s in slots:
+        B.clear_tally(s)
+    steps = max(1, min(a.steps, 3))
+    ms = []
+    ev = 0
+    for _ in range(steps):
+        st = B.run(slots)
+        ms.append(st.run_ms)
+        ev = st.n_events
+    mean_ms = sum(ms) / len(ms)
+    out["value"] = total / (mean_ms / 1e3)
+    out["unit"] = "histories/s"
+    out["events_per_s"] = ev / (mean_ms / 1e3)
+    out["ms_per_step"] = mean_ms
+    out["gpu_launches_per_step"] = 2
+    mixed_bins = [B.bins(s) for s in slots]
+    # e2e: the public call plus the read-back of every problem's bins to the host
+    t0 = time.perf_counter()
+    B.run(slots)
+    d2h = 0
+    for s in slots:
+        d2h += B.bins(s).nbytes
+    we = time.perf_counter() - t0
+    out["e2e"] = {"value": total / we, "unit": "histories/s", "h2d_bytes_per_step": 16 * st.n_items + 4 * len(slots),
+                  "d2h_bytes_per_step": d2h}
+    # roofline of the batched kernel (same per-event bytes as the single-problem history loop)
+    peak, kind = measured_peaks()
+    ach = ev * BYTES_PER_EVENT_MIXED / (mean_ms / 1e3) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                       "peak_source": kind, "kernel": "k_batch (batched history loop)"}
+    if not a.no_plain:
+        for name, form in (("plain_event", abi.FORM_EVENT), ("plain_history", abi.FORM_HISTORY)):
+            B.run_plain(slots[:4], form=form)                          # warm-up (work handle, modules)
+            for s in slots:
+                B.clear_tally(s)
+            t0 = time.perf_counter()
+            st = B.run_plain(slots, form=form)
+            w = time.perf_counter() - t0
+            out[name] = {"value": total / w, "unit": "histories/s", "wall_s": w, "kernels": int(st.n_kernels),
+                         "transport_kernel_ms": st.kernel_ms}
+        out["speedup_vs_plain_event"] = out["value"] / out["plain_event"]["value"]
+        out["speedup_vs_plain_history"] = out["value"] / out["plain_history"]["value"]
+    if not a.no_fp64_batch:
+        B64, s64 = load(abi.PREC_FP64)
+        t0 = time.perf_counter()
+        st = B64.run(s64)
+        out["fp64"] = {"value": total / (st.run_ms / 1e3), "unit": "histories/s", "ms_per_step": st.run_ms}
+        ratios, zs = [], []
+        for mb, s in zip(mixed_bins, s64):
+            fb = B64.bins(s)
+            n = 10
+            m1, m2 = fb[:, 1] / n, mb[:, 1] / n
+            v1 = np.maximum(fb[:, 2] / n - m1 ** 2, 0) / (n - 1)
+            v2 = np.maximum(mb[:, 2] / n - m2 ** 2, 0) / (n - 1)
+            ok = (v1 > 0) & (v2 > 0) & (m1 > 0)
+            ratios += (np.sqrt(v2[ok]) / m2[ok] / (np.sqrt(v1[ok]) / m1[ok])).tolist()
+            zs += ((m2[ok] - m1[ok]) / np.sqrt(v1[ok] + v2[ok])).tolist()
+        r = np.abs(np.array(ratios) - 1.0)
+        out["tally_rel_error_vs_fp64"] = {"bins": len(ratios), "median_abs_dev": float(np.median(r)),
+                                          "p99_abs_dev": float(np.percentile(r, 99)),
+                                          "frac_within_10pct": float(np.mean(r < 0.10)),
+                                          "max_abs_z": float(np.max(np.abs(zs)))}
+        B64.close()
+    if not a.no_serve and a.serve_seconds > 0:
+        templates = [(pop, c) for _, pop, c, _ in batch]
+        mean_hist = float(np.mean([pop * c for pop, c in templates]))
+        lat = problems.lattice_17x17_7g()
+        res = {}
+        cap = out["value"]
+        tuning = out["tuning"]
+        B.close()
+        B = None
+        for name, rate, efrac in (("config4_2000rps", 2000.0, 0.05),
+                                  ("half_capacity", 0.5 * cap / mean_hist, 0.0)):
+            Bs, cat = load(abi.PREC_MIXED)
+            Bs.set_tuning(**tuning)
+            pool = serve.EigenPool(lat, 4, abi.PREC_MIXED, abi.TRANSPORT_DT, 100000) if efrac > 0 else None
+            S = serve.SolveServer(Bs, cat, wave_histories=1 << 21, eigen=pool)
+            offered = rate * ((1 - efrac) * mean_hist + efrac * 100000 * 60)
+            done, wall, n = serve.poisson_run(S, templates, rate, a.serve_seconds, seed=7, eigen_fraction=efrac,
+                                              drain=(efrac == 0), max_drain_s=30.0)
+            S.stop()
+            summ = serve.latency_summary(done, wall, offered)
+            summ.update({"arrival_rate": rate, "arrived": n, "eigen_fraction": efrac,
+                         "eigen_completed": sum(1 for r in done if r.kind == "eigen"),
+                         "waves": Bs.serve_status()[2]})
+            res[name] = summ
+            if pool:
+                for t, _ in pool.free:
+                    t.close()
+            Bs.close()
+        out["serving"] = res
+    if B is not None:
+        B.close()
+    return out
 
 
 def main():
@@ -358,6 +493,13 @@ def main():
             cpu = {"value": None, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
 
+    batched = None
+    if not a.no_batch and world == 1:
+        try:
+            batched = batched_section(a, local)
+        except Exception as e:  # reported, never silently replaced by anything else
+            batched = {"error": repr(e)}
+
     line = {
         "metric": "histories/s", "value": hist / sec, "unit": "histories/s", "n_gpus": world,
         "steps": a.steps, "warmup": warm, "ms_per_step": 1e3 * sec / a.steps, "higher_is_better": True,
@@ -371,7 +513,7 @@ def main():
                    "parallelism": f"replicas{world}"},
         "events_per_s": events / sec, "k_eff": ks[-1], "wall_ms_per_step": 1e3 * wall / a.steps,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-        "other_transport": alt,
+        "other_transport": alt, "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if pg:

@@ -333,6 +333,111 @@ int32_t sg_transport_bank_noalloc(sg_handle h, int32_t admin, const sg_bank* dev
                                   uint64_t master_state, double k_eff, sg_bank* dev_next,
                                   int32_t next_cap, int32_t* n_next);
 
+/* ---------------------------------------------------------------- batched solves */
+
+/* No single SCONE counterpart: SCONE solves one problem per process
+ * (fixedSourcePhysicsPackage%cycles, fixedSourcePhysicsPackage_class.f90:183-289).  A batch keeps
+ * many independent fixed-source MG problems resident in one device arena (its HBM budget) and
+ * transports every cycle of the problems it is given in ONE persistent launch fed from a device
+ * work queue.  Each problem gives the results that sg_fixed_source_cycle, called `cycles` times on
+ * a handle holding that problem alone, gives: the same RNG stream per history (bit-identical in
+ * SG_PREC_FP64), the same per-cycle scoreMemory closes. */
+typedef struct sg_batch_t* sg_batch;
+
+typedef struct sg_batch_config {
+  int32_t precision;            /* SG_PREC_*                               */
+  int32_t transport;            /* SG_TRANSPORT_*                          */
+  int32_t device;
+  int32_t max_problems;         /* resident problem slots                  */
+  int64_t arena_bytes;          /* device memory for problem data and score memory (admission budget) */
+  int32_t max_work_items;       /* capacity of the device work queue       */
+  int32_t reserved;
+} sg_batch_config;
+
+/* one fixed-source problem: geometry, MG data, point source, one tally admin (batch_size 1: every
+ * cycle closes a batch; k clerks are rejected), `cycles` cycles of `pop` histories from master_state */
+typedef struct sg_problem_desc {
+  const sg_geometry_desc*     geometry;
+  const sg_mg_desc*           mg;
+  const sg_point_source_desc* source;
+  const sg_tally_desc*        tally;
+  int32_t                     pop;
+  int32_t                     cycles;
+  uint64_t                    master_state;
+} sg_problem_desc;
+
+/* launch shape of the batched kernel, picked by sg_batch_autotune or set by hand */
+typedef struct sg_batch_tuning {
+  int32_t item_histories;       /* histories per work item                                      */
+  int32_t blocks_per_sm;        /* persistent grid = SMs x blocks_per_sm (capped by occupancy)  */
+  int32_t block_threads;        /* 32, 64, 96 or 128                                            */
+  int32_t order;                /* 0: submission order; 1: largest problem first                */
+} sg_batch_tuning;
+
+typedef struct sg_batch_stats {
+  int64_t n_histories;
+  int64_t n_events;             /* flight segments (device-counted) */
+  int64_t n_collisions;
+  int32_t n_problems;
+  int32_t n_items;              /* work items (batched) or 0 (plain) */
+  double  kernel_ms;            /* transport time, CUDA events: the run graph (batched) or the sum of
+                                   the transport kernels (plain) */
+  double  run_ms;               /* the whole call, CUDA events on the batch stream */
+  int64_t n_kernels;            /* kernels launched by the call */
+} sg_batch_stats;
+
+int32_t sg_batch_create(const sg_batch_config* cfg, sg_batch* out);
+int32_t sg_batch_destroy(sg_batch b);
+int32_t sg_batch_last_error(sg_batch b, char* buf, size_t len);
+/* uploads a problem into a free slot; SG_ERR_OOM when the arena or the slots are full */
+int32_t sg_batch_add(sg_batch b, const sg_problem_desc* p, int32_t* slot);
+/* a new request on the data of resident problem `parent` (geometry, MG data, source and clerks shared,
+ * nothing re-uploaded): its own pop, cycles, RNG seed and score memory, taken from the arena
+ * (SG_ERR_OOM when full).  Does not wait for the device. */
+int32_t sg_batch_instance(sg_batch b, int32_t parent, int32_t pop, int32_t cycles, uint64_t master_state,
+                          int32_t* slot);
+/* frees a slot and its arena memory (a parent only after its instances) */
+int32_t sg_batch_remove(sg_batch b, int32_t slot);
+/* arena bytes in use and capacity */
+int32_t sg_batch_memory(sg_batch b, int64_t* used, int64_t* capacity);
+int32_t sg_batch_set_tuning(sg_batch b, const sg_batch_tuning* t);
+int32_t sg_batch_get_tuning(sg_batch b, sg_batch_tuning* t);
+/* every cycle of the listed problems in one persistent launch, then the cycle closes (one CUDA
+ * graph launch); slots must be distinct */
+int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats* stats);
+/* the plain form: the listed problems one after another, each through sg_fixed_source_cycle's path
+ * (one problem per launch sequence), `form` SG_FORM_EVENT or SG_FORM_HISTORY */
+int32_t sg_batch_run_plain(sg_batch b, const int32_t* slots, int32_t n, int32_t form, sg_batch_stats* stats);
+/* measures candidate launch shapes on the listed problems (their tallies are cleared afterwards),
+ * keeps the fastest and returns it */
+int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_tuning* best);
+/* scoreMemory bins(N,3) of a problem, as sg_get_bins; while serving, only for completed requests
+ * (read beside the running waves) */
+int32_t sg_batch_tally_size(sg_batch b, int32_t slot, int64_t* n_bins);
+int32_t sg_batch_get_bins(sg_batch b, int32_t slot, double* bins, int64_t n_bins);
+int32_t sg_batch_clear_tally(sg_batch b, int32_t slot);
+
+/* ---------------------------------------------------------------- served solves (continuous batching) */
+
+/* Requests are resident problems.  sg_serve_submit queues every cycle of a problem (its tally is
+ * cleared); sg_serve_pump keeps up to two waves in flight on the device, each wave one launch of the
+ * batched kernel over work drawn from ALL active requests (each gets an equal share of the wave's
+ * `wave_histories`, so a request that arrives while others run joins the next wave), and retires
+ * requests whose last history ran: their cycles are closed in that wave.  Latency is submit time to
+ * the device completion of the request's last wave (CUDA event time mapped onto the host clock). */
+int32_t sg_serve_start(sg_batch b, int64_t wave_histories);
+int32_t sg_serve_submit(sg_batch b, int32_t slot);
+/* launches/retires waves; wait != 0 blocks until at least one in-flight wave completes.
+ * Completed requests since the last call are written to done_slots / latency_s (up to cap). */
+int32_t sg_serve_pump(sg_batch b, int32_t wait, int32_t* done_slots, double* latency_s, int32_t cap,
+                      int32_t* n_done);
+/* waits for the waves in flight and leaves serving mode (completed requests not yet pumped are dropped) */
+int32_t sg_serve_stop(sg_batch b);
+/* histories queued but not yet launched, requests active, waves launched so far */
+int32_t sg_serve_status(sg_batch b, int64_t* queued, int32_t* active, int64_t* waves);
+/* host clock (seconds, the one submit and latency use) */
+double sg_serve_clock(void);
+
 /* ---------------------------------------------------------------- verification records */
 
 /* Per-history records of the last gen loop (needs cfg.record_histories): number of real

@@ -115,6 +115,40 @@ class CycleStats(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("transport", C.c_int32), ("device", C.c_int32),
+        ("max_problems", C.c_int32), ("arena_bytes", C.c_int64), ("max_work_items", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [
+        ("geometry", C.POINTER(GeometryDesc)), ("mg", C.POINTER(MGDesc)),
+        ("source", C.POINTER(PointSourceDesc)), ("tally", C.POINTER(TallyDesc)),
+        ("pop", C.c_int32), ("cycles", C.c_int32), ("master_state", C.c_uint64),
+    ]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [
+        ("item_histories", C.c_int32), ("blocks_per_sm", C.c_int32), ("block_threads", C.c_int32),
+        ("order", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("n_histories", C.c_int64), ("n_events", C.c_int64), ("n_collisions", C.c_int64),
+        ("n_problems", C.c_int32), ("n_items", C.c_int32), ("kernel_ms", C.c_double),
+        ("run_ms", C.c_double), ("n_kernels", C.c_int64),
+    ]
+
+
 def _p(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 

@@ -24,6 +24,9 @@ UNITS = {
     "sg_support.cu": ["-fmad=false"],
     "sg_host.cu": ["-fmad=false"],
     "sg_noalloc.cu": ["-fmad=false"],
+    "sg_batch_fp64.cu": ["-fmad=false"],
+    "sg_batch_mixed.cu": [],
+    "sg_batch_host.cu": ["-fmad=false"],
 }
 
 

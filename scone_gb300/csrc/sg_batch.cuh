@@ -1,0 +1,167 @@
+// sg_batch.cuh -- the batched form of the gen loop: every cycle of many independent fixed-source
+// problems transported by one persistent launch, fed from a device work queue.
+//
+// SCONE runs one problem per process: fixedSourcePhysicsPackage%cycles generates the source, runs
+// the `gen:` loop and closes the tallies, cycle after cycle (fixedSourcePhysicsPackage_class.f90:
+// 183-289).  Here the cycles of all problems are flattened into one history space per problem
+// (f = c * pop + n - 1) and cut into work items; warps take items from a global queue.  A warp works
+// on one problem at a time: the problem's record (geometry, MG data, clerks) sits in the warp's slot
+// of shared memory, and lanes that end a history take the next history of the same item at once.
+// The warp moves to an item of another problem only when all of its lanes are idle.
+//
+// Each history reproduces the single-problem path exactly: pointSource sampling with master_c +
+// stride(n) (source_inter.f90:98-119, pointSource_class.f90:189-270), then transport with
+// master_c + stride(pop + n), where master_c is the problem's master strided by 2 * pop per cycle
+// (fixedSourcePhysicsPackage_class.f90:186-189,264).  Scores of cycle c go to that cycle's own
+// accumulator; the cycles are closed in order after the launch.
+#pragma once
+#include "sg_transport.cuh"
+#include "sg_batch.h"
+
+namespace sg {
+
+static constexpr int BATCH_MAX_WARPS = 4;   // __launch_bounds__(128)
+
+template <class R>
+__device__ __forceinline__ void stage_problem_warp(BatchProblem<R>* dst, const BatchProblem<R>* src, int lane) {
+  static_assert(sizeof(BatchProblem<R>) % 16 == 0, "record size");
+  const int4* s = reinterpret_cast<const int4*>(src);
+  int4* d = reinterpret_cast<int4*>(dst);
+  for (int i = lane; i < (int)(sizeof(BatchProblem<R>) / 16); i += 32) d[i] = __ldg(s + i);
+  __syncwarp();
+}
+
+// pointSource%sampleParticle (pointSource_class.f90:189-270), then the particle enters the gen loop
+// as thisCycle%copy + placeCoord would leave it.
+template <class R, int MAXL, bool DT>
+__device__ __forceinline__ void start_batched(Tracker<R, MAXL, DT, false>& T, const BatchProblem<R>& P, int f) {
+  const int c = f / P.pop;
+  const int n = f - c * P.pop + 1;
+  const long long base = 2LL * P.pop * c;
+  Rng<double> rs;
+  rs.s = lcg_skip(P.master, RNG_STRIDE * (base + n));
+  double d0 = P.src_dir[0], d1 = P.src_dir[1], d2 = P.src_dir[2];
+  if (P.src_isotropic) {
+    const double mu = 2.0 * rs.get() - 1.0;
+    double sp, cp;
+    sincos_phi<double>(rs.get(), sp, cp);
+    d0 = 1.0; d1 = 0.0; d2 = 0.0;
+    rotate_vector<double>(d0, d1, d2, mu, sp, cp);
+  }
+  int g = P.src_G;
+  if (P.src_n_prob_g > 0) {
+    double r = rs.get();
+    for (g = 1; g <= P.src_n_prob_g; ++g) {
+      r = r - P.src_prob_g[g - 1];
+      if (r < 0.0) break;
+    }
+  }
+  T.hist = n;
+  T.c.r0[0] = P.src_r[0];
+  T.c.r0[1] = P.src_r[1];
+  T.c.r0[2] = P.src_r[2];
+  T.c.u[0] = (R)d0;
+  T.c.u[1] = (R)d1;
+  T.c.u[2] = (R)d2;
+  T.w = R(1);
+  T.w0 = R(1);
+  T.G = g;
+  T.time = R(0);
+  T.rng.s = lcg_skip(P.master, RNG_STRIDE * (base + P.pop + n));
+  T.collN = 0;
+  T.nsites = 0;
+  T.segs = 0;
+  T.cache.lvl = 0;
+  T.acc = P.t.acc + (long long)c * P.n_bins;
+  if (!T.geom.place(T.c)) raise_error(P.t.ctr, SG_ERR_UNDEF_MAT, n);
+}
+
+template <class R, int MAXL, bool DT>
+__global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaunch L) {
+  __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
+  const int lane = threadIdx.x & 31;
+  BatchProblem<R>& P = *reinterpret_cast<BatchProblem<R>*>(s_rec[threadIdx.x >> 5]);
+  const BatchProblem<R>* probs = static_cast<const BatchProblem<R>*>(L.problems);
+  if (lane == 0) {                  // a neutral record until the first item is staged
+    P.t.k_eff = L.k_one;
+    P.t.ctr = L.ctr;
+    P.t.keff_clerk = -1;
+    P.t.n_clerks = 0;
+    P.t.acc = nullptr;
+  }
+  __syncwarp();
+  Tracker<R, MAXL, DT, false> T(P.t, nullptr);
+  const int nItems = *L.n_items;
+  int cur = -1;                     // slot of the staged problem (warp-uniform)
+  int pend = -1;                    // claimed item of another problem, waiting for the warp to drain
+  int q_next = 0, q_end = 0;        // warp-uniform range of flat histories of the current item
+  bool alive = false, done = false;
+
+  while (true) {
+    unsigned need = __ballot_sync(FULL, !alive && !done);
+    while (need) {
+      if (q_next >= q_end) {
+        int it = pend;
+        if (it < 0) {
+          int b = 0;
+          if (lane == 0) b = atomicAdd(L.head, 1);
+          it = __shfl_sync(FULL, b, 0);
+          if (it >= nItems) {
+            if (!alive) done = true;
+            break;
+          }
+        }
+        const WorkItem wi = L.items[it];
+        if (wi.slot != cur) {
+          if (__any_sync(FULL, alive)) { pend = it; break; }
+          stage_problem_warp<R>(&P, probs + wi.slot, lane);
+          cur = wi.slot;
+        }
+        pend = -1;
+        q_next = wi.first;
+        q_end = wi.first + wi.count;
+      }
+      const int avail = q_end - q_next;
+      const int rank = __popc(need & ((1u << lane) - 1u));
+      const bool mine = ((need >> lane) & 1u) && rank < avail;
+      if (mine) { start_batched<R, MAXL, DT>(T, P, q_next + rank); alive = true; }
+      q_next += min(__popc(need), avail);
+      need &= ~__ballot_sync(FULL, mine);
+    }
+    if (__all_sync(FULL, !alive)) {
+      if (__all_sync(FULL, done)) break;
+      continue;
+    }
+    if (alive) {
+      if (T.step()) { T.finish(); alive = false; }
+    }
+  }
+  flush_counters(T, P.t, lane);
+}
+
+}  // namespace sg
+
+namespace sg {
+
+template <class R>
+const void* batch_kernel_ptr(int maxl, bool dt) {
+  if (maxl <= 2) return dt ? (const void*)k_batch<R, 2, true> : (const void*)k_batch<R, 2, false>;
+  return dt ? (const void*)k_batch<R, 4, true> : (const void*)k_batch<R, 4, false>;
+}
+
+template <class R>
+cudaError_t launch_batch_impl(const BatchLaunch& L, bool dt, int grid, int block, cudaStream_t s) {
+  if (block < 32 || block > 32 * BATCH_MAX_WARPS || block % 32) return cudaErrorInvalidValue;
+  void* args[] = {(void*)&L};
+  return cudaLaunchKernel(batch_kernel_ptr<R>(L.maxl, dt), dim3(grid), dim3(block), args, 0, s);
+}
+
+template <class R>
+int batch_occupancy_impl(int maxl, bool dt, int block) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel_ptr<R>(maxl, dt), block, 0) != cudaSuccess)
+    return 1;
+  return per < 1 ? 1 : per;
+}
+
+}  // namespace sg

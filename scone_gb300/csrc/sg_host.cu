@@ -17,6 +17,7 @@
 #include "sg_launch.h"
 #include "sg_support.h"
 #include "sg_noalloc.h"
+#include "sg_batch.h"
 
 using namespace sg;
 
@@ -36,28 +37,56 @@ const double NUDGE_M = 1.0e-4;
     if (e_ != cudaSuccess) return h->fail(SG_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
+// While a Staging is installed on the calling thread, DArr takes its memory from a caller-owned
+// device block instead of cudaMalloc and writes uploads into that block's host image; the caller
+// commits the image with one copy.  `dev` null measures: offsets are counted, nothing is written.
+struct Staging {
+  char* dev = nullptr;
+  std::vector<char>* host = nullptr;
+  size_t used = 0;
+  size_t cap = 0;
+};
+thread_local Staging* t_staging = nullptr;
+
 template <class T>
 struct DArr {
   T* p = nullptr;
   size_t n = 0;
+  bool borrowed = false;
   cudaError_t alloc(size_t count) {
     free();
     n = count;
     if (count == 0) return cudaSuccess;
+    if (Staging* st = t_staging) {
+      const size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+      if (st->dev && st->used + bytes > st->cap) return cudaErrorMemoryAllocation;
+      p = reinterpret_cast<T*>((st->dev ? st->dev : reinterpret_cast<char*>(256)) + st->used);
+      st->used += bytes;
+      if (st->dev && st->host) st->host->resize(st->used, 0);
+      borrowed = true;
+      return cudaSuccess;
+    }
     return cudaMalloc((void**)&p, count * sizeof(T));
   }
   cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
     cudaError_t e = alloc(v.size() ? v.size() : 1);
     if (e != cudaSuccess) return e;
     if (v.empty()) return cudaSuccess;
+    if (borrowed) {
+      Staging* st = t_staging;
+      if (st && st->dev && st->host)
+        std::memcpy(st->host->data() + (reinterpret_cast<char*>(p) - st->dev), v.data(), v.size() * sizeof(T));
+      return cudaSuccess;
+    }
     e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(s);
   }
   void free() {
-    if (p) cudaFree(p);
+    if (p && !borrowed) cudaFree(p);
     p = nullptr;
     n = 0;
+    borrowed = false;
   }
 };
 
@@ -105,6 +134,7 @@ struct sg_handle_t {
   DArr<double> pinRsq, pinTol64, pinTolMx;
   DArr<float> pinRsqF, pinTolF;
   DArr<int2> graph;
+  std::vector<int2> graphHost;   // host copy of the graph (majorant materials)
   DGeom g64{}, gMx{};
 
   // MG data
@@ -387,6 +417,7 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
     CK(h->pinTolF.upload(tf, st));
   }
   CK(h->graph.upload(graph, st));
+  h->graphHost = graph;
   // mixed-form tie tolerance: 16 FP32 ulps of the largest root coordinate
   double scale = 1.0;
   for (int i = 0; i < 6; ++i) scale = std::max(scale, std::fabs(h->bounds[i]));
@@ -444,9 +475,7 @@ int build_mg(sg_handle h, const sg_mg_desc* d) {
       }
     }
   }
-  std::vector<int2> graph(h->graph.n);
-  CK(cudaMemcpy(graph.data(), h->graph.p, graph.size() * sizeof(int2), cudaMemcpyDeviceToHost));
-  std::vector<int> act = active_mats(h, graph);
+  std::vector<int> act = active_mats(h, h->graphHost);
   for (int a : act) if (a > M) return h->fail(SG_ERR_BAD_ARG, "mg: geometry uses a material beyond n_mat");
   std::vector<double> maj(nG, 0.0);                // initMajorant (baseMgNeutronDatabase :458-503)
   for (int g = 0; g < nG; ++g) {
@@ -520,10 +549,9 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
   for (int m = 0; m < nM; ++m)
     for (int k = d->mat_ptr[m]; k < d->mat_ptr[m + 1]; ++k)
       if (d->mat_nuc[k] < 0 || d->mat_nuc[k] >= nN) return h->fail(SG_ERR_BAD_ARG, "ce: bad nuclide index");
-  std::vector<int2> graph(h->graph.n);
-  CK(cudaMemcpy(graph.data(), h->graph.p, graph.size() * sizeof(int2), cudaMemcpyDeviceToHost));
-  std::vector<int> act;
-  for (auto& e : graph) if (e.x > 0) act.push_back(e.x);
+  const std::vector<int2>& graph = h->graphHost;
+  std::vector<int> act;                // materials the geometry uses (VOID, UNDEF and OVERLAP excluded)
+  for (auto& e : graph) if (e.x > 0 && e.x < SG_OVERLAP_MAT) act.push_back(e.x);
   std::sort(act.begin(), act.end());
   act.erase(std::unique(act.begin(), act.end()), act.end());
   for (int a : act)
@@ -1004,6 +1032,45 @@ int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
   return SG_OK;
 }
 
+// tallyAdmin%init (tallyAdmin_class.f90:162-255): clerk validation and scoreMemory layout of one admin
+int build_admin(sg_handle h, const sg_tally_desc* t, Admin& A) {
+  long long loc = 1;
+  for (int i = 0; i < t->n_clerks; ++i) {
+    const sg_clerk_desc& d = t->clerks[i];
+    long long size;
+    if (d.type == SG_CLERK_KEFF_ANALOG) { size = 3; A.keffAnalog = loc - 1; }
+    else if (d.type == SG_CLERK_KEFF_IMPLICIT) { size = 5; A.keffImplicit = loc - 1; }
+    else if (d.type == SG_CLERK_COLLISION || d.type == SG_CLERK_TRACK || d.type == SG_CLERK_SURFACE_CURRENT) {
+      const bool cur = d.type == SG_CLERK_SURFACE_CURRENT;
+      if ((!cur && (d.n_resp < 1 || d.n_resp > 4)) || d.n_axes < 0 || d.n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "tally: bad clerk");
+      if (cur && (d.current_axis < SG_AXIS_X || d.current_axis > SG_AXIS_Z || d.n_planes < 1 || d.n_planes > 8))
+        return h->fail(SG_ERR_BAD_ARG, "tally: surface-current clerk needs an axis and 1-8 planes");
+      long long nb = 1;
+      for (int a = 0; a < d.n_axes; ++a) {
+        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_ENERGY)
+          return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
+        if (d.axes[a].kind <= SG_AXIS_Z && !(d.axes[a].max > d.axes[a].min))
+          return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap needs max > min");
+        if (d.axes[a].kind == SG_AXIS_ENERGY && !(d.axes[a].min > 0.0 && d.axes[a].max > d.axes[a].min))
+          return h->fail(SG_ERR_BAD_ARG, "tally: log energy grid needs 0 < min < max");
+        nb *= d.axes[a].n;
+      }
+      size = cur ? nb * d.n_planes * 2 : nb * d.n_resp;
+    } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown clerk type");
+    A.clerks.push_back(d);
+    A.addr.push_back(loc);
+    loc += size;
+  }
+  A.N = loc - 1;
+  A.batchSize = t->batch_size > 0 ? t->batch_size : 1;
+  if (t->norm_clerk >= 0) {
+    if (t->norm_clerk >= t->n_clerks) return h->fail(SG_ERR_BAD_ARG, "tally: bad norm clerk");
+    A.normAddr = A.addr[t->norm_clerk];
+    A.normVal = t->norm_val;
+  }
+  return SG_OK;
+}
+
 }  // namespace
 
 // Bridge for sg_transport_bank_noalloc (sg_noalloc.cu): the launch arguments that do not depend on
@@ -1034,6 +1101,132 @@ int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<doubl
   t64->use_cache = t32->use_cache = h->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
   t64->max_segments = t32->max_segments = 1000000;
   return SG_OK;
+}
+
+// Bridge for the batched form (sg_batch_host.cu): builds one problem's resident data with the
+// single-problem builders, into a caller-owned device block through a host image (no allocation).
+int sg::stage_problem(const sg_geometry_desc* g, const sg_mg_desc* mg, const sg_point_source_desc* src,
+                      const sg_tally_desc* tally, char* dev, std::vector<char>* host, size_t cap, size_t* bytes,
+                      StagedProblem* out, std::string* err) {
+  sg_handle_t H;
+  H.cfg = sg_config{};
+  Staging st;
+  st.dev = dev;
+  st.host = host;
+  st.cap = cap;
+  if (dev && host) host->clear();
+  Staging* prev = t_staging;
+  t_staging = &st;
+  int rc = build_geometry(&H, g);
+  if (!rc) rc = build_mg(&H, mg);
+  if (!rc && src->n_prob_g > 0) {
+    std::vector<double> v(src->prob_g, src->prob_g + src->n_prob_g);
+    if (H.probG.upload(v, nullptr) != cudaSuccess) rc = H.fail(SG_ERR_OOM, "batch: problem larger than its block");
+  }
+  Admin A;
+  if (!rc) rc = build_admin(&H, tally, A);
+  if (!rc)
+    for (const auto& d : A.clerks)
+      if (d.type == SG_CLERK_KEFF_ANALOG || d.type == SG_CLERK_KEFF_IMPLICIT)
+        rc = H.fail(SG_ERR_BAD_ARG, "batch: k clerks need an eigenvalue run; batched problems are fixed-source");
+  if (!rc && H.anyFissile) rc = H.fail(SG_ERR_BAD_ARG, "batch: fixed-source problems with fissile materials are not supported");
+  if (!rc) {
+    A.off = 0;
+    H.admins.push_back(A);
+    long long lo = 0, hi = 0;
+    std::memset(&out->t64, 0, sizeof(out->t64));
+    std::memset(&out->t32, 0, sizeof(out->t32));
+    rc = build_clerks<double>(&H, 0, out->t64, lo, hi);
+    if (!rc) rc = build_clerks<float>(&H, 0, out->t32, lo, hi);
+  }
+  t_staging = prev;
+  *bytes = st.used;
+  if (rc) {
+    if (err) *err = H.err;
+    return rc;
+  }
+  out->t64.geom = H.g64;
+  out->t64.mg = H.mg64;
+  out->t32.geom = H.gMx;
+  out->t32.mg = H.mgMx;
+  out->maxl = H.maxl;
+  out->n_bins = A.N;
+  out->norm_addr = A.normAddr >= 1 ? A.normAddr - 1 : -1;
+  out->norm_val = A.normVal;
+  out->prob_g = H.probG.p;
+  out->any_fissile = H.anyFissile;
+  out->clerks = A.clerks;
+  out->addr = A.addr;
+  return SG_OK;
+}
+
+int sg::plain_fixed_source(sg_handle h, const StagedProblem& p, const sg_point_source_desc* src, double* acc,
+                           double* bin, double* csum, double* csum2, int pop, int cycles,
+                           unsigned long long master, sg_cycle_stats* total) {
+  if (pop > h->cap) return h->fail(SG_ERR_BANK_OVERFLOW, "plain: population larger than the work handle's banks");
+  // bind
+  const DGeom g64 = h->g64, gMx = h->gMx;
+  const DMG<double> mg64 = h->mg64;
+  const DMG<float> mgMx = h->mgMx;
+  const int maxl = h->maxl;
+  const bool hasGeom = h->hasGeom, hasMG = h->hasMG, hasCE = h->hasCE, anyFissile = h->anyFissile, hasSource = h->hasSource;
+  const PointSourceArgs psrc = h->psrc;
+  std::vector<Admin> admins;
+  admins.swap(h->admins);
+  DArr<double>* arrs[4] = {&h->acc, &h->bin, &h->csum, &h->csum2};
+  double* mine[4] = {acc, bin, csum, csum2};
+  DArr<double> kept[4];
+  for (int i = 0; i < 4; ++i) {
+    kept[i] = *arrs[i];
+    arrs[i]->p = mine[i];
+    arrs[i]->n = (size_t)p.n_bins;
+    arrs[i]->borrowed = true;
+  }
+  h->g64 = p.t64.geom;
+  h->gMx = p.t32.geom;
+  h->mg64 = p.t64.mg;
+  h->mgMx = p.t32.mg;
+  h->maxl = p.maxl;
+  h->hasGeom = h->hasMG = true;
+  h->hasCE = false;
+  h->anyFissile = p.any_fissile;
+  PointSourceArgs& q = h->psrc;
+  for (int i = 0; i < 3; ++i) { q.r[i] = src->r[i]; q.dir[i] = src->dir[i]; }
+  q.isotropic = src->isotropic;
+  q.G = src->G;
+  q.E = 0.0;
+  q.n_prob_g = src->n_prob_g;
+  q.prob_g = src->n_prob_g > 0 ? p.prob_g : nullptr;
+  h->hasSource = true;
+  Admin A;
+  A.clerks = p.clerks;
+  A.addr = p.addr;
+  A.N = p.n_bins;
+  A.off = 0;
+  A.normAddr = p.norm_addr >= 0 ? p.norm_addr + 1 : -1;
+  A.normVal = p.norm_val;
+  h->admins.push_back(A);
+  // run: fixedSourcePhysicsPackage%cycles, one call per cycle
+  int rc = SG_OK;
+  std::memset(total, 0, sizeof(*total));
+  uint64_t m = master;
+  for (int c = 0; c < cycles && rc == SG_OK; ++c) {
+    sg_cycle_stats st{};
+    rc = sg_fixed_source_cycle(h, 0, pop, &m, &st);
+    total->n_histories += st.n_histories;
+    total->n_events += st.n_events;
+    total->n_collisions += st.n_collisions;
+    total->transport_ms += st.transport_ms;
+    total->cycle_ms += st.cycle_ms;
+    total->n_kernels += st.n_kernels;
+  }
+  // restore
+  h->admins.swap(admins);
+  for (int i = 0; i < 4; ++i) *arrs[i] = kept[i];
+  h->g64 = g64; h->gMx = gMx; h->mg64 = mg64; h->mgMx = mgMx; h->maxl = maxl;
+  h->hasGeom = hasGeom; h->hasMG = hasMG; h->hasCE = hasCE; h->anyFissile = anyFissile;
+  h->psrc = psrc; h->hasSource = hasSource;
+  return rc;
 }
 
 // ====================================================================== C ABI
@@ -1112,40 +1305,8 @@ int32_t sg_upload_ce(sg_handle h, const sg_ce_desc* ce) {
 int32_t sg_upload_tally(sg_handle h, const sg_tally_desc* t, int32_t* admin_out) {
   if (!h || !t || !admin_out || t->n_clerks < 0) return SG_ERR_BAD_ARG;
   Admin A;
-  long long loc = 1;
-  for (int i = 0; i < t->n_clerks; ++i) {
-    const sg_clerk_desc& d = t->clerks[i];
-    long long size;
-    if (d.type == SG_CLERK_KEFF_ANALOG) { size = 3; A.keffAnalog = loc - 1; }
-    else if (d.type == SG_CLERK_KEFF_IMPLICIT) { size = 5; A.keffImplicit = loc - 1; }
-    else if (d.type == SG_CLERK_COLLISION || d.type == SG_CLERK_TRACK || d.type == SG_CLERK_SURFACE_CURRENT) {
-      const bool cur = d.type == SG_CLERK_SURFACE_CURRENT;
-      if ((!cur && (d.n_resp < 1 || d.n_resp > 4)) || d.n_axes < 0 || d.n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "tally: bad clerk");
-      if (cur && (d.current_axis < SG_AXIS_X || d.current_axis > SG_AXIS_Z || d.n_planes < 1 || d.n_planes > 8))
-        return h->fail(SG_ERR_BAD_ARG, "tally: surface-current clerk needs an axis and 1-8 planes");
-      long long nb = 1;
-      for (int a = 0; a < d.n_axes; ++a) {
-        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_ENERGY)
-          return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
-        if (d.axes[a].kind <= SG_AXIS_Z && !(d.axes[a].max > d.axes[a].min))
-          return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap needs max > min");
-        if (d.axes[a].kind == SG_AXIS_ENERGY && !(d.axes[a].min > 0.0 && d.axes[a].max > d.axes[a].min))
-          return h->fail(SG_ERR_BAD_ARG, "tally: log energy grid needs 0 < min < max");
-        nb *= d.axes[a].n;
-      }
-      size = cur ? nb * d.n_planes * 2 : nb * d.n_resp;
-    } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown clerk type");
-    A.clerks.push_back(d);
-    A.addr.push_back(loc);
-    loc += size;
-  }
-  A.N = loc - 1;
-  A.batchSize = t->batch_size > 0 ? t->batch_size : 1;
-  if (t->norm_clerk >= 0) {
-    if (t->norm_clerk >= t->n_clerks) return h->fail(SG_ERR_BAD_ARG, "tally: bad norm clerk");
-    A.normAddr = A.addr[t->norm_clerk];
-    A.normVal = t->norm_val;
-  }
+  int rc = build_admin(h, t, A);
+  if (rc) return rc;
   A.off = h->totalBins;
   // grow the device score memory, keeping what earlier admins hold
   long long newTotal = h->totalBins + A.N;

@@ -52,6 +52,20 @@ def load(build=True):
         "sg_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
         "sg_rng_draws": (i32, [P(u64), P(f64), i32]), "sg_rng_skip": (u64, [u64, i64]),
         "sg_transport_bank_noalloc": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(i32)]),
+        "sg_batch_create": (i32, [P(abi.BatchConfig), P(vp)]), "sg_batch_destroy": (i32, [vp]),
+        "sg_batch_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "sg_batch_add": (i32, [vp, P(abi.ProblemDesc), P(i32)]), "sg_batch_remove": (i32, [vp, i32]),
+        "sg_batch_instance": (i32, [vp, i32, i32, i32, u64, P(i32)]),
+        "sg_batch_memory": (i32, [vp, P(i64), P(i64)]),
+        "sg_batch_set_tuning": (i32, [vp, P(abi.BatchTuning)]), "sg_batch_get_tuning": (i32, [vp, P(abi.BatchTuning)]),
+        "sg_batch_run": (i32, [vp, P(i32), i32, P(abi.BatchStats)]),
+        "sg_batch_run_plain": (i32, [vp, P(i32), i32, i32, P(abi.BatchStats)]),
+        "sg_batch_autotune": (i32, [vp, P(i32), i32, P(abi.BatchTuning)]),
+        "sg_batch_tally_size": (i32, [vp, i32, P(i64)]), "sg_batch_get_bins": (i32, [vp, i32, P(f64), i64]),
+        "sg_batch_clear_tally": (i32, [vp, i32]),
+        "sg_serve_start": (i32, [vp, i64]), "sg_serve_submit": (i32, [vp, i32]),
+        "sg_serve_pump": (i32, [vp, i32, P(i32), P(f64), i32, P(i32)]), "sg_serve_stop": (i32, [vp]),
+        "sg_serve_status": (i32, [vp, P(i64), P(i32), P(i64)]), "sg_serve_clock": (f64, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -197,6 +211,160 @@ class TransportOperatorGPU:
         st = abi.CycleStats()
         self._check(self.L.sg_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
         return m.value, st
+
+
+class BatchGPU:
+    """Many independent fixed-source problems resident on one GPU (sg_batch_* / sg_serve_*).
+
+    ``add(problem, pop, cycles, master)`` uploads a problem into the batch arena and returns its slot;
+    ``run(slots)`` transports every cycle of the listed problems in one persistent launch (the batched
+    form); ``run_plain(slots, form)`` runs them one problem per launch sequence (the plain form);
+    ``bins(slot)`` returns scoreMemory bins(N, {BIN, CSUM, CSUM2}) as an (N, 3) array.  Serving:
+    ``serve_start(wave_histories)``, ``submit(slot)``, ``pump(wait)`` -> [(slot, latency_s)]."""
+
+    def __init__(self, precision=abi.PREC_MIXED, transport=abi.TRANSPORT_DT, device=0, max_problems=4096,
+                 arena_bytes=1 << 30, max_work_items=1 << 20):
+        self.L = load()
+        self.b = C.c_void_p()
+        cfg = abi.BatchConfig(precision, transport, device, max_problems, arena_bytes, max_work_items, 0)
+        rc = self.L.sg_batch_create(C.byref(cfg), C.byref(self.b))
+        if rc != 0:
+            raise SconeGpuError(f"sg_batch_create failed with {rc} (is a CUDA device present?)")
+        self.meta = {}
+
+    def _check(self, rc, ok=(0,)):
+        if rc not in ok:
+            buf = C.create_string_buffer(512)
+            self.L.sg_batch_last_error(self.b, buf, 512)
+            raise SconeGpuError(f"libsconegpu error {rc}: {buf.value.decode()}")
+        return rc
+
+    def close(self):
+        if self.b:
+            self.L.sg_batch_destroy(self.b)
+            self.b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, problem, pop, cycles, master, clerks=None):
+        """Upload a fixed-source MG problem; returns its slot (SconeGpuError with code -2 when the
+        arena or the slots are full)."""
+        g, kg = abi.geometry_struct(problem.geometry)
+        m, km = abi.mg_struct(problem.mg)
+        src = dict(problem.source)
+        s, ks = abi.point_source_struct(src.pop("r"), **src)
+        t, kt = abi.tally_struct(clerks if clerks is not None else problem.tallies["flux"])
+        d = abi.ProblemDesc(C.pointer(g), C.pointer(m), C.pointer(s), C.pointer(t), int(pop), int(cycles),
+                            C.c_uint64(master))
+        slot = C.c_int32()
+        self._check(self.L.sg_batch_add(self.b, C.byref(d), C.byref(slot)))
+        self.meta[slot.value] = dict(pop=int(pop), cycles=int(cycles))
+        del kg, km, ks, kt
+        return slot.value
+
+    def try_add(self, problem, pop, cycles, master, clerks=None):
+        """As add, but returns None when the arena or the slots are full (admission by HBM budget)."""
+        try:
+            return self.add(problem, pop, cycles, master, clerks)
+        except SconeGpuError as e:
+            if "error -2:" in str(e):
+                return None
+            raise
+
+    def instance(self, parent, pop, cycles, master):
+        """A request on resident problem `parent`'s data with its own size, seed and score memory;
+        None when the arena or the slots are full (admission by HBM budget)."""
+        slot = C.c_int32()
+        rc = self._check(self.L.sg_batch_instance(self.b, parent, int(pop), int(cycles), C.c_uint64(master),
+                                                  C.byref(slot)), ok=(0, -2))
+        if rc == -2:
+            return None
+        self.meta[slot.value] = dict(pop=int(pop), cycles=int(cycles), parent=parent)
+        return slot.value
+
+    def remove(self, slot):
+        self._check(self.L.sg_batch_remove(self.b, slot))
+        self.meta.pop(slot, None)
+
+    def memory(self):
+        u, c = C.c_int64(), C.c_int64()
+        self._check(self.L.sg_batch_memory(self.b, C.byref(u), C.byref(c)))
+        return u.value, c.value
+
+    @staticmethod
+    def _slots(slots):
+        a = np.ascontiguousarray(slots, dtype=np.int32)
+        return a, a.ctypes.data_as(C.POINTER(C.c_int32))
+
+    def tuning(self):
+        t = abi.BatchTuning()
+        self._check(self.L.sg_batch_get_tuning(self.b, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = abi.BatchTuning()
+        self._check(self.L.sg_batch_get_tuning(self.b, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self.L.sg_batch_set_tuning(self.b, C.byref(t)))
+
+    def run(self, slots):
+        a, p = self._slots(slots)
+        st = abi.BatchStats()
+        self._check(self.L.sg_batch_run(self.b, p, len(a), C.byref(st)))
+        return st
+
+    def run_plain(self, slots, form=abi.FORM_EVENT):
+        a, p = self._slots(slots)
+        st = abi.BatchStats()
+        self._check(self.L.sg_batch_run_plain(self.b, p, len(a), form, C.byref(st)))
+        return st
+
+    def autotune(self, slots):
+        a, p = self._slots(slots)
+        t = abi.BatchTuning()
+        self._check(self.L.sg_batch_autotune(self.b, p, len(a), C.byref(t)))
+        return t.as_dict()
+
+    def bins(self, slot):
+        n = C.c_int64()
+        self._check(self.L.sg_batch_tally_size(self.b, slot, C.byref(n)))
+        out = np.zeros(3 * max(n.value, 1))
+        self._check(self.L.sg_batch_get_bins(self.b, slot, out.ctypes.data_as(C.POINTER(C.c_double)), n.value))
+        return out[:3 * n.value].reshape(3, n.value).T.copy()
+
+    def clear_tally(self, slot):
+        self._check(self.L.sg_batch_clear_tally(self.b, slot))
+
+    # ---- serving
+    def serve_start(self, wave_histories):
+        self._check(self.L.sg_serve_start(self.b, int(wave_histories)))
+
+    def submit(self, slot):
+        self._check(self.L.sg_serve_submit(self.b, slot))
+
+    def pump(self, wait=False, cap=4096):
+        s = np.zeros(cap, np.int32)
+        lat = np.zeros(cap)
+        n = C.c_int32()
+        self._check(self.L.sg_serve_pump(self.b, 1 if wait else 0, s.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         lat.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(n)))
+        return list(zip(s[:n.value].tolist(), lat[:n.value].tolist()))
+
+    def serve_status(self):
+        q, a, w = C.c_int64(), C.c_int32(), C.c_int64()
+        self._check(self.L.sg_serve_status(self.b, C.byref(q), C.byref(a), C.byref(w)))
+        return q.value, a.value, w.value
+
+    def serve_stop(self):
+        self._check(self.L.sg_serve_stop(self.b))
+
+    def clock(self):
+        return self.L.sg_serve_clock()
 
 
 def rng_draws(state, n):

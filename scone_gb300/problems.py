@@ -11,6 +11,8 @@ Workloads (all synthetic, seeded with numpy default_rng):
   * ``lattice_17x17_7g``    -- 17x17 pin lattice, 7 groups, k-eigenvalue.
   * ``ce_slab_3layer``      -- continuous-energy 3-layer slab (5/20/5 cm), 10 synthetic nuclides,
                                fixed source, log-energy surface-current tally.
+  * ``batched_uneven``      -- many independent fixed-source problems of uneven size (group counts
+                               {1,2,4,7,16}, a sphere or a 1-D multi-slab, log-uniform history counts).
 """
 import numpy as np
 
@@ -358,3 +360,85 @@ def ce_infinite_medium(A=1.0, sigma_s=20.0, sigma_c=0.1, dens=0.05, kT=KT_293K, 
     gb.root_universe(box, 1, bc=[abi.BC_REFLECTIVE] * 6)
     return Problem(gb.arrays(), None, name="ce_infinite_medium", ce=ce,
                    source=dict(r=(0.0, 0.0, 0.0), E=kT if source_E is None else source_E))
+
+
+# ----------------------------------------------------------------------------- batched workload
+GROUP_CHOICES = (1, 2, 4, 7, 16)
+
+
+def _fixed_source_xs(rng, n_g):
+    """One material's data as in the infinite-medium workload, for n_g groups: Sigma_t ~ U[0.5, 2.0],
+    scattering ratio 0.9 with downscatter only (an in-group fraction, the rest spread over the lower
+    energy groups, decaying), capture 0.1 Sigma_t, no fission."""
+    sig_t = rng.uniform(0.5, 2.0, size=n_g)
+    P0 = np.zeros((n_g, n_g))
+    for g in range(n_g):
+        s = 0.9 * sig_t[g]
+        if g == n_g - 1:
+            P0[g, g] = s
+            continue
+        w = np.zeros(n_g)
+        w[g] = rng.uniform(0.3, 0.9)
+        for d in range(1, n_g - g):
+            w[g + d] = (1.0 - w[g]) * 0.5 ** d
+        P0[g] = s * w / w.sum()
+    return sig_t, P0, 0.1 * sig_t
+
+
+def fixed_source_problem(rng, n_g, kind, radius=None, layers=None):
+    """One problem of the batched workload: a homogeneous sphere (vacuum boundary) or a 1-D multi-slab
+    (xPlane layers in a cellUniverse, vacuum in x, reflective in y and z), n_g groups, an isotropic
+    point source in group 1 at the origin, and a collision-estimator flux tally per group."""
+    gb = GeometryBuilder()
+    if kind == "sphere":
+        R = float(radius if radius is not None else rng.uniform(1.0, 50.0))
+        sph = gb.surface(abi.SPHERE, 0.0, 0.0, 0.0, R)
+        gb.root_universe(sph, 1, bc=[abi.BC_VACUUM] * 6)
+        mats = [_fixed_source_xs(rng, n_g)]
+        meta = dict(kind="sphere", radius=R)
+    else:
+        L = int(layers if layers is not None else rng.integers(2, 11))
+        widths = rng.uniform(1.0, 10.0, size=L)
+        edges = np.concatenate([[0.0], np.cumsum(widths)])
+        edges = edges - edges[-1] / 2.0                      # slab centred on the source
+        half = edges[-1]
+        box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, half, 10.0, 10.0)
+        planes = [gb.surface(abi.XPLANE, float(x)) for x in edges[1:-1]]
+        cells = []
+        for i in range(L):
+            sides = []
+            if i > 0:
+                sides.append(planes[i - 1] + 1)
+            if i < L - 1:
+                sides.append(-(planes[i] + 1))
+            cells.append(gb.cell(sides))
+        slab = gb.cell_universe(cells, list(range(1, L + 1)))
+        gb.root_universe(box, uni_fill(slab), bc=[abi.BC_VACUUM, abi.BC_VACUUM] + [abi.BC_REFLECTIVE] * 4)
+        mats = [_fixed_source_xs(rng, n_g) for _ in range(L)]
+        meta = dict(kind="slab", layers=L, edges=edges.tolist())
+    mg = mg_data(n_g, np.array([m[0] for m in mats]), np.array([m[1] for m in mats]),
+                 capture=np.array([m[2] for m in mats]))
+    tallies = dict(flux=[abi.clerk(abi.CLERK_COLLISION, resp=(abi.RESP_FLUX,),
+                                   axes=[(abi.AXIS_GROUP, n_g, 0.0, 0.0)])])
+    meta["groups"] = n_g
+    return Problem(gb.arrays(), mg, name=f"{meta['kind']}_{n_g}g", eigen=False,
+                   source=dict(r=(0.0, 0.0, 0.0), G=1), tallies=tallies, meta=meta)
+
+
+def batched_uneven(n_problems=4096, seed=31, hist_min=1.0e3, hist_max=1.0e6, cycles=10):
+    """The uneven batch: n_problems independent fixed-source problems, each with a seeded group count
+    in {1, 2, 4, 7, 16}, a sphere (radius U[1, 50] cm) or a 1-D multi-slab (2-10 layers), synthetic XS
+    as in the infinite-medium workload and a log-uniform history count in [hist_min, hist_max], run as
+    `cycles` cycles of pop = histories / cycles.  Returns [(problem, pop, cycles, master)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_problems):
+        n_g = int(rng.choice(GROUP_CHOICES))
+        kind = "sphere" if rng.uniform() < 0.5 else "slab"
+        p = fixed_source_problem(rng, n_g, kind)
+        hist = float(np.exp(rng.uniform(np.log(hist_min), np.log(hist_max))))
+        pop = max(1, int(round(hist / cycles)))
+        master = int(rng.integers(1, 2 ** 63 - 1))
+        p.meta["index"] = i
+        out.append((p, pop, cycles, master))
+    return out

@@ -1,0 +1,192 @@
+"""Request loop of the served form: independent fixed-source solves arriving over time, run by
+continuous batching on one GPU.
+
+The problem catalogue (geometry, MG data, sources, clerks) stays resident in a BatchGPU arena.  A
+request names a catalogue entry, a history count and an RNG seed; it is admitted as an instance
+(its own score memory, taken from the arena, so the arena's size is the HBM budget that admission
+obeys) as soon as memory allows, and joins the next wave of the batched kernel: every wave gives
+each active request an equal share of its histories, so requests that arrive while others run start
+at once and overlap with them on the device.  Completed requests return their scoreMemory bins and
+their latency (arrival to device completion of their last wave).
+
+Eigenvalue requests (the lattice k-eigenvalue problem) run on a small pool of resident
+TransportOperatorGPU handles, one cycle per loop turn, on their own CUDA streams beside the waves.
+"""
+import collections
+import math
+
+import numpy as np
+
+from . import abi, gpu
+
+
+class Request:
+    __slots__ = ("rid", "kind", "template", "pop", "cycles", "master", "arrival", "slot", "submitted",
+                 "latency", "bins", "k", "handle", "cycle", "histories")
+
+    def __init__(self, rid, kind, template, pop, cycles, master, arrival):
+        self.rid, self.kind, self.template = rid, kind, template
+        self.pop, self.cycles, self.master, self.arrival = pop, cycles, master, arrival
+        self.slot = self.submitted = self.latency = self.bins = self.k = self.handle = None
+        self.cycle = 0
+        self.histories = pop * cycles
+
+
+class EigenPool:
+    """Resident lattice eigenvalue handles; a request takes one, runs inactive + active cycles."""
+
+    def __init__(self, problem, size, precision, transport, pop, form=abi.FORM_HISTORY):
+        self.problem = problem
+        self.free = []
+        for _ in range(size):
+            t = gpu.TransportOperatorGPU(problem, precision=precision, transport=transport,
+                                         max_bank=int(2.5 * pop) + 4096, form=form)
+            inact = t.upload_tally([])
+            ia = t.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+            act = t.upload_tally([])
+            aa = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+            t.attach_tally(inact, ia)
+            t.attach_tally(act, aa)
+            self.free.append((t, (inact, ia, act, aa)))
+
+    def take(self):
+        return self.free.pop() if self.free else None
+
+    def give(self, h):
+        self.free.append(h)
+
+
+class SolveServer:
+    """Continuous-batching request loop over a BatchGPU (fixed-source requests) and an optional
+    EigenPool (eigenvalue requests)."""
+
+    def __init__(self, batch, catalogue, wave_histories=1 << 21, eigen=None, eigen_cycles=(20, 40)):
+        self.B = batch
+        self.catalogue = catalogue            # resident slots that requests instantiate
+        self.waiting = collections.deque()    # fixed-source requests not yet admitted (arena full)
+        self.running = {}                     # slot -> request
+        self.eigen = eigen
+        self.eigen_cycles = eigen_cycles
+        self.eigen_waiting = collections.deque()
+        self.eigen_running = []
+        self.done = []
+        self.B.serve_start(wave_histories)
+
+    # ---- requests
+    def submit(self, req):
+        if req.kind == "eigen":
+            self.eigen_waiting.append(req)
+        else:
+            self.waiting.append(req)
+        self._admit()
+
+    def _admit(self):
+        while self.waiting:
+            r = self.waiting[0]
+            slot = self.B.instance(self.catalogue[r.template], r.pop, r.cycles, r.master)
+            if slot is None:
+                break                          # HBM budget exhausted: wait for completions
+            self.waiting.popleft()
+            r.slot = slot
+            r.submitted = self.B.clock()
+            self.B.submit(slot)
+            self.running[slot] = r
+        while self.eigen_waiting and self.eigen is not None:
+            h = self.eigen.take()
+            if h is None:
+                break
+            r = self.eigen_waiting.popleft()
+            t, (inact, ia, act, aa) = h
+            t.eigen_init(r.pop, r.master)
+            r.handle = h
+            r.submitted = self.B.clock()
+            self.eigen_running.append(r)
+
+    def _eigen_step(self):
+        """One cycle of every running eigenvalue request."""
+        still = []
+        for r in self.eigen_running:
+            t, (inact, ia, act, aa) = r.handle
+            if r.cycle < self.eigen_cycles[0]:
+                t.eigen_cycle(inact, ia)
+            else:
+                st = t.eigen_cycle(act, aa)
+                r.k = st.k_new
+            r.cycle += 1
+            if r.cycle >= sum(self.eigen_cycles):
+                r.latency = self.B.clock() - r.arrival
+                r.k = t.keff(aa)
+                self.eigen.give(r.handle)
+                r.handle = None
+                self.done.append(r)
+            else:
+                still.append(r)
+        self.eigen_running = still
+
+    def pump(self, wait=False):
+        """Launch and retire waves; returns the requests completed since the last call."""
+        for slot, lat in self.B.pump(wait=wait and bool(self.running) and not self.eigen_running):
+            r = self.running.pop(slot)
+            r.latency = lat + (r.submitted - r.arrival)
+            r.bins = self.B.bins(slot)
+            self.B.remove(slot)
+            self.done.append(r)
+        if self.eigen_running:
+            self._eigen_step()
+        self._admit()
+        out, self.done = self.done, []
+        return out
+
+    def outstanding(self):
+        return len(self.waiting) + len(self.running) + len(self.eigen_waiting) + len(self.eigen_running)
+
+    def stop(self):
+        self.B.serve_stop()
+
+
+def poisson_run(server, templates, rate, duration, seed=1, eigen_fraction=0.0, eigen_pop=100000,
+                drain=True, max_drain_s=120.0):
+    """Drives `server` with a Poisson arrival stream of `rate` requests/s for `duration` seconds.
+    templates: [(pop, cycles)] of the catalogue entries (fixed-source requests copy their entry's
+    size); a fraction `eigen_fraction` of requests are eigenvalue requests.  Returns the completed
+    requests and the wall time."""
+    rng = np.random.default_rng(seed)
+    clock = server.B.clock
+    t0 = clock()
+    next_at = t0 + rng.exponential(1.0 / rate)
+    rid = 0
+    finished = []
+    end = t0 + duration
+    while True:
+        now = clock()
+        while next_at <= now and next_at < end:
+            if eigen_fraction > 0 and rng.uniform() < eigen_fraction:
+                cyc = sum(server.eigen_cycles)
+                r = Request(rid, "eigen", -1, eigen_pop, cyc, int(rng.integers(1, 2 ** 62)), next_at)
+            else:
+                k = int(rng.integers(len(templates)))
+                pop, cycles = templates[k]
+                r = Request(rid, "fixed", k, pop, cycles, int(rng.integers(1, 2 ** 62)), next_at)
+            server.submit(r)
+            rid += 1
+            next_at += rng.exponential(1.0 / rate)
+        if now >= end and (not drain or server.outstanding() == 0 or now > end + max_drain_s):
+            break
+        idle = next_at - now
+        finished += server.pump(wait=idle > 0.002 or now >= end)
+    wall = clock() - t0
+    return finished, wall, rid
+
+
+def latency_summary(reqs, wall, offered_histories):
+    lat = np.array([r.latency for r in reqs]) if reqs else np.zeros(1)
+    hist = float(sum(r.histories for r in reqs))
+    return {
+        "completed": len(reqs),
+        "p50_ms": float(np.percentile(lat, 50) * 1e3),
+        "p99_ms": float(np.percentile(lat, 99) * 1e3),
+        "mean_ms": float(lat.mean() * 1e3),
+        "histories_per_s": hist / wall if wall > 0 else 0.0,
+        "offered_histories_per_s": offered_histories,
+        "wall_s": wall,
+    }

@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "scone_gpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int32_t|uint64_t)\s+(sg_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int32_t|uint64_t|double)\s+(sg_\w+)\s*\(", text, re.M)))
 
 
 def test_library_exports_all_declared_symbols():

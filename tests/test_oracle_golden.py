@@ -355,3 +355,40 @@ def test_lattice_eigen_st_dt_agree(oracle_mod):
         res.append(o.keff(aa))
     (k1, s1), (k2, s2) = res
     assert abs(k1 - k2) < 4 * math.hypot(s1, s2)
+
+
+def test_batched_workload_shape():
+    """The uneven batch has the stated distribution: group counts {1,2,4,7,16}, spheres of radius
+    1-50 cm or 2-10 layer slabs, log-uniform history counts in [1e3, 1e6] (mean ~1.45e5)."""
+    from scone_gb300 import problems
+    b = problems.batched_uneven(n_problems=512, seed=31)
+    groups = {p.meta["groups"] for p, *_ in b}
+    assert groups == set(problems.GROUP_CHOICES)
+    for p, pop, cycles, master in b:
+        h = pop * cycles
+        assert 995 <= h <= 1_000_005 and cycles == 10 and 0 < master < 2 ** 63
+        if p.meta["kind"] == "sphere":
+            assert 1.0 <= p.meta["radius"] <= 50.0
+        else:
+            assert 2 <= p.meta["layers"] <= 10
+        assert p.mg["n_g"] == p.meta["groups"]
+    logh = np.log10([pop * c for _, pop, c, _ in b])
+    assert abs(logh.mean() - 4.5) < 0.15
+
+
+def test_oracle_runs_batched_problem_kinds(oracle_mod):
+    """Sphere and multi-slab problems run through the oracle's fixed-source cycle; the flux tally has
+    one bin per group and every history ends (leakage through the vacuum boundary)."""
+    from scone_gb300 import problems
+    rng = np.random.default_rng(5)
+    for kind in ("sphere", "slab"):
+        for ng in (1, 16):
+            p = problems.fixed_source_problem(rng, ng, kind)
+            o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_DT)
+            a = o.upload_tally(p.tallies["flux"])
+            m = 777
+            for _ in range(2):
+                m, st = o.fixed_source_cycle(a, 300, m)
+            b = o.bins(a)
+            assert b.shape == (ng, 3) and np.all(b[:, 1] >= 0) and b[0, 1] > 0
+            assert st.n_histories == 300
