@@ -65,8 +65,17 @@ def args_():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-problem-per-launch forms")
     ap.add_argument("--no-fp64-batch", action="store_true", help="skip the all-FP64 batched reference run")
     ap.add_argument("--serve-seconds", type=float, default=15.0)
+    ap.add_argument("--wave-histories", type=int, default=1 << 23, help="histories per serving wave")
+    ap.add_argument("--serve-item", type=int, default=256, help="histories per work item while serving")
     ap.add_argument("--no-serve", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape of the batch")
+    ap.add_argument("--no-configs", action="store_true", help="skip the infinite-medium and CE-slab lines")
+    a = ap.parse_args()
+    if a.profile:   # a short run for ncu: lattice cycles and one small batch, nothing else
+        a.no_cpu_baseline = a.no_e2e = a.no_alt = a.no_plain = a.no_fp64_batch = a.no_serve = True
+        a.no_autotune = a.no_configs = True
+        a.batch_problems = min(a.batch_problems, 256)
+    return a
 
 
 def dist_env():
@@ -218,6 +227,55 @@ def reference_arm(a, p):
     return line
 
 
+def configs_section(a, local):
+    """The other two workloads, each through sg_fixed_source_cycle on its own handle (device-resident
+    source, gen loop and batch close) and through the oracle on the host cores:
+    infinite homogeneous medium, 2 groups, 1e5 histories; continuous-energy 3-layer slab, 1e7
+    histories (10 cycles of 1e6), FP32 tables with FP64 energy and position."""
+    from oracle import oracle
+    from scone_gb300 import abi, gpu, problems
+    threads = os.cpu_count() or 1
+    out = {}
+    cases = [("infinite_medium_2g", problems.infinite_medium_2g(), "flux", 100000, 1, abi.TRANSPORT_ST),
+             ("ce_slab_3layer", problems.ce_slab_3layer(), "current", 1000000, 10, abi.TRANSPORT_DT)]
+    for name, p, tally, pop, cycles, tr in cases:
+        res = {"histories": pop * cycles, "transport": "ST" if tr == abi.TRANSPORT_ST else "DT"}
+        for prec_name, prec in (("mixed", abi.PREC_MIXED), ("fp64", abi.PREC_FP64)):
+            t = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=pop + 4096, device=local,
+                                         form=abi.FORM_HISTORY)
+            adm = t.upload_tally(p.tallies[tally])
+            m = SEED
+            t.fixed_source_cycle(adm, min(pop, 10000), m)                # warm-up
+            ms = ev = 0.0
+            for _ in range(cycles):
+                m, st = t.fixed_source_cycle(adm, pop, m)
+                ms += st.cycle_ms
+                ev += st.n_events
+            res[prec_name] = {"value": pop * cycles / (ms / 1e3), "unit": "histories/s",
+                              "events_per_s": ev / (ms / 1e3), "ms": ms}
+            t.close()
+        # the oracle on the host cores, a bounded sample (about 10 s)
+        o = oracle.Oracle(p, transport=tr)
+        adm = o.upload_tally(p.tallies[tally])
+        n = min(pop, 200000 if name.startswith("ce") else 1000000)
+        bank = o.generate_source(SEED, n)
+        hist = ev = 0
+        t0 = time.perf_counter()
+        rep = 0
+        while time.perf_counter() - t0 < 10.0:
+            nh, e = o.timed_gen_loop(adm, bank, 4242 + rep, 1.0, threads)
+            hist += nh
+            ev += e
+            rep += 1
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": hist / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+                               "sample": f"{hist} histories ({rep} x the gen loop over {n} source particles), "
+                                         f"{dt:.1f} s"}
+        res["speedup_mixed_vs_cpu"] = res["mixed"]["value"] / res["cpu_baseline"]["value"]
+        out[name] = res
+    return out
+
+
 def batched_section(a, local):
     """The uneven batch: batched form vs the plain forms, tally error vs all-FP64, and serving."""
     import numpy as np
@@ -236,7 +294,7 @@ def batched_section(a, local):
     B, slots = load(abi.PREC_MIXED)
     # autotuner on a stratified sample (every 8th problem), then the full batch
     t0 = time.perf_counter()
-    out["tuning"] = B.autotune(slots[::8])
+    out["tuning"] = B.tuning() if a.no_autotune else B.autotune(slots[::8])
     out["autotune_s"] = time.perf_counter() - t0
     B.run(slots)                                                       # warm-up
     for s in slots:
@@ -254,6 +312,10 @@ def batched_section(a, local):
     out["events_per_s"] = ev / (mean_ms / 1e3)
     out["ms_per_step"] = mean_ms
     out["gpu_launches_per_step"] = 2
+    # one clean run for the tally comparison with the FP64 form (the timed runs accumulated)
+    for s in slots:
+        B.clear_tally(s)
+    B.run(slots)
     mixed_bins = [B.bins(s) for s in slots]
     # e2e: the public call plus the read-back of every problem's bins to the host
     t0 = time.perf_counter()
@@ -270,6 +332,7 @@ def batched_section(a, local):
     out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                        "peak_source": kind, "kernel": "k_batch (batched history loop)"}
     if not a.no_plain:
+      try:
         for name, form in (("plain_event", abi.FORM_EVENT), ("plain_history", abi.FORM_HISTORY)):
             B.run_plain(slots[:4], form=form)                          # warm-up (work handle, modules)
             for s in slots:
@@ -281,7 +344,10 @@ def batched_section(a, local):
                          "transport_kernel_ms": st.kernel_ms}
         out["speedup_vs_plain_event"] = out["value"] / out["plain_event"]["value"]
         out["speedup_vs_plain_history"] = out["value"] / out["plain_history"]["value"]
+      except Exception as e:
+        out["plain_error"] = repr(e)
     if not a.no_fp64_batch:
+      try:
         B64, s64 = load(abi.PREC_FP64)
         t0 = time.perf_counter()
         st = B64.run(s64)
@@ -302,7 +368,10 @@ def batched_section(a, local):
                                           "frac_within_10pct": float(np.mean(r < 0.10)),
                                           "max_abs_z": float(np.max(np.abs(zs)))}
         B64.close()
+      except Exception as e:
+        out["fp64_error"] = repr(e)
     if not a.no_serve and a.serve_seconds > 0:
+      try:
         templates = [(pop, c) for _, pop, c, _ in batch]
         mean_hist = float(np.mean([pop * c for pop, c in templates]))
         lat = problems.lattice_17x17_7g()
@@ -316,7 +385,7 @@ def batched_section(a, local):
             Bs, cat = load(abi.PREC_MIXED)
             Bs.set_tuning(**tuning)
             pool = serve.EigenPool(lat, 4, abi.PREC_MIXED, abi.TRANSPORT_DT, 100000) if efrac > 0 else None
-            S = serve.SolveServer(Bs, cat, wave_histories=1 << 21, eigen=pool)
+            S = serve.SolveServer(Bs, cat, wave_histories=a.wave_histories, item_histories=a.serve_item, eigen=pool)
             offered = rate * ((1 - efrac) * mean_hist + efrac * 100000 * 60)
             done, wall, n = serve.poisson_run(S, templates, rate, a.serve_seconds, seed=7, eigen_fraction=efrac,
                                               drain=(efrac == 0), max_drain_s=30.0)
@@ -331,6 +400,8 @@ def batched_section(a, local):
                     t.close()
             Bs.close()
         out["serving"] = res
+      except Exception as e:
+        out["serving_error"] = repr(e)
     if B is not None:
         B.close()
     return out
@@ -493,6 +564,12 @@ def main():
             cpu = {"value": None, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
 
+    configs = None
+    if not a.no_configs and world == 1:
+        try:
+            configs = configs_section(a, local)
+        except Exception as e:
+            configs = {"error": repr(e)}
     batched = None
     if not a.no_batch and world == 1:
         try:
@@ -513,7 +590,7 @@ def main():
                    "parallelism": f"replicas{world}"},
         "events_per_s": events / sec, "k_eff": ks[-1], "wall_ms_per_step": 1e3 * wall / a.steps,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-        "other_transport": alt, "batched": batched,
+        "other_transport": alt, "batched": batched, "other_configs": configs,
     }
     print(json.dumps(line), flush=True)
     if pg:

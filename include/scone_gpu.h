@@ -87,6 +87,8 @@ extern "C" {
 #define SG_TRANSPORT_ST    1      /* transportOperatorST, distance cache on                      */
 #define SG_TRANSPORT_DT    2      /* transportOperatorDT                                         */
 #define SG_TRANSPORT_ST_NOCACHE 3 /* transportOperatorST { cache 0; }                           */
+#define SG_TRANSPORT_HT    4      /* transportOperatorHT (hybrid: DT or ST chosen per transit)   */
+#define SG_TRANSPORT_HT_NOCACHE 5 /* transportOperatorHT { cache 0; }                           */
 
 /* tally clerks (Tallies/TallyClerks) */
 #define SG_CLERK_COLLISION      1 /* collisionClerk_class.f90                                    */
@@ -212,6 +214,8 @@ typedef struct sg_config {
   int32_t max_bank;             /* capacity of each device bank (particles) */
   int32_t record_histories;     /* 1: keep per-history collision counts and end RNG states */
   int32_t form;                 /* SG_FORM_EVENT (default) or SG_FORM_HISTORY */
+  double  ht_cutoff;            /* SG_TRANSPORT_HT* `cutoff`: delta tracking when Sigma_t/Sigma_maj >
+                                   1 - cutoff (transportOperatorHT_class.f90:49-81); 0 = 0.9 (default) */
 } sg_config;
 
 /* A particle bank as SoA host arrays of SCONE's particleStateData (particle_class.f90:50-65).
@@ -352,6 +356,7 @@ typedef struct sg_batch_config {
   int64_t arena_bytes;          /* device memory for problem data and score memory (admission budget) */
   int32_t max_work_items;       /* capacity of the device work queue       */
   int32_t reserved;
+  double  ht_cutoff;            /* as sg_config.ht_cutoff                  */
 } sg_batch_config;
 
 /* one fixed-source problem: geometry, MG data, point source, one tally admin (batch_size 1: every
@@ -425,7 +430,8 @@ int32_t sg_batch_clear_tally(sg_batch b, int32_t slot);
  * `wave_histories`, so a request that arrives while others run joins the next wave), and retires
  * requests whose last history ran: their cycles are closed in that wave.  Latency is submit time to
  * the device completion of the request's last wave (CUDA event time mapped onto the host clock). */
-int32_t sg_serve_start(sg_batch b, int64_t wave_histories);
+/* wave_histories: histories per wave; item_histories: work-item size while serving (0: the tuning's) */
+int32_t sg_serve_start(sg_batch b, int64_t wave_histories, int32_t item_histories);
 int32_t sg_serve_submit(sg_batch b, int32_t slot);
 /* launches/retires waves; wait != 0 blocks until at least one in-flight wave completes.
  * Completed requests since the last call are written to done_slots / latency_s (up to cap). */

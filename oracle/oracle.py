@@ -35,6 +35,7 @@ def lib():
         P = C.POINTER
         sig = {
             "or_create": (i32, [i32, P(vp)]), "or_destroy": (i32, [vp]),
+            "or_set_ht_cutoff": (i32, [vp, C.c_double]),
             "or_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
             "or_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
             "or_upload_mg": (i32, [vp, P(abi.MGDesc)]),
@@ -85,11 +86,13 @@ def _d(a):
 class Oracle:
     """Python face of the oracle with the same methods as scone_gb300.TransportOperatorGPU."""
 
-    def __init__(self, problem=None, transport=abi.TRANSPORT_ST):
+    def __init__(self, problem=None, transport=abi.TRANSPORT_ST, ht_cutoff=0.0):
         self.L = lib()
         self.h = C.c_void_p()
         self._keep = []
         self._check(self.L.or_create(transport, C.byref(self.h)))
+        if ht_cutoff > 0.0:
+            self._check(self.L.or_set_ht_cutoff(self.h, ht_cutoff))
         if problem is not None:
             self.upload_geometry(problem.geometry)
             if problem.mg is not None:

@@ -1159,6 +1159,7 @@ struct Oracle {
   bool isCE = false;
   std::vector<TallyAdmin> admins;
   int transport = SG_TRANSPORT_ST;
+  double htCutoff = 0.9;                             // transportOperatorHT `cutoff` (:297)
   std::string err;
   sg_point_source_desc src{};
   std::vector<double> srcProbG;
@@ -1664,7 +1665,13 @@ struct Oracle {
     while (true) {
       double trackXS = 0.0;
       if (transport == SG_TRANSPORT_DT) deltaTracking(p, admin, trackXS);
-      else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_ST);
+      else if (transport == SG_TRANSPORT_HT || transport == SG_TRANSPORT_HT_NOCACHE) {
+        // tracking_selection (transportOperatorHT_class.f90:49-81): DT if Sigma_t/Sigma_maj > 1 - cutoff
+        double majorant_inv = 1.0 / majorantXS(p);
+        double sigmaT = (p.matIdx() == VOID_MAT) ? 0.0 : trackMatXS(p);
+        if (sigmaT * majorant_inv > 1.0 - htCutoff) deltaTracking(p, admin, trackXS);
+        else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_HT);
+      } else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_ST);
       if (p.isDead) { reportHist(admin, p); break; }
       if (isCE) collideCE(p, admin, trackXS);
       else collide(p, admin, trackXS, sites);
@@ -1824,6 +1831,11 @@ int32_t or_create(int32_t transport, or_handle* out) {
   return SG_OK;
 }
 int32_t or_destroy(or_handle h) { delete O(h); return SG_OK; }
+int32_t or_set_ht_cutoff(or_handle h, double c) {
+  if (!(c > 0.0 && c < 1.0)) return SG_ERR_BAD_ARG;
+  O(h)->htCutoff = c;
+  return SG_OK;
+}
 int32_t or_last_error(or_handle h, char* buf, size_t len) {
   std::snprintf(buf, len, "%s", O(h)->err.c_str());
   return SG_OK;

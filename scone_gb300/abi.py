@@ -23,7 +23,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 # execution forms
 FORM_EVENT, FORM_HISTORY = 0, 1
 # transport operators
-TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE = 1, 2, 3
+TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE, TRANSPORT_HT, TRANSPORT_HT_NOCACHE = 1, 2, 3, 4, 5
 # clerks
 CLERK_COLLISION, CLERK_TRACK, CLERK_KEFF_ANALOG, CLERK_KEFF_IMPLICIT = 1, 2, 3, 4
 CLERK_SURFACE_CURRENT = 5
@@ -87,6 +87,7 @@ class Config(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("transport", C.c_int32), ("device", C.c_int32),
         ("max_bank", C.c_int32), ("record_histories", C.c_int32), ("form", C.c_int32),
+        ("ht_cutoff", C.c_double),
     ]
 
 
@@ -119,7 +120,7 @@ class BatchConfig(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("transport", C.c_int32), ("device", C.c_int32),
         ("max_problems", C.c_int32), ("arena_bytes", C.c_int64), ("max_work_items", C.c_int32),
-        ("reserved", C.c_int32),
+        ("reserved", C.c_int32), ("ht_cutoff", C.c_double),
     ]
 
 

@@ -1,13 +1,16 @@
 """Builds libsconegpu.so in-tree (scone_gb300/_build/) with nvcc for sm_103a.
 
-Translation units compile in parallel.  The FP64 verification history loop and the support kernels
-are compiled with -fmad=false (every multiply and add rounded separately, as SCONE's gfortran build
-does on x86-64); the mixed-precision history loop keeps FMA contraction.
+Translation units compile in parallel, one per (nuclear data, precision form, transport operator)
+for the transport kernels and one per (precision, operator) for the batched kernel.  The FP64
+verification units and the support kernels are compiled with -fmad=false (every multiply and add
+rounded separately, as SCONE's gfortran build does on x86-64); the mixed-precision units keep FMA
+contraction.
 """
 import os
 import shutil
 import subprocess
 import sys
+import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
@@ -16,18 +19,14 @@ LIB = os.path.join(OUT, "libsconegpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
-UNITS = {
-    "sg_tr_fp64.cu": ["-fmad=false"],
-    "sg_tr_mixed.cu": [],
-    "sg_tr_ce_fp64.cu": ["-fmad=false"],
-    "sg_tr_ce_mixed.cu": [],
-    "sg_support.cu": ["-fmad=false"],
-    "sg_host.cu": ["-fmad=false"],
-    "sg_noalloc.cu": ["-fmad=false"],
-    "sg_batch_fp64.cu": ["-fmad=false"],
-    "sg_batch_mixed.cu": [],
-    "sg_batch_host.cu": ["-fmad=false"],
-}
+UNITS = {"sg_support.cu": ["-fmad=false"], "sg_host.cu": ["-fmad=false"], "sg_noalloc.cu": ["-fmad=false"],
+         "sg_fission_source.cu": ["-fmad=false"], "sg_batch_host.cu": ["-fmad=false"]}
+for _op in ("st", "dt", "ht"):
+    for _data in ("mg", "ce"):
+        UNITS[f"sg_tr_{_data}_fp64_{_op}.cu"] = ["-fmad=false"]
+        UNITS[f"sg_tr_{_data}_mixed_{_op}.cu"] = []
+    UNITS[f"sg_batch_fp64_{_op}.cu"] = ["-fmad=false"]
+    UNITS[f"sg_batch_mixed_{_op}.cu"] = []
 
 
 def nvcc():
@@ -54,24 +53,45 @@ def build(force=False, verbose=False, extra=()):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     cc = nvcc()
-    procs = []
     objs = []
+    cmds = []
     for unit, flags in UNITS.items():
         obj = os.path.join(OUT, unit.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *COMMON, *flags, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        procs.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        cmds.append((unit, [cc, *ARCH, *COMMON, *flags, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]))
         objs.append(obj)
+    # the long transport units first, at most one compiler per host core
+    cmds.sort(key=lambda c: (not c[0].startswith("sg_tr_"), not c[0].startswith("sg_batch_")))
+    jobs = max(1, os.cpu_count() or 1)
     failed = []
-    for unit, p in procs:
+    running = []
+
+    def finish(item):
+        unit, p = item
         out, _ = p.communicate()
+        running.remove(item)
         text = out.decode(errors="replace")
         if p.returncode != 0:
             failed.append(unit)
             sys.stderr.write(text)
         elif verbose and text.strip():
             print(text)
+
+    def wait_one():
+        while True:
+            for item in running:
+                if item[1].poll() is not None:
+                    finish(item)
+                    return
+            time.sleep(0.1)
+
+    for unit, cmd in cmds:
+        if len(running) >= jobs:
+            wait_one()
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        running.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    while running:
+        wait_one()
     if failed:
         raise RuntimeError("nvcc failed for " + ", ".join(failed))
     tmp = LIB + ".tmp"

@@ -9,11 +9,12 @@
 // of shared memory, and lanes that end a history take the next history of the same item at once.
 // The warp moves to an item of another problem only when all of its lanes are idle.
 //
-// Each history reproduces the single-problem path exactly: pointSource sampling with master_c +
-// stride(n) (source_inter.f90:98-119, pointSource_class.f90:189-270), then transport with
-// master_c + stride(pop + n), where master_c is the problem's master strided by 2 * pop per cycle
-// (fixedSourcePhysicsPackage_class.f90:186-189,264).  Scores of cycle c go to that cycle's own
-// accumulator; the cycles are closed in order after the launch.
+// Each history follows the single-problem path: pointSource sampling with master_c + stride(n)
+// (source_inter.f90:98-119, pointSource_class.f90:189-270), then transport with master_c +
+// stride(pop + n), where master_c is the problem's master strided by 2 * pop per cycle
+// (fixedSourcePhysicsPackage_class.f90:186-189,264).  In the FP64 form every draw and result is
+// the single-problem path's; the mixed form samples the source direction in FP32.  Scores of cycle
+// c go to that cycle's own accumulator; the cycles are closed in order after the launch.
 #pragma once
 #include "sg_transport.cuh"
 #include "sg_batch.h"
@@ -33,36 +34,39 @@ __device__ __forceinline__ void stage_problem_warp(BatchProblem<R>* dst, const B
 
 // pointSource%sampleParticle (pointSource_class.f90:189-270), then the particle enters the gen loop
 // as thisCycle%copy + placeCoord would leave it.
-template <class R, int MAXL, bool DT>
-__device__ __forceinline__ void start_batched(Tracker<R, MAXL, DT, false>& T, const BatchProblem<R>& P, int f) {
+template <class R, int MAXL, int OP>
+__device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, const BatchProblem<R>& P, int f) {
   const int c = f / P.pop;
   const int n = f - c * P.pop + 1;
   const long long base = 2LL * P.pop * c;
-  Rng<double> rs;
+  // the source direction in the working precision: FP64 as SCONE in the verification form; FP32
+  // in the mixed form (the direction is kept in FP32 there, and FP64 is scarce on this GPU)
+  Rng<R> rs;
   rs.s = lcg_skip(P.master, RNG_STRIDE * (base + n));
-  double d0 = P.src_dir[0], d1 = P.src_dir[1], d2 = P.src_dir[2];
+  R d0 = (R)P.src_dir[0], d1 = (R)P.src_dir[1], d2 = (R)P.src_dir[2];
   if (P.src_isotropic) {
-    const double mu = 2.0 * rs.get() - 1.0;
-    double sp, cp;
-    sincos_phi<double>(rs.get(), sp, cp);
-    d0 = 1.0; d1 = 0.0; d2 = 0.0;
-    rotate_vector<double>(d0, d1, d2, mu, sp, cp);
+    const R mu = R(2) * rs.get() - R(1);
+    R sp, cp;
+    sincos_phi<R>(rs.get(), sp, cp);
+    d0 = R(1); d1 = R(0); d2 = R(0);
+    rotate_vector<R>(d0, d1, d2, mu, sp, cp);
   }
   int g = P.src_G;
   if (P.src_n_prob_g > 0) {
-    double r = rs.get();
+    R r = rs.get();
     for (g = 1; g <= P.src_n_prob_g; ++g) {
-      r = r - P.src_prob_g[g - 1];
-      if (r < 0.0) break;
+      r = r - (R)P.src_prob_g[g - 1];
+      if (r < R(0)) break;
     }
+    if (g > P.src_n_prob_g) g = P.src_n_prob_g;
   }
   T.hist = n;
   T.c.r0[0] = P.src_r[0];
   T.c.r0[1] = P.src_r[1];
   T.c.r0[2] = P.src_r[2];
-  T.c.u[0] = (R)d0;
-  T.c.u[1] = (R)d1;
-  T.c.u[2] = (R)d2;
+  T.c.u[0] = d0;
+  T.c.u[1] = d1;
+  T.c.u[2] = d2;
   T.w = R(1);
   T.w0 = R(1);
   T.G = g;
@@ -74,9 +78,10 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, DT, false>& T, co
   T.cache.lvl = 0;
   T.acc = P.t.acc + (long long)c * P.n_bins;
   if (!T.geom.place(T.c)) raise_error(P.t.ctr, SG_ERR_UNDEF_MAT, n);
+  T.select_ht();
 }
 
-template <class R, int MAXL, bool DT>
+template <class R, int MAXL, int OP>
 __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaunch L) {
   __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
   const int lane = threadIdx.x & 31;
@@ -90,7 +95,7 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
     P.t.acc = nullptr;
   }
   __syncwarp();
-  Tracker<R, MAXL, DT, false> T(P.t, nullptr);
+  Tracker<R, MAXL, OP, false> T(P.t, nullptr);
   const int nItems = *L.n_items;
   int cur = -1;                     // slot of the staged problem (warp-uniform)
   int pend = -1;                    // claimed item of another problem, waiting for the warp to drain
@@ -124,7 +129,7 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
       const int avail = q_end - q_next;
       const int rank = __popc(need & ((1u << lane) - 1u));
       const bool mine = ((need >> lane) & 1u) && rank < avail;
-      if (mine) { start_batched<R, MAXL, DT>(T, P, q_next + rank); alive = true; }
+      if (mine) { start_batched<R, MAXL, OP>(T, P, q_next + rank); alive = true; }
       q_next += min(__popc(need), avail);
       need &= ~__ballot_sync(FULL, mine);
     }
@@ -143,23 +148,23 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
 
 namespace sg {
 
-template <class R>
-const void* batch_kernel_ptr(int maxl, bool dt) {
-  if (maxl <= 2) return dt ? (const void*)k_batch<R, 2, true> : (const void*)k_batch<R, 2, false>;
-  return dt ? (const void*)k_batch<R, 4, true> : (const void*)k_batch<R, 4, false>;
+template <class R, int OP>
+const void* batch_kernel_ptr(int maxl) {
+  return maxl <= 2 ? (const void*)k_batch<R, 2, OP> : (const void*)k_batch<R, 4, OP>;
 }
 
-template <class R>
-cudaError_t launch_batch_impl(const BatchLaunch& L, bool dt, int grid, int block, cudaStream_t s) {
+// the bodies of one translation unit's launch_batch_op / batch_occupancy_op specialisations
+template <class R, int OP>
+cudaError_t launch_batch_unit(const BatchLaunch& L, int grid, int block, cudaStream_t s) {
   if (block < 32 || block > 32 * BATCH_MAX_WARPS || block % 32) return cudaErrorInvalidValue;
   void* args[] = {(void*)&L};
-  return cudaLaunchKernel(batch_kernel_ptr<R>(L.maxl, dt), dim3(grid), dim3(block), args, 0, s);
+  return cudaLaunchKernel(batch_kernel_ptr<R, OP>(L.maxl), dim3(grid), dim3(block), args, 0, s);
 }
 
-template <class R>
-int batch_occupancy_impl(int maxl, bool dt, int block) {
+template <class R, int OP>
+int batch_occupancy_unit(int maxl, int block) {
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel_ptr<R>(maxl, dt), block, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel_ptr<R, OP>(maxl), block, 0) != cudaSuccess)
     return 1;
   return per < 1 ? 1 : per;
 }

@@ -59,10 +59,24 @@ struct BatchLaunch {
   int maxl;
 };
 
+// the batched kernel for precision R and transport operator OP (one translation unit each)
+template <class R, int OP>
+cudaError_t launch_batch_op(const BatchLaunch& L, int grid, int block, cudaStream_t s);
+template <class R, int OP>
+int batch_occupancy_op(int maxl, int block);
+
 template <class R>
-cudaError_t launch_batch(const BatchLaunch& L, bool dt, int grid, int block, cudaStream_t s);
+inline cudaError_t launch_batch(const BatchLaunch& L, int op, int grid, int block, cudaStream_t s) {
+  if (op == OP_DT) return launch_batch_op<R, OP_DT>(L, grid, block, s);
+  if (op == OP_HT) return launch_batch_op<R, OP_HT>(L, grid, block, s);
+  return launch_batch_op<R, OP_ST>(L, grid, block, s);
+}
 template <class R>
-int batch_occupancy(int maxl, bool dt, int block);
+inline int batch_occupancy(int maxl, int op, int block) {
+  if (op == OP_DT) return batch_occupancy_op<R, OP_DT>(maxl, block);
+  if (op == OP_HT) return batch_occupancy_op<R, OP_HT>(maxl, block);
+  return batch_occupancy_op<R, OP_ST>(maxl, block);
+}
 
 // scoreMemory%closeCycle for every cycle of the listed problems, in cycle order (sg_batch_host.cu)
 cudaError_t launch_batch_close(const BatchTally* tallies, const int* slots, const int* n, int grid, cudaStream_t s);

@@ -148,6 +148,7 @@ struct sg_batch_t {
   // serving
   bool serving = false;
   long long waveHist = 0;
+  int serveItem = 1024;
   std::deque<Request> active;
   std::deque<Wave> waves;
   std::vector<int> doneSlots;      // completed requests not yet handed out
@@ -213,7 +214,7 @@ int check_slot(sg_batch b, int slot) {
 }
 
 int grid_for(sg_batch b, int maxl) {
-  const bool dt = b->cfg.transport == SG_TRANSPORT_DT;
+  const int dt = transport_op(b->cfg.transport);
   const int occ = fp64(b) ? batch_occupancy<double>(maxl, dt, b->tune.block_threads)
                           : batch_occupancy<float>(maxl, dt, b->tune.block_threads);
   int per = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, occ) : occ;
@@ -238,7 +239,7 @@ int build_graph(sg_batch b, int m, int x) {
   }
   const int maxl = x ? 4 : 2;
   cudaStream_t s = b->stream;
-  const bool dt = b->cfg.transport == SG_TRANSPORT_DT;
+  const int dt = transport_op(b->cfg.transport);
   BatchLaunch L;
   L.problems = b->dProbs;
   L.items = b->dItems;
@@ -320,8 +321,9 @@ int write_record(sg_batch b, int slot) {
     rec.t.acc_n = (int)N;
     rec.t.use_smem = 0;
     rec.t.ctr = b->dCtr;
-    rec.t.use_cache = b->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
+    rec.t.use_cache = transport_cache(b->cfg.transport);
     rec.t.max_segments = 1000000;
+    rec.t.ht_cutoff = (decltype(rec.t.ht_cutoff))(b->cfg.ht_cutoff > 0.0 ? b->cfg.ht_cutoff : 0.9);
     for (int i = 0; i < 3; ++i) { rec.src_r[i] = S.src.r[i]; rec.src_dir[i] = S.src.dir[i]; }
     rec.src_prob_g = S.src.n_prob_g > 0 ? S.sp.prob_g : nullptr;
     rec.src_isotropic = S.src.isotropic;
@@ -390,7 +392,8 @@ int32_t sg_batch_create(const sg_batch_config* cfg, sg_batch* out) {
   if (!cfg || !out) return SG_ERR_BAD_ARG;
   *out = nullptr;
   if (cfg->precision != SG_PREC_FP64 && cfg->precision != SG_PREC_MIXED) return SG_ERR_BAD_ARG;
-  if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_ST_NOCACHE) return SG_ERR_BAD_ARG;
+  if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_HT_NOCACHE) return SG_ERR_BAD_ARG;
+  if (!(cfg->ht_cutoff >= 0.0 && cfg->ht_cutoff < 1.0)) return SG_ERR_BAD_ARG;
   if (cfg->max_problems <= 0 || cfg->arena_bytes <= 0 || cfg->max_work_items <= 0) return SG_ERR_BAD_ARG;
   sg_batch b = new sg_batch_t();
   b->cfg = *cfg;
@@ -656,6 +659,7 @@ int32_t sg_batch_run_plain(sg_batch b, const int32_t* slots, int32_t n, int32_t 
     c.max_bank = std::max(maxPop, 1024);
     c.record_histories = 0;
     c.form = form;
+    c.ht_cutoff = b->cfg.ht_cutoff;
     int rc = sg_create(&c, &b->plainWork);
     if (rc) return b->fail(rc, "batch: cannot create the plain-form work handle");
     b->plainForm = form;
@@ -716,7 +720,7 @@ int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_
     if (pass == 2) {
       int maxl = 2;
       for (int i = 0; i < n; ++i) maxl = std::max(maxl, b->slots[slots[i]].sp.maxl);
-      const bool dt = b->cfg.transport == SG_TRANSPORT_DT;
+      const int dt = transport_op(b->cfg.transport);
       const int occ = fp64(b) ? batch_occupancy<double>(maxl, dt, cur.block_threads)
                               : batch_occupancy<float>(maxl, dt, cur.block_threads);
       for (int v = std::max(1, occ / 2); v <= occ; ++v) { sg_batch_tuning t = cur; t.blocks_per_sm = v; cands.push_back(t); }
@@ -788,11 +792,13 @@ int32_t sg_batch_clear_tally(sg_batch b, int32_t slot) {
 
 double sg_serve_clock(void) { return host_now(); }
 
-int32_t sg_serve_start(sg_batch b, int64_t wave_histories) {
-  if (!b || wave_histories < 32) return SG_ERR_BAD_ARG;
+int32_t sg_serve_start(sg_batch b, int64_t wave_histories, int32_t item_histories) {
+  if (!b || wave_histories < 32 || item_histories < 0 || (item_histories > 0 && item_histories < 32))
+    return SG_ERR_BAD_ARG;
   if (b->serving) return b->fail(SG_ERR_STATE, "serve: already started");
   b->serving = true;
   b->waveHist = wave_histories;
+  b->serveItem = item_histories > 0 ? item_histories : b->tune.item_histories;
   b->wavesLaunched = 0;
   b->mirror = 0;
   if (!b->ref) BCK(cudaEventCreate(&b->ref));
@@ -857,7 +863,7 @@ int retire_wave(sg_batch b, bool block, bool* retired) {
 // (whole work items; what a request cannot use goes to the others), oldest request first.
 int launch_wave(sg_batch b) {
   const int m = (int)(b->wavesLaunched & 1);
-  const int item = b->tune.item_histories;
+  const int item = b->serveItem;
   std::vector<WorkItem> items;
   Wave w;
   w.mirror = m;

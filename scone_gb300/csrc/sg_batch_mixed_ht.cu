@@ -1,0 +1,11 @@
+// sg_batch_mixed_ht.cu -- the batched gen loop, mixed form, transportOperatorHT.
+#include "sg_batch.cuh"
+
+namespace sg {
+template <>
+cudaError_t launch_batch_op<float, OP_HT>(const BatchLaunch& L, int grid, int block, cudaStream_t s) {
+  return launch_batch_unit<float, OP_HT>(L, grid, block, s);
+}
+template <>
+int batch_occupancy_op<float, OP_HT>(int maxl, int block) { return batch_occupancy_unit<float, OP_HT>(maxl, block); }
+}  // namespace sg

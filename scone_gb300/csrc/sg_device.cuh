@@ -548,12 +548,19 @@ struct Geom {
   // Mixed form: the level-2 coordinates are re-derived from the FP64 level-1 position instead of
   // being accumulated separately in FP32, so both levels see one position wherever their surfaces
   // coincide (a lattice filling the root box).  The FP64 form accumulates every level as SCONE does.
+  // The root universe carries no cell offset, so a level-2 universe without an origin offset takes
+  // float(r0) directly (the same value, without two FP64 subtractions of zero).
   __device__ __forceinline__ void sync_level2(Coords<R, MAXL>& c) const {
     if constexpr (sizeof(R) == 4 && MAXL > 1) {
       if (c.nest > 1) {
+        const DUni& N = g.unis[c.uni[1]];
+        if (N.i[6]) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
+          return;
+        }
         double off[3];
         cell_offset<double>(c.uni[0], c.local[0], off);
-        const DUni& N = g.unis[c.uni[1]];
 #pragma unroll
         for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
       }
@@ -581,10 +588,15 @@ struct Geom {
       int nu = -gf.x - 1;
       const DUni& N = g.unis[nu];
       if (i == 0) {
-        double off[3];
-        cell_offset<double>(c.uni[0], c.local[0], off);
+        if (sizeof(R) == 4 && N.i[6]) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+          for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
+        } else {
+          double off[3];
+          cell_offset<double>(c.uni[0], c.local[0], off);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+        }
       } else {
         R off[3];
         cell_offset<R>(c.uni[i], c.local[i], off);
@@ -602,10 +614,24 @@ struct Geom {
 
   // geometryStd%placeCoord (geometryStd_class.f90:119-147): level-1 position is c.r0 (global;
   // the root universe carries no origin offset)
+  // Mixed form: the root border test is first made in FP32 at float(r0); only a value within the
+  // surface's filter margin (tolerance plus the FP32 error bound) goes to the FP64 test, so the side
+  // found is always the FP64 one.
   __device__ __forceinline__ bool place(Coords<R, MAXL>& c) const {
     c.uni[0] = g.root;
     c.base[0] = 0;
-    c.local[0] = find_cell<double>(g.root, c.r0, c.u);
+    int loc = 0;
+    if constexpr (sizeof(R) == 4) {
+      const DSurf& S = g.surfs[g.border];
+      if (S.filt > 0.0f) {
+        const float rf[3] = {(float)c.r0[0], (float)c.r0[1], (float)c.r0[2]};
+        const float v = surf_evaluate<float>(S, rf);
+        if (v > S.filt) loc = 2;
+        else if (v < -S.filt) loc = 1;
+      }
+    }
+    if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u);
+    c.local[0] = loc;
     return dive(c, 0);
   }
 

@@ -121,6 +121,7 @@ struct Admin {
 
 struct sg_handle_t {
   sg_config cfg;
+  double htCutoff = 0.9;       // transportOperatorHT `cutoff` (transportOperatorHT_class.f90:297)
   cudaStream_t stream = nullptr;
   std::string err;
 
@@ -349,6 +350,7 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
       default:
         return h->fail(SG_ERR_BAD_ARG, "geometry: unknown universe type");
     }
+    U.i[6] = (U.origin[0] == 0.0 && U.origin[1] == 0.0 && U.origin[2] == 0.0) ? 1 : 0;
     Um = U;
     if (U.type == SG_UNI_LAT)
       for (int i = 0; i < 3; ++i) Um.d[6 + i] = U.d[i] * 0.5 - U.d[i] * SURF_TOL_M;
@@ -397,6 +399,19 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
     else if (b.type >= SG_SURF_XCYL && b.type <= SG_SURF_ZCYL) { int pl[2] = {b.pl0, b.pl1}; for (int i : pl) { h->bounds[i] = b.p[i] - b.p[3]; h->bounds[3 + i] = b.p[i] + b.p[3]; } }
     for (int i = 0; i < 3; ++i)
       if (h->bounds[i] <= -INF && h->bounds[3 + i] >= INF) { h->bounds[i] = 0.0; h->bounds[3 + i] = 0.0; }
+  }
+  // mixed form: FP32 filter of the root border test.  The FP32 value of the surface function at
+  // float(r) differs from the FP64 value by at most a few FP32 ulps of the geometry scale (squared
+  // for quadrics); beyond that bound plus the surface tolerance the FP64 test gives the same side.
+  {
+    double scale = 1.0;
+    for (int i = 0; i < 6; ++i) scale = std::max(scale, std::fabs(h->bounds[i]));
+    DSurf& b = sMx[g->border_surf];
+    const bool quad = b.type == SG_SURF_SPHERE || (b.type >= SG_SURF_XCYL && b.type <= SG_SURF_ZCYL);
+    const bool bounded = b.type == SG_SURF_SPHERE || b.type == SG_SURF_BOX || b.type >= SG_SURF_XCYL;
+    const double ulp = 0x1p-24;
+    const double err = quad ? 128.0 * ulp * scale * scale : 32.0 * ulp * scale;
+    b.filt = bounded ? (float)(b.tol + err) : 0.0f;
   }
   cudaStream_t st = h->stream;
   CK(h->surfs64.upload(s64, st));
@@ -816,16 +831,17 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.rec_coll = h->cfg.record_histories ? h->recColl.p : nullptr;
   t.rec_rng = h->cfg.record_histories ? h->recRng.p : nullptr;
   t.ctr = h->ctr.p;
-  t.use_cache = h->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
+  t.use_cache = transport_cache(h->cfg.transport);
   t.max_segments = 1000000;
+  t.ht_cutoff = (R)h->htCutoff;
   CK(cudaMemsetAsync(h->ctr.p, 0, sizeof(DCounters), s));
   CK(cudaMemsetAsync(h->sCursor.p, 0, SITE_REGIONS * sizeof(int), s));
   CK(cudaMemsetAsync(h->histN.p, 0, (size_t)(n + 1) * sizeof(int), s));
   CK(cudaMemsetAsync(h->totals.p, 0, 8 * sizeof(int), s));
   CK(cudaEventRecord(h->ev[0], s));
-  const bool dt = h->cfg.transport == SG_TRANSPORT_DT;
-  auto launch_kind = [&](int kind, const TransportArgs<R>& a, int maxl, bool dtt, size_t sm, cudaStream_t ss, int* g) {
-    return h->hasCE ? launch_kind_ce<R>(kind, a, maxl, dtt, sm, ss, g) : sg::launch_kind<R>(kind, a, maxl, dtt, sm, ss, g);
+  const int dt = transport_op(h->cfg.transport);
+  auto launch_kind = [&](int kind, const TransportArgs<R>& a, int maxl, int opk, size_t sm, cudaStream_t ss, int* g) {
+    return h->hasCE ? launch_kind_ce<R>(kind, a, maxl, opk, sm, ss, g) : sg::launch_kind<R>(kind, a, maxl, opk, sm, ss, g);
   };
   if (h->cfg.form == SG_FORM_HISTORY) {
     CK(launch_kind(K_HISTORY, t, h->maxl, dt, smem, s, nullptr));
@@ -1098,8 +1114,10 @@ int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<doubl
   t64->acc = h->acc.p + *lo;
   t32->acc = h->acc.p + *lo;
   t64->acc_n = t32->acc_n = (int)(hi - *lo);
-  t64->use_cache = t32->use_cache = h->cfg.transport != SG_TRANSPORT_ST_NOCACHE;
+  t64->use_cache = t32->use_cache = transport_cache(h->cfg.transport);
   t64->max_segments = t32->max_segments = 1000000;
+  t64->ht_cutoff = h->htCutoff;
+  t32->ht_cutoff = (float)h->htCutoff;
   return SG_OK;
 }
 
@@ -1236,12 +1254,14 @@ int32_t sg_create(const sg_config* cfg, sg_handle* out) {
   if (!cfg || !out) return SG_ERR_BAD_ARG;
   *out = nullptr;
   if (cfg->precision != SG_PREC_FP64 && cfg->precision != SG_PREC_MIXED) return SG_ERR_BAD_ARG;
-  if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_ST_NOCACHE) return SG_ERR_BAD_ARG;
+  if (cfg->transport < SG_TRANSPORT_ST || cfg->transport > SG_TRANSPORT_HT_NOCACHE) return SG_ERR_BAD_ARG;
+  if (!(cfg->ht_cutoff >= 0.0 && cfg->ht_cutoff < 1.0)) return SG_ERR_BAD_ARG;
   if (cfg->max_bank <= 0) return SG_ERR_BAD_ARG;
   if (cfg->form != SG_FORM_EVENT && cfg->form != SG_FORM_HISTORY) return SG_ERR_BAD_ARG;
   sg_handle h = new sg_handle_t();
   h->cfg = *cfg;
   h->cap = cfg->max_bank;
+  h->htCutoff = cfg->ht_cutoff > 0.0 ? cfg->ht_cutoff : 0.9;
   if (cudaSetDevice(cfg->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return SG_ERR_CUDA;

@@ -20,7 +20,7 @@ struct DSurf {
   double tol;
   float pf[SG_SURF_NPAR];
   float tolf;
-  float padf;
+  float filt;      // mixed form, root border: |FP32 value| above this decides the halfspace (0: none)
 };
 
 // One universe.  i[] / d[] by type:
@@ -29,6 +29,7 @@ struct DSurf {
 //   PIN : i0 first annulus in pin_rsq/pin_tol, i1 number of annuli (last one has radius 1.1*INF)
 //   LAT : i0..i2 sizeN, i3 outLocalID, i4 outline surface, i5 offset flag;
 //         d0..2 pitch, d3..5 corner, d6..8 a_bar (half pitch reduced by the surface tolerance)
+//   all : i6 = 1 when the origin is (0, 0, 0)
 struct DUni {
   int type;
   int i[7];
@@ -195,6 +196,17 @@ struct DQueues {
   int* work;       // next entry of `in` to hand out (persistent kernels)
 };
 
+// transport operators as compiled kernel variants
+enum { OP_ST = 0, OP_DT = 1, OP_HT = 2 };
+inline int transport_op(int transport) {
+  if (transport == SG_TRANSPORT_DT) return OP_DT;
+  if (transport == SG_TRANSPORT_HT || transport == SG_TRANSPORT_HT_NOCACHE) return OP_HT;
+  return OP_ST;
+}
+inline bool transport_cache(int transport) {
+  return transport != SG_TRANSPORT_ST_NOCACHE && transport != SG_TRANSPORT_HT_NOCACHE;
+}
+
 template <class R>
 struct TransportArgs {
   DGeom geom;
@@ -218,6 +230,7 @@ struct TransportArgs {
   DCounters* ctr;
   int use_cache;        // transportOperatorST cache flag
   int max_segments;     // safety limit per history
+  R ht_cutoff;          // transportOperatorHT `cutoff`
   DPart<R> part;        // event form: particle state
   DQueues q;            // event form: queues of the launch
 };

@@ -1,4 +1,5 @@
-// sg_launch.h -- host-callable launch wrappers of the kernels (one definition per translation unit).
+// sg_launch.h -- host-callable launch wrappers of the kernels.  Each transport-kernel translation
+// unit (sg_tr_<data>_<precision>_<operator>.cu) defines one launch_kind_op specialisation.
 #pragma once
 #include "sg_internal.h"
 
@@ -7,19 +8,40 @@ namespace sg {
 // kernel kinds of the history loop and of the event form
 enum { K_HISTORY = 0, K_EV_START = 1, K_EV_TRANSIT = 2, K_EV_COLLIDE = 3, K_EV_TAIL = 4, K_KINDS = 5 };
 
-template <class R>
-cudaError_t launch_kind(int kind, const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
-                        cudaStream_t s, int* grid_out);
+// launch of kernel `kind` for working precision R, data kind CE (continuous energy) and transport
+// operator OP; maxl is the geometry's nesting bound (2 or 4 compiled)
+template <class R, bool CE, int OP>
+cudaError_t launch_kind_op(int kind, const TransportArgs<R>& a, int maxl, size_t smem, cudaStream_t s,
+                           int* grid_out);
 
-// persistent history-loop kernel; maxl is the compile-time nesting bound (2 or 4)
-template <class R>
-cudaError_t launch_transport(const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
-                             cudaStream_t s, int* grid_out);
+template <class R, bool CE>
+inline cudaError_t launch_kind_data(int kind, const TransportArgs<R>& a, int maxl, int op, size_t smem,
+                                    cudaStream_t s, int* grid_out) {
+  if (op == OP_DT) return launch_kind_op<R, CE, OP_DT>(kind, a, maxl, smem, s, grid_out);
+  if (op == OP_HT) return launch_kind_op<R, CE, OP_HT>(kind, a, maxl, smem, s, grid_out);
+  return launch_kind_op<R, CE, OP_ST>(kind, a, maxl, smem, s, grid_out);
+}
 
-// the same kernels for continuous-energy data (neutronCEstd physics); defined in sg_tr_ce_*.cu
+// multigroup data (neutronMGstd physics)
 template <class R>
-cudaError_t launch_kind_ce(int kind, const TransportArgs<R>& a, int maxl, bool dt, size_t smem,
-                           cudaStream_t s, int* grid_out);
+inline cudaError_t launch_kind(int kind, const TransportArgs<R>& a, int maxl, int op, size_t smem,
+                               cudaStream_t s, int* grid_out) {
+  return launch_kind_data<R, false>(kind, a, maxl, op, smem, s, grid_out);
+}
+
+// persistent history-loop kernel, multigroup data
+template <class R>
+inline cudaError_t launch_transport(const TransportArgs<R>& a, int maxl, int op, size_t smem,
+                                    cudaStream_t s, int* grid_out) {
+  return launch_kind_data<R, false>(K_HISTORY, a, maxl, op, smem, s, grid_out);
+}
+
+// continuous-energy data (neutronCEstd physics)
+template <class R>
+inline cudaError_t launch_kind_ce(int kind, const TransportArgs<R>& a, int maxl, int op, size_t smem,
+                                  cudaStream_t s, int* grid_out) {
+  return launch_kind_data<R, true>(kind, a, maxl, op, smem, s, grid_out);
+}
 
 // fissionSource sampling on the device (fissionSource_class.f90:149-271), FP64 arithmetic
 cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank out, int n,

@@ -116,7 +116,7 @@ int run_noalloc(const sg::NoAllocView& v, sg::TransportArgs<R> t, unsigned char*
       (e = cudaMemsetAsync(histN, 0, sizeof(int) * (n + 1), s)) ||
       (e = cudaMemsetAsync(totals, 0, sizeof(int) * 8, s)))
     return fail(SG_ERR_CUDA, cudaGetErrorString(e));
-  if ((e = launch_transport<R>(t, v.maxl, v.transport == SG_TRANSPORT_DT, smem, s, nullptr)) ||
+  if ((e = launch_transport<R>(t, v.maxl, transport_op(v.transport), smem, s, nullptr)) ||
       (e = exclusive_scan(histN, n + 1, start, scanTmp, totals + 0, s)))
     return fail(SG_ERR_CUDA, cudaGetErrorString(e));
   DBank out{next->r, next->dir, next->wgt, next->G, next->brood_id, next->time};

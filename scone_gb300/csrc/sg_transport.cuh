@@ -32,7 +32,7 @@ __device__ __forceinline__ void raise_error(DCounters* ctr, int code, int hist) 
   if (atomicCAS(&ctr->err_code, 0, code) == 0) ctr->err_hist = hist;
 }
 
-template <class R, int MAXL, bool DT, bool CE>
+template <class R, int MAXL, int OP, bool CE>
 struct Tracker {
   const TransportArgs<R>& A;
   const Geom<R, MAXL> geom;
@@ -67,12 +67,14 @@ struct Tracker {
   // ANA_LEAK), in R; the batch sums they are added to are FP64
   R kprod, kscat, kabs, kleak;
   unsigned long long nEv, nColl;
+  bool htDT;         // hybrid tracking: the current transit uses delta tracking
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
       : A(a), geom(a.geom), mg(a.mg), ce(a.ce), acc(accp) {
     k_eff = (R)(*a.k_eff);
     kprod = kscat = kabs = kleak = R(0);
     nEv = nColl = 0;
+    htDT = false;
   }
 
   __device__ __forceinline__ R xs(const R* t, int mat, int g) const { return t[(mat - 1) * mg.nG + (g - 1)]; }
@@ -342,6 +344,21 @@ struct Tracker {
     nsites += 1;
   }
 
+  // A CDF walk (multiScatterMG%sampleGout, fissionMG%sampleOut) that ran past the last group.  In
+  // FP64 this is SCONE's fatal error (multiScatterMG_class.f90:250-251).  In the mixed form the FP32
+  // table total can exceed the FP32 running sum of its entries by a few ulps, so a number xi within
+  // a few ulps of 1 can outlast the walk: it belongs to the last group with a nonzero entry.
+  __device__ __forceinline__ int walk_failed(const R* entries, int stride) {
+    if constexpr (sizeof(R) == 8) {
+      raise_error(A.ctr, SG_ERR_NAN, hist);
+      return mg.nG;
+    } else {
+      int g = mg.nG;
+      while (g > 1 && !(entries[(g - 1) * stride] > R(0))) --g;
+      return g;
+    }
+  }
+
   // collisionProcessor%collide with neutronMGstd (collisionProcessor_inter.f90:114-195,
   // neutronMGstd_class.f90:85-297).  Returns true if the particle died.
   __device__ __forceinline__ bool collide(R trackXS) {
@@ -377,7 +394,7 @@ struct Tracker {
             rem = rem - mg.chi[(mat - 1) * mg.nG + (go - 1)];
             if (rem < R(0)) break;
           }
-          if (go > mg.nG) { raise_error(A.ctr, SG_ERR_NAN, hist); go = mg.nG; }
+          if (go > mg.nG) go = walk_failed(mg.chi + (mat - 1) * mg.nG, 1);
           R d[3] = {c.u[0], c.u[1], c.u[2]};
           rotate_vector<R>(d[0], d[1], d[2], mu, sp, cp);
           write_site(d, go, sw);
@@ -394,7 +411,7 @@ struct Tracker {
         rem = rem - row[go - 1];
         if (rem < R(0)) break;
       }
-      if (go > mg.nG) { raise_error(A.ctr, SG_ERR_NAN, hist); go = mg.nG; }
+      if (go > mg.nG) go = walk_failed(row, 1);
       R mu = R(2) * rng.get() - R(1);
       R sp, cp;
       sincos_phi<R>(rng.get(), sp, cp);
@@ -437,6 +454,7 @@ struct Tracker {
     segs = 0;
     cache.lvl = 0;
     if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
+    select_ht();
   }
 
   __device__ __forceinline__ void finish() {
@@ -449,10 +467,32 @@ struct Tracker {
   // SEG_END (the history ended: leak or error) or SEG_COLLIDE (a real collision; trackXS holds the
   // tracking cross section the collision estimators use).
   __device__ __forceinline__ int segment() {
-    const R INF_R = R(D_INF);
     if (++segs > A.max_segments) { raise_error(A.ctr, SG_ERR_LOST, hist); return SEG_END; }
+    if constexpr (OP == OP_DT) return seg_dt();
+    else if constexpr (OP == OP_ST) return seg_st();
+    else return htDT ? seg_dt() : seg_st();
+  }
+
+  // transportOperatorHT%tracking_selection (transportOperatorHT_class.f90:49-81), made at the start
+  // of every transit: delta tracking when Sigma_t / Sigma_majorant > 1 - cutoff (surface tracking
+  // in void).  No random number is drawn.
+  __device__ __forceinline__ void select_ht() {
+    if constexpr (OP == OP_HT) {
+      R maj, sigT;
+      if constexpr (CE) maj = fmax(ce_major(), ce.collisionXS);
+      else maj = fmax(mg.majorant[G - 1], mg.collisionXS);
+      const R majInv = R(1) / maj;
+      if (c.mat == SG_VOID_MAT) sigT = R(0);
+      else if constexpr (CE) sigT = ce_total(c.mat);
+      else sigT = xs(mg.total, c.mat, G);
+      htDT = sigT * majInv > R(1) - A.ht_cutoff;
+    }
+  }
+
+  __device__ __forceinline__ int seg_st() {
+    const R INF_R = R(D_INF);
     int mat = c.mat;
-    if constexpr (!DT) {
+    {
       // surfaceTracking (transportOperatorST_class.f90:48-166)
       const bool isVoid = (mat == SG_VOID_MAT);
       R sigTot, sigmaTrack;
@@ -490,7 +530,12 @@ struct Tracker {
         report_in_coll(true, sigmaTrack);
       }
       return SEG_MORE;
-    } else {
+    }
+  }
+
+  __device__ __forceinline__ int seg_dt() {
+    int mat = c.mat;
+    {
       // deltaTracking (transportOperatorDT_class.f90:47-131)
       R maj;
       if constexpr (CE) maj = fmax(ce_major(), ce.collisionXS);
@@ -528,7 +573,11 @@ struct Tracker {
   // One segment and, when it ends in a real collision, the collision.  True when the history ended.
   __device__ __forceinline__ bool step() {
     const int e = segment();
-    if (e == SEG_COLLIDE) return collide(trackXS);
+    if (e == SEG_COLLIDE) {
+      const bool dead = collide(trackXS);
+      if (!dead) select_ht();
+      return dead;
+    }
     return e == SEG_END;
   }
 
@@ -591,6 +640,7 @@ struct Tracker {
     segs = P.ints[4 * cap + i];
     cache.lvl = 0;
     if constexpr (CE) set_energy(P.E[i]);
+    select_ht();
   }
 
   // reportHist for a leaked particle (keffImplicitClerk ANA_LEAK, :276-290)
@@ -600,8 +650,8 @@ struct Tracker {
 
 
 // k-implicit partial sums and event counters of a warp, reduced and added to global memory
-template <class R, int MAXL, bool DT, bool CE>
-__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, DT, CE>& T, const TransportArgs<R>& A, int lane) {
+template <class R, int MAXL, int OP, bool CE>
+__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, OP, CE>& T, const TransportArgs<R>& A, int lane) {
   if (A.keff_clerk >= 0) {
     double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
 #pragma unroll
@@ -635,7 +685,7 @@ __device__ __forceinline__ int warp_append(int* counter) {
   return base + __popc(m & ((1u << lane) - 1u));
 }
 
-template <class R, int MAXL, bool DT, bool CE>
+template <class R, int MAXL, int OP, bool CE>
 __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ TransportArgs<R> A) {
   extern __shared__ double s_acc[];
   const bool smem = A.use_smem != 0;
@@ -643,7 +693,7 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
     for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) s_acc[i] = 0.0;
     __syncthreads();
   }
-  Tracker<R, MAXL, DT, CE> T(A, smem ? s_acc : A.acc);
+  Tracker<R, MAXL, OP, CE> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
   bool alive = false, done = false;
   int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
@@ -694,9 +744,9 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
 // finished by the tail kernel (the history loop over the remaining queue).  Per-history RNG streams
 // make the results independent of this scheduling.
 
-template <class R, int MAXL, bool DT, bool CE>
+template <class R, int MAXL, int OP, bool CE>
 __global__ void __launch_bounds__(128) k_ev_start(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT, CE> T(A, A.acc);
+  Tracker<R, MAXL, OP, CE> T(A, A.acc);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
     T.start(i + 1);
     T.store(A.part, i);
@@ -707,9 +757,9 @@ __global__ void __launch_bounds__(128) k_ev_start(const __grid_constant__ Transp
 
 // TAIL = false: stop at a real collision and queue the particle for k_ev_collide.
 // TAIL = true : run each particle to the end of its history (collisions included).
-template <class R, int MAXL, bool DT, bool CE, bool TAIL>
+template <class R, int MAXL, int OP, bool CE, bool TAIL>
 __global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT, CE> T(A, A.acc);
+  Tracker<R, MAXL, OP, CE> T(A, A.acc);
   const int lane = threadIdx.x & 31;
   const int nIn = *A.q.n_in;
   bool alive = false, done = false;
@@ -758,9 +808,9 @@ __global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ Tran
   flush_counters(T, A, lane);
 }
 
-template <class R, int MAXL, bool DT, bool CE>
+template <class R, int MAXL, int OP, bool CE>
 __global__ void __launch_bounds__(128) k_ev_collide(const __grid_constant__ TransportArgs<R> A) {
-  Tracker<R, MAXL, DT, CE> T(A, A.acc);
+  Tracker<R, MAXL, OP, CE> T(A, A.acc);
   const int nIn = *A.q.n_in;
   const int stride = gridDim.x * blockDim.x;
   const int first = blockIdx.x * blockDim.x + threadIdx.x;

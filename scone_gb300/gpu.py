@@ -63,7 +63,7 @@ def load(build=True):
         "sg_batch_autotune": (i32, [vp, P(i32), i32, P(abi.BatchTuning)]),
         "sg_batch_tally_size": (i32, [vp, i32, P(i64)]), "sg_batch_get_bins": (i32, [vp, i32, P(f64), i64]),
         "sg_batch_clear_tally": (i32, [vp, i32]),
-        "sg_serve_start": (i32, [vp, i64]), "sg_serve_submit": (i32, [vp, i32]),
+        "sg_serve_start": (i32, [vp, i64, i32]), "sg_serve_submit": (i32, [vp, i32]),
         "sg_serve_pump": (i32, [vp, i32, P(i32), P(f64), i32, P(i32)]), "sg_serve_stop": (i32, [vp]),
         "sg_serve_status": (i32, [vp, P(i64), P(i32), P(i64)]), "sg_serve_clock": (f64, []),
     }
@@ -82,11 +82,11 @@ class TransportOperatorGPU:
     """A GPU transport operator for whole banks (the `gen:` loop of SCONE's physics packages)."""
 
     def __init__(self, problem=None, precision=abi.PREC_FP64, transport=abi.TRANSPORT_ST, max_bank=1 << 20,
-                 device=0, record_histories=False, form=abi.FORM_EVENT):
+                 device=0, record_histories=False, form=abi.FORM_EVENT, ht_cutoff=0.0):
         self.L = load()
         self.h = C.c_void_p()
         self._keep = []
-        cfg = abi.Config(precision, transport, device, max_bank, 1 if record_histories else 0, form)
+        cfg = abi.Config(precision, transport, device, max_bank, 1 if record_histories else 0, form, ht_cutoff)
         rc = self.L.sg_create(C.byref(cfg), C.byref(self.h))
         if rc != 0:
             raise SconeGpuError(f"sg_create failed with {rc} (is a CUDA device present?)")
@@ -223,10 +223,10 @@ class BatchGPU:
     ``serve_start(wave_histories)``, ``submit(slot)``, ``pump(wait)`` -> [(slot, latency_s)]."""
 
     def __init__(self, precision=abi.PREC_MIXED, transport=abi.TRANSPORT_DT, device=0, max_problems=4096,
-                 arena_bytes=1 << 30, max_work_items=1 << 20):
+                 arena_bytes=1 << 30, max_work_items=1 << 20, ht_cutoff=0.0):
         self.L = load()
         self.b = C.c_void_p()
-        cfg = abi.BatchConfig(precision, transport, device, max_problems, arena_bytes, max_work_items, 0)
+        cfg = abi.BatchConfig(precision, transport, device, max_problems, arena_bytes, max_work_items, 0, ht_cutoff)
         rc = self.L.sg_batch_create(C.byref(cfg), C.byref(self.b))
         if rc != 0:
             raise SconeGpuError(f"sg_batch_create failed with {rc} (is a CUDA device present?)")
@@ -341,8 +341,8 @@ class BatchGPU:
         self._check(self.L.sg_batch_clear_tally(self.b, slot))
 
     # ---- serving
-    def serve_start(self, wave_histories):
-        self._check(self.L.sg_serve_start(self.b, int(wave_histories)))
+    def serve_start(self, wave_histories, item_histories=0):
+        self._check(self.L.sg_serve_start(self.b, int(wave_histories), int(item_histories)))
 
     def submit(self, slot):
         self._check(self.L.sg_serve_submit(self.b, slot))

@@ -60,7 +60,8 @@ class SolveServer:
     """Continuous-batching request loop over a BatchGPU (fixed-source requests) and an optional
     EigenPool (eigenvalue requests)."""
 
-    def __init__(self, batch, catalogue, wave_histories=1 << 21, eigen=None, eigen_cycles=(20, 40)):
+    def __init__(self, batch, catalogue, wave_histories=1 << 23, item_histories=256, eigen=None,
+                 eigen_cycles=(20, 40)):
         self.B = batch
         self.catalogue = catalogue            # resident slots that requests instantiate
         self.waiting = collections.deque()    # fixed-source requests not yet admitted (arena full)
@@ -70,7 +71,7 @@ class SolveServer:
         self.eigen_waiting = collections.deque()
         self.eigen_running = []
         self.done = []
-        self.B.serve_start(wave_histories)
+        self.B.serve_start(wave_histories, item_histories)
 
     # ---- requests
     def submit(self, req):

@@ -55,7 +55,8 @@ def load_batch(gpu, batch, precision, transport, **kw):
     return B, slots
 
 
-@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE,
+                                       abi.TRANSPORT_HT])
 def test_batched_fp64_matches_oracle(gpu_mod, oracle_mod, transport):
     batch = small_batch()
     ref = oracle_bins(oracle_mod, batch, transport)

@@ -26,11 +26,15 @@ FORMS = [abi.FORM_EVENT, abi.FORM_HISTORY]
 
 
 def make_pair(gpu, orl, prob, transport=abi.TRANSPORT_ST, precision=abi.PREC_FP64, max_bank=1 << 18,
-              form=abi.FORM_EVENT):
+              form=abi.FORM_EVENT, ht_cutoff=0.0):
     g = gpu.TransportOperatorGPU(prob, precision=precision, transport=transport, max_bank=max_bank,
-                                 record_histories=True, form=form)
-    o = orl.Oracle(prob, transport=transport)
+                                 record_histories=True, form=form, ht_cutoff=ht_cutoff)
+    o = orl.Oracle(prob, transport=transport, ht_cutoff=ht_cutoff)
     return g, o
+
+
+ALL_TRANSPORTS = [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE, abi.TRANSPORT_HT,
+                  abi.TRANSPORT_HT_NOCACHE]
 
 
 def test_point_source_bank_bitexact(gpu_mod, oracle_mod):
@@ -45,7 +49,7 @@ def test_point_source_bank_bitexact(gpu_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("form", FORMS)
-@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
+@pytest.mark.parametrize("transport", ALL_TRANSPORTS)
 def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
     p = problems.infinite_medium_2g()
     g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
@@ -68,10 +72,11 @@ def test_infinite_medium_fp64_history_parity(gpu_mod, oracle_mod, transport, for
 
 
 @pytest.mark.parametrize("form", FORMS)
-@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
-def test_lattice_fp64_bank_parity(gpu_mod, oracle_mod, transport, form):
+@pytest.mark.parametrize("transport,cutoff", [(t, 0.0) for t in ALL_TRANSPORTS] +
+                         [(abi.TRANSPORT_HT, 0.5), (abi.TRANSPORT_HT, 0.3)])
+def test_lattice_fp64_bank_parity(gpu_mod, oracle_mod, transport, cutoff, form):
     p = problems.lattice_17x17_7g()
-    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form, ht_cutoff=cutoff)
     n = 4000
     o.eigen_init(n, SEED)
     bank, pop = o.eigen_bank(n)

@@ -392,3 +392,27 @@ def test_oracle_runs_batched_problem_kinds(oracle_mod):
             b = o.bins(a)
             assert b.shape == (ng, 3) and np.all(b[:, 1] >= 0) and b[0, 1] > 0
             assert st.n_histories == 300
+
+
+def test_oracle_hybrid_tracking_limits(oracle_mod):
+    """transportOperatorHT chooses per transit (transportOperatorHT_class.f90:49-81): with a cutoff near
+    1 every transit in matter uses delta tracking, so the histories are those of transportOperatorDT.
+    With a smaller cutoff both kinds occur and the histories differ from both operators' (a material
+    whose total is the majorant has ratio 1 and takes delta tracking at any cutoff)."""
+    p = problems.lattice_17x17_7g()
+    n = 1500
+
+    def run(transport, cutoff=0.0):
+        o = oracle_mod.Oracle(p, transport=transport, ht_cutoff=cutoff)
+        o.eigen_init(n, 0x5C3A84C9)
+        bank, _ = o.eigen_bank(n)
+        a = o.upload_tally(p.tallies["mesh"])
+        o.transport_bank(a, bank, 31337, k_eff=1.0)
+        return o.history_records(n)
+
+    st, dt = run(abi.TRANSPORT_ST), run(abi.TRANSPORT_DT)
+    hi = run(abi.TRANSPORT_HT, 0.999999)
+    assert np.array_equal(hi[0], dt[0]) and np.array_equal(hi[1], dt[1])
+    for c in (0.5, 1e-9):
+        mid = run(abi.TRANSPORT_HT, c)
+        assert not np.array_equal(mid[1], st[1]) and not np.array_equal(mid[1], dt[1])

@@ -20,7 +20,7 @@ class FakeBatch:
     def clock(self):
         return self.t
 
-    def serve_start(self, wave):
+    def serve_start(self, wave, item=0):
         self.wave = wave
 
     def instance(self, parent, pop, cycles, master):
