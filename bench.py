@@ -94,11 +94,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    p = os.path.join(ROOT, "profiles", "transport_traffic.json")
+def committed_traffic(kernel):
+    """Measured DRAM bytes per event of `kernel` (an ncu capture summarised under profiles/)."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f)
+            return json.load(f).get(kernel, {}).get("bytes_per_event")
     return None
 
 
@@ -329,8 +330,11 @@ def batched_section(a, local):
     # roofline of the batched kernel (same per-event bytes as the single-problem history loop)
     peak, kind = measured_peaks()
     ach = ev * BYTES_PER_EVENT_MIXED / (mean_ms / 1e3) / 1e9
+    bpe_dram = committed_traffic("k_batch_uneven")
     out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                       "peak_source": kind, "kernel": "k_batch (batched history loop)"}
+                       "peak_source": kind, "kernel": "k_batch (batched history loop)",
+                       "traffic": bpe_dram * ev if bpe_dram else None, "bytes_per_event": BYTES_PER_EVENT_MIXED,
+                       "events_per_launch": ev, "launch_ms": mean_ms}
     if not a.no_plain:
       try:
         for name, form in (("plain_event", abi.FORM_EVENT), ("plain_history", abi.FORM_HISTORY)):
@@ -540,10 +544,8 @@ def main():
     ev_per_launch = events / (a.steps * world)
     launch_ms = tr_ms / a.steps
     achieved = ev_per_launch * bpe / (launch_ms / 1e3) / 1e9
-    tr_info = committed_traffic()
-    traffic = None
-    if tr_info and tr_info.get("bytes_per_event"):
-        traffic = tr_info["bytes_per_event"] * ev_per_launch
+    bpe_dram = committed_traffic("k_transport_lattice")
+    traffic = bpe_dram * ev_per_launch if bpe_dram else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": peak_kind, "kernel": ("event loop: k_ev_start + k_ev_transit + k_ev_collide + k_ev_transit<tail>"
                        if a.form == "event" else "k_transport (history loop)"),

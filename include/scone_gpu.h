@@ -133,7 +133,7 @@ typedef struct sg_geometry_desc {
   int32_t        root_uni;      /* 0-based index of the root universe */
 } sg_geometry_desc;
 
-typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN = P0 */
+typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN = P0 or P1 */
   int32_t        n_mat;
   int32_t        n_g;
   const double*  capture;       /* [n_mat][n_g]                 */
@@ -144,6 +144,8 @@ typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN =
   const double*  prod;          /* [n_mat][n_g (in)][n_g (out)] scatteringMultiplicity */
   const int32_t* fissile;       /* [n_mat] 0/1                  */
   double         avg_dist;      /* `avgDist`; <= 0 means none   */
+  const double*  p1;            /* [n_mat][n_g (in)][n_g (out)] xsFile `P1` (baseMgNeutronMaterial
+                                   `PN P1`, multiScatterP1MG_class.f90:96-128); NULL: P0 scattering */
 } sg_mg_desc;
 
 /* Continuous-energy neutron data: the part of aceNeutronDatabase / aceNeutronNuclide /

@@ -36,6 +36,7 @@ def lib():
         sig = {
             "or_create": (i32, [i32, P(vp)]), "or_destroy": (i32, [vp]),
             "or_set_ht_cutoff": (i32, [vp, C.c_double]),
+            "or_sample_legendre_p1": (i32, [C.c_double, P(C.c_uint64), P(C.c_double), i32]),
             "or_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
             "or_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
             "or_upload_mg": (i32, [vp, P(abi.MGDesc)]),
@@ -279,6 +280,16 @@ class Oracle:
         n = self.L.or_timed_gen_loop(self.h, admin, C.byref(bank.struct), bank.n, C.c_uint64(master), k_eff,
                                      threads, C.byref(ev))
         return n, ev.value
+
+
+def sample_legendre_p1(a, state, n):
+    """n samples of SCONE's sampleLegendre_P1 for a = 3 P1/P0 from RNG `state`."""
+    s = C.c_uint64(state)
+    out = np.zeros(n)
+    rc = lib().or_sample_legendre_p1(a, C.byref(s), out.ctypes.data_as(C.POINTER(C.c_double)), n)
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc}")
+    return out, s.value
 
 
 def rng_draws(state, n):

@@ -110,6 +110,23 @@ static double norm2_3(const double v[3]) {
   return scale * std::sqrt(ssq);
 }
 
+// sampleLegendre_P1 (SharedModules/legendrePoly_func.f90:35-99), mixing method (Lux & Koblinger)
+static double sampleLegendreP1(double P1, RNG& rng, std::string& err) {
+  const double a = std::fabs(P1);
+  double threshold;
+  int top, low;                                          // 1 uniform, 2 linear, 3 delta
+  if (a < 1.0) { threshold = a; top = 2; low = 1; }
+  else if (a <= 3.0) { threshold = 0.5 * (a - 1.0); top = 3; low = 2; }
+  else { err = "P1 must have absolute value < 3.0"; return 0.0; }
+  const int exec = (rng.get() < threshold) ? top : low;
+  double x;
+  if (exec == 1) x = 2.0 * rng.get() - 1.0;
+  else if (exec == 2) x = 2.0 * std::sqrt(rng.get()) - 1.0;
+  else x = 1.0;
+  if (P1 < 0.0) x = -x;
+  return x;
+}
+
 // rotateVector (SharedModules/genericProcedures.f90:1047-1084)
 static void rotateVector(const double dir[3], double mu, double phi, double out[3]) {
   double sinPol = std::sin(phi);
@@ -801,6 +818,7 @@ struct Geometry {
 struct MGData {
   int nMat = 0, nG = 0;
   std::vector<double> total, scatter, capture, fission, nuFission, chi, P0, prod;  // [m][g], P0/prod [m][gin][gout]
+  std::vector<double> P1;                              // multiScatterP1MG: 3 P1/P0 [m][gin][gout]; empty for P0
   std::vector<int> fissile;
   std::vector<double> majorant;
   double collisionXS = 0.0;
@@ -839,6 +857,12 @@ struct MGData {
       }
     }
     if (d->avg_dist > 0.0) collisionXS = 1.0 / d->avg_dist;
+    P1.clear();
+    if (d->p1) {                                         // multiScatterP1MG buildFromDict (:117-126)
+      P1.assign(M * nG, 0.0);
+      for (size_t k = 0; k < M * nG; ++k)
+        if (P0[k] != 0.0) P1[k] = d->p1[k] / P0[k] * 3.0;
+    }
     (void)err;
     return 0;
   }
@@ -1546,7 +1570,10 @@ struct Oracle {
         if (rem < 0.0) break;
       }
       if (Gout > mg.nG) { err = "scatter G_out sampling failed"; Gout = mg.nG; }
-      double mu = 2.0 * p.rng.get() - 1.0;
+      double mu;
+      if (!mg.P1.empty())                                // multiScatterP1MG%sampleOut (:69-85)
+        mu = sampleLegendreP1(mg.P1[((size_t)(matIdx - 1) * mg.nG + (p.G - 1)) * mg.nG + (Gout - 1)], p.rng, err);
+      else mu = 2.0 * p.rng.get() - 1.0;
       double phi = TWO_PI * p.rng.get();
       double w_mul = mg.prod[((size_t)(matIdx - 1) * mg.nG + (p.G - 1)) * mg.nG + (Gout - 1)];
       MT = macroIEscatter;
@@ -1831,6 +1858,15 @@ int32_t or_create(int32_t transport, or_handle* out) {
   return SG_OK;
 }
 int32_t or_destroy(or_handle h) { delete O(h); return SG_OK; }
+// n draws of sampleLegendre_P1 for the normalised coefficient a = 3 P1/P0 (state advanced)
+int32_t or_sample_legendre_p1(double a, uint64_t* state, double* out, int32_t n) {
+  orc::RNG r;
+  r.s = *state;
+  std::string err;
+  for (int i = 0; i < n; ++i) out[i] = orc::sampleLegendreP1(a, r, err);
+  *state = r.s;
+  return err.empty() ? SG_OK : SG_ERR_BAD_ARG;
+}
 int32_t or_set_ht_cutoff(or_handle h, double c) {
   if (!(c > 0.0 && c < 1.0)) return SG_ERR_BAD_ARG;
   O(h)->htCutoff = c;

@@ -52,7 +52,7 @@ class MGDesc(C.Structure):
     _fields_ = [
         ("n_mat", C.c_int32), ("n_g", C.c_int32),
         ("capture", f64p), ("fission", f64p), ("nu", f64p), ("chi", f64p),
-        ("p0", f64p), ("prod", f64p), ("fissile", i32p), ("avg_dist", C.c_double),
+        ("p0", f64p), ("prod", f64p), ("fissile", i32p), ("avg_dist", C.c_double), ("p1", f64p),
     ]
 
 
@@ -236,6 +236,7 @@ def mg_struct(m):
     s.prod = arr("prod", np.float64)
     s.fissile = arr("fissile", np.int32)
     s.avg_dist = float(m.get("avg_dist", 0.0))
+    s.p1 = arr("p1", np.float64) if m.get("p1") is not None else C.cast(None, f64p)
     return s, keep
 
 

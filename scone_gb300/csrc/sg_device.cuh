@@ -123,6 +123,25 @@ __device__ __forceinline__ double norm2_scaled(double a0, double a1, double a2) 
 }
 
 // rotateVector (SharedModules/genericProcedures.f90:1047-1084)
+// sampleLegendre_P1 (SharedModules/legendrePoly_func.f90:35-99): the mixing method of Lux and
+// Koblinger for the linearly anisotropic density 1/2 (1 + a mu), a = 3 P1/P0: with |a| < 1 the
+// linear density (1 + mu)/2 with probability |a|, else uniform; with 1 <= |a| <= 3 a delta at
+// mu = 1 with probability (|a| - 1)/2, else the linear density; mirrored for a < 0.
+template <class R, class G>
+__device__ __forceinline__ R sample_legendre_p1(R a, G& rng) {
+  const R al = fabs(a);
+  R thr;
+  int top, low;                            // 1 uniform, 2 linear, 3 delta
+  if (al < R(1)) { thr = al; top = 2; low = 1; }
+  else { thr = R(0.5) * (al - R(1)); top = 3; low = 2; }
+  const int ex = (rng.get() < thr) ? top : low;
+  R x;
+  if (ex == 1) x = R(2) * rng.get() - R(1);
+  else if (ex == 2) x = R(2) * dsqrt<R>(rng.get()) - R(1);
+  else x = R(1);
+  return a < R(0) ? -x : x;
+}
+
 template <class R>
 __device__ __forceinline__ void rotate_vector(R& u, R& v, R& w, R mu, R sinPol, R cosPol) {
   R A = dsqrt<R>(fmax(R(0), R(1) - mu * mu));

@@ -142,8 +142,8 @@ struct sg_handle_t {
   bool hasMG = false;
   bool anyFissile = false;
   int nMat = 0, nG = 0;
-  DArr<double> mgD[9];
-  DArr<float> mgF[9];
+  DArr<double> mgD[10];
+  DArr<float> mgF[10];
   DArr<int> fissile;
   DMG<double> mg64{};
   DMG<float> mgMx{};
@@ -498,9 +498,22 @@ int build_mg(sg_handle h, const sg_mg_desc* d) {
     for (int a : act) xs = std::max(xs, total[(size_t)(a - 1) * nG + g]);
     maj[g] = xs * 1.0;
   }
-  const std::vector<double>* src[9] = {&total, &scatter, &capture, &fission, &nuf, &chi, &P0, &prod, &maj};
+  // multiScatterP1MG buildFromDict (multiScatterP1MG_class.f90:96-128): 3 P1/P0 where P0 /= 0
+  std::vector<double> P1n;
+  if (d->p1) {
+    P1n.assign(MG * nG, 0.0);
+    for (size_t k = 0; k < MG * nG; ++k) {
+      if (P0[k] != 0.0) P1n[k] = d->p1[k] / P0[k] * 3.0;
+      if (!(std::fabs(P1n[k]) <= 3.0))                // sampleLegendre_P1 (legendrePoly_func.f90:62-63)
+        return h->fail(SG_ERR_BAD_ARG, "mg: P1 must have absolute value below 3 P0");
+    }
+  }
+  const std::vector<double>* src[10] = {&total, &scatter, &capture, &fission, &nuf, &chi, &P0, &prod, &maj, &P1n};
+  const int nArr = d->p1 ? 10 : 9;
   cudaStream_t st = h->stream;
-  for (int i = 0; i < 9; ++i) {
+  h->mgD[9].free();
+  h->mgF[9].free();
+  for (int i = 0; i < nArr; ++i) {
     CK(h->mgD[i].upload(*src[i], st));
     std::vector<float> f(src[i]->begin(), src[i]->end());
     CK(h->mgF[i].upload(f, st));
@@ -508,9 +521,9 @@ int build_mg(sg_handle h, const sg_mg_desc* d) {
   CK(h->fissile.upload(fis, st));
   double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
   h->mg64 = DMG<double>{M, nG, h->mgD[0].p, h->mgD[1].p, h->mgD[2].p, h->mgD[3].p, h->mgD[4].p, h->mgD[5].p,
-                        h->mgD[6].p, h->mgD[7].p, h->fissile.p, h->mgD[8].p, cxs};
+                        h->mgD[6].p, h->mgD[7].p, h->fissile.p, h->mgD[8].p, cxs, d->p1 ? h->mgD[9].p : nullptr};
   h->mgMx = DMG<float>{M, nG, h->mgF[0].p, h->mgF[1].p, h->mgF[2].p, h->mgF[3].p, h->mgF[4].p, h->mgF[5].p,
-                       h->mgF[6].p, h->mgF[7].p, h->fissile.p, h->mgF[8].p, (float)cxs};
+                       h->mgF[6].p, h->mgF[7].p, h->fissile.p, h->mgF[8].p, (float)cxs, d->p1 ? h->mgF[9].p : nullptr};
   h->hasMG = true;
   return SG_OK;
 }

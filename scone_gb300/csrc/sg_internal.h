@@ -71,6 +71,7 @@ struct DMG {
   const int* fissile;
   const R* majorant;
   R collisionXS;
+  const R* P1n;         // [mat][Gin][Gout] 3 P1/P0 (multiScatterP1MG), null for P0 scattering
 };
 
 // Continuous-energy neutron data (aceNeutronNuclide mainData / eGrid, ceNeutronMaterial composition,

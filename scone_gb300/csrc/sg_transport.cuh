@@ -412,7 +412,9 @@ struct Tracker {
         if (rem < R(0)) break;
       }
       if (go > mg.nG) go = walk_failed(row, 1);
-      R mu = R(2) * rng.get() - R(1);
+      R mu;                                              // multiScatterP1MG%sampleOut (:69-85)
+      if (mg.P1n) mu = sample_legendre_p1<R>(mg.P1n[(long long)k * mg.nG + (go - 1)], rng);
+      else mu = R(2) * rng.get() - R(1);
       R sp, cp;
       sincos_phi<R>(rng.get(), sp, cp);
       R w_mul = mg.prod[(long long)k * mg.nG + (go - 1)];

@@ -105,8 +105,9 @@ def lattice_fills_from_map(map_values, shape):
 
 # ----------------------------------------------------------------------------- MG data
 def mg_data(n_g, total, scatter_matrix, capture=None, fission=None, nu=None, chi=None,
-            prod=None, avg_dist=0.0):
-    """Assemble an MG desc dict; scatter_matrix[m][g_in][g_out] (xsFile `P0` layout)."""
+            prod=None, avg_dist=0.0, p1=None):
+    """Assemble an MG desc dict; scatter_matrix[m][g_in][g_out] (xsFile `P0` layout); p1 in the same
+    layout makes the scattering linearly anisotropic (xsFile `P1`, `PN P1`)."""
     total = np.asarray(total, np.float64)
     n_mat = total.shape[0]
     P0 = np.asarray(scatter_matrix, np.float64).reshape(n_mat, n_g, n_g)
@@ -121,7 +122,8 @@ def mg_data(n_g, total, scatter_matrix, capture=None, fission=None, nu=None, chi
         nu=np.zeros((n_mat, n_g)) if nu is None else np.asarray(nu, np.float64),
         chi=np.zeros((n_mat, n_g)) if chi is None else np.asarray(chi, np.float64),
         p0=P0, prod=np.ones_like(P0) if prod is None else np.asarray(prod, np.float64),
-        fissile=fissile, avg_dist=avg_dist)
+        fissile=fissile, avg_dist=avg_dist,
+        p1=None if p1 is None else np.asarray(p1, np.float64).reshape(n_mat, n_g, n_g))
 
 
 class Problem:
@@ -139,7 +141,7 @@ class Problem:
 
 
 # ----------------------------------------------------------------------------- workloads
-def infinite_medium_2g(seed=7, half_width=10.0):
+def infinite_medium_2g(seed=7, half_width=10.0, p1_ratio=None):
     """Fixed-source transport in an infinite homogeneous medium, 2 groups.
 
     Sigma_t ~ U[0.5, 2.0] /cm per group, scattering ratio 0.9 with a lower-triangular (downscatter)
@@ -154,7 +156,9 @@ def infinite_medium_2g(seed=7, half_width=10.0):
     P0[0, 0, 1] = 0.9 * sig_t[0] * (1.0 - split)
     P0[0, 1, 1] = 0.9 * sig_t[1]
     capture = 0.1 * sig_t
-    mg = mg_data(2, sig_t[None, :], P0, capture=capture[None, :])
+    # optional linearly anisotropic scattering: P1 = p1_ratio * P0 (mean scattering cosine p1_ratio)
+    p1 = None if p1_ratio is None else np.asarray(p1_ratio, np.float64) * P0
+    mg = mg_data(2, sig_t[None, :], P0, capture=capture[None, :], p1=p1)
     gb = GeometryBuilder()
     box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, half_width, half_width, half_width)
     gb.root_universe(box, 1, bc=[abi.BC_REFLECTIVE] * 6)

@@ -416,3 +416,35 @@ def test_oracle_hybrid_tracking_limits(oracle_mod):
     for c in (0.5, 1e-9):
         mid = run(abi.TRANSPORT_HT, c)
         assert not np.array_equal(mid[1], st[1]) and not np.array_equal(mid[1], dt[1])
+
+
+def test_legendre_p1_sampler_moments(oracle_mod):
+    """sampleLegendre_P1 (legendrePoly_func.f90:35-99) draws the linearly anisotropic cosine of
+    multiScatterP1MG: for a = 3 P1/P0 the mean cosine is a/3 over the whole range |a| <= 3 (mixing of
+    uniform, linear and delta parts), every draw lies in [-1, 1], and |a| > 3 is an error."""
+    for a in (-2.5, -0.6, 0.0, 0.3, 0.99, 1.0, 2.0, 3.0):
+        x, _ = oracle_mod.sample_legendre_p1(a, 0x1234567, 200000)
+        assert np.all(np.abs(x) <= 1.0)
+        assert abs(x.mean() - a / 3.0) < 5.0 * x.std() / np.sqrt(len(x)) + 1e-12, (a, x.mean())
+        if abs(a) < 1.0:                     # density (1 + a mu)/2: second moment 1/3
+            assert abs((x ** 2).mean() - 1.0 / 3.0) < 0.005
+    with pytest.raises(RuntimeError):
+        oracle_mod.sample_legendre_p1(3.5, 1, 10)
+
+
+def test_p1_scattering_changes_leakage(oracle_mod):
+    """Forward-peaked P1 scattering raises leakage from a finite sphere against P0 with the same
+    cross sections (same RNG streams; only the scattering cosine differs)."""
+    rng = np.random.default_rng(21)
+    p = problems.fixed_source_problem(rng, 2, "sphere", radius=2.0)
+    leak = {}
+    for ratio in (None, 0.6):
+        mg = dict(p.mg)
+        if ratio is not None:
+            mg["p1"] = ratio * np.asarray(mg["p0"])
+        q = problems.Problem(p.geometry, mg, source=p.source, tallies=p.tallies)
+        o = oracle_mod.Oracle(q, transport=abi.TRANSPORT_ST)
+        a = o.upload_tally(q.tallies["flux"])
+        m, st = o.fixed_source_cycle(a, 20000, 99)
+        leak[ratio] = st.n_collisions / 20000.0      # fewer collisions per history = more leakage
+    assert leak[0.6] < 0.95 * leak[None], leak
