@@ -318,6 +318,13 @@ int32_t sg_eigen_get_bank(sg_handle h, sg_bank* out, int32_t cap, int32_t* pop);
  * stride(n), gen loop, stride(n), reportCycleEnd.  master_state is updated in place. */
 int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* master_state,
                               sg_cycle_stats* stats);
+/* The same cycle for one process of a population split over processes (SCONE with MPI,
+ * fixedSourcePhysicsPackage_class.f90:131,186-189,264 with getWorkshare/getOffset,
+ * mpi_func.f90:133-159): `share` histories of `total`; master_state enters strided by this
+ * process's offset and is strided by `total` after the source and after the gen loop, so the
+ * union of all processes' histories is the single-process run's. */
+int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t share, int32_t total,
+                                    uint64_t* master_state, sg_cycle_stats* stats);
 
 /* ---------------------------------------------------------------- gen loop without allocation */
 

@@ -36,6 +36,7 @@ def lib():
         sig = {
             "or_create": (i32, [i32, P(vp)]), "or_destroy": (i32, [vp]),
             "or_set_ht_cutoff": (i32, [vp, C.c_double]),
+            "or_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(C.c_uint64), P(abi.CycleStats)]),
             "or_sample_legendre_p1": (i32, [C.c_double, P(C.c_uint64), P(C.c_double), i32]),
             "or_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
             "or_upload_geometry": (i32, [vp, P(abi.GeometryDesc)]),
@@ -229,10 +230,15 @@ class Oracle:
         self._check(self.L.or_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
         return b, pop.value
 
-    def fixed_source_cycle(self, admin, n, master):
+    def fixed_source_cycle(self, admin, n, master, total=None):
+        """One fixed-source cycle of n histories; with `total`, n is this process's share of a
+        population of `total` split over processes (master already strided by the offset)."""
         m = C.c_uint64(master)
         st = abi.CycleStats()
-        self._check(self.L.or_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        if total is None:
+            self._check(self.L.or_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        else:
+            self._check(self.L.or_fixed_source_cycle_shard(self.h, admin, n, total, C.byref(m), C.byref(st)))
         return m.value, st
 
     # geometry probes

@@ -2049,18 +2049,26 @@ int32_t or_eigen_get_bank(or_handle h, sg_bank* out, int32_t cap, int32_t* pop) 
 }
 
 // fixedSourcePhysicsPackage%cycles, one batch (fixedSourcePhysicsPackage_class.f90:183-289)
-int32_t or_fixed_source_cycle(or_handle h, int32_t admin, int32_t n, uint64_t* master, sg_cycle_stats* st) {
+// fixedSourcePhysicsPackage%cycles, one cycle of this process's share n of `total` histories
+// (fixedSourcePhysicsPackage_class.f90:183-289): the master is strided by the total population
+// after the source and after the gen loop; `master` enters already strided by the process's offset
+// (getOffset, mpi_func.f90:143-159).
+int32_t or_fixed_source_cycle_shard(or_handle h, int32_t admin, int32_t n, int32_t total, uint64_t* master,
+                                    sg_cycle_stats* st) {
   Oracle* o = O(h);
   std::vector<orc::PState> bank(n), next;
   for (int i = 1; i <= n; ++i) { orc::RNG r; r.s = *master; r.stride(i); bank[i - 1] = o->samplePoint(r); }
-  orc::RNG m; m.s = *master; m.stride(n);
+  orc::RNG m; m.s = *master; m.stride(total);
   o->reportCycleStart(admin, (double)n);
   int rc = o->transportBank(admin, bank, m.s, 1.0, next);
-  m.stride(n);
+  m.stride(total);
   o->reportCycleEnd(admin, 0.0, 1.0);
   *master = m.s;
   if (st) { st->n_histories = n; st->n_events = o->nEvents; st->n_collisions = o->nColl; st->n_next = (int64_t)next.size(); }
   return rc;
+}
+int32_t or_fixed_source_cycle(or_handle h, int32_t admin, int32_t n, uint64_t* master, sg_cycle_stats* st) {
+  return or_fixed_source_cycle_shard(h, admin, n, n, master, st);
 }
 
 // ---- unit-test probes

@@ -1564,7 +1564,12 @@ int32_t sg_eigen_get_bank(sg_handle h, sg_bank* out, int32_t cap, int32_t* pop) 
 }
 
 int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* master_state, sg_cycle_stats* stats) {
-  if (!h || !master_state || n <= 0 || n > h->cap) return SG_ERR_BAD_ARG;
+  return sg_fixed_source_cycle_shard(h, admin, n, n, master_state, stats);
+}
+
+int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t n, int32_t total, uint64_t* master_state,
+                                    sg_cycle_stats* stats) {
+  if (!h || !master_state || n <= 0 || n > h->cap || total < n) return SG_ERR_BAD_ARG;
   if (!h->hasSource) return h->fail(SG_ERR_STATE, "no point source set");
   if (h->anyFissile) return h->fail(SG_ERR_BAD_ARG, "fixed-source runs with fissile materials are not supported");
   cudaStream_t s = h->stream;
@@ -1577,7 +1582,7 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
   a.n = n;
   a.master = *master_state;
   CK(launch_point_source(a, s));
-  unsigned long long m = rng_stride(*master_state, n);                   // :189
+  unsigned long long m = rng_stride(*master_state, total);               // :189
   int rc = cycle_start(h, admin, nullptr, (double)n);
   if (rc) return rc;
   const double one = 1.0;
@@ -1587,7 +1592,7 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
   sg_cycle_stats st{};
   rc = gen_loop(h, admin, A, n, m, h->scal.p + 0, B, h->cap, &S, &st);
   if (rc) return rc;
-  m = rng_stride(m, n);                                                  // :264
+  m = rng_stride(m, total);                                              // :264
   const double wn = (double)n;
   CK(cudaMemcpyAsync(h->scal.p + 3, &wn, sizeof(double), cudaMemcpyHostToDevice, s));
   rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, -1, nullptr);   // :267

@@ -49,6 +49,7 @@ def load(build=True):
         "sg_eigen_init": (i32, [vp, i32, u64, f64]), "sg_eigen_cycle": (i32, [vp, i32, i32, P(abi.CycleStats)]),
         "sg_eigen_state": (i32, [vp, P(u64), P(f64)]), "sg_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
         "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
+        "sg_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
         "sg_rng_draws": (i32, [P(u64), P(f64), i32]), "sg_rng_skip": (u64, [u64, i64]),
         "sg_transport_bank_noalloc": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(i32)]),
@@ -206,10 +207,15 @@ class TransportOperatorGPU:
         self._check(self.L.sg_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
         return b, pop.value
 
-    def fixed_source_cycle(self, admin, n, master):
+    def fixed_source_cycle(self, admin, n, master, total=None):
+        """One fixed-source cycle of n histories; with `total`, n is this process's share of a
+        population of `total` split over processes (master already strided by the offset)."""
         m = C.c_uint64(master)
         st = abi.CycleStats()
-        self._check(self.L.sg_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        if total is None:
+            self._check(self.L.sg_fixed_source_cycle(self.h, admin, n, C.byref(m), C.byref(st)))
+        else:
+            self._check(self.L.sg_fixed_source_cycle_shard(self.h, admin, n, total, C.byref(m), C.byref(st)))
         return m.value, st
 
 

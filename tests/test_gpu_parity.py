@@ -194,3 +194,27 @@ def test_p1_scattering_fp64_history_parity(gpu_mod, oracle_mod, transport, form)
     g.tally_cycle_end(ag, float(n))
     o.tally_cycle_end(ao, float(n))
     np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_fixed_source_shards_sum_to_single_process(gpu_mod, oracle_mod, world):
+    """sg_fixed_source_cycle_shard: the ranks of a population split (run here one after another on
+    one GPU, each on its own handle, nothing shared) sum to the single-process oracle run."""
+    from scone_gb300 import replicas
+    p = problems.infinite_medium_2g()
+    n, cycles = 30001, 3
+    total = None
+    for rank in range(world):
+        g = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_FP64, transport=abi.TRANSPORT_ST, max_bank=n,
+                                         form=abi.FORM_HISTORY)
+        a = g.upload_tally(p.tallies["flux"])
+        replicas.fixed_source_shard(g, a, n, rank, world, 777, cycles, gpu_mod.rng_skip)
+        c = g.bins(a)[:, 1]
+        total = c if total is None else total + c
+        g.close()
+    o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_ST)
+    ao = o.upload_tally(p.tallies["flux"])
+    m = 777
+    for _ in range(cycles):
+        m, _ = o.fixed_source_cycle(ao, n, m)
+    np.testing.assert_allclose(total, o.bins(ao)[:, 1], rtol=1e-10, atol=0)
