@@ -337,6 +337,10 @@ def batched_section(a, local):
                        "events_per_launch": ev, "launch_ms": mean_ms}
     if not a.no_plain:
       try:
+        # the event form's queue thresholds tuned on a sample (every 64th problem), as the batch's
+        t0 = time.perf_counter()
+        out["plain_event_tuning"] = B.autotune_plain(slots[::64])
+        out["plain_autotune_s"] = time.perf_counter() - t0
         for name, form in (("plain_event", abi.FORM_EVENT), ("plain_history", abi.FORM_HISTORY)):
             B.run_plain(slots[:4], form=form)                          # warm-up (work handle, modules)
             for s in slots:

@@ -70,6 +70,13 @@ extern "C" {
 #define SG_UNI_LAT         4      /* ipar: nx ny nz(0 = 2D) offset(0/1)    dpar: px py pz
                                      fills: nx*ny*nz in local-ID order (x fastest, y, z) + pad   */
 
+/* unionCell operators in a cell's surface list (Geometry/Cells/unionCell_class.f90:80-225): '<', '>',
+ * ':' (union) and '#' (complement); intersections stay implicit, as in SCONE's input */
+#define SG_CELL_OPEN       (-2147483647)
+#define SG_CELL_CLOSE      (-2147483646)
+#define SG_CELL_UNION      (-2147483645)
+#define SG_CELL_COMPLEMENT (-2147483644)
+
 /* boundary conditions (universalVariables.f90:57-59) */
 #define SG_BC_VACUUM       0
 #define SG_BC_REFLECTIVE   1
@@ -120,7 +127,8 @@ typedef struct sg_geometry_desc {
   int32_t        bc[6];         /* -x +x -y +y -z +z, applied to the border (geometryStd `boundary`) */
   int32_t        n_cell;
   const int32_t* cell_ptr;      /* [n_cell+1] into cell_surf    */
-  const int32_t* cell_surf;     /* signed 1-based surface index (-k: -ve halfspace of surface k) */
+  const int32_t* cell_surf;     /* signed 1-based surface index (-k: -ve halfspace of surface k);
+                                   a cell that also holds SG_CELL_* operator tokens is a unionCell */
   int32_t        n_uni;
   const int32_t* uni_type;      /* [n_uni]                      */
   const double*  uni_origin;    /* [n_uni][3]                   */
@@ -346,6 +354,20 @@ int32_t sg_transport_bank_noalloc(sg_handle h, int32_t admin, const sg_bank* dev
                                   uint64_t master_state, double k_eff, sg_bank* dev_next,
                                   int32_t next_cap, int32_t* n_next);
 
+/* ---------------------------------------------------------------- event-form queue thresholds */
+
+/* No SCONE counterpart (SCONE has no event form).  The event form (SG_FORM_EVENT) alternates
+ * transit and collision kernels over compacted queues; the host checks the queue length every
+ * `rounds_per_check` rounds and hands the rest to the history-loop tail kernel once it is at most
+ * max(tail_min, n / tail_divisor).  Defaults 4, 4096, 64; sg_batch_autotune_plain picks them. */
+typedef struct sg_event_tuning {
+  int32_t rounds_per_check;
+  int32_t tail_min;
+  int32_t tail_divisor;
+} sg_event_tuning;
+int32_t sg_set_event_tuning(sg_handle h, const sg_event_tuning* t);
+int32_t sg_get_event_tuning(sg_handle h, sg_event_tuning* t);
+
 /* ---------------------------------------------------------------- batched solves */
 
 /* No single SCONE counterpart: SCONE solves one problem per process
@@ -425,6 +447,9 @@ int32_t sg_batch_run_plain(sg_batch b, const int32_t* slots, int32_t n, int32_t 
 /* measures candidate launch shapes on the listed problems (their tallies are cleared afterwards),
  * keeps the fastest and returns it */
 int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_tuning* best);
+/* the same for the plain event form: queue thresholds timed (wall clock) on the listed problems;
+ * the best are kept for sg_batch_run_plain */
+int32_t sg_batch_autotune_plain(sg_batch b, const int32_t* slots, int32_t n, sg_event_tuning* best);
 /* scoreMemory bins(N,3) of a problem, as sg_get_bins; while serving, only for completed requests
  * (read beside the running waves) */
 int32_t sg_batch_tally_size(sg_batch b, int32_t slot, int64_t* n_bins);

@@ -467,7 +467,100 @@ struct Universe {
 
 struct Geometry {
   std::vector<Surface> surfs;
-  std::vector<std::vector<int>> cells;   // signed 1-based surface index per cell
+  std::vector<std::vector<int>> cells;   // signed 1-based surface index per cell (unionCell: its evalArray)
+  std::vector<char> cellComplex;         // unionCell with unions: evaluated by insideComplex
+
+  // unionCell operator codes inside an evaluation array (unionCell_class.f90:15-19)
+  static constexpr int OP_OPEN = SG_CELL_OPEN, OP_CLOSE = SG_CELL_CLOSE, OP_UNION = SG_CELL_UNION,
+                       OP_COMPLEM = SG_CELL_COMPLEMENT, OP_INTERSECT = SG_CELL_COMPLEMENT + 1;
+  static bool isOp(int t) { return t >= OP_OPEN && t <= OP_INTERSECT; }
+
+  // unionCell%init (unionCell_class.f90:80-199) with deMorgan (:202-262) and checkPrecedence (:267-305)
+  static bool unionCellInit(const std::vector<int>& in, std::vector<int>& ev, bool& cx, std::string& err) {
+    bool ops = false;
+    for (int t : in) if (isOp(t)) ops = true;
+    cx = false;
+    if (!ops) { ev = in; return true; }
+    std::vector<int> a;
+    bool surfacePrev = false, closePrev = false;
+    int depth = 0;
+    for (int t : in) {
+      if (isOp(t)) {
+        if (t == OP_OPEN) {
+          depth += 1;
+          if (surfacePrev || closePrev) a.push_back(OP_INTERSECT);
+          a.push_back(OP_OPEN); closePrev = false;
+        } else if (t == OP_CLOSE) {
+          depth -= 1; a.push_back(OP_CLOSE); closePrev = true;
+        } else if (t == OP_UNION) {
+          a.push_back(OP_UNION); closePrev = false;
+        } else if (t == OP_COMPLEM) {
+          if (surfacePrev || closePrev) a.push_back(OP_INTERSECT);
+          a.push_back(OP_COMPLEM); closePrev = false;
+        } else { err = "unrecognised entry in surfaces"; return false; }
+        surfacePrev = false;
+      } else {
+        if (surfacePrev || closePrev) a.push_back(OP_INTERSECT);
+        a.push_back(t); surfacePrev = true; closePrev = false;
+      }
+    }
+    if (depth != 0) { err = "Inconsistent use of parentheses in cell definition"; return false; }
+    if (a.back() == OP_UNION) { err = "Cell definition ends with a union"; return false; }
+    if (a.back() == OP_COMPLEM) { err = "Cell definition ends with a complement"; return false; }
+    // deMorgan: 1-based i while i < sz
+    int sz = (int)a.size();
+    int i = 1;
+    while (i < sz) {
+      if (a[i - 1] == OP_COMPLEM) {
+        for (int k = i; k < sz; ++k) a[k - 1] = a[k];
+        sz -= 1;
+        int endPos = i;
+        if (a[i - 1] == OP_OPEN) {
+          int d = 1, j;
+          for (j = i + 1; j <= sz; ++j) {
+            if (a[j - 1] == OP_OPEN) d += 1;
+            else if (a[j - 1] == OP_CLOSE) d -= 1;
+            if (d == 0) break;
+          }
+          endPos = std::min(j, sz);
+        }
+        for (int j = i; j <= endPos; ++j) {
+          int e = a[j - 1];
+          if (!isOp(e)) a[j - 1] = -e;
+          else if (e == OP_UNION) a[j - 1] = OP_INTERSECT;
+          else if (e == OP_INTERSECT) a[j - 1] = OP_UNION;
+        }
+      }
+      i += 1;
+    }
+    a.resize(sz);
+    // checkPrecedence
+    i = 1;
+    while (i < sz) {
+      int e1 = a[i - 1];
+      bool cycled = false;
+      if (e1 == OP_UNION || e1 == OP_INTERSECT) {
+        for (int j = i + 1; j <= sz; ++j) {
+          int e2 = a[j - 1];
+          if (e2 == OP_INTERSECT || e2 == OP_UNION) {
+            if (e2 != e1) { err = "The order of operations in a cell is ambiguous"; return false; }
+            i = j; cycled = true; break;
+          } else if (e2 == OP_OPEN || e2 == OP_CLOSE) { i = j + 1; cycled = true; break; }
+        }
+      }
+      if (!cycled) i += 1;
+    }
+    for (int e : a) if (e == OP_UNION) cx = true;
+    if (!cx) {
+      std::vector<int> ids;
+      for (int e : a) if (!isOp(e)) ids.push_back(std::abs(e));
+      std::sort(ids.begin(), ids.end());
+      for (size_t k = 1; k < ids.size(); ++k)
+        if (ids[k] == ids[k - 1]) { err = "There are repeated surfaces in definition of cell"; return false; }
+    }
+    ev = a;
+    return true;
+  }
   std::vector<Universe> unis;
   std::vector<int> graphIdx, graphId;   // geomGraph array (1-based locations)
   std::vector<int> uniBase;             // uniRootID per universe (1-based), shrunk graph
@@ -481,8 +574,13 @@ struct Geometry {
     borderIdx = g->border_surf;
     for (int i = 0; i < 6; ++i) surfs[borderIdx].bc[i] = g->bc[i];
     cells.resize(g->n_cell);
-    for (int c = 0; c < g->n_cell; ++c)
-      for (int k = g->cell_ptr[c]; k < g->cell_ptr[c + 1]; ++k) cells[c].push_back(g->cell_surf[k]);
+    cellComplex.assign(g->n_cell, 0);
+    for (int c = 0; c < g->n_cell; ++c) {
+      std::vector<int> in(g->cell_surf + g->cell_ptr[c], g->cell_surf + g->cell_ptr[c + 1]);
+      bool cx = false;
+      if (!unionCellInit(in, cells[c], cx, err)) return SG_ERR_BAD_ARG;
+      cellComplex[c] = cx;
+    }
     unis.resize(g->n_uni);
     for (int u = 0; u < g->n_uni; ++u) {
       Universe& U = unis[u];
@@ -594,12 +692,41 @@ struct Geometry {
   }
 
   bool cellInside(int c, const double r[3], const double u[3]) {    // simpleCell_class.f90:90-111
+    if (cellComplex[c]) return insideComplex(c, r, u);
     bool isIt = false;
     for (int s : cells[c]) {
+      if (isOp(s)) continue;                                          // unionCell%inside, isSimple
       bool sense = s > 0;
       bool hs = surfs[std::abs(s) - 1].halfspace(r, u);
       isIt = (hs == sense);
       if (!isIt) return false;
+    }
+    return isIt;
+  }
+
+  bool insideComplex(int c, const double r[3], const double u[3]) {  // unionCell_class.f90:365-422
+    const std::vector<int>& a = cells[c];
+    bool isIt = true;
+    int depth = 0;
+    int n = (int)a.size();
+    for (int i = 1; i <= n; ++i) {
+      int el = a[i - 1];
+      if (!isOp(el)) {
+        bool sense = el > 0;
+        bool hs = surfs[std::abs(el) - 1].halfspace(r, u);
+        isIt = (hs == sense);
+      } else if ((el == OP_UNION && isIt) || (el == OP_INTERSECT && !isIt)) {
+        if (depth == 0) return isIt;
+        depth -= 1;
+        int d = 1;                                                    // shortCircuit
+        while (d > 0) {
+          i += 1;
+          int e2 = a[i - 1];
+          if (e2 == OP_OPEN) d += 1;
+          else if (e2 == OP_CLOSE) d -= 1;
+        }
+      } else if (el == OP_OPEN) depth += 1;
+      else if (el == OP_CLOSE) depth -= 1;
     }
     return isIt;
   }
@@ -625,6 +752,7 @@ struct Geometry {
         int cidx = U.ip[c.localID - 1];
         d = INF; surfIdx = 0;
         for (int s : cells[cidx]) {
+          if (isOp(s)) continue;
           double td = surfs[std::abs(s) - 1].distance(c.r, c.dir);
           if (td < d) { d = td; surfIdx = std::abs(s); }
         }

@@ -18,6 +18,8 @@ XSQCYL, YSQCYL, ZSQCYL = 10, 11, 12
 UNI_ROOT, UNI_CELL, UNI_PIN, UNI_LAT = 1, 2, 3, 4
 # boundary conditions
 BC_VACUUM, BC_REFLECTIVE, BC_PERIODIC = 0, 1, 2
+# unionCell operators in a cell's surface list: '<', '>', ':' (union), '#' (complement)
+CELL_OPEN, CELL_CLOSE, CELL_UNION, CELL_COMPLEMENT = -2147483647, -2147483646, -2147483645, -2147483644
 # precision forms
 PREC_FP64, PREC_MIXED = 0, 1
 # execution forms
@@ -137,6 +139,13 @@ class BatchTuning(C.Structure):
         ("item_histories", C.c_int32), ("blocks_per_sm", C.c_int32), ("block_threads", C.c_int32),
         ("order", C.c_int32),
     ]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class EventTuning(C.Structure):
+    _fields_ = [("rounds_per_check", C.c_int32), ("tail_min", C.c_int32), ("tail_divisor", C.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -23,12 +23,16 @@ namespace sg {
 
 static constexpr int BATCH_MAX_WARPS = 4;   // __launch_bounds__(128)
 
+// the record of a problem into the warp's shared slot; counters and errors go to this launch's
 template <class R>
-__device__ __forceinline__ void stage_problem_warp(BatchProblem<R>* dst, const BatchProblem<R>* src, int lane) {
+__device__ __forceinline__ void stage_problem_warp(BatchProblem<R>* dst, const BatchProblem<R>* src, int lane,
+                                                   DCounters* ctr) {
   static_assert(sizeof(BatchProblem<R>) % 16 == 0, "record size");
   const int4* s = reinterpret_cast<const int4*>(src);
   int4* d = reinterpret_cast<int4*>(dst);
   for (int i = lane; i < (int)(sizeof(BatchProblem<R>) / 16); i += 32) d[i] = __ldg(s + i);
+  __syncwarp();
+  if (lane == 0) dst->t.ctr = ctr;
   __syncwarp();
 }
 
@@ -119,7 +123,7 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
         const WorkItem wi = L.items[it];
         if (wi.slot != cur) {
           if (__any_sync(FULL, alive)) { pend = it; break; }
-          stage_problem_warp<R>(&P, probs + wi.slot, lane);
+          stage_problem_warp<R>(&P, probs + wi.slot, lane, L.ctr);
           cur = wi.slot;
         }
         pend = -1;

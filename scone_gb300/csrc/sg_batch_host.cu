@@ -113,10 +113,16 @@ struct sg_batch_t {
   void* dProbs = nullptr;          // BatchProblem<R>[max_problems]
   size_t recBytes = 0;
   BatchTally* dTallies = nullptr;
-  WorkItem* dItems = nullptr;
-  int* dInts = nullptr;            // [0] n_items, [1] head, [2] n_close
-  int* dClose = nullptr;           // [max_problems]
-  DCounters* dCtr = nullptr;
+  // device work list, counts, close list and counters of each mirror set (serving keeps two waves
+  // in flight, on two streams)
+  WorkItem* dItems[2] = {nullptr, nullptr};
+  int* dInts[2] = {nullptr, nullptr};      // [0] n_items, [1] head, [2] n_close
+  int* dClose[2] = {nullptr, nullptr};     // [max_problems]
+  DCounters* dCtr[2] = {nullptr, nullptr};
+  cudaStream_t ws[2] = {nullptr, nullptr}; // wave streams
+  cudaStream_t cstream = nullptr;          // cycle closes of the waves
+  cudaEvent_t kdone[2] = {nullptr, nullptr};
+  cudaEvent_t upl = nullptr;
   double* dOne = nullptr;
 
   cudaStream_t rstream = nullptr;  // read-back of completed score memory while waves run
@@ -144,6 +150,7 @@ struct sg_batch_t {
   sg_handle plainWork = nullptr;
   int plainForm = -1;
   int plainCap = 0;
+  sg_event_tuning plainTune{4, 4096, 64};
 
   // serving
   bool serving = false;
@@ -227,10 +234,10 @@ void drop_graph(sg_batch_t::Graph& G) {
   G = sg_batch_t::Graph();
 }
 
-// The run graph of mirror set m and nesting class x (0: maxl 2, 1: maxl 4): copies of the work
-// list, the count block and the close list from pinned memory, counter reset, the batched kernel,
-// the closes, the counters back to pinned memory.  The two list copies are resized to the current
-// counts before each launch; the kernels read the counts from device memory.
+// The transport graph of mirror set m and nesting class x (0: maxl 2, 1: maxl 4): copies of the
+// work list, the count block and the close list from pinned memory, counter reset and the batched
+// kernel.  The two list copies are resized to the current counts before each launch; the kernels
+// read the counts from device memory.  The cycle closes run after it (run_closes).
 int build_graph(sg_batch b, int m, int x) {
   sg_batch_t::Graph& G = b->graph[m][x];
   if (G.exec) {
@@ -242,24 +249,22 @@ int build_graph(sg_batch b, int m, int x) {
   const int dt = transport_op(b->cfg.transport);
   BatchLaunch L;
   L.problems = b->dProbs;
-  L.items = b->dItems;
-  L.n_items = b->dInts + 0;
-  L.head = b->dInts + 1;
-  L.ctr = b->dCtr;
+  L.items = b->dItems[m];
+  L.n_items = b->dInts[m] + 0;
+  L.head = b->dInts[m] + 1;
+  L.ctr = b->dCtr[m];
   L.k_one = b->dOne;
   L.maxl = maxl;
   const int grid = grid_for(b, maxl);
   BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   auto step = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
-  step(cudaMemcpyAsync(b->dItems, b->hItems[m], sizeof(WorkItem), cudaMemcpyHostToDevice, s));
-  step(cudaMemcpyAsync(b->dInts, b->hInts[m], 4 * sizeof(int), cudaMemcpyHostToDevice, s));
-  step(cudaMemcpyAsync(b->dClose, b->hClose[m], sizeof(int), cudaMemcpyHostToDevice, s));
-  step(cudaMemsetAsync(b->dCtr, 0, sizeof(DCounters), s));
+  step(cudaMemcpyAsync(b->dItems[m], b->hItems[m], sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+  step(cudaMemcpyAsync(b->dInts[m], b->hInts[m], 4 * sizeof(int), cudaMemcpyHostToDevice, s));
+  step(cudaMemcpyAsync(b->dClose[m], b->hClose[m], sizeof(int), cudaMemcpyHostToDevice, s));
+  step(cudaMemsetAsync(b->dCtr[m], 0, sizeof(DCounters), s));
   step(fp64(b) ? launch_batch<double>(L, dt, grid, b->tune.block_threads, s)
                : launch_batch<float>(L, dt, grid, b->tune.block_threads, s));
-  step(launch_batch_close(b->dTallies, b->dClose, b->dInts + 2, b->sms * 4, s));
-  step(cudaMemcpyAsync(b->hCtr[m], b->dCtr, sizeof(DCounters), cudaMemcpyDeviceToHost, s));
   cudaError_t ee = cudaStreamEndCapture(s, &G.g);
   if (e == cudaSuccess) e = ee;
   if (e == cudaSuccess) {
@@ -273,8 +278,8 @@ int build_graph(sg_batch b, int m, int x) {
       if (e != cudaSuccess || t != cudaGraphNodeTypeMemcpy) continue;
       cudaMemcpy3DParms pr{};
       e = cudaGraphMemcpyNodeGetParams(nodes[i], &pr);
-      if (pr.dstPtr.ptr == (void*)b->dItems) G.itemsCopy = nodes[i];
-      if (pr.dstPtr.ptr == (void*)b->dClose) G.closeCopy = nodes[i];
+      if (pr.dstPtr.ptr == (void*)b->dItems[m]) G.itemsCopy = nodes[i];
+      if (pr.dstPtr.ptr == (void*)b->dClose[m]) G.closeCopy = nodes[i];
     }
     if (e == cudaSuccess && (!G.itemsCopy || !G.closeCopy)) e = cudaErrorUnknown;
   }
@@ -320,7 +325,7 @@ int write_record(sg_batch b, int slot) {
     rec.t.acc = acc;
     rec.t.acc_n = (int)N;
     rec.t.use_smem = 0;
-    rec.t.ctr = b->dCtr;
+    rec.t.ctr = b->dCtr[0];           // replaced by the launch's counters when staged
     rec.t.use_cache = transport_cache(b->cfg.transport);
     rec.t.max_segments = 1000000;
     rec.t.ht_cutoff = (decltype(rec.t.ht_cutoff))(b->cfg.ht_cutoff > 0.0 ? b->cfg.ht_cutoff : 0.9);
@@ -351,18 +356,26 @@ int clear_tally(sg_batch b, int slot) {
   return SG_OK;
 }
 
-// launches the run graph of mirror set m for the items and closes already written to that set
-int launch_graph(sg_batch b, int m, int maxl) {
+// launches the transport graph of mirror set m, for the items and closes written to that set, on
+// stream `s`
+int launch_graph(sg_batch b, int m, int maxl, cudaStream_t s) {
   const int x = maxl > 2 ? 1 : 0;
   int rc = build_graph(b, m, x);
   if (rc) return rc;
   sg_batch_t::Graph& G = b->graph[m][x];
   const size_t ni = (size_t)std::max(1, b->hInts[m][0]), nc = (size_t)std::max(1, b->hInts[m][2]);
-  BCK(cudaGraphExecMemcpyNodeSetParams1D(G.exec, G.itemsCopy, b->dItems, b->hItems[m], sizeof(WorkItem) * ni,
+  BCK(cudaGraphExecMemcpyNodeSetParams1D(G.exec, G.itemsCopy, b->dItems[m], b->hItems[m], sizeof(WorkItem) * ni,
                                          cudaMemcpyHostToDevice));
-  BCK(cudaGraphExecMemcpyNodeSetParams1D(G.exec, G.closeCopy, b->dClose, b->hClose[m], sizeof(int) * nc,
+  BCK(cudaGraphExecMemcpyNodeSetParams1D(G.exec, G.closeCopy, b->dClose[m], b->hClose[m], sizeof(int) * nc,
                                          cudaMemcpyHostToDevice));
-  BCK(cudaGraphLaunch(G.exec, b->stream));
+  BCK(cudaGraphLaunch(G.exec, s));
+  return SG_OK;
+}
+
+// the cycle closes of the problems in mirror set m's close list, then its counters to the host
+int run_closes(sg_batch b, int m, cudaStream_t s) {
+  BCK(launch_batch_close(b->dTallies, b->dClose[m], b->dInts[m] + 2, b->sms * 4, s));
+  BCK(cudaMemcpyAsync(b->hCtr[m], b->dCtr[m], sizeof(DCounters), cudaMemcpyDeviceToHost, s));
   return SG_OK;
 }
 
@@ -408,10 +421,21 @@ int32_t sg_batch_create(const sg_batch_config* cfg, sg_batch* out) {
   if (cudaMalloc((void**)&b->arena, (size_t)cfg->arena_bytes) != cudaSuccess) return bad(SG_ERR_OOM);
   b->alloc.init((size_t)cfg->arena_bytes);
   if (cudaMalloc(&b->dProbs, b->recBytes * P) != cudaSuccess || cudaMalloc((void**)&b->dTallies, sizeof(BatchTally) * P) != cudaSuccess ||
-      cudaMalloc((void**)&b->dItems, sizeof(WorkItem) * W) != cudaSuccess || cudaMalloc((void**)&b->dInts, 4 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc((void**)&b->dClose, sizeof(int) * P) != cudaSuccess || cudaMalloc((void**)&b->dCtr, sizeof(DCounters)) != cudaSuccess ||
       cudaMalloc((void**)&b->dOne, sizeof(double)) != cudaSuccess)
     return bad(SG_ERR_OOM);
+  for (int m = 0; m < 2; ++m) {
+    if (cudaMalloc((void**)&b->dItems[m], sizeof(WorkItem) * W) != cudaSuccess ||
+        cudaMalloc((void**)&b->dInts[m], 4 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->dClose[m], sizeof(int) * P) != cudaSuccess ||
+        cudaMalloc((void**)&b->dCtr[m], sizeof(DCounters)) != cudaSuccess)
+      return bad(SG_ERR_OOM);
+    if (cudaStreamCreateWithFlags(&b->ws[m], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->kdone[m], cudaEventDisableTiming) != cudaSuccess)
+      return bad(SG_ERR_CUDA);
+  }
+  if (cudaStreamCreateWithFlags(&b->cstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->upl, cudaEventDisableTiming) != cudaSuccess)
+    return bad(SG_ERR_CUDA);
   if (cudaMallocHost((void**)&b->hRec, b->recBytes * P) != cudaSuccess ||
       cudaMallocHost((void**)&b->hTl, sizeof(BatchTally) * P) != cudaSuccess)
     return bad(SG_ERR_OOM);
@@ -441,10 +465,17 @@ int32_t sg_batch_destroy(sg_batch b) {
   cudaFree(b->arena);
   cudaFree(b->dProbs);
   cudaFree(b->dTallies);
-  cudaFree(b->dItems);
-  cudaFree(b->dInts);
-  cudaFree(b->dClose);
-  cudaFree(b->dCtr);
+  for (int m = 0; m < 2; ++m) {
+    if (b->ws[m]) cudaStreamSynchronize(b->ws[m]);
+    cudaFree(b->dItems[m]);
+    cudaFree(b->dInts[m]);
+    cudaFree(b->dClose[m]);
+    cudaFree(b->dCtr[m]);
+    if (b->kdone[m]) cudaEventDestroy(b->kdone[m]);
+    if (b->ws[m]) cudaStreamDestroy(b->ws[m]);
+  }
+  if (b->cstream) { cudaStreamSynchronize(b->cstream); cudaStreamDestroy(b->cstream); }
+  if (b->upl) cudaEventDestroy(b->upl);
   cudaFree(b->dOne);
   for (int m = 0; m < 2; ++m) {
     cudaFreeHost(b->hItems[m]);
@@ -615,7 +646,9 @@ int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats
   b->hInts[m][3] = 0;
   for (int i = 0; i < n; ++i) b->hClose[m][i] = order[i];
   BCK(cudaEventRecord(b->ev[2], b->stream));
-  int rc = launch_graph(b, m, maxl);
+  int rc = launch_graph(b, m, maxl, b->stream);
+  if (rc) return rc;
+  rc = run_closes(b, m, b->stream);
   if (rc) return rc;
   BCK(cudaEventRecord(b->ev[3], b->stream));
   BCK(cudaStreamSynchronize(b->stream));
@@ -665,6 +698,7 @@ int32_t sg_batch_run_plain(sg_batch b, const int32_t* slots, int32_t n, int32_t 
     b->plainForm = form;
     b->plainCap = c.max_bank;
   }
+  if (sg_set_event_tuning(b->plainWork, &b->plainTune) != SG_OK) return b->fail(SG_ERR_BAD_ARG, "batch: bad event tuning");
   BCK(cudaStreamSynchronize(b->stream));
   sg_batch_stats tot{};
   const double t0 = host_now();
@@ -736,6 +770,52 @@ int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_
     }
   }
   b->tune = cur;
+  for (int i = 0; i < n; ++i) {
+    rc = clear_tally(b, slots[i]);
+    if (rc) return rc;
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  if (best) *best = cur;
+  return SG_OK;
+}
+
+int32_t sg_batch_autotune_plain(sg_batch b, const int32_t* slots, int32_t n, sg_event_tuning* best) {
+  if (!b || !slots || n <= 0) return SG_ERR_BAD_ARG;
+  // coordinate search over the queue-check interval and the tail threshold; wall time of the
+  // plain event form on the listed problems, best of 2
+  sg_event_tuning cur = b->plainTune;
+  auto time_it = [&](const sg_event_tuning& t, double* ms) -> int {
+    b->plainTune = t;
+    double bestMs = 1e300;
+    for (int r = 0; r < 2; ++r) {
+      sg_batch_stats st{};
+      int rc = sg_batch_run_plain(b, slots, n, SG_FORM_EVENT, &st);
+      if (rc) return rc;
+      bestMs = std::min(bestMs, st.run_ms);
+    }
+    *ms = bestMs;
+    return SG_OK;
+  };
+  double curMs = 0.0;
+  int rc = time_it(cur, &curMs);
+  if (rc) return rc;
+  const int rounds[] = {1, 2, 4, 8, 16};
+  const int tmin[] = {0, 1024, 4096, 16384, 65536};
+  const int tdiv[] = {8, 16, 64, 256};
+  for (int pass = 0; pass < 3; ++pass) {
+    std::vector<sg_event_tuning> cands;
+    if (pass == 0) for (int v : rounds) { sg_event_tuning t = cur; t.rounds_per_check = v; cands.push_back(t); }
+    if (pass == 1) for (int v : tmin) { sg_event_tuning t = cur; t.tail_min = v; cands.push_back(t); }
+    if (pass == 2) for (int v : tdiv) { sg_event_tuning t = cur; t.tail_divisor = v; cands.push_back(t); }
+    for (const auto& t : cands) {
+      if (std::memcmp(&t, &cur, sizeof(t)) == 0) continue;
+      double ms = 0.0;
+      rc = time_it(t, &ms);
+      if (rc) return rc;
+      if (ms < curMs) { cur = t; curMs = ms; }
+    }
+  }
+  b->plainTune = cur;
   for (int i = 0; i < n; ++i) {
     rc = clear_tally(b, slots[i]);
     if (rc) return rc;
@@ -906,10 +986,22 @@ int launch_wave(sg_batch b) {
   b->hInts[m][2] = (int)w.closing.size();
   b->hInts[m][3] = 0;
   for (size_t i = 0; i < w.closing.size(); ++i) b->hClose[m][i] = w.closing[i].slot;
-  int rc = launch_graph(b, m, maxl);
+  // wave k runs on stream m = k mod 2, after everything the batch stream has queued (instances,
+  // tally clears); its closes run on the close stream once its own kernel and the previous wave's
+  // have ended (a request's earlier histories may be in the previous wave)
+  BCK(cudaEventRecord(b->upl, b->stream));
+  BCK(cudaStreamWaitEvent(b->ws[m], b->upl, 0));
+  int rc = launch_graph(b, m, maxl, b->ws[m]);
+  if (rc) return rc;
+  BCK(cudaEventRecord(b->kdone[m], b->ws[m]));
+  BCK(cudaStreamWaitEvent(b->cstream, b->kdone[m], 0));
+  if (b->wavesLaunched > 0) BCK(cudaStreamWaitEvent(b->cstream, b->kdone[1 - m], 0));
+  rc = run_closes(b, m, b->cstream);
   if (rc) return rc;
   BCK(cudaEventCreate(&w.done));
-  BCK(cudaEventRecord(w.done, b->stream));
+  BCK(cudaEventRecord(w.done, b->cstream));
+  // the next wave on stream m rewrites this set's lists and counters: after these closes read them
+  BCK(cudaStreamWaitEvent(b->ws[m], w.done, 0));
   b->waves.push_back(std::move(w));
   b->wavesLaunched += 1;
   return SG_OK;

@@ -420,6 +420,33 @@ struct Geom {
   const DGeom& g;
   __device__ __forceinline__ explicit Geom(const DGeom& gg) : g(gg) {}
 
+  // unionCell%insideComplex (unionCell_class.f90:365-401): left to right over the evaluation array;
+  // a union that is already true or an intersection that is already false ends the current bracket
+  // (shortCircuit, :406-422) or, at depth 0, the whole cell
+  template <class T>
+  __device__ __forceinline__ bool inside_complex(int cell, const T r[3], const R dir[3]) const {
+    bool isIt = true;
+    int depth = 0;
+    const int end = g.cell_ptr[cell + 1];
+    for (int i = g.cell_ptr[cell]; i < end; ++i) {
+      const int el = g.cell_surf[i];
+      if (!cell_is_op(el)) {
+        const bool hs = surf_halfspace<R, T>(g.surfs[abs(el) - 1], r, dir);
+        isIt = (hs == (el > 0));
+      } else if ((el == CELL_UNION && isIt) || (el == CELL_INTERSECT && !isIt)) {
+        if (depth == 0) return isIt;
+        depth -= 1;
+        for (int d = 1; d > 0 && i + 1 < end;) {
+          const int e2 = g.cell_surf[++i];
+          if (e2 == CELL_OPEN) d += 1;
+          else if (e2 == CELL_CLOSE) d -= 1;
+        }
+      } else if (el == CELL_OPEN) depth += 1;
+      else if (el == CELL_CLOSE) depth -= 1;
+    }
+    return isIt;
+  }
+
   // universe%findCell for the universe `u` at local position r
   template <class T>
   __device__ __forceinline__ int find_cell(int u, const T r[3], const R dir[3]) const {
@@ -432,12 +459,15 @@ struct Geom {
         for (int c = 0; c < nc; ++c) {
           int cell = g.uni_cells[U.i[0] + c];
           bool isIt = false;
-          for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
-            int ss = g.cell_surf[k];
-            bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir);
-            isIt = (hs == (ss > 0));
-            if (!isIt) break;
-          }
+          if (g.cell_complex && g.cell_complex[cell]) isIt = inside_complex<T>(cell, r, dir);
+          else
+            for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
+              int ss = g.cell_surf[k];
+              if (cell_is_op(ss)) continue;                    // brackets of an all-intersection cell
+              bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir);
+              isIt = (hs == (ss > 0));
+              if (!isIt) break;
+            }
           if (isIt) return c + 1;
         }
         return nc + 1;
@@ -507,8 +537,9 @@ struct Geom {
       case SG_UNI_CELL: {                                        // simpleCell_class.f90:120-141
         int cell = g.uni_cells[U.i[0] + localID - 1];
         d = INF_R; surfIdx = 0;
-        for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {
+        for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // unionCell :426-443 alike
           int ss = g.cell_surf[k];
+          if (cell_is_op(ss)) continue;
           R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir);
           if (td < d) { d = td; surfIdx = abs(ss); }
         }
@@ -595,8 +626,9 @@ struct Geom {
     }
   }
 
-  // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow
-  __device__ __forceinline__ bool dive(Coords<R, MAXL>& c, int start) const {
+  // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow.
+  // rf: float(r0) when the caller has it (mixed form), so an origin-free level 2 reuses it
+  __device__ __forceinline__ bool dive(Coords<R, MAXL>& c, int start, const float* rf = nullptr) const {
 #pragma unroll
     for (int i = 0; i < MAXL; ++i) {
       if (i < start) continue;
@@ -608,8 +640,13 @@ struct Geom {
       const DUni& N = g.unis[nu];
       if (i == 0) {
         if (sizeof(R) == 4 && N.i[6]) {
+          if (rf) {
 #pragma unroll
-          for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
+            for (int k = 0; k < 3; ++k) c.rl[0][k] = R(rf[k]);
+          } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
+          }
         } else {
           double off[3];
           cell_offset<double>(c.uni[0], c.local[0], off);
@@ -641,13 +678,16 @@ struct Geom {
     c.base[0] = 0;
     int loc = 0;
     if constexpr (sizeof(R) == 4) {
+      const float rf[3] = {(float)c.r0[0], (float)c.r0[1], (float)c.r0[2]};
       const DSurf& S = g.surfs[g.border];
       if (S.filt > 0.0f) {
-        const float rf[3] = {(float)c.r0[0], (float)c.r0[1], (float)c.r0[2]};
         const float v = surf_evaluate<float>(S, rf);
         if (v > S.filt) loc = 2;
         else if (v < -S.filt) loc = 1;
       }
+      if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u);
+      c.local[0] = loc;
+      return dive(c, 0, rf);
     }
     if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u);
     c.local[0] = loc;

@@ -131,7 +131,7 @@ struct sg_handle_t {
   double bounds[6];
   DArr<DSurf> surfs64, surfsMx;
   DArr<DUni> unis64, unisMx;
-  DArr<int> uniCells, cellPtr, cellSurf;
+  DArr<int> uniCells, cellPtr, cellSurf, cellComplex;
   DArr<double> pinRsq, pinTol64, pinTolMx;
   DArr<float> pinRsqF, pinTolF;
   DArr<int2> graph;
@@ -185,6 +185,7 @@ struct sg_handle_t {
   DArr<double> pE;
   DArr<unsigned long long> pRng;
   int evIterations = 0;
+  sg_event_tuning evTune{4, 4096, 64};   // rounds per queue check, tail threshold (min, divisor)
   int lastN = 0;
   long long launches = 0;      // kernels launched since the last reset (cycle stats)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -212,6 +213,105 @@ namespace {
 int check_handle(sg_handle h) { return h ? SG_OK : SG_ERR_BAD_ARG; }
 
 unsigned long long rng_stride(unsigned long long s, long long n) { return lcg_skip(s, 152917LL * n); }
+
+// ------------------------------------------------------------------ unionCell
+// unionCell%init (Geometry/Cells/unionCell_class.f90:80-199): the token list of a cell becomes its
+// evaluation array.  Implicit intersections are inserted (after a surface or a closing bracket,
+// before a surface, an opening bracket or a complement); complements are removed by De Morgan's law
+// (deMorgan, :202-262: the complemented surface or bracket flips every surface's sense and swaps
+// unions and intersections); mixed unions and intersections without brackets are rejected
+// (checkPrecedence, :267-305).  A list without operators is a simpleCell and is kept as it is.
+bool cell_eval_array(const std::vector<int>& in, int ns, std::vector<int>& a, bool& complex_, std::string& why) {
+  const int COMPLEM = SG_CELL_COMPLEMENT;
+  bool hasOp = false;
+  for (int t : in) {
+    if (t == SG_CELL_OPEN || t == SG_CELL_CLOSE || t == SG_CELL_UNION || t == SG_CELL_COMPLEMENT) hasOp = true;
+    else if (t == 0 || std::abs(t) > ns) { why = "bad surface index"; return false; }
+  }
+  complex_ = false;
+  if (!hasOp) { a = in; return true; }
+  a.clear();
+  bool surfPrev = false, closePrev = false;
+  int depth = 0;
+  for (int t : in) {
+    if (t == SG_CELL_OPEN) {
+      depth += 1;
+      if (surfPrev || closePrev) a.push_back(CELL_INTERSECT);
+      a.push_back(CELL_OPEN);
+      closePrev = false;
+      surfPrev = false;
+    } else if (t == SG_CELL_CLOSE) {
+      depth -= 1;
+      a.push_back(CELL_CLOSE);
+      closePrev = true;
+      surfPrev = false;
+    } else if (t == SG_CELL_UNION) {
+      a.push_back(CELL_UNION);
+      closePrev = false;
+      surfPrev = false;
+    } else if (t == SG_CELL_COMPLEMENT) {
+      if (surfPrev || closePrev) a.push_back(CELL_INTERSECT);
+      a.push_back(COMPLEM);
+      closePrev = false;
+      surfPrev = false;
+    } else {
+      if (surfPrev || closePrev) a.push_back(CELL_INTERSECT);
+      a.push_back(t);
+      surfPrev = true;
+      closePrev = false;
+    }
+  }
+  if (depth != 0) { why = "inconsistent use of parentheses"; return false; }
+  if (a.empty() || a.back() == CELL_UNION) { why = "definition ends with a union"; return false; }
+  if (a.back() == COMPLEM) { why = "definition ends with a complement"; return false; }
+  for (size_t i = 0; i + 1 < a.size(); ++i) {            // De Morgan
+    if (a[i] != COMPLEM) continue;
+    a.erase(a.begin() + i);
+    size_t endPos = i;
+    if (a[i] == CELL_OPEN) {
+      int d = 1;
+      size_t j = i + 1;
+      for (; j < a.size(); ++j) {
+        if (a[j] == CELL_OPEN) d += 1;
+        else if (a[j] == CELL_CLOSE) d -= 1;
+        if (d == 0) break;
+      }
+      endPos = std::min(j, a.size() - 1);
+    }
+    for (size_t j = i; j <= endPos; ++j) {
+      if (!cell_is_op(a[j]) && a[j] != COMPLEM) a[j] = -a[j];
+      else if (a[j] == CELL_UNION) a[j] = CELL_INTERSECT;
+      else if (a[j] == CELL_INTERSECT) a[j] = CELL_UNION;
+    }
+  }
+  for (size_t i = 0; i + 1 < a.size();) {                // precedence
+    const int e1 = a[i];
+    if (e1 == CELL_UNION || e1 == CELL_INTERSECT) {
+      size_t j = i + 1, next = i + 1;
+      for (; j < a.size(); ++j) {
+        const int e2 = a[j];
+        if (e2 == CELL_UNION || e2 == CELL_INTERSECT) {
+          if (e2 != e1) { why = "the order of operations is ambiguous"; return false; }
+          next = j;
+          break;
+        }
+        if (e2 == CELL_OPEN || e2 == CELL_CLOSE) { next = j + 1; break; }
+      }
+      if (j == a.size()) next = i + 1;
+      i = next;
+      continue;
+    }
+    i += 1;
+  }
+  for (int t : a) if (t == CELL_UNION) complex_ = true;
+  if (!complex_) {                                      // repeated surfaces of an intersection-only cell
+    std::vector<int> ids;
+    for (int t : a) if (!cell_is_op(t)) ids.push_back(std::abs(t));
+    std::sort(ids.begin(), ids.end());
+    if (std::adjacent_find(ids.begin(), ids.end()) != ids.end()) { why = "repeated surfaces in a cell"; return false; }
+  }
+  return true;
+}
 
 // ------------------------------------------------------------------ geometry build
 int build_geometry(sg_handle h, const sg_geometry_desc* g) {
@@ -268,11 +368,20 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
     s64[g->border_surf].bc[i] = g->bc[i];
     sMx[g->border_surf].bc[i] = g->bc[i];
   }
-  // cells
-  std::vector<int> cptr(g->cell_ptr, g->cell_ptr + g->n_cell + 1);
-  std::vector<int> csurf(g->cell_surf, g->cell_surf + (g->n_cell ? g->cell_ptr[g->n_cell] : 0));
-  for (int v : csurf)
-    if (v == 0 || std::abs(v) > ns) return h->fail(SG_ERR_BAD_ARG, "geometry: bad cell surface index");
+  // cells: simpleCell surface lists, or unionCell token lists turned into their evaluation arrays
+  std::vector<int> cptr(1, 0), csurf, ccomplex(g->n_cell, 0);
+  bool anyComplex = false;
+  for (int c = 0; c < g->n_cell; ++c) {
+    std::vector<int> in(g->cell_surf + g->cell_ptr[c], g->cell_surf + g->cell_ptr[c + 1]), ev;
+    bool cx = false;
+    std::string why;
+    if (!cell_eval_array(in, ns, ev, cx, why))
+      return h->fail(SG_ERR_BAD_ARG, "geometry: cell " + std::to_string(c) + ": " + why);
+    csurf.insert(csurf.end(), ev.begin(), ev.end());
+    cptr.push_back((int)csurf.size());
+    ccomplex[c] = cx ? 1 : 0;
+    anyComplex |= cx;
+  }
   // universes
   std::vector<DUni> u64(nu), uMx(nu);
   std::vector<std::vector<int>> fills(nu);
@@ -421,6 +530,8 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   CK(h->uniCells.upload(uniCells, st));
   CK(h->cellPtr.upload(cptr, st));
   CK(h->cellSurf.upload(csurf, st));
+  if (anyComplex) CK(h->cellComplex.upload(ccomplex, st));
+  else h->cellComplex.free();
   CK(h->pinRsq.upload(rsq, st));
   CK(h->pinTol64.upload(tol64, st));
   CK(h->pinTolMx.upload(tolMx, st));
@@ -437,10 +548,11 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   double scale = 1.0;
   for (int i = 0; i < 6; ++i) scale = std::max(scale, std::fabs(h->bounds[i]));
   const double tie_abs = 16.0 * scale * 0x1p-23;
+  const int* cx = anyComplex ? h->cellComplex.p : nullptr;
   h->g64 = DGeom{h->surfs64.p, h->unis64.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0};
+                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0, cx};
   h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs};
+                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs, cx};
   h->hasGeom = true;
   // active materials for the majorant
   return SG_OK;
@@ -869,8 +981,8 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
     t.q = DQueues{nullptr, nullptr, qT[0], qc + 0, qc + 3};
     CK(launch_kind(K_EV_START, t, h->maxl, dt, 0, s, nullptr));
     int cur = 0, it = 0;
-    const int tail = std::max(4096, n / 64);
-    const int CHUNK = 4;
+    const int tail = std::max(h->evTune.tail_min, n / h->evTune.tail_divisor);
+    const int CHUNK = h->evTune.rounds_per_check;
     h->launches += 1;
     while (true) {
       for (int k = 0; k < CHUNK; ++k, ++it) {
@@ -1292,7 +1404,7 @@ int32_t sg_destroy(sg_handle h) {
   cudaStreamSynchronize(h->stream);
   for (auto& b : h->bank) b.free();
   h->surfs64.free(); h->surfsMx.free(); h->unis64.free(); h->unisMx.free(); h->uniCells.free();
-  h->cellPtr.free(); h->cellSurf.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
+  h->cellPtr.free(); h->cellSurf.free(); h->cellComplex.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
   h->pinRsqF.free(); h->pinTolF.free();
   for (auto& a : h->mgD) a.free();
   for (auto& a : h->mgF) a.free();
@@ -1612,6 +1724,20 @@ int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t n, int32
     stats->cycle_ms = cyc;
     stats->n_kernels = h->launches;
   }
+  return SG_OK;
+}
+
+int32_t sg_set_event_tuning(sg_handle h, const sg_event_tuning* t) {
+  if (!h || !t) return SG_ERR_BAD_ARG;
+  if (t->rounds_per_check < 1 || t->rounds_per_check > 64 || t->tail_min < 0 || t->tail_divisor < 1)
+    return h->fail(SG_ERR_BAD_ARG, "event tuning: rounds 1-64, tail_min >= 0, tail_divisor >= 1");
+  h->evTune = *t;
+  return SG_OK;
+}
+
+int32_t sg_get_event_tuning(sg_handle h, sg_event_tuning* t) {
+  if (!h || !t) return SG_ERR_BAD_ARG;
+  *t = h->evTune;
   return SG_OK;
 }
 

@@ -54,7 +54,14 @@ struct DGeom {
   int border;           // border surface (0-based)
   double nudge;         // cellUniverse crossing nudge of the precision form
   double tie_abs;       // absolute part of the tie rule between nesting levels (0 in the FP64 form)
+  const int* cell_complex;  // [n_cell] 1: unionCell with unions (cell_surf holds its evaluation array)
 };
+
+// unionCell evaluation tokens in cell_surf (surfaces are signed 1-based indices); OPEN, CLOSE and
+// UNION are the input codes, INTERSECT is inserted where SCONE's input leaves it implicit
+static constexpr int CELL_OPEN = SG_CELL_OPEN, CELL_CLOSE = SG_CELL_CLOSE, CELL_UNION = SG_CELL_UNION;
+static constexpr int CELL_INTERSECT = -2147483643;
+__host__ __device__ inline bool cell_is_op(int t) { return t <= CELL_INTERSECT && t >= CELL_OPEN; }
 
 // MG macroscopic data in the working precision R ([mat][G], P0/prod [mat][Gin][Gout])
 template <class R>

@@ -62,6 +62,8 @@ def load(build=True):
         "sg_batch_run": (i32, [vp, P(i32), i32, P(abi.BatchStats)]),
         "sg_batch_run_plain": (i32, [vp, P(i32), i32, i32, P(abi.BatchStats)]),
         "sg_batch_autotune": (i32, [vp, P(i32), i32, P(abi.BatchTuning)]),
+        "sg_batch_autotune_plain": (i32, [vp, P(i32), i32, P(abi.EventTuning)]),
+        "sg_set_event_tuning": (i32, [vp, P(abi.EventTuning)]), "sg_get_event_tuning": (i32, [vp, P(abi.EventTuning)]),
         "sg_batch_tally_size": (i32, [vp, i32, P(i64)]), "sg_batch_get_bins": (i32, [vp, i32, P(f64), i64]),
         "sg_batch_clear_tally": (i32, [vp, i32]),
         "sg_serve_start": (i32, [vp, i64, i32]), "sg_serve_submit": (i32, [vp, i32]),
@@ -334,6 +336,13 @@ class BatchGPU:
         a, p = self._slots(slots)
         t = abi.BatchTuning()
         self._check(self.L.sg_batch_autotune(self.b, p, len(a), C.byref(t)))
+        return t.as_dict()
+
+    def autotune_plain(self, slots):
+        """Queue thresholds of the plain event form, picked by timing on the listed problems."""
+        a, p = self._slots(slots)
+        t = abi.EventTuning()
+        self._check(self.L.sg_batch_autotune_plain(self.b, p, len(a), C.byref(t)))
         return t.as_dict()
 
     def bins(self, slot):

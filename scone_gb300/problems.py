@@ -42,7 +42,8 @@ class GeometryBuilder:
         return len(self.surf_type) - 1
 
     def cell(self, signed_surfs):
-        """signed 1-based surface indices: -(s+1) for the -ve halfspace of surface s (0-based)."""
+        """signed 1-based surface indices: -(s+1) for the -ve halfspace of surface s (0-based); a list
+        with abi.CELL_* operator tokens ('<', '>', ':', '#') is a unionCell."""
         self.cells.append(list(signed_surfs))
         return len(self.cells) - 1
 
@@ -446,3 +447,27 @@ def batched_uneven(n_problems=4096, seed=31, hist_min=1.0e3, hist_max=1.0e6, cyc
         p.meta["index"] = i
         out.append((p, pop, cycles, master))
     return out
+
+
+def union_cell_slab(seed=41):
+    """Two overlapping spheres (r 2 cm at x = 0 and x = 3) inside a reflective box (half-width 6 cm)
+    as unionCells: material 1 fills the union `< -1 : -2 >`, material 2 its complement
+    `# < -1 : -2 >`; an isotropic point source at the origin, 2 groups (synthetic XS as in the
+    infinite-medium workload) and a collision flux per material and group."""
+    rng = np.random.default_rng(seed)
+    gb = GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 6.0, 6.0, 6.0)
+    s1 = gb.surface(abi.SPHERE, 0.0, 0.0, 0.0, 2.0)
+    s2 = gb.surface(abi.SPHERE, 3.0, 0.0, 0.0, 2.0)
+    O, C, U, N = abi.CELL_OPEN, abi.CELL_CLOSE, abi.CELL_UNION, abi.CELL_COMPLEMENT
+    inside = gb.cell([O, -(s1 + 1), U, -(s2 + 1), C])
+    outside = gb.cell([N, O, -(s1 + 1), U, -(s2 + 1), C])
+    uni = gb.cell_universe([inside, outside], [1, 2])
+    gb.root_universe(box, uni_fill(uni), bc=[abi.BC_REFLECTIVE] * 6)
+    mats = [_fixed_source_xs(rng, 2), _fixed_source_xs(rng, 2)]
+    mg = mg_data(2, np.array([m[0] for m in mats]), np.array([m[1] for m in mats]),
+                 capture=np.array([m[2] for m in mats]))
+    tallies = dict(flux=[abi.clerk(abi.CLERK_COLLISION, axes=[(abi.AXIS_MATERIAL, 2, 0.0, 0.0),
+                                                              (abi.AXIS_GROUP, 2, 0.0, 0.0)])])
+    return Problem(gb.arrays(), mg, name="union_cell_spheres", source=dict(r=(0.0, 0.0, 0.0), G=1),
+                   tallies=tallies)

@@ -172,6 +172,20 @@ def test_autotune_keeps_results(gpu_mod):
         np.testing.assert_allclose(B.bins(s), x, rtol=1e-9, atol=0)
 
 
+def test_autotune_plain_keeps_results(gpu_mod):
+    """Queue thresholds of the event form change scheduling only: FP64 results stay the same."""
+    batch = small_batch(seed=23, n=6)
+    B, slots = load_batch(gpu_mod, batch, abi.PREC_FP64, abi.TRANSPORT_ST)
+    B.run_plain(slots, form=abi.FORM_EVENT)
+    ref = [B.bins(s) for s in slots]
+    best = B.autotune_plain(slots)
+    assert best["rounds_per_check"] >= 1 and best["tail_divisor"] >= 1 and best["tail_min"] >= 0
+    assert all(np.all(B.bins(s) == 0.0) for s in slots)
+    B.run_plain(slots, form=abi.FORM_EVENT)
+    for s, r in zip(slots, ref):
+        np.testing.assert_allclose(B.bins(s), r, rtol=RTOL, atol=0)
+
+
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
 def test_served_result_alone_equals_result_in_mix(gpu_mod, precision):
     """Continuous batching: a request served alone and the same request admitted while others are

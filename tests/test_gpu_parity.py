@@ -218,3 +218,40 @@ def test_fixed_source_shards_sum_to_single_process(gpu_mod, oracle_mod, world):
     for _ in range(cycles):
         m, _ = o.fixed_source_cycle(ao, n, m)
     np.testing.assert_allclose(total, o.bins(ao)[:, 1], rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_HT])
+def test_union_cell_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
+    """unionCell geometry (a union of two spheres and its complement): per-history bit-level
+    agreement with the oracle and equal tallies."""
+    p = problems.union_cell_slab()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
+    n = 20000
+    bank = o.generate_source(SEED, n)
+    ag, ao = g.upload_tally(p.tallies["flux"]), o.upload_tally(p.tallies["flux"])
+    g.transport_bank(ag, bank, 13579)
+    o.transport_bank(ao, bank, 13579)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co) and np.array_equal(rg, ro)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    bg, bo = g.bins(ag), o.bins(ao)
+    assert bg[:, 1].reshape(2, 2).sum(axis=1).min() > 0          # both cells are visited
+    np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=0)
+
+
+def test_union_cell_bad_definition_is_rejected(gpu_mod):
+    O, C, U = abi.CELL_OPEN, abi.CELL_CLOSE, abi.CELL_UNION
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 6.0, 6.0, 6.0)
+    s1 = gb.surface(abi.SPHERE, 0.0, 0.0, 0.0, 2.0)
+    s2 = gb.surface(abi.SPHERE, 3.0, 0.0, 0.0, 2.0)
+    a = gb.cell([-(s1 + 1), U, -(s2 + 1), s1 + 1])             # mixes union and intersection
+    b = gb.cell([O, s1 + 1, C])
+    uni = gb.cell_universe([a, b], [1, 2])
+    gb.root_universe(box, problems.uni_fill(uni), bc=[abi.BC_REFLECTIVE] * 6)
+    t = gpu_mod.TransportOperatorGPU(max_bank=16)
+    with pytest.raises(gpu_mod.SconeGpuError, match="ambiguous"):
+        t.upload_geometry(gb.arrays())

@@ -448,3 +448,55 @@ def test_p1_scattering_changes_leakage(oracle_mod):
         m, st = o.fixed_source_cycle(a, 20000, 99)
         leak[ratio] = st.n_collisions / 20000.0      # fewer collisions per history = more leakage
     assert leak[0.6] < 0.95 * leak[None], leak
+
+
+def _union_geometry(tokens_a, tokens_b):
+    """Root box (half-width 6) -> cellUniverse of two cells given as token lists over surfaces
+    1: sphere r 2 at the origin, 2: sphere r 2 at x = 3, 3: plane x = 1."""
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 6.0, 6.0, 6.0)
+    gb.surface(abi.SPHERE, 0.0, 0.0, 0.0, 2.0)
+    gb.surface(abi.SPHERE, 3.0, 0.0, 0.0, 2.0)
+    gb.surface(abi.XPLANE, 1.0)
+    a = gb.cell(tokens_a)
+    b = gb.cell(tokens_b)
+    uni = gb.cell_universe([a, b], [1, 2])
+    gb.root_universe(box, problems.uni_fill(uni), bc=[abi.BC_REFLECTIVE] * 6)
+    return gb.arrays()
+
+
+def test_union_cell_point_containment(oracle_mod):
+    """unionCell (Geometry/Cells/unionCell_class.f90): unions, complements (De Morgan) and brackets
+    decide containment as the boolean expression does, at random points.  Surface indices are
+    1-based (the box is surface 1, the spheres 2 and 3, the plane 4)."""
+    O, C, U, N = abi.CELL_OPEN, abi.CELL_CLOSE, abi.CELL_UNION, abi.CELL_COMPLEMENT
+    in1 = lambda p: p[0] ** 2 + p[1] ** 2 + p[2] ** 2 < 4.0
+    in2 = lambda p: (p[0] - 3.0) ** 2 + p[1] ** 2 + p[2] ** 2 < 4.0
+    left = lambda p: p[0] < 1.0
+    cases = [
+        ([O, -2, U, -3, C], [N, O, -2, U, -3, C], lambda p: in1(p) or in2(p)),
+        ([-2, U, -3], [2, 3], lambda p: in1(p) or in2(p)),                     # union at depth 0
+        ([O, -2, U, -3, C, -4], [N, O, O, -2, U, -3, C, -4, C], lambda p: (in1(p) or in2(p)) and left(p)),
+        ([N, O, 2, 3, C], [2, 3], lambda p: in1(p) or in2(p)),                 # # < 2 3 > = -2 : -3
+        ([-2, N, -4], [N, O, -2, N, -4, C], lambda p: in1(p) and not left(p)),
+    ]
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(-5.5, 5.5, size=(400, 3))
+    for ta, tb, truth in cases:
+        g = _union_geometry(ta, tb)
+        o = oracle_mod.Oracle()
+        o.upload_geometry(g)
+        for p in pts:
+            m, _ = o.what_is_at(p)
+            assert m == (1 if truth(p) else 2), (ta, p, m)
+
+
+def test_union_cell_rejects_bad_definitions(oracle_mod):
+    """Ambiguous precedence, unbalanced brackets and trailing operators are errors
+    (unionCell%init, checkPrecedence)."""
+    O, C, U, N = abi.CELL_OPEN, abi.CELL_CLOSE, abi.CELL_UNION, abi.CELL_COMPLEMENT
+    for bad in ([-2, U, -3, -4], [O, -2, U, -3], [-2, U], [-2, N], [-2, -2, O, -3, C]):
+        g = _union_geometry(bad, [2])
+        o = oracle_mod.Oracle()
+        with pytest.raises(RuntimeError):
+            o.upload_geometry(g)
