@@ -228,6 +228,28 @@ def reference_arm(a, p):
     return line
 
 
+def lattice_k_section(a, local):
+    """Lattice k of the mixed form against the all-FP64 form: the same inactive and active cycles
+    (1e5 particles, 10 + 20 cycles, delta tracking) in both; z = difference over the combined sigma."""
+    from scone_gb300 import abi, gpu, problems
+    p = problems.lattice_17x17_7g()
+    res = {}
+    for name, prec in (("mixed", abi.PREC_MIXED), ("fp64", abi.PREC_FP64)):
+        t = gpu.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_DT, max_bank=300000, device=local,
+                                     form=abi.FORM_HISTORY)
+        inact, ia, act, aa = lattice_setup(t, p)
+        t.eigen_init(100000, SEED)
+        for _ in range(10):
+            t.eigen_cycle(inact, ia)
+        for _ in range(20):
+            t.eigen_cycle(act, aa)
+        res[name] = t.keff(aa)
+        t.close()
+    (km, sm), (kd, sd) = res["mixed"], res["fp64"]
+    return {"k_mixed": km, "sigma_mixed": sm, "k_fp64": kd, "sigma_fp64": sd,
+            "z": (km - kd) / (sm * sm + sd * sd) ** 0.5, "cycles": "10 inactive + 20 active, 1e5 particles"}
+
+
 def configs_section(a, local):
     """The other two workloads, each through sg_fixed_source_cycle on its own handle (device-resident
     source, gen loop and batch close) and through the oracle on the host cores:
@@ -398,7 +420,10 @@ def batched_section(a, local):
             done, wall, n = serve.poisson_run(S, templates, rate, a.serve_seconds, seed=7, eigen_fraction=efrac,
                                               drain=(efrac == 0), max_drain_s=30.0)
             S.stop()
+            sh, se = Bs.serve_counts()
             summ = serve.latency_summary(done, wall, offered)
+            summ["fixed_source_events_per_s"] = se / wall
+            summ["roofline_frac"] = se * BYTES_PER_EVENT_MIXED / wall / 1e9 / measured_peaks()[0]
             summ.update({"arrival_rate": rate, "arrived": n, "eigen_fraction": efrac,
                          "eigen_completed": sum(1 for r in done if r.kind == "eigen"),
                          "waves": Bs.serve_status()[2]})
@@ -576,6 +601,10 @@ def main():
             configs = configs_section(a, local)
         except Exception as e:
             configs = {"error": repr(e)}
+        try:
+            configs["lattice_k_vs_fp64"] = lattice_k_section(a, local)
+        except Exception as e:
+            configs["lattice_k_error"] = repr(e)
     batched = None
     if not a.no_batch and world == 1:
         try:

@@ -475,6 +475,11 @@ int32_t sg_serve_pump(sg_batch b, int32_t wait, int32_t* done_slots, double* lat
 int32_t sg_serve_stop(sg_batch b);
 /* histories queued but not yet launched, requests active, waves launched so far */
 int32_t sg_serve_status(sg_batch b, int64_t* queued, int32_t* active, int64_t* waves);
+/* while `on`, waves run with `blocks_per_sm` fewer resident blocks per SM than their tuning, so
+ * kernels of other streams (eigenvalue requests on their own handles) find room on every SM */
+int32_t sg_serve_share(sg_batch b, int32_t blocks_per_sm, int32_t on);
+/* histories and flight events of the waves retired since sg_serve_start */
+int32_t sg_serve_counts(sg_batch b, int64_t* histories, int64_t* events);
 /* host clock (seconds, the one submit and latency use) */
 double sg_serve_clock(void);
 

@@ -144,7 +144,9 @@ struct sg_batch_t {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t itemsCopy = nullptr, closeCopy = nullptr;
     sg_batch_tuning tune{};
-  } graph[2][2];
+  } graph[2][2][2];               // [mirror][nesting class][SMs reserved for other streams]
+  int reserve = 0;                 // blocks per SM the serving waves leave to other streams' kernels
+  int reserving = 0;               // reserve in force (serving with other work on the device)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
   sg_handle plainWork = nullptr;
@@ -161,6 +163,7 @@ struct sg_batch_t {
   std::vector<int> doneSlots;      // completed requests not yet handed out
   std::vector<double> doneLat;
   long long wavesLaunched = 0;
+  long long servedEvents = 0, servedHistories = 0;   // of retired waves
   int mirror = 0;
   cudaEvent_t ref = nullptr;
   double refHost = 0.0;
@@ -225,6 +228,7 @@ int grid_for(sg_batch b, int maxl) {
   const int occ = fp64(b) ? batch_occupancy<double>(maxl, dt, b->tune.block_threads)
                           : batch_occupancy<float>(maxl, dt, b->tune.block_threads);
   int per = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, occ) : occ;
+  if (b->reserving) per -= b->reserve;
   return b->sms * std::max(per, 1);
 }
 
@@ -239,7 +243,7 @@ void drop_graph(sg_batch_t::Graph& G) {
 // kernel.  The two list copies are resized to the current counts before each launch; the kernels
 // read the counts from device memory.  The cycle closes run after it (run_closes).
 int build_graph(sg_batch b, int m, int x) {
-  sg_batch_t::Graph& G = b->graph[m][x];
+  sg_batch_t::Graph& G = b->graph[m][x][b->reserving];
   if (G.exec) {
     if (std::memcmp(&G.tune, &b->tune, sizeof(G.tune)) == 0) return SG_OK;
     drop_graph(G);
@@ -362,7 +366,7 @@ int launch_graph(sg_batch b, int m, int maxl, cudaStream_t s) {
   const int x = maxl > 2 ? 1 : 0;
   int rc = build_graph(b, m, x);
   if (rc) return rc;
-  sg_batch_t::Graph& G = b->graph[m][x];
+  sg_batch_t::Graph& G = b->graph[m][x][b->reserving];
   const size_t ni = (size_t)std::max(1, b->hInts[m][0]), nc = (size_t)std::max(1, b->hInts[m][2]);
   BCK(cudaGraphExecMemcpyNodeSetParams1D(G.exec, G.itemsCopy, b->dItems[m], b->hItems[m], sizeof(WorkItem) * ni,
                                          cudaMemcpyHostToDevice));
@@ -459,8 +463,9 @@ int32_t sg_batch_destroy(sg_batch b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   for (auto& w : b->waves) cudaEventDestroy(w.done);
   if (b->ref) cudaEventDestroy(b->ref);
-  for (auto& row : b->graph)
-    for (auto& g : row) drop_graph(g);
+  for (auto& plane : b->graph)
+    for (auto& row : plane)
+      for (auto& g : row) drop_graph(g);
   if (b->plainWork) sg_destroy(b->plainWork);
   cudaFree(b->arena);
   cudaFree(b->dProbs);
@@ -878,6 +883,7 @@ int32_t sg_serve_start(sg_batch b, int64_t wave_histories, int32_t item_historie
   if (b->serving) return b->fail(SG_ERR_STATE, "serve: already started");
   b->serving = true;
   b->waveHist = wave_histories;
+  b->servedEvents = b->servedHistories = 0;
   b->serveItem = item_histories > 0 ? item_histories : b->tune.item_histories;
   b->wavesLaunched = 0;
   b->mirror = 0;
@@ -929,6 +935,8 @@ int retire_wave(sg_batch b, bool block, bool* retired) {
   BCK(cudaEventElapsedTime(&ms, b->ref, w.done));
   const double at = b->refHost + 1e-3 * (double)ms;
   int rc = read_counters(b, w.mirror);
+  b->servedEvents += (long long)b->hCtr[w.mirror]->events;
+  b->servedHistories += w.histories;
   for (const Request& r : w.closing) {
     b->doneSlots.push_back(r.slot);
     b->doneLat.push_back(std::max(0.0, at - r.submit));
@@ -1067,6 +1075,25 @@ int32_t sg_serve_status(sg_batch b, int64_t* queued, int32_t* active, int64_t* w
   if (queued) *queued = q;
   if (active) *active = (int32_t)b->active.size();
   if (waves) *waves = b->wavesLaunched;
+  return SG_OK;
+}
+
+int32_t sg_serve_share(sg_batch b, int32_t blocks_per_sm, int32_t on) {
+  if (!b || blocks_per_sm < 0) return SG_ERR_BAD_ARG;
+  if (b->reserve != blocks_per_sm) {
+    // a new reserve size: the reserving graphs are rebuilt at their next launch
+    for (auto& plane : b->graph)
+      for (auto& row : plane) drop_graph(row[1]);
+    b->reserve = blocks_per_sm;
+  }
+  b->reserving = (on && blocks_per_sm > 0) ? 1 : 0;
+  return SG_OK;
+}
+
+int32_t sg_serve_counts(sg_batch b, int64_t* histories, int64_t* events) {
+  if (!b) return SG_ERR_BAD_ARG;
+  if (histories) *histories = b->servedHistories;
+  if (events) *events = b->servedEvents;
   return SG_OK;
 }
 

@@ -776,6 +776,8 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
   if constexpr (CE) al |= (unsigned long long)A.in.E;
   bool bulkOK = (al & 15ull) == 0 && A.in.r && A.in.dir && A.in.wgt && A.in.time && A.in.G && (!CE || A.in.E);
   bool staged = false;         // warp-uniform: the current chunk is in shared memory
+  bool pending = false;        // warp-uniform: the current chunk's copies are in flight
+  int pendRounds = 0;
   bool abandoned = false;      // warp-uniform: a chunk timed out, the warp stops
   bool alive = false, done = false;
   int q_next = 0, q_end = 0, q_base = 0;   // warp-uniform range of histories taken from the counter
@@ -783,6 +785,29 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
   while (true) {
     unsigned need = __ballot_sync(FULL, !alive && !done);
     while (need) {
+      if (pending) {
+        // the chunk's bulk copies were issued on an earlier round; lanes with work kept stepping
+        int ready = 0;
+        if (lane == 0) ready = mbar_test(&s_bar[wid], phase) ? 1 : 0;
+        ready = __shfl_sync(FULL, ready, 0);
+        if (ready) {
+          phase ^= 1u;
+          pending = false;
+          staged = true;
+        } else if (++pendRounds > BULK_WAIT_LIMIT) {
+          // the copy engine did not complete the chunk in time: report, wait (again bounded) for
+          // the copies in flight, and retire this warp without starting more histories
+          if (lane == 0) raise_error(A.ctr, SG_ERR_TIMEOUT, q_base + 1);
+          (void)mbar_wait(&s_bar[wid], phase);
+          bulkOK = false;
+          pending = false;
+          abandoned = true;
+          done = true;
+          break;
+        } else {
+          break;                                       // idle lanes wait; the others step on
+        }
+      }
       if (q_next >= q_end) {
         int base = 0;
         if (lane == 0) base = atomicAdd(&A.ctr->work, 32);
@@ -808,20 +833,10 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
             bulk_to_smem(S.G, A.in.G + base, 128, bar);
             if constexpr (CE) bulk_to_smem(S.E, A.in.E + base, 256, bar);
           }
-          const bool ok = __all_sync(FULL, mbar_wait(&s_bar[wid], phase));
-          if (ok) {
-            phase ^= 1u;
-            staged = true;
-          } else {
-            // the copy engine did not complete the chunk in time: report, wait (again bounded) for
-            // the copies in flight, and retire this warp without starting more histories
-            if (lane == 0) raise_error(A.ctr, SG_ERR_TIMEOUT, base + 1);
-            (void)mbar_wait(&s_bar[wid], phase);
-            bulkOK = false;
-            abandoned = true;
-            done = true;
-            break;
-          }
+          pending = true;
+          pendRounds = 0;
+          if (__any_sync(FULL, alive)) break;            // let the busy lanes step meanwhile
+          continue;
         }
       }
       const int avail = q_end - q_next;
@@ -836,7 +851,8 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
       need &= ~__ballot_sync(FULL, mine);
     }
     if (abandoned) break;
-    if (__all_sync(FULL, !alive)) break;
+    // no lane busy and no chunk on its way: every lane has run out of work
+    if (!pending && __all_sync(FULL, !alive)) break;
     if (alive) {
       if (T.step()) { T.finish(); alive = false; }
     }

@@ -69,6 +69,7 @@ def load(build=True):
         "sg_serve_start": (i32, [vp, i64, i32]), "sg_serve_submit": (i32, [vp, i32]),
         "sg_serve_pump": (i32, [vp, i32, P(i32), P(f64), i32, P(i32)]), "sg_serve_stop": (i32, [vp]),
         "sg_serve_status": (i32, [vp, P(i64), P(i32), P(i64)]), "sg_serve_clock": (f64, []),
+        "sg_serve_counts": (i32, [vp, P(i64), P(i64)]), "sg_serve_share": (i32, [vp, i32, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -374,6 +375,16 @@ class BatchGPU:
         q, a, w = C.c_int64(), C.c_int32(), C.c_int64()
         self._check(self.L.sg_serve_status(self.b, C.byref(q), C.byref(a), C.byref(w)))
         return q.value, a.value, w.value
+
+    def serve_share(self, blocks_per_sm, on):
+        """Leave `blocks_per_sm` resident blocks per SM to other streams while `on`."""
+        self._check(self.L.sg_serve_share(self.b, int(blocks_per_sm), 1 if on else 0))
+
+    def serve_counts(self):
+        """(histories, flight events) of the waves retired since serve_start."""
+        h, e = C.c_int64(), C.c_int64()
+        self._check(self.L.sg_serve_counts(self.b, C.byref(h), C.byref(e)))
+        return h.value, e.value
 
     def serve_stop(self):
         self._check(self.L.sg_serve_stop(self.b))

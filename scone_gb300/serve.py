@@ -61,7 +61,7 @@ class SolveServer:
     EigenPool (eigenvalue requests)."""
 
     def __init__(self, batch, catalogue, wave_histories=1 << 23, item_histories=256, eigen=None,
-                 eigen_cycles=(20, 40)):
+                 eigen_cycles=(20, 40), eigen_share=2):
         self.B = batch
         self.catalogue = catalogue            # resident slots that requests instantiate
         self.waiting = collections.deque()    # fixed-source requests not yet admitted (arena full)
@@ -71,6 +71,7 @@ class SolveServer:
         self.eigen_waiting = collections.deque()
         self.eigen_running = []
         self.done = []
+        self.eigen_share = eigen_share        # blocks per SM the waves leave free while eigen requests run
         self.B.serve_start(wave_histories, item_histories)
 
     # ---- requests
@@ -135,6 +136,8 @@ class SolveServer:
         if self.eigen_running:
             self._eigen_step()
         self._admit()
+        if self.eigen is not None and hasattr(self.B, "serve_share"):
+            self.B.serve_share(self.eigen_share, bool(self.eigen_running))
         out, self.done = self.done, []
         return out
 

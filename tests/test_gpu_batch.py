@@ -202,7 +202,9 @@ def test_served_result_alone_equals_result_in_mix(gpu_mod, precision):
         done += B.pump(wait=True)
     assert done[0][0] == probe and done[0][1] > 0
     alone = B.bins(probe)
-    # in the mix: others first, the probe arrives while they run, more arrive after it
+    # in the mix: others first, the probe arrives while they run, more arrive after it; the waves
+    # leave room for other streams' kernels meanwhile (smaller grid, same results)
+    B.serve_share(2, True)
     for s in slots[:3]:
         B.submit(s)
     B.pump()
