@@ -308,6 +308,23 @@ int32_t sg_get_keff(sg_handle h, int32_t admin, double* k, double* std);
 
 /* ---------------------------------------------------------------- device-resident cycles */
 
+/* ---------------------------------------------------------------- bank files and file sources */
+
+/* particleDungeon%printToFile (particleDungeon_class.f90:1077-1112): particles 1..n of a bank to
+ * `path` + ".bin" (binary: a stream of 10 doubles per particle: r(3), dir(3), E, G, broodID, wgt)
+ * or `path` + ".txt" (the same ten numbers per line, as text).  NULL arrays write zeros (E for MG,
+ * G for CE, broodID); a NULL wgt writes 1. */
+int32_t sg_bank_write_file(const char* path, const sg_bank* bank, int32_t n, int32_t binary);
+/* fileSource%init (fileSource_class.f90:47-144): the number of particles in such a file (`path` as
+ * given, extension included), then the particles themselves into a bank of capacity cap */
+int32_t sg_bank_count_file(const char* path, int32_t binary, int64_t* n);
+int32_t sg_bank_read_file(const char* path, int32_t binary, sg_bank* bank, int32_t cap, int32_t* n);
+/* fileSource as the source of fixed-source cycles (replaces the point source): particle i of a
+ * cycle copies entry int(xi N) + 1 of these N particles, xi the first draw of master + stride(i)
+ * (fileSource%sampleParticle, fileSource_class.f90:146-190); time 0; a particle outside the geometry
+ * or in an undefined cell is an error.  MG problems read G, CE problems E. */
+int32_t sg_set_file_source(sg_handle h, const sg_bank* particles, int32_t n);
+
 /* fissionSource (fissionSource_class.f90:149-271) sampled on the device into the resident
  * bank: particle i uses master + stride(i); afterwards master is strided by pop
  * (eigenPhysicsPackage_class.f90:348-366). */

@@ -36,6 +36,7 @@ def lib():
         sig = {
             "or_create": (i32, [i32, P(vp)]), "or_destroy": (i32, [vp]),
             "or_set_ht_cutoff": (i32, [vp, C.c_double]),
+            "or_set_file_source": (i32, [vp, P(abi.Bank), i32]),
             "or_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(C.c_uint64), P(abi.CycleStats)]),
             "or_sample_legendre_p1": (i32, [C.c_double, P(C.c_uint64), P(C.c_double), i32]),
             "or_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
@@ -229,6 +230,10 @@ class Oracle:
         pop = C.c_int32()
         self._check(self.L.or_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
         return b, pop.value
+
+    def set_file_source(self, bank):
+        self._keep.append(bank)
+        self._check(self.L.or_set_file_source(self.h, C.byref(bank.struct), bank.n))
 
     def fixed_source_cycle(self, admin, n, master, total=None):
         """One fixed-source cycle of n histories; with `total`, n is this process's share of a

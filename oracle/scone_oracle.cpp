@@ -1852,6 +1852,22 @@ struct Oracle {
   }
 
   // pointSource / configSource sampleParticle (pointSource_class.f90:189-270)
+  // fileSource (fileSource_class.f90:47-190): the particle table and its sampling
+  std::vector<PState> fileSrc;
+  int sampleFile(RNG& rand, PState& s) {
+    const long long N = (long long)fileSrc.size();
+    const long long idx = (long long)(rand.get() * (double)N) + 1;
+    if (idx > N) return SG_ERR_STATE;
+    s = fileSrc[idx - 1];
+    int matIdx, uid;
+    double u0[3] = {1.0, 0.0, 0.0};
+    geom.whatIsAt(matIdx, uid, s.r, u0);
+    if (matIdx == OUTSIDE_MAT || matIdx == UNDEF_MAT) return SG_ERR_UNDEF_MAT;
+    s.time = 0.0;
+    s.broodID = 0;
+    return SG_OK;
+  }
+
   PState samplePoint(RNG& rand) {
     PState s;
     for (int i = 0; i < 3; ++i) s.r[i] = src.r[i];
@@ -1994,6 +2010,18 @@ int32_t or_sample_legendre_p1(double a, uint64_t* state, double* out, int32_t n)
   for (int i = 0; i < n; ++i) out[i] = orc::sampleLegendreP1(a, r, err);
   *state = r.s;
   return err.empty() ? SG_OK : SG_ERR_BAD_ARG;
+}
+int32_t or_set_file_source(or_handle h, const sg_bank* p, int32_t n) {
+  Oracle* o = O(h);
+  o->fileSrc.assign(n, orc::PState());
+  for (int i = 0; i < n; ++i) {
+    orc::PState& s = o->fileSrc[i];
+    for (int k = 0; k < 3; ++k) { s.r[k] = p->r[3 * i + k]; s.dir[k] = p->dir[3 * i + k]; }
+    s.wgt = p->wgt ? p->wgt[i] : 1.0;
+    s.E = p->E ? p->E[i] : 0.0;
+    s.G = p->G ? p->G[i] : 0;
+  }
+  return SG_OK;
 }
 int32_t or_set_ht_cutoff(or_handle h, double c) {
   if (!(c > 0.0 && c < 1.0)) return SG_ERR_BAD_ARG;
@@ -2185,7 +2213,14 @@ int32_t or_fixed_source_cycle_shard(or_handle h, int32_t admin, int32_t n, int32
                                     sg_cycle_stats* st) {
   Oracle* o = O(h);
   std::vector<orc::PState> bank(n), next;
-  for (int i = 1; i <= n; ++i) { orc::RNG r; r.s = *master; r.stride(i); bank[i - 1] = o->samplePoint(r); }
+  for (int i = 1; i <= n; ++i) {
+    orc::RNG r; r.s = *master; r.stride(i);
+    if (o->fileSrc.empty()) bank[i - 1] = o->samplePoint(r);
+    else {
+      int rc = o->sampleFile(r, bank[i - 1]);
+      if (rc) { o->err = "file source: particle outside the geometry or in an undefined cell"; return rc; }
+    }
+  }
   orc::RNG m; m.s = *master; m.stride(total);
   o->reportCycleStart(admin, (double)n);
   int rc = o->transportBank(admin, bank, m.s, 1.0, next);

@@ -23,17 +23,29 @@ namespace sg {
 
 static constexpr int BATCH_MAX_WARPS = 4;   // __launch_bounds__(128)
 
-// the record of a problem into the warp's shared slot; counters and errors go to this launch's
+// The record of a problem into the warp's shared slot by one bulk asynchronous copy (the copy
+// engine moves the ~3 KB record while the warp waits on its mbarrier); counters and errors then go
+// to this launch's.  Returns false if the copy did not complete within the bounded wait (after a
+// second bounded wait for the copy in flight): the warp must stop.
 template <class R>
-__device__ __forceinline__ void stage_problem_warp(BatchProblem<R>* dst, const BatchProblem<R>* src, int lane,
-                                                   DCounters* ctr) {
+__device__ __forceinline__ bool stage_problem_warp(BatchProblem<R>* dst, const BatchProblem<R>* src, int lane,
+                                                   DCounters* ctr, unsigned long long* bar, unsigned& phase) {
   static_assert(sizeof(BatchProblem<R>) % 16 == 0, "record size");
-  const int4* s = reinterpret_cast<const int4*>(src);
-  int4* d = reinterpret_cast<int4*>(dst);
-  for (int i = lane; i < (int)(sizeof(BatchProblem<R>) / 16); i += 32) d[i] = __ldg(s + i);
-  __syncwarp();
+  __syncwarp();                                        // the previous record is no longer read
+  if (lane == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect(bar, (unsigned)sizeof(BatchProblem<R>));
+    bulk_to_smem(dst, src, (unsigned)sizeof(BatchProblem<R>), bar);
+  }
+  const bool ok = __all_sync(FULL, mbar_wait(bar, phase));
+  if (!ok) {
+    (void)mbar_wait(bar, phase);
+    return false;
+  }
+  phase ^= 1u;
   if (lane == 0) dst->t.ctr = ctr;
   __syncwarp();
+  return true;
 }
 
 // pointSource%sampleParticle (pointSource_class.f90:189-270), then the particle enters the gen loop
@@ -62,7 +74,6 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
       r = r - (R)P.src_prob_g[g - 1];
       if (r < R(0)) break;
     }
-    if (g > P.src_n_prob_g) g = P.src_n_prob_g;
   }
   T.hist = n;
   T.c.r0[0] = P.src_r[0];
@@ -88,8 +99,12 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
 template <class R, int MAXL, int OP>
 __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaunch L) {
   __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
+  __shared__ __align__(8) unsigned long long s_bar[BATCH_MAX_WARPS];
   const int lane = threadIdx.x & 31;
   BatchProblem<R>& P = *reinterpret_cast<BatchProblem<R>*>(s_rec[threadIdx.x >> 5]);
+  unsigned long long* bar = &s_bar[threadIdx.x >> 5];
+  unsigned phase = 0;
+  if (lane == 0) mbar_init(bar);
   const BatchProblem<R>* probs = static_cast<const BatchProblem<R>*>(L.problems);
   if (lane == 0) {                  // a neutral record until the first item is staged
     P.t.k_eff = L.k_one;
@@ -105,6 +120,7 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
   int pend = -1;                    // claimed item of another problem, waiting for the warp to drain
   int q_next = 0, q_end = 0;        // warp-uniform range of flat histories of the current item
   bool alive = false, done = false;
+  bool stopped = false;             // warp-uniform: a record copy timed out
 
   while (true) {
     unsigned need = __ballot_sync(FULL, !alive && !done);
@@ -123,7 +139,12 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
         const WorkItem wi = L.items[it];
         if (wi.slot != cur) {
           if (__any_sync(FULL, alive)) { pend = it; break; }
-          stage_problem_warp<R>(&P, probs + wi.slot, lane, L.ctr);
+          if (!stage_problem_warp<R>(&P, probs + wi.slot, lane, L.ctr, bar, phase)) {
+            if (lane == 0) raise_error(L.ctr, SG_ERR_TIMEOUT, wi.first + 1);
+            done = true;                               // no lane is alive here: the warp stops
+            stopped = true;
+            break;
+          }
           cur = wi.slot;
         }
         pend = -1;
@@ -137,6 +158,7 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
       q_next += min(__popc(need), avail);
       need &= ~__ballot_sync(FULL, mine);
     }
+    if (stopped) break;
     if (__all_sync(FULL, !alive)) {
       if (__all_sync(FULL, done)) break;
       continue;
@@ -144,6 +166,10 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
     if (alive) {
       if (T.step()) { T.finish(); alive = false; }
     }
+  }
+  if (stopped) {                    // the record slot may hold a partial copy: count into this launch
+    if (lane == 0) { P.t.ctr = L.ctr; P.t.keff_clerk = -1; }
+    __syncwarp();
   }
   flush_counters(T, P.t, lane);
 }

@@ -17,4 +17,11 @@ cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank o
   return cudaGetLastError();
 }
 
+cudaError_t launch_file_source(const FileSourceArgs& a, int maxl, cudaStream_t s) {
+  const int grid = (a.n + 127) / 128;
+  if (maxl <= 2) k_file_source<2><<<grid, 128, 0, s>>>(a);
+  else k_file_source<4><<<grid, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace sg

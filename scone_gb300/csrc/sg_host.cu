@@ -15,6 +15,7 @@
 
 #include "sg_device.cuh"
 #include "sg_launch.h"
+#include "sg_source.cuh"
 #include "sg_support.h"
 #include "sg_noalloc.h"
 #include "sg_batch.h"
@@ -194,6 +195,11 @@ struct sg_handle_t {
   // point source
   bool hasSource = false;
   PointSourceArgs psrc{};
+  // file source (fileSource): the particle table on the device
+  bool hasFileSource = false;
+  long long fileN = 0;
+  DArr<double> fsR, fsDir, fsWgt, fsE;
+  DArr<int> fsG;
   DArr<double> probG;
 
   // eigen state
@@ -1404,7 +1410,8 @@ int32_t sg_destroy(sg_handle h) {
   cudaStreamSynchronize(h->stream);
   for (auto& b : h->bank) b.free();
   h->surfs64.free(); h->surfsMx.free(); h->unis64.free(); h->unisMx.free(); h->uniCells.free();
-  h->cellPtr.free(); h->cellSurf.free(); h->cellComplex.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
+  h->cellPtr.free(); h->cellSurf.free(); h->cellComplex.free();
+  h->fsR.free(); h->fsDir.free(); h->fsWgt.free(); h->fsE.free(); h->fsG.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
   h->pinRsqF.free(); h->pinTolF.free();
   for (auto& a : h->mgD) a.free();
   for (auto& a : h->mgF) a.free();
@@ -1682,18 +1689,37 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
 int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t n, int32_t total, uint64_t* master_state,
                                     sg_cycle_stats* stats) {
   if (!h || !master_state || n <= 0 || n > h->cap || total < n) return SG_ERR_BAD_ARG;
-  if (!h->hasSource) return h->fail(SG_ERR_STATE, "no point source set");
+  if (!h->hasSource && !h->hasFileSource) return h->fail(SG_ERR_STATE, "no point or file source set");
   if (h->anyFissile) return h->fail(SG_ERR_BAD_ARG, "fixed-source runs with fissile materials are not supported");
   cudaStream_t s = h->stream;
   DBank A = h->bank[0].view(), B = h->bank[1].view();
   h->launches = 0;
   CK(cudaEventRecord(h->ev[2], s));
-  PointSourceArgs a = h->psrc;                                           // fixedSource%generate
-  h->launches += 1;
-  a.out = A;
-  a.n = n;
-  a.master = *master_state;
-  CK(launch_point_source(a, s));
+  h->launches += 1;                                                      // fixedSource%generate
+  if (h->hasFileSource) {
+    FileSourceArgs f;
+    f.geom = h->g64;
+    f.r = h->fsR.p; f.dir = h->fsDir.p; f.wgt = h->fsWgt.p;
+    f.E = h->hasCE ? h->fsE.p : nullptr;
+    f.G = h->hasCE ? nullptr : h->fsG.p;
+    f.N = h->fileN;
+    f.out = A;
+    f.n = n;
+    f.master = *master_state;
+    f.err = h->totals.p + 5;
+    CK(cudaMemsetAsync(h->totals.p + 5, 0, sizeof(int), s));
+    CK(launch_file_source(f, h->maxl, s));
+    int ferr = 0;
+    CK(cudaMemcpyAsync(&ferr, h->totals.p + 5, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (ferr) return h->fail(ferr, "file source: a particle is outside the geometry or in an undefined cell");
+  } else {
+    PointSourceArgs a = h->psrc;
+    a.out = A;
+    a.n = n;
+    a.master = *master_state;
+    CK(launch_point_source(a, s));
+  }
   unsigned long long m = rng_stride(*master_state, total);               // :189
   int rc = cycle_start(h, admin, nullptr, (double)n);
   if (rc) return rc;
@@ -1724,6 +1750,91 @@ int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t n, int32
     stats->cycle_ms = cyc;
     stats->n_kernels = h->launches;
   }
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ bank files
+int32_t sg_bank_write_file(const char* path, const sg_bank* b, int32_t n, int32_t binary) {
+  if (!path || !b || n < 0 || (n > 0 && (!b->r || !b->dir))) return SG_ERR_BAD_ARG;
+  std::string name = std::string(path) + (binary ? ".bin" : ".txt");
+  FILE* f = std::fopen(name.c_str(), binary ? "wb" : "w");
+  if (!f) return SG_ERR_BAD_ARG;
+  for (int i = 0; i < n; ++i) {                 // r, dir, E, real(G), real(broodID), wgt
+    double v[10];
+    for (int k = 0; k < 3; ++k) { v[k] = b->r[3 * i + k]; v[3 + k] = b->dir[3 * i + k]; }
+    v[6] = b->E ? b->E[i] : 0.0;
+    v[7] = b->G ? (double)b->G[i] : 0.0;
+    v[8] = b->brood_id ? (double)b->brood_id[i] : 0.0;
+    v[9] = b->wgt ? b->wgt[i] : 1.0;
+    bool ok;
+    if (binary) ok = std::fwrite(v, sizeof(double), 10, f) == 10;
+    else ok = std::fprintf(f, "%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", v[0], v[1], v[2],
+                           v[3], v[4], v[5], v[6], v[7], v[8], v[9]) > 0;
+    if (!ok) { std::fclose(f); return SG_ERR_BAD_ARG; }
+  }
+  return std::fclose(f) == 0 ? SG_OK : SG_ERR_BAD_ARG;
+}
+
+namespace {
+// readArray (genericProcedures.f90) of fileSource: ten numbers per particle
+bool read_particle(FILE* f, bool binary, double v[10]) {
+  if (binary) return std::fread(v, sizeof(double), 10, f) == 10;
+  for (int k = 0; k < 10; ++k)
+    if (std::fscanf(f, "%lf", &v[k]) != 1) return false;
+  return true;
+}
+}  // namespace
+
+int32_t sg_bank_count_file(const char* path, int32_t binary, int64_t* n) {
+  if (!path || !n) return SG_ERR_BAD_ARG;
+  FILE* f = std::fopen(path, binary ? "rb" : "r");
+  if (!f) return SG_ERR_BAD_ARG;
+  double v[10];
+  long long c = 0;
+  while (read_particle(f, binary != 0, v)) ++c;
+  std::fclose(f);
+  *n = c;
+  return SG_OK;
+}
+
+int32_t sg_bank_read_file(const char* path, int32_t binary, sg_bank* b, int32_t cap, int32_t* n) {
+  if (!path || !b || !n || cap < 0) return SG_ERR_BAD_ARG;
+  FILE* f = std::fopen(path, binary ? "rb" : "r");
+  if (!f) return SG_ERR_BAD_ARG;
+  double v[10];
+  int c = 0;
+  while (c < cap && read_particle(f, binary != 0, v)) {
+    for (int k = 0; k < 3; ++k) {
+      if (b->r) b->r[3 * c + k] = v[k];
+      if (b->dir) b->dir[3 * c + k] = v[3 + k];
+    }
+    if (b->E) b->E[c] = v[6];
+    if (b->G) b->G[c] = (int)v[7];
+    if (b->brood_id) b->brood_id[c] = (int)v[8];
+    if (b->wgt) b->wgt[c] = v[9];
+    if (b->time) b->time[c] = 0.0;
+    ++c;
+  }
+  std::fclose(f);
+  *n = c;
+  return SG_OK;
+}
+
+int32_t sg_set_file_source(sg_handle h, const sg_bank* p, int32_t n) {
+  if (!h || !p || n <= 0 || !p->r || !p->dir) return SG_ERR_BAD_ARG;
+  if (!h->hasGeom) return h->fail(SG_ERR_STATE, "file source: upload the geometry first");
+  if (h->hasCE && !p->E) return h->fail(SG_ERR_BAD_ARG, "file source: CE problems need E");
+  if (!h->hasCE && !p->G) return h->fail(SG_ERR_BAD_ARG, "file source: MG problems need G");
+  cudaStream_t s = h->stream;
+  CK(h->fsR.upload(std::vector<double>(p->r, p->r + 3 * (size_t)n), s));
+  CK(h->fsDir.upload(std::vector<double>(p->dir, p->dir + 3 * (size_t)n), s));
+  std::vector<double> w(n, 1.0);
+  if (p->wgt) w.assign(p->wgt, p->wgt + n);
+  CK(h->fsWgt.upload(w, s));
+  if (p->E) CK(h->fsE.upload(std::vector<double>(p->E, p->E + n), s));
+  if (p->G) CK(h->fsG.upload(std::vector<int>(p->G, p->G + n), s));
+  h->fileN = n;
+  h->hasFileSource = true;
   return SG_OK;
 }
 

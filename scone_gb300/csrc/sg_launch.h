@@ -48,4 +48,8 @@ cudaError_t launch_fission_source(const DGeom& g, const DMG<double>& mg, DBank o
                                   unsigned long long master, const double* bounds6, int maxl,
                                   int* err, cudaStream_t s);
 
+struct FileSourceArgs;
+// fileSource sampling on the device (fileSource_class.f90:146-190), FP64
+cudaError_t launch_file_source(const FileSourceArgs& a, int maxl, cudaStream_t s);
+
 }  // namespace sg

@@ -58,4 +58,44 @@ __global__ void __launch_bounds__(128) k_fission_source(const __grid_constant__ 
   atomicCAS(a.err, 0, SG_ERR_STATE);
 }
 
+// fileSource%sampleParticle (fileSource_class.f90:146-190): particle i (1-based) takes entry
+// int(xi N) + 1 of the table, xi the first draw of master + stride(i); the entry must lie inside the
+// geometry (whatIsAt), as the reference checks.
+struct FileSourceArgs {
+  DGeom geom;
+  const double* r;      // [N][3]
+  const double* dir;    // [N][3]
+  const double* wgt;    // [N]
+  const double* E;      // [N] (CE) or null
+  const int* G;         // [N] (MG) or null
+  long long N;
+  DBank out;
+  int n;
+  unsigned long long master;
+  int* err;
+};
+
+template <int MAXL>
+__global__ void __launch_bounds__(128) k_file_source(const __grid_constant__ FileSourceArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  Rng<double> rng;
+  rng.s = lcg_skip(a.master, RNG_STRIDE * (long long)(i + 1));
+  const long long idx = (long long)(rng.get() * (double)a.N) + 1;
+  if (idx > a.N) { atomicCAS(a.err, 0, SG_ERR_STATE); return; }
+  const long long j = idx - 1;
+  Geom<double, MAXL> geom(a.geom);
+  Coords<double, MAXL> c;
+  for (int k = 0; k < 3; ++k) c.r0[k] = a.r[3 * j + k];
+  c.u[0] = 1.0; c.u[1] = 0.0; c.u[2] = 0.0;          // whatIsAt without a direction (geometryStd :163-168)
+  geom.place(c);
+  if (c.mat == 0 || c.mat == SG_UNDEF_MAT) { atomicCAS(a.err, 0, SG_ERR_UNDEF_MAT); return; }
+  for (int k = 0; k < 3; ++k) { a.out.r[3 * i + k] = a.r[3 * j + k]; a.out.dir[3 * i + k] = a.dir[3 * j + k]; }
+  a.out.wgt[i] = a.wgt[j];
+  a.out.G[i] = a.G ? a.G[j] : 0;
+  if (a.out.E) a.out.E[i] = a.E ? a.E[j] : 0.0;
+  a.out.brood[i] = 0;
+  a.out.time[i] = 0.0;
+}
+
 }  // namespace sg

@@ -32,20 +32,8 @@ __device__ __forceinline__ void raise_error(DCounters* ctr, int code, int hist) 
   if (atomicCAS(&ctr->err_code, 0, code) == 0) ctr->err_hist = hist;
 }
 
-// ---- bank staging through bulk asynchronous copies (cp.async.bulk + mbarrier)
-// A warp's chunk of 32 consecutive source particles, copied from the bank's SoA arrays into shared
-// memory by the copy engine of the SM (one bulk copy per array, completion counted in bytes on an
-// mbarrier), then read by the lanes that start those histories.
-struct __align__(16) BankChunk {
-  double r[96];
-  double dir[96];
-  double wgt[32];
-  double time[32];
-  double E[32];
-  int G[32];
-};
-static constexpr unsigned CHUNK_BYTES_MG = 768 + 768 + 256 + 256 + 128;
-static constexpr unsigned CHUNK_BYTES_CE = CHUNK_BYTES_MG + 256;
+// ---- bulk asynchronous copies global -> shared (cp.async.bulk, completion counted in bytes on an
+// mbarrier); every wait is bounded
 static constexpr int BULK_WAIT_LIMIT = 1 << 22;   // try_wait rounds before a chunk is given up
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -500,29 +488,6 @@ struct Tracker {
     select_ht();
   }
 
-  // start() from a staged chunk: history h is entry j of the chunk
-  __device__ __forceinline__ void start_staged(int h, const BankChunk& S, int j) {
-    hist = h;
-    c.r0[0] = S.r[3 * j + 0];
-    c.r0[1] = S.r[3 * j + 1];
-    c.r0[2] = S.r[3 * j + 2];
-    c.u[0] = (R)S.dir[3 * j + 0];
-    c.u[1] = (R)S.dir[3 * j + 1];
-    c.u[2] = (R)S.dir[3 * j + 2];
-    w = (R)S.wgt[j];
-    w0 = w;
-    G = CE ? 0 : S.G[j];
-    if constexpr (CE) set_energy(S.E[j]);
-    time = (R)S.time[j];
-    rng.s = lcg_skip(A.master, RNG_STRIDE * (long long)h);
-    collN = 0;
-    nsites = 0;
-    segs = 0;
-    cache.lvl = 0;
-    if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
-    select_ht();
-  }
-
   __device__ __forceinline__ void finish() {
     if (A.hist_nsites) A.hist_nsites[hist - 1] = nsites;
     if (A.rec_coll) A.rec_coll[hist - 1] = collN;
@@ -761,53 +726,12 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
   }
   Tracker<R, MAXL, OP, CE> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  // per-warp bank staging (blocks have at most 4 warps: __launch_bounds__(128))
-  __shared__ BankChunk s_chunk[4];
-  __shared__ __align__(8) unsigned long long s_bar[4];
-  if (lane == 0) mbar_init(&s_bar[wid]);
-  __syncwarp();
-  unsigned phase = 0;
-  // warp-uniform: chunks go through the copy engine (bulk copies need 16-byte aligned sources;
-  // banks the caller owns need not be)
-  unsigned long long al = (unsigned long long)A.in.r | (unsigned long long)A.in.dir |
-                          (unsigned long long)A.in.wgt | (unsigned long long)A.in.time |
-                          (unsigned long long)A.in.G;
-  if constexpr (CE) al |= (unsigned long long)A.in.E;
-  bool bulkOK = (al & 15ull) == 0 && A.in.r && A.in.dir && A.in.wgt && A.in.time && A.in.G && (!CE || A.in.E);
-  bool staged = false;         // warp-uniform: the current chunk is in shared memory
-  bool pending = false;        // warp-uniform: the current chunk's copies are in flight
-  int pendRounds = 0;
-  bool abandoned = false;      // warp-uniform: a chunk timed out, the warp stops
   bool alive = false, done = false;
-  int q_next = 0, q_end = 0, q_base = 0;   // warp-uniform range of histories taken from the counter
+  int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
 
   while (true) {
     unsigned need = __ballot_sync(FULL, !alive && !done);
     while (need) {
-      if (pending) {
-        // the chunk's bulk copies were issued on an earlier round; lanes with work kept stepping
-        int ready = 0;
-        if (lane == 0) ready = mbar_test(&s_bar[wid], phase) ? 1 : 0;
-        ready = __shfl_sync(FULL, ready, 0);
-        if (ready) {
-          phase ^= 1u;
-          pending = false;
-          staged = true;
-        } else if (++pendRounds > BULK_WAIT_LIMIT) {
-          // the copy engine did not complete the chunk in time: report, wait (again bounded) for
-          // the copies in flight, and retire this warp without starting more histories
-          if (lane == 0) raise_error(A.ctr, SG_ERR_TIMEOUT, q_base + 1);
-          (void)mbar_wait(&s_bar[wid], phase);
-          bulkOK = false;
-          pending = false;
-          abandoned = true;
-          done = true;
-          break;
-        } else {
-          break;                                       // idle lanes wait; the others step on
-        }
-      }
       if (q_next >= q_end) {
         int base = 0;
         if (lane == 0) base = atomicAdd(&A.ctr->work, 32);
@@ -816,43 +740,17 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
           if (!alive) done = true;
           break;
         }
-        q_next = q_base = base;
+        q_next = base;
         q_end = min(base + 32, A.n);
-        staged = false;
-        if (bulkOK && q_end - base == 32) {
-          __syncwarp();                                  // the previous chunk has been read
-          if (lane == 0) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            BankChunk& S = s_chunk[wid];
-            unsigned long long* bar = &s_bar[wid];
-            mbar_expect(bar, CE ? CHUNK_BYTES_CE : CHUNK_BYTES_MG);
-            bulk_to_smem(S.r, A.in.r + 3LL * base, 768, bar);
-            bulk_to_smem(S.dir, A.in.dir + 3LL * base, 768, bar);
-            bulk_to_smem(S.wgt, A.in.wgt + base, 256, bar);
-            bulk_to_smem(S.time, A.in.time + base, 256, bar);
-            bulk_to_smem(S.G, A.in.G + base, 128, bar);
-            if constexpr (CE) bulk_to_smem(S.E, A.in.E + base, 256, bar);
-          }
-          pending = true;
-          pendRounds = 0;
-          if (__any_sync(FULL, alive)) break;            // let the busy lanes step meanwhile
-          continue;
-        }
       }
       const int avail = q_end - q_next;
       const int rank = __popc(need & ((1u << lane) - 1u));
       const bool mine = ((need >> lane) & 1u) && rank < avail;
-      if (mine) {
-        if (staged) T.start_staged(q_next + rank + 1, s_chunk[wid], q_next + rank - q_base);
-        else T.start(q_next + rank + 1);
-        alive = true;
-      }
+      if (mine) { T.start(q_next + rank + 1); alive = true; }
       q_next += min(__popc(need), avail);
       need &= ~__ballot_sync(FULL, mine);
     }
-    if (abandoned) break;
-    // no lane busy and no chunk on its way: every lane has run out of work
-    if (!pending && __all_sync(FULL, !alive)) break;
+    if (__all_sync(FULL, !alive)) break;
     if (alive) {
       if (T.step()) { T.finish(); alive = false; }
     }

@@ -50,6 +50,10 @@ def load(build=True):
         "sg_eigen_state": (i32, [vp, P(u64), P(f64)]), "sg_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
         "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(u64), P(abi.CycleStats)]),
+        "sg_set_file_source": (i32, [vp, P(abi.Bank), i32]),
+        "sg_bank_write_file": (i32, [C.c_char_p, P(abi.Bank), i32, i32]),
+        "sg_bank_count_file": (i32, [C.c_char_p, i32, P(i64)]),
+        "sg_bank_read_file": (i32, [C.c_char_p, i32, P(abi.Bank), i32, P(i32)]),
         "sg_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
         "sg_rng_draws": (i32, [P(u64), P(f64), i32]), "sg_rng_skip": (u64, [u64, i64]),
         "sg_transport_bank_noalloc": (i32, [vp, i32, P(abi.Bank), i32, u64, f64, P(abi.Bank), i32, P(i32)]),
@@ -209,6 +213,11 @@ class TransportOperatorGPU:
         pop = C.c_int32()
         self._check(self.L.sg_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
         return b, pop.value
+
+    def set_file_source(self, bank):
+        """fileSource: fixed-source cycles sample their particles from this host bank."""
+        self._keep.append(bank)
+        self._check(self.L.sg_set_file_source(self.h, C.byref(bank.struct), bank.n))
 
     def fixed_source_cycle(self, admin, n, master, total=None):
         """One fixed-source cycle of n histories; with `total`, n is this process's share of a
@@ -391,6 +400,26 @@ class BatchGPU:
 
     def clock(self):
         return self.L.sg_serve_clock()
+
+
+def write_bank_file(path, bank, n=None, binary=True):
+    """particleDungeon%printToFile: `path` + .bin / .txt."""
+    rc = load().sg_bank_write_file(path.encode(), C.byref(bank.struct), bank.n if n is None else n, int(binary))
+    if rc != 0:
+        raise SconeGpuError(f"sg_bank_write_file failed with {rc}")
+
+
+def read_bank_file(path, binary=True):
+    """The particles of a printToFile file (fileSource's reader), as an abi.HostBank."""
+    L = load()
+    cnt = C.c_int64()
+    if L.sg_bank_count_file(path.encode(), int(binary), C.byref(cnt)) != 0:
+        raise SconeGpuError(f"cannot read {path}")
+    b = abi.HostBank(cnt.value)
+    got = C.c_int32()
+    if L.sg_bank_read_file(path.encode(), int(binary), C.byref(b.struct), cnt.value, C.byref(got)) != 0:
+        raise SconeGpuError(f"cannot read {path}")
+    return b
 
 
 def rng_draws(state, n):

@@ -41,3 +41,34 @@ def test_create_without_gpu_fails_loudly():
     except gpu.SconeGpuError:
         return
     raise AssertionError("creating a handle without a GPU must raise")
+
+
+def test_bank_file_round_trip(tmp_path):
+    """particleDungeon%printToFile layout (10 doubles per particle: r, dir, E, G, broodID, wgt) written
+    and read back by the library's host code, in binary and text form; no GPU is involved."""
+    from scone_gb300 import abi, gpu
+    rng = np.random.default_rng(9)
+    n = 257
+    b = abi.HostBank(n)
+    b["r"][:] = rng.normal(size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    b["dir"][:] = d / np.linalg.norm(d, axis=1)[:, None]
+    b["wgt"][:] = rng.uniform(0.5, 2.0, n)
+    b["G"][:] = rng.integers(1, 8, n)
+    b["brood_id"][:] = np.arange(1, n + 1)
+    b["E"][:] = rng.uniform(1e-9, 10.0, n)
+    for binary in (True, False):
+        stem = str(tmp_path / ("bank" + str(binary)))
+        gpu.write_bank_file(stem, b, binary=binary)
+        path = stem + (".bin" if binary else ".txt")
+        if binary:
+            raw = np.fromfile(path, dtype=np.float64).reshape(n, 10)
+            np.testing.assert_array_equal(raw[:, 0:3], b["r"])
+            np.testing.assert_array_equal(raw[:, 7], b["G"].astype(float))
+            np.testing.assert_array_equal(raw[:, 9], b["wgt"])
+        c = gpu.read_bank_file(path, binary=binary)
+        assert c.n == n
+        for k in ("r", "dir", "wgt", "E"):
+            np.testing.assert_array_equal(c[k], b[k])
+        np.testing.assert_array_equal(c["G"], b["G"])
+        np.testing.assert_array_equal(c["brood_id"], b["brood_id"])

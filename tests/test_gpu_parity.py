@@ -255,3 +255,31 @@ def test_union_cell_bad_definition_is_rejected(gpu_mod):
     t = gpu_mod.TransportOperatorGPU(max_bank=16)
     with pytest.raises(gpu_mod.SconeGpuError, match="ambiguous"):
         t.upload_geometry(gb.arrays())
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_file_source_cycles_match_oracle(gpu_mod, oracle_mod, form, tmp_path):
+    """fileSource: a bank written with printToFile's layout, read back and used as the source of
+    fixed-source cycles (particle int(xi N) + 1 per history) gives the oracle's results."""
+    p = problems.infinite_medium_2g()
+    o0 = oracle_mod.Oracle(p)
+    seed_bank = o0.generate_source(SEED, 500)
+    rng = np.random.default_rng(5)
+    seed_bank["r"][:] = rng.uniform(-9.0, 9.0, size=(500, 3))   # spread inside the reflective box
+    seed_bank["G"][:] = rng.integers(1, 3, 500)
+    stem = str(tmp_path / "src")
+    gpu_mod.write_bank_file(stem, seed_bank, binary=True)
+    fb = gpu_mod.read_bank_file(stem + ".bin")
+    g = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_FP64, transport=abi.TRANSPORT_DT, max_bank=20000,
+                                     form=form)
+    o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_DT)
+    res = []
+    for t in (g, o):
+        t.set_file_source(fb)
+        a = t.upload_tally(p.tallies["flux"])
+        m = 99
+        for _ in range(3):
+            m, _ = t.fixed_source_cycle(a, 10000, m)
+        res.append((m, t.bins(a)))
+    assert res[0][0] == res[1][0]
+    np.testing.assert_allclose(res[0][1], res[1][1], rtol=1e-10, atol=0)
