@@ -113,6 +113,16 @@ extern "C" {
 #define SG_AXIS_MATERIAL   5      /* materialMap over 1..n                                       */
 #define SG_AXIS_ENERGY     6      /* energyMap, log grid over [min,max] (energyMap_class.f90:278-293,
                                      grid_class.f90:76-90,164-166); MG particles map to 0        */
+#define SG_AXIS_CELL       7      /* cellMap (cellMap_class.f90:80-205): one bin per listed cell
+                                     (the cell the particle is in at its lowest level); elsewhere
+                                     bin n+1 with cell_rest (trackRest), else outside the map    */
+
+/* grids of the space and energy axes (grid_class.f90:154-175): the default is lin for space axes and
+ * log for the energy axis; unstructured grids take n+1 ascending bounds (a floor binary search) */
+#define SG_GRID_DEFAULT    0
+#define SG_GRID_LIN        1
+#define SG_GRID_LOG        2
+#define SG_GRID_UNSTRUCT   3
 
 /* tally responses: 0 = fluxResponse, otherwise a macroResponse MT (endfConstants.f90:116-130) */
 #define SG_RESP_FLUX       0
@@ -181,8 +191,12 @@ typedef struct sg_ce_desc {
 
 typedef struct sg_axis_desc {
   int32_t kind;                 /* SG_AXIS_*                    */
-  int32_t n;                    /* number of bins               */
-  double  min, max;             /* lin grid bounds (space axes) */
+  int32_t n;                    /* number of bins (cell axis: of listed cells) */
+  double  min, max;             /* lin / log grid bounds        */
+  int32_t grid;                 /* SG_GRID_* (space and energy axes) */
+  int32_t cell_rest;            /* cell axis: 1 adds bin n+1 for every other place */
+  const double*  bounds;        /* SG_GRID_UNSTRUCT: [n+1] ascending */
+  const int32_t* cells;         /* SG_AXIS_CELL: [n] 0-based cell indices of the geometry */
 } sg_axis_desc;
 
 typedef struct sg_clerk_desc {
@@ -424,7 +438,8 @@ typedef struct sg_batch_tuning {
   int32_t item_histories;       /* histories per work item                                      */
   int32_t blocks_per_sm;        /* persistent grid = SMs x blocks_per_sm (capped by occupancy)  */
   int32_t block_threads;        /* 32, 64, 96 or 128                                            */
-  int32_t order;                /* 0: submission order; 1: largest problem first                */
+  int32_t order;                /* 0: submission order; 1: largest problem first; 2: problems of
+                                   one kind (nesting depth, group count) together, largest first */
 } sg_batch_tuning;
 
 typedef struct sg_batch_stats {

@@ -73,6 +73,7 @@ def lib():
             "or_ce_majorant": (i32, [vp, f64, P(f64)]), "or_ce_union_size": (i32, [vp, P(i64)]),
             "or_asymptotic_scatter": (i32, [f64, f64, f64, P(f64)]),
             "or_target_velocity": (i32, [f64, P(f64), f64, f64, P(u64), P(f64)]),
+            "or_grid_search": (i32, [P(f64), i32, f64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -157,6 +158,11 @@ class Oracle:
         n = C.c_int64()
         self._check(self.L.or_ce_union_size(self.h, C.byref(n)))
         return n.value
+
+    def grid_search(self, bounds, v):
+        """grid%search of an unstructured grid: 1-based bin of `v`, 0 outside."""
+        b, pb = _d(bounds)
+        return self.L.or_grid_search(pb, len(b), float(v))
 
     def upload_tally(self, clerks, batch_size=1, norm_clerk=-1, norm_val=1.0):
         t, arr = abi.tally_struct(clerks, batch_size, norm_clerk, norm_val)

@@ -422,6 +422,7 @@ struct CoordList {
     nesting = 1;
   }
   void takeAboveGeom() { nesting = 1; matIdx = UNDEF_MAT; uniqueID = -3; }   // :283-290
+  int cell() const { return lvl[std::max(nesting, 1) - 1].cellIdx; }          // :419-425
   void moveGlobal(double d) {                                                  // :326-332
     takeAboveGeom();
     for (int i = 0; i < 3; ++i) lvl[0].r[i] = lvl[0].r[i] + d * lvl[0].dir[i];
@@ -1275,7 +1276,7 @@ struct Particle {
   double preHistWgt = 1.0, preCollWgt = 1.0;
   // prePath snapshot used by track clerks
   double prePathR[3] = {0, 0, 0};
-  int prePathMat = 0, prePathG = 1;
+  int prePathMat = 0, prePathG = 1, prePathCell = 0;
   double prePathE = 0.0;
   int matIdx() const { return coords.matIdx; }
 };
@@ -1288,6 +1289,9 @@ struct Clerk {
   int64_t nbins = 1;
   int64_t multi[3] = {1, 1, 1};
   double step[3] = {0, 0, 0};
+  int grid[3] = {0, 0, 0};                // SG_GRID_LIN / LOG / UNSTRUCT
+  std::vector<double> bounds[3];          // unstructured grid bounds
+  std::vector<int> cellBin[3];            // cellMap: bin of every 1-based cell index ([0]: no cell)
   int64_t size() const {
     if (d.type == SG_CLERK_KEFF_ANALOG) return 3;
     if (d.type == SG_CLERK_KEFF_IMPLICIT) return 5;
@@ -1331,26 +1335,44 @@ struct Oracle {
   int64_t nEvents = 0, nColl = 0;
 
   // ----- clerk evaluation helpers (Tallies/TallyMaps, TallyFilters, TallyResponses)
-  int mapState(const Clerk& c, const double r[3], int G, int mat, double E = 0.0, bool isMG = true) const {
+  // binaryFloorIdxClosed_Real (genericProcedures.f90:132-166): 1-based floor index, 0 outside
+  static int binaryFloor(const std::vector<double>& a, double v) {
+    int bottom = 1, top = (int)a.size();
+    if (v < a[bottom - 1] || v > a[top - 1]) return 0;
+    for (int i = 0; i < 70; ++i) {
+      int idx = (top + bottom) / 2;
+      if (bottom == idx) return idx;
+      if (a[idx - 1] <= v) bottom = idx;
+      else top = idx;
+    }
+    return 0;
+  }
+  // grid%search (grid_class.f90:154-175)
+  static int gridSearch(const Clerk& c, int a, double v) {
+    const sg_axis_desc& ax = c.d.axes[a];
+    int idx;
+    if (c.grid[a] == SG_GRID_UNSTRUCT) idx = binaryFloor(c.bounds[a], v);
+    else if (c.grid[a] == SG_GRID_LOG) idx = (int)std::floor(std::log(v / ax.min) / c.step[a]) + 1;
+    else idx = (int)std::floor((v - ax.min) / c.step[a]) + 1;
+    if (idx < 1 || idx >= ax.n + 1) idx = 0;
+    return idx;
+  }
+  int mapState(const Clerk& c, const double r[3], int G, int mat, int cell, double E = 0.0, bool isMG = true) const {
     if (c.d.n_axes == 0) return 1;
     int64_t idx = 1;
     for (int a = 0; a < c.d.n_axes; ++a) {
       const sg_axis_desc& ax = c.d.axes[a];
       int b = 0;
       if (ax.kind >= SG_AXIS_X && ax.kind <= SG_AXIS_Z) {        // spaceMap (spaceMap_class.f90:211-221)
-        double v = r[ax.kind - SG_AXIS_X];
-        b = (int)std::floor((v - ax.min) / c.step[a]) + 1;       // grid%search lin (grid_class.f90:225-245)
-        if (b < 1 || b >= ax.n + 1) b = 0;
+        b = gridSearch(c, a, r[ax.kind - SG_AXIS_X]);
       } else if (ax.kind == SG_AXIS_GROUP) {
         b = (G >= 1 && G <= ax.n) ? G : 0;
       } else if (ax.kind == SG_AXIS_MATERIAL) {
         b = (mat >= 1 && mat <= ax.n) ? mat : 0;
       } else if (ax.kind == SG_AXIS_ENERGY) {                     // energyMap (energyMap_class.f90:278-293)
-        if (isMG) b = 0;
-        else {
-          b = (int)std::floor(std::log(E / ax.min) / c.step[a]) + 1;   // grid%search log (grid_class.f90:164-166)
-          if (b < 1 || b >= ax.n + 1) b = 0;
-        }
+        b = isMG ? 0 : gridSearch(c, a, E);
+      } else if (ax.kind == SG_AXIS_CELL) {                       // cellMap (cellMap_class.f90:198-205)
+        b = c.cellBin[a][cell];
       }
       if (b == 0) return 0;                                       // multiMap (multiMap_class.f90:153-173)
       idx = idx + (int64_t)(b - 1) * c.multi[a];
@@ -1419,7 +1441,7 @@ struct Oracle {
       if (c.d.type == SG_CLERK_COLLISION) {                      // collisionClerk_class.f90:192-242
         if (!c.d.handle_virtual && virt) continue;
         if (!filterPass(c, p.G)) continue;
-        int bin = mapState(c, p.coords.lvl[0].r, p.G, p.matIdx(), p.E, p.isMG);
+        int bin = mapState(c, p.coords.lvl[0].r, p.G, p.matIdx(), p.coords.cell(), p.E, p.isMG);
         if (bin == 0) continue;
         double flux;
         if (c.d.handle_virtual) flux = p.w / trackXS;
@@ -1459,7 +1481,7 @@ struct Oracle {
     for (Clerk& c : A.clerks) {
       if (c.d.type == SG_CLERK_TRACK) {                          // trackClerk_class.f90:185-232
         if (!filterPass(c, p.prePathG)) continue;
-        int bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathE, p.isMG);
+        int bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathCell, p.prePathE, p.isMG);
         if (bin == 0) continue;
         int64_t addr = c.addr + (int64_t)c.width * (bin - 1) - 1;
         for (int i = 0; i < c.width; ++i)
@@ -1487,7 +1509,7 @@ struct Oracle {
         if (leaked) crossed = (u > 0.0) ? (a0 < pl) : (u < 0.0 && a0 >= pl);
         else crossed = (a0 < pl) != (a1 < pl);
         if (!crossed) continue;
-        if (bin == 0) bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathE, p.isMG);
+        if (bin == 0) bin = mapState(c, p.prePathR, p.prePathG, p.prePathMat, p.prePathCell, p.prePathE, p.isMG);
         if (bin == 0) return;
         int dirBin = (leaked ? u > 0.0 : a1 > a0) ? 1 : 0;
         int64_t idx = ((int64_t)k * c.nbins + (bin - 1)) * 2 + dirBin;
@@ -1591,7 +1613,7 @@ struct Oracle {
       if (p.isDead) break;
       double spd = speed(p);                         // timeMax = 0 -> no ageing
       for (int i = 0; i < 3; ++i) p.prePathR[i] = p.coords.lvl[0].r[i];
-      p.prePathMat = p.matIdx(); p.prePathG = p.G; p.prePathE = p.E;
+      p.prePathMat = p.matIdx(); p.prePathG = p.G; p.prePathE = p.E; p.prePathCell = p.coords.cell();
       double u0[3] = {p.coords.lvl[0].dir[0], p.coords.lvl[0].dir[1], p.coords.lvl[0].dir[2]};
       int event;
       geom.move(p.coords, dist, event, useCache ? &cache : nullptr);
@@ -1621,13 +1643,13 @@ struct Oracle {
       double spd = speed(p);
       double x0[3] = {p.coords.lvl[0].r[0], p.coords.lvl[0].r[1], p.coords.lvl[0].r[2]};
       double u0[3] = {p.coords.lvl[0].dir[0], p.coords.lvl[0].dir[1], p.coords.lvl[0].dir[2]};
-      int m0 = p.matIdx();
+      int m0 = p.matIdx(), c0 = p.coords.cell();
       geom.teleport(p.coords, distance);
       p.time = p.time + distance / spd;
       nEvents++;
       int m = p.matIdx();
       for (int i = 0; i < 3; ++i) p.prePathR[i] = x0[i];
-      p.prePathMat = m0; p.prePathG = p.G; p.prePathE = p.E;
+      p.prePathMat = m0; p.prePathG = p.G; p.prePathE = p.E; p.prePathCell = c0;
       reportCurrent(admin, p, x0, p.coords.lvl[0].r, u0, m == OUTSIDE_MAT);
       if (m == OUTSIDE_MAT) { p.fate = LEAK_FATE; p.isDead = true; break; }
       if (m == VOID_MAT) { reportInColl(admin, p, true, trackXS); continue; }
@@ -2083,6 +2105,11 @@ int32_t or_target_velocity(double E, const double* dir, double A, double kT, uin
   return SG_OK;
 }
 
+int32_t or_grid_search(const double* bounds, int32_t nb, double v) {
+  std::vector<double> b(bounds, bounds + nb);
+  return Oracle::binaryFloor(b, v);
+}
+
 int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
   Oracle* o = O(h);
   orc::TallyAdmin A;
@@ -2092,9 +2119,22 @@ int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
     c.width = c.d.n_resp > 0 ? c.d.n_resp : 1;
     int64_t mul = 1;
     for (int a = 0; a < c.d.n_axes; ++a) {
-      c.multi[a] = mul; mul *= c.d.axes[a].n;
-      if (c.d.axes[a].kind <= SG_AXIS_Z) c.step[a] = (c.d.axes[a].max - c.d.axes[a].min) / c.d.axes[a].n;
-      if (c.d.axes[a].kind == SG_AXIS_ENERGY) c.step[a] = std::log(c.d.axes[a].max / c.d.axes[a].min) / c.d.axes[a].n;
+      const sg_axis_desc& ax = c.d.axes[a];
+      int64_t nb = ax.n;
+      c.grid[a] = ax.grid != SG_GRID_DEFAULT ? ax.grid : (ax.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN);
+      if (c.grid[a] == SG_GRID_LOG) c.step[a] = std::log(ax.max / ax.min) / ax.n;   // grid_class.f90:76-90
+      else c.step[a] = (ax.max - ax.min) / ax.n;                                    // grid_class.f90:63-74
+      if (c.grid[a] == SG_GRID_UNSTRUCT && (ax.kind <= SG_AXIS_Z || ax.kind == SG_AXIS_ENERGY))
+        c.bounds[a].assign(ax.bounds, ax.bounds + ax.n + 1);
+      if (ax.kind == SG_AXIS_CELL) {                            // cellMap%build (cellMap_class.f90:87-138)
+        int rest = ax.cell_rest ? ax.n + 1 : 0;
+        c.cellBin[a].assign(o->geom.cells.size() + 1, rest);
+        for (int i = 0; i < ax.n; ++i) c.cellBin[a][ax.cells[i] + 1] = i + 1;
+        if (ax.cell_rest) nb += 1;
+      }
+      c.d.axes[a].bounds = nullptr;                             // the caller's arrays are not kept
+      c.d.axes[a].cells = nullptr;
+      c.multi[a] = mul; mul *= nb;
     }
     c.nbins = mul;
     c.addr = memLoc;

@@ -30,7 +30,9 @@ TRANSPORT_ST, TRANSPORT_DT, TRANSPORT_ST_NOCACHE, TRANSPORT_HT, TRANSPORT_HT_NOC
 CLERK_COLLISION, CLERK_TRACK, CLERK_KEFF_ANALOG, CLERK_KEFF_IMPLICIT = 1, 2, 3, 4
 CLERK_SURFACE_CURRENT = 5
 # map axes
-AXIS_X, AXIS_Y, AXIS_Z, AXIS_GROUP, AXIS_MATERIAL, AXIS_ENERGY = 1, 2, 3, 4, 5, 6
+AXIS_X, AXIS_Y, AXIS_Z, AXIS_GROUP, AXIS_MATERIAL, AXIS_ENERGY, AXIS_CELL = 1, 2, 3, 4, 5, 6, 7
+# grids of space and energy axes (grid_class.f90): default = lin for space, log for energy
+GRID_DEFAULT, GRID_LIN, GRID_LOG, GRID_UNSTRUCT = 0, 1, 2, 3
 # responses (macro MTs from SharedModules/endfConstants.f90:116-130)
 RESP_FLUX = 0
 MACRO_TOTAL, MACRO_CAPTURE, MACRO_FISSION, MACRO_NUFISSION, MACRO_ABSORPTION = -1, -2, -6, -7, -21
@@ -59,7 +61,8 @@ class MGDesc(C.Structure):
 
 
 class AxisDesc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("n", C.c_int32), ("min", C.c_double), ("max", C.c_double)]
+    _fields_ = [("kind", C.c_int32), ("n", C.c_int32), ("min", C.c_double), ("max", C.c_double),
+                ("grid", C.c_int32), ("cell_rest", C.c_int32), ("bounds", f64p), ("cells", i32p)]
 
 
 class ClerkDesc(C.Structure):
@@ -249,8 +252,28 @@ def mg_struct(m):
     return s, keep
 
 
+def unstruct_axis(kind, bounds):
+    """A spaceMap / energyMap axis on an unstructured grid of ascending bounds (grid 'unstruct')."""
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    return {"kind": kind, "n": len(b) - 1, "grid": GRID_UNSTRUCT, "bounds": b}
+
+
+def cell_axis(cells, undef_bin=False):
+    """A cellMap axis over 0-based cell indices of the geometry; `undef_bin` adds the rest bin."""
+    c = np.ascontiguousarray(cells, dtype=np.int32)
+    return {"kind": AXIS_CELL, "n": len(c), "cells": c, "cell_rest": 1 if undef_bin else 0}
+
+
+def axis_bins(ax):
+    """Bins of one axis given to clerk()."""
+    if isinstance(ax, dict):
+        return ax["n"] + (1 if ax.get("cell_rest") else 0)
+    return ax[1]
+
+
 def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None, current_axis=0, planes=()):
-    """Describe one tally clerk; axes = [(kind, n, min, max), ...] (multiMap order).
+    """Describe one tally clerk; axes in multiMap order, each (kind, n, min, max[, grid]) or a dict
+    from unstruct_axis() / cell_axis().
 
     Surface-current clerks take the normal axis (AXIS_X/Y/Z) and up to 8 plane positions."""
     c = ClerkDesc()
@@ -260,8 +283,23 @@ def clerk(type_, resp=(RESP_FLUX,), axes=(), handle_virtual=1, g_filter=None, cu
     for i, r in enumerate(resp):
         c.resp[i] = r
     c.n_axes = len(axes)
-    for i, (k, n, lo, hi) in enumerate(axes):
-        c.axes[i].kind, c.axes[i].n, c.axes[i].min, c.axes[i].max = k, n, lo, hi
+    keep = []
+    for i, ax in enumerate(axes):
+        d = c.axes[i]
+        if isinstance(ax, dict):
+            d.kind, d.n = ax["kind"], ax["n"]
+            d.min, d.max = ax.get("min", 0.0), ax.get("max", 0.0)
+            d.grid, d.cell_rest = ax.get("grid", GRID_DEFAULT), ax.get("cell_rest", 0)
+            if ax.get("bounds") is not None:
+                keep.append(ax["bounds"])
+                d.bounds = ax["bounds"].ctypes.data_as(f64p)
+            if ax.get("cells") is not None:
+                keep.append(ax["cells"])
+                d.cells = ax["cells"].ctypes.data_as(i32p)
+        else:
+            d.kind, d.n, d.min, d.max = ax[:4]
+            d.grid = ax[4] if len(ax) > 4 else GRID_DEFAULT
+    c._keep = keep
     if g_filter is not None:
         c.filter_g_top, c.filter_g_low = g_filter
     c.current_axis = current_axis

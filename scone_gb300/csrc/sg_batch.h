@@ -97,6 +97,7 @@ struct StagedProblem {
   bool any_fissile;
   std::vector<sg_clerk_desc> clerks;   // the admin's clerks and their 1-based addresses
   std::vector<long long> addr;
+  std::vector<const void*> tab64, tab32;   // map tables in the problem's block, [3 * clerk + axis]
 };
 int stage_problem(const sg_geometry_desc* g, const sg_mg_desc* mg, const sg_point_source_desc* src,
                   const sg_tally_desc* tally, char* dev, std::vector<char>* host, size_t cap, size_t* bytes,

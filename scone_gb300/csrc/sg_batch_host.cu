@@ -608,7 +608,7 @@ int32_t sg_batch_memory(sg_batch b, int64_t* used, int64_t* capacity) {
 int32_t sg_batch_set_tuning(sg_batch b, const sg_batch_tuning* t) {
   if (!b || !t) return SG_ERR_BAD_ARG;
   if (t->item_histories < 32 || t->block_threads < 32 || t->block_threads > 128 || t->block_threads % 32 ||
-      t->blocks_per_sm < 0 || t->order < 0 || t->order > 1)
+      t->blocks_per_sm < 0 || t->order < 0 || t->order > 2)
     return b->fail(SG_ERR_BAD_ARG, "batch: bad tuning");
   b->tune = *t;
   return SG_OK;
@@ -636,9 +636,15 @@ int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats
     maxl = std::max(maxl, b->slots[s].sp.maxl);
     hist += (long long)b->slots[s].pop * b->slots[s].cycles;
   }
+  auto size_of = [&](int x) { return (long long)b->slots[x].pop * b->slots[x].cycles; };
   if (b->tune.order == 1)
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return size_of(x) > size_of(y); });
+  else if (b->tune.order == 2)      // problems of one kind together (nesting, group count), largest first
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-      return (long long)b->slots[x].pop * b->slots[x].cycles > (long long)b->slots[y].pop * b->slots[y].cycles;
+      const Slot &X = b->slots[x], &Y = b->slots[y];
+      if (X.sp.maxl != Y.sp.maxl) return X.sp.maxl < Y.sp.maxl;
+      if (X.sp.t64.mg.nG != Y.sp.t64.mg.nG) return X.sp.t64.mg.nG < Y.sp.t64.mg.nG;
+      return size_of(x) > size_of(y);
     });
   std::vector<WorkItem> items;
   for (int s : order) cut_items(items, s, 0, (long long)b->slots[s].pop * b->slots[s].cycles, b->tune.item_histories);
@@ -764,7 +770,7 @@ int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_
                               : batch_occupancy<float>(maxl, dt, cur.block_threads);
       for (int v = std::max(1, occ / 2); v <= occ; ++v) { sg_batch_tuning t = cur; t.blocks_per_sm = v; cands.push_back(t); }
     }
-    if (pass == 3) for (int v = 0; v <= 1; ++v) { sg_batch_tuning t = cur; t.order = v; cands.push_back(t); }
+    if (pass == 3) for (int v = 0; v <= 2; ++v) { sg_batch_tuning t = cur; t.order = v; cands.push_back(t); }
     for (const auto& t : cands) {
       if (std::memcmp(&t, &cur, sizeof(t)) == 0) continue;
       double ms = 0.0;

@@ -115,6 +115,9 @@ struct Admin {
   double normVal = 1.0;
   int atch = -1;
   long long keffAnalog = -1, keffImplicit = -1;   // 0-based admin-relative addresses
+  // per clerk and axis ([3 * clerk + axis]): device table of an unstructured grid (FP64 and FP32
+  // copies) or of a cell axis (int, both entries), null otherwise
+  std::vector<const void*> tab64, tab32;
   bool lastCycle() const { return (cycles + 1) % batchSize == 0; }
 };
 
@@ -162,6 +165,10 @@ struct sg_handle_t {
 
   // tallies
   std::vector<Admin> admins;
+  std::vector<DArr<double>> mapTab64;   // map tables of the admins (unstructured bounds, cell bins)
+  std::vector<DArr<float>> mapTab32;
+  std::vector<DArr<int>> mapTabCell;
+  int nCell = 0;                        // cells of the uploaded geometry
   long long totalBins = 0;
   DArr<double> acc, bin, csum, csum2;
 
@@ -215,8 +222,6 @@ struct sg_handle_t {
 };
 
 namespace {
-
-int check_handle(sg_handle h) { return h ? SG_OK : SG_ERR_BAD_ARG; }
 
 unsigned long long rng_stride(unsigned long long s, long long n) { return lcg_skip(s, 152917LL * n); }
 
@@ -559,6 +564,7 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
                  h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0, cx};
   h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
                  h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs, cx};
+  h->nCell = g->n_cell;
   h->hasGeom = true;
   // active materials for the majorant
   return SG_OK;
@@ -865,6 +871,11 @@ DSites site_view(sg_handle h) {
   return DSites{h->sR.p, h->sDir.p, h->sWgt.p, h->sG.p, h->sBrood.p, h->sSeq.p, h->sTime.p, h->sCursor.p, h->regionCap};
 }
 
+// Bins of one map axis: cellMap has n cells plus the `undefBin` rest bin (cellMap_class.f90:129-136)
+long long axis_bins(const sg_axis_desc& x) {
+  return x.kind == SG_AXIS_CELL ? (long long)x.n + (x.cell_rest ? 1 : 0) : x.n;
+}
+
 // clerks of admin `a` and its attachment flattened for one launch (attachment first)
 template <class R>
 int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long long& hi) {
@@ -886,6 +897,7 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
   t.n_clerks = 0;
   t.keff_clerk = -1;
   t.has_current = 0;
+  t.has_cellmap = 0;
   for (int x : chain) {
     const Admin& A = h->admins[x];
     for (size_t c = 0; c < A.clerks.size(); ++c) {
@@ -901,17 +913,23 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
       K.n_axes = d.n_axes;
       long long mul = 1;
       for (int i = 0; i < d.n_axes; ++i) {
-        K.ax_kind[i] = d.axes[i].kind;
-        K.ax_n[i] = d.axes[i].n;
-        K.ax_min[i] = d.axes[i].min;
-        if (d.axes[i].kind == SG_AXIS_ENERGY)          // grid log step (grid_class.f90:76-90)
-          K.ax_step[i] = std::log(d.axes[i].max / d.axes[i].min) / d.axes[i].n;
-        else K.ax_step[i] = (d.axes[i].max - d.axes[i].min) / d.axes[i].n;
+        const sg_axis_desc& x = d.axes[i];
+        K.ax_kind[i] = x.kind;
+        K.ax_n[i] = x.n;
+        K.ax_min[i] = x.min;
+        int grid = x.grid;
+        if (grid == SG_GRID_DEFAULT) grid = x.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN;
+        K.ax_grid[i] = grid;
+        if (grid == SG_GRID_LOG)                       // grid step (grid_class.f90:60-90)
+          K.ax_step[i] = std::log(x.max / x.min) / x.n;
+        else K.ax_step[i] = (x.max - x.min) / x.n;
         K.ax_inv_step[i] = 1.0 / K.ax_step[i];
         K.ax_minf[i] = (float)K.ax_min[i];
         K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
+        K.ax_tab[i] = (sizeof(R) == 8 ? A.tab64 : A.tab32)[3 * c + i];
+        if (x.kind == SG_AXIS_CELL) t.has_cellmap = 1;
         K.multi[i] = mul;
-        mul *= d.axes[i].n;
+        mul *= axis_bins(x);
       }
       K.g_top = d.filter_g_top;
       K.g_low = d.filter_g_low;
@@ -1179,6 +1197,53 @@ int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
   return SG_OK;
 }
 
+// Checks one map axis and uploads its table: the bounds of an unstructured grid (grid%init_unstruct,
+// grid_class.f90:100-113: sorted, at least 2 bounds) or the bin of every cell for a cellMap
+// (cellMap%build, cellMap_class.f90:87-138: listed cells take bins 1..n in order, every other cell
+// and the places outside any cellUniverse take the rest bin n+1 or none).
+int build_axis(sg_handle h, const sg_axis_desc& x, Admin& A) {
+  const void *t64 = nullptr, *t32 = nullptr;
+  if (x.n < 1 || x.kind < SG_AXIS_X || x.kind > SG_AXIS_CELL) return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
+  if (x.kind <= SG_AXIS_Z || x.kind == SG_AXIS_ENERGY) {
+    const bool energy = x.kind == SG_AXIS_ENERGY;
+    const int grid = x.grid == SG_GRID_DEFAULT ? (energy ? SG_GRID_LOG : SG_GRID_LIN) : x.grid;
+    if (!energy && grid == SG_GRID_LOG) return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap grids are lin or unstruct");
+    if (grid == SG_GRID_LIN) {
+      if (!(x.max > x.min)) return h->fail(SG_ERR_BAD_ARG, "tally: lin grid needs max > min");
+    } else if (grid == SG_GRID_LOG) {
+      if (!(x.min > 0.0 && x.max > x.min)) return h->fail(SG_ERR_BAD_ARG, "tally: log grid needs 0 < min < max");
+    } else if (grid == SG_GRID_UNSTRUCT) {
+      if (!x.bounds) return h->fail(SG_ERR_BAD_ARG, "tally: unstructured grid without bounds");
+      std::vector<double> b(x.bounds, x.bounds + x.n + 1);
+      for (int i = 0; i < x.n; ++i)
+        if (!(b[i] <= b[i + 1])) return h->fail(SG_ERR_BAD_ARG, "tally: unstructured grid is not sorted");
+      std::vector<float> f(b.begin(), b.end());
+      h->mapTab64.emplace_back();
+      h->mapTab32.emplace_back();
+      if (h->mapTab64.back().upload(b, h->stream) != cudaSuccess || h->mapTab32.back().upload(f, h->stream) != cudaSuccess)
+        return h->fail(SG_ERR_OOM, "tally: grid table");
+      t64 = h->mapTab64.back().p;
+      t32 = h->mapTab32.back().p;
+    } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown grid type");
+  } else if (x.kind == SG_AXIS_CELL) {
+    if (!h->hasGeom) return h->fail(SG_ERR_STATE, "tally: a cellMap needs the geometry uploaded first");
+    if (!x.cells) return h->fail(SG_ERR_BAD_ARG, "tally: cellMap without cells");
+    std::vector<int> bin(h->nCell + 1, x.cell_rest ? x.n + 1 : 0);
+    bin[0] = x.cell_rest ? x.n + 1 : 0;
+    for (int i = 0; i < x.n; ++i) {
+      const int c = x.cells[i];
+      if (c < 0 || c >= h->nCell) return h->fail(SG_ERR_BAD_ARG, "tally: cellMap names a cell the geometry lacks");
+      bin[c + 1] = i + 1;     // a cell listed twice keeps its last bin (intMap%add replaces)
+    }
+    h->mapTabCell.emplace_back();
+    if (h->mapTabCell.back().upload(bin, h->stream) != cudaSuccess) return h->fail(SG_ERR_OOM, "tally: cell table");
+    t64 = t32 = h->mapTabCell.back().p;
+  }
+  A.tab64.push_back(t64);
+  A.tab32.push_back(t32);
+  return SG_OK;
+}
+
 // tallyAdmin%init (tallyAdmin_class.f90:162-255): clerk validation and scoreMemory layout of one admin
 int build_admin(sg_handle h, const sg_tally_desc* t, Admin& A) {
   long long loc = 1;
@@ -1194,16 +1259,15 @@ int build_admin(sg_handle h, const sg_tally_desc* t, Admin& A) {
         return h->fail(SG_ERR_BAD_ARG, "tally: surface-current clerk needs an axis and 1-8 planes");
       long long nb = 1;
       for (int a = 0; a < d.n_axes; ++a) {
-        if (d.axes[a].n < 1 || d.axes[a].kind < SG_AXIS_X || d.axes[a].kind > SG_AXIS_ENERGY)
-          return h->fail(SG_ERR_BAD_ARG, "tally: bad map axis");
-        if (d.axes[a].kind <= SG_AXIS_Z && !(d.axes[a].max > d.axes[a].min))
-          return h->fail(SG_ERR_BAD_ARG, "tally: spaceMap needs max > min");
-        if (d.axes[a].kind == SG_AXIS_ENERGY && !(d.axes[a].min > 0.0 && d.axes[a].max > d.axes[a].min))
-          return h->fail(SG_ERR_BAD_ARG, "tally: log energy grid needs 0 < min < max");
-        nb *= d.axes[a].n;
+        const int rc = build_axis(h, d.axes[a], A);
+        if (rc) return rc;
+        nb *= axis_bins(d.axes[a]);
       }
+      for (int a = d.n_axes; a < 3; ++a) { A.tab64.push_back(nullptr); A.tab32.push_back(nullptr); }
       size = cur ? nb * d.n_planes * 2 : nb * d.n_resp;
     } else return h->fail(SG_ERR_BAD_ARG, "tally: unknown clerk type");
+    if (A.tab64.size() < 3 * (A.clerks.size() + 1))
+      for (int a = 0; a < 3; ++a) { A.tab64.push_back(nullptr); A.tab32.push_back(nullptr); }
     A.clerks.push_back(d);
     A.addr.push_back(loc);
     loc += size;
@@ -1306,6 +1370,8 @@ int sg::stage_problem(const sg_geometry_desc* g, const sg_mg_desc* mg, const sg_
   out->any_fissile = H.anyFissile;
   out->clerks = A.clerks;
   out->addr = A.addr;
+  out->tab64 = A.tab64;
+  out->tab32 = A.tab32;
   return SG_OK;
 }
 
@@ -1350,6 +1416,8 @@ int sg::plain_fixed_source(sg_handle h, const StagedProblem& p, const sg_point_s
   Admin A;
   A.clerks = p.clerks;
   A.addr = p.addr;
+  A.tab64 = p.tab64;
+  A.tab32 = p.tab32;
   A.N = p.n_bins;
   A.off = 0;
   A.normAddr = p.norm_addr >= 0 ? p.norm_addr + 1 : -1;
@@ -1426,6 +1494,9 @@ int32_t sg_destroy(sg_handle h) {
   h->ceMaj64.free(); h->ceXsF.free(); h->ceAF.free(); h->ceKTF.free(); h->ceDensF.free(); h->ceMajF.free();
   h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
   h->pE.free();
+  for (auto& a : h->mapTab64) a.free();
+  for (auto& a : h->mapTab32) a.free();
+  for (auto& a : h->mapTabCell) a.free();
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   cudaStreamDestroy(h->stream);
   delete h;
@@ -1520,6 +1591,9 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
   int rc = h2d_bank(h, in, n, A);
   if (rc) return rc;
   CK(cudaMemcpyAsync(h->scal.p + 0, &k_eff, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  // popWeight of the bank given (particleDungeon_class.f90:358-375), summed on the device
+  CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, h->stream));
+  h->launches += 2;
   int S = 0;
   sg_cycle_stats st{};
   rc = gen_loop(h, admin, A, n, master_state, h->scal.p + 0, B, h->cap, &S, &st);
@@ -1527,6 +1601,8 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
   h->eigenReady = false;   // the resident banks were overwritten
   if (next && S > 0) {
     if (S > next_cap) return h->fail(SG_ERR_BANK_OVERFLOW, "next bank capacity too small");
+    CK(deterministic_sum(B.wgt, S, h->sumPart.p, h->scal.p + 3, h->stream));
+    h->launches += 2;
     rc = d2h_bank(h, B, S, next);
     if (rc) return rc;
   }
@@ -1535,16 +1611,15 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
   float cyc = 0.f;
   CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
   if (stats) {
+    double w[2] = {0.0, 0.0};
+    CK(cudaMemcpy(w, h->scal.p + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost));
     *stats = st;
     stats->cycle_ms = cyc;
     stats->n_kernels = h->launches;
     stats->k_eff = k_eff;
     stats->k_new = k_eff;
-    double sw = 0, ew = 0;
-    if (in->wgt) for (int i = 0; i < n; ++i) sw += in->wgt[i]; else sw = n;
-    if (next && next->wgt) for (int i = 0; i < S && i < next_cap; ++i) ew += next->wgt[i];
-    stats->start_weight = sw;
-    stats->end_weight = ew;
+    stats->start_weight = n > 0 ? w[0] : 0.0;
+    stats->end_weight = (next && S > 0) ? w[1] : 0.0;
   }
   return SG_OK;
 }

@@ -137,6 +137,9 @@ struct DClerk {
   int cur_axis;          // surface-current clerk: 0..2 normal of the planes
   int n_planes;
   double planes[8];
+  int ax_grid[3];        // SG_GRID_LIN / LOG / UNSTRUCT of space and energy axes
+  const void* ax_tab[3]; // unstructured grid: n+1 bounds (double in the FP64 form, float in the mixed
+                         // form); cell axis: int bin of every global cell index + 1 ([0]: no cell)
 };
 
 static constexpr int MAX_CLERKS = 8;
@@ -228,6 +231,7 @@ struct TransportArgs {
   int n_clerks;
   int keff_clerk;       // index of the keff-implicit clerk (accumulated in registers), -1 if none
   int has_current;      // a surface-current clerk is present
+  int has_cellmap;      // some clerk maps by cell
   double* acc;          // tally accumulators of the launch (global)
   int acc_n;
   int use_smem;         // accumulate map clerks in shared memory

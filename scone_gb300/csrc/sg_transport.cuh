@@ -148,27 +148,60 @@ struct Tracker {
     else return macro(mat, g, code);
   }
 
-  // multiMap of spaceMap / group / material axes (multiMap_class.f90:153-173, grid_class.f90:225-245)
-  __device__ __forceinline__ int map_bin(const DClerk& K, const double r[3], int g, int mat) const {
-    return map_bin_e(K, r, g, mat, E);
+  // the cell the particle is in at its lowest level, as a 1-based index of the geometry's cells; 0
+  // when that level is not a cellUniverse (coord%cell, coord_class.f90:419-425)
+  __device__ __forceinline__ int lowest_cell() const {
+    const int l = c.nest - 1;
+    const DUni& U = geom.g.unis[c.uni[l]];
+    if (U.type != SG_UNI_CELL || c.local[l] > U.i[1]) return 0;   // local n+1: no cell of the universe
+    return geom.g.uni_cells[U.i[0] + c.local[l] - 1] + 1;
   }
-  __device__ __forceinline__ int map_bin_e(const DClerk& K, const double r[3], int g, int mat, double En) const {
+
+  // binaryFloorIdxClosed (genericProcedures.f90:132-166) on an unstructured grid of nb ascending
+  // bounds, as grid%search (grid_class.f90:154-175): 1-based bin, 0 outside
+  template <class T>
+  __device__ __forceinline__ static int grid_floor(const T* a, int nb, T v) {
+    if (!(v >= a[0] && v <= a[nb - 1])) return 0;
+    int lo = 0, hi = nb - 1;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (a[mid] <= v) lo = mid;
+      else hi = mid;
+    }
+    return lo + 1;
+  }
+
+  // multiMap (multiMap_class.f90:153-173) of spaceMap / energyMap (lin, log and unstructured grids,
+  // grid_class.f90:154-175) / group / material / cell axes; `cell` from lowest_cell()
+  __device__ __forceinline__ int map_bin(const DClerk& K, const double r[3], int g, int mat, int cell) const {
+    return map_bin_e(K, r, g, mat, cell, E);
+  }
+  __device__ __forceinline__ int map_bin_e(const DClerk& K, const double r[3], int g, int mat, int cell,
+                                           double En) const {
     long long idx = 1;
     for (int a = 0; a < K.n_axes; ++a) {
       int b = 0;
-      int kind = K.ax_kind[a];
-      if (kind <= SG_AXIS_Z) {
-        double v = at3(r, kind - 1);
-        if constexpr (sizeof(R) == 8) b = (int)floor((v - K.ax_min[a]) / K.ax_step[a]) + 1;
-        else b = (int)floorf(((float)v - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;
+      const int kind = K.ax_kind[a];
+      if (kind <= SG_AXIS_Z || kind == SG_AXIS_ENERGY) {
+        if (kind == SG_AXIS_ENERGY && !CE) return 0;     // energyMap of an MG particle
+        const double v = (kind == SG_AXIS_ENERGY) ? En : at3(r, kind - 1);
+        const int grid = K.ax_grid[a];
+        if (grid == SG_GRID_UNSTRUCT) {
+          if constexpr (sizeof(R) == 8) b = grid_floor<double>((const double*)K.ax_tab[a], K.ax_n[a] + 1, v);
+          else b = grid_floor<float>((const float*)K.ax_tab[a], K.ax_n[a] + 1, (float)v);
+        } else if (grid == SG_GRID_LOG) {
+          if (!(v > 0.0)) return 0;
+          if constexpr (sizeof(R) == 8) b = (int)floor(log(v / K.ax_min[a]) / K.ax_step[a]) + 1;
+          else b = (int)floorf(__logf((float)(v / K.ax_min[a])) * K.ax_inv_stepf[a]) + 1;
+        } else {
+          if constexpr (sizeof(R) == 8) b = (int)floor((v - K.ax_min[a]) / K.ax_step[a]) + 1;
+          else b = (int)floorf(((float)v - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;
+        }
         if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
       } else if (kind == SG_AXIS_GROUP) {
         b = (CE ? 0 : ((g >= 1 && g <= K.ax_n[a]) ? g : 0));
-      } else if (kind == SG_AXIS_ENERGY) {            // energyMap log grid (grid_class.f90:164-166)
-        if constexpr (!CE) b = 0;
-        else if constexpr (sizeof(R) == 8) b = (int)floor(log(En / K.ax_min[a]) / K.ax_step[a]) + 1;
-        else b = (int)floorf(__logf((float)(En / K.ax_min[a])) * K.ax_inv_stepf[a]) + 1;
-        if (b < 1 || b >= K.ax_n[a] + 1) b = 0;
+      } else if (kind == SG_AXIS_CELL) {
+        b = ((const int*)K.ax_tab[a])[cell];
       } else {
         b = (mat >= 1 && mat <= K.ax_n[a]) ? mat : 0;
       }
@@ -183,12 +216,13 @@ struct Tracker {
   // tallyAdmin%reportInColl -> collisionClerk (collisionClerk_class.f90:192-242) and
   // keffImplicitClerk (keffImplicitClerk_class.f90:180-227)
   __device__ __forceinline__ void report_in_coll(bool virt, R trackXS) {
+    const int cell = A.has_cellmap ? lowest_cell() : 0;
     for (int k = 0; k < A.n_clerks; ++k) {
       const DClerk& K = A.clerks[k];
       if (K.type == SG_CLERK_COLLISION) {
         if (!K.handle_virtual && virt) continue;
         if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
-        int bin = map_bin(K, c.r0, G, c.mat);
+        int bin = map_bin(K, c.r0, G, c.mat, cell);
         if (bin == 0) continue;
         R flux;
         if (K.handle_virtual) flux = w / trackXS;
@@ -209,12 +243,12 @@ struct Tracker {
     }
   }
   // trackClerk%reportPath (trackClerk_class.f90:185-232): pre-path position and material
-  __device__ __forceinline__ void report_path(const double rpre[3], int matPre, R L) {
+  __device__ __forceinline__ void report_path(const double rpre[3], int matPre, int cellPre, R L) {
     for (int k = 0; k < A.n_clerks; ++k) {
       const DClerk& K = A.clerks[k];
       if (K.type != SG_CLERK_TRACK) continue;
       if (K.g_top > 0 && !(K.g_top <= G && G <= K.g_low)) continue;
-      int bin = map_bin(K, rpre, G, matPre);
+      int bin = map_bin(K, rpre, G, matPre, cellPre);
       if (bin == 0) continue;
       long long at = K.acc_off + (long long)K.width * (bin - 1);
       for (int i = 0; i < K.width; ++i) score(at + i, (double)(response(K.resp[i], matPre, G) * w * L));
@@ -224,7 +258,8 @@ struct Tracker {
   // Surface-current clerk (no SCONE counterpart): each tally plane crossed by the flight from rpre
   // to the current position scores the weight in [plane][bin of the pre-flight state][direction].
   // Side of a plane: coordinate < plane.  A leaking flight crosses every plane ahead of rpre.
-  __device__ __forceinline__ void report_current(const double rpre[3], int matPre, const R u0[3], bool leaked) {
+  __device__ __forceinline__ void report_current(const double rpre[3], int matPre, int cellPre, const R u0[3],
+                                                 bool leaked) {
     for (int k = 0; k < A.n_clerks; ++k) {
       const DClerk& K = A.clerks[k];
       if (K.type != SG_CLERK_SURFACE_CURRENT) continue;
@@ -235,7 +270,7 @@ struct Tracker {
         const double pl = K.planes[q];
         const bool crossed = leaked ? ((u > R(0)) ? (a0 < pl) : (u < R(0) && a0 >= pl)) : ((a0 < pl) != (a1 < pl));
         if (!crossed) continue;
-        if (bin < 0) bin = map_bin(K, rpre, G, matPre);
+        if (bin < 0) bin = map_bin(K, rpre, G, matPre, cellPre);
         if (bin == 0) break;
         const int dirBin = (leaked ? (u > R(0)) : (a1 > a0)) ? 1 : 0;
         score(K.acc_off + ((long long)q * K.nbins + (bin - 1)) * 2 + dirBin, (double)w);
@@ -540,13 +575,14 @@ struct Tracker {
       const double rpre[3] = {c.r0[0], c.r0[1], c.r0[2]};
       const R u0[3] = {c.u[0], c.u[1], c.u[2]};
       const int matPre = mat;
+      const int cellPre = A.has_cellmap ? lowest_cell() : 0;
       const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0);
       if constexpr (CE) time = time + dist * invSpeed;
       else time = time + dist;
       nEv += 1;
-      report_path(rpre, matPre, dist);
+      report_path(rpre, matPre, cellPre, dist);
       mat = c.mat;
-      if (A.has_current) report_current(rpre, matPre, u0, mat == 0);
+      if (A.has_current) report_current(rpre, matPre, cellPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
@@ -580,12 +616,13 @@ struct Tracker {
         for (int i = 0; i < 3; ++i) { rpre[i] = c.r0[i]; u0[i] = c.u[i]; }
       }
       const int matPre = mat;
+      const int cellPre = (A.has_cellmap && A.has_current) ? lowest_cell() : 0;
       if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return SEG_END; }
       if constexpr (CE) time = time + dist * invSpeed;
       else time = time + dist;
       nEv += 1;
       mat = c.mat;
-      if (A.has_current) report_current(rpre, matPre, u0, mat == 0);
+      if (A.has_current) report_current(rpre, matPre, cellPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return SEG_MORE; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {

@@ -283,3 +283,67 @@ def test_file_source_cycles_match_oracle(gpu_mod, oracle_mod, form, tmp_path):
         res.append((m, t.bins(a)))
     assert res[0][0] == res[1][0]
     np.testing.assert_allclose(res[0][1], res[1][1], rtol=1e-10, atol=0)
+
+
+def _map_clerks():
+    """Collision and track clerks over the unionCell spheres binned by cell (with and without the
+    rest bin), by x on an unstructured grid and on a lin grid."""
+    C_, T_ = abi.CLERK_COLLISION, abi.CLERK_TRACK
+    xb = np.array([-6.0, -2.5, -0.3, 0.0, 1.0, 3.3, 6.0])
+    return [
+        abi.clerk(C_, axes=[abi.cell_axis([1, 0]), (abi.AXIS_GROUP, 2, 0.0, 0.0)]),
+        abi.clerk(T_, axes=[abi.cell_axis([0], undef_bin=True), abi.unstruct_axis(abi.AXIS_X, xb)]),
+        abi.clerk(C_, axes=[abi.unstruct_axis(abi.AXIS_X, xb), (abi.AXIS_Y, 3, -6.0, 6.0, abi.GRID_LIN)]),
+        abi.clerk(T_, resp=(abi.RESP_FLUX, abi.MACRO_TOTAL), axes=[abi.cell_axis([1])]),
+    ]
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_cell_and_grid_maps_fp64_parity(gpu_mod, oracle_mod, transport, form):
+    """cellMap and unstructured / lin grids on the device against the oracle: equal tallies."""
+    p = problems.union_cell_slab()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
+    n = 20000
+    bank = o.generate_source(SEED, n)
+    clerks = _map_clerks()
+    ag, ao = g.upload_tally(clerks), o.upload_tally(clerks)
+    g.transport_bank(ag, bank, 24680)
+    o.transport_bank(ao, bank, 24680)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co) and np.array_equal(rg, ro)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    bg, bo = g.bins(ag), o.bins(ao)
+    assert bg[:4, 1].min() > 0
+    np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=0)
+
+
+def test_cell_and_grid_maps_mixed(gpu_mod, oracle_mod):
+    """The mixed form (FP32 grid search) on the same maps: within 3 % of the FP64 form per bin of
+    the cell map and the total of the unstructured grid."""
+    p = problems.union_cell_slab()
+    out = {}
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        g = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_ST, max_bank=1 << 18)
+        a = g.upload_tally(_map_clerks())
+        g.fixed_source_cycle(a, 200000, 777)
+        out[prec] = g.bins(a)[:, 1]
+        g.close()
+    f, m = out[abi.PREC_FP64], out[abi.PREC_MIXED]
+    np.testing.assert_allclose(m[:4], f[:4], rtol=0.03)
+    np.testing.assert_allclose(m.sum(), f.sum(), rtol=0.03)
+
+
+def test_bad_map_axes_are_rejected(gpu_mod):
+    p = problems.union_cell_slab()
+    g = gpu_mod.TransportOperatorGPU(p, max_bank=16)
+    C_ = abi.CLERK_COLLISION
+    for ax, msg in [(abi.unstruct_axis(abi.AXIS_X, [0.0, 2.0, 1.0]), "not sorted"),
+                    (abi.cell_axis([5]), "lacks"),
+                    ((abi.AXIS_X, 4, 0.0, 1.0, abi.GRID_LOG), "lin or unstruct"),
+                    ((abi.AXIS_ENERGY, 4, 0.0, 1.0, abi.GRID_LOG), "0 < min")]:
+        with pytest.raises(gpu_mod.SconeGpuError, match=msg):
+            g.upload_tally([abi.clerk(C_, axes=[ax])])
+    g.close()

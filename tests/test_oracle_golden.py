@@ -500,3 +500,49 @@ def test_union_cell_rejects_bad_definitions(oracle_mod):
         o = oracle_mod.Oracle()
         with pytest.raises(RuntimeError):
             o.upload_geometry(g)
+
+
+def _map_tallies(extra_x=None):
+    """Collision clerks over the unionCell spheres: by material, by cell (cells listed in the
+    materials' order), by the first cell with the `undefBin` rest bin, a lin x grid and the same x
+    grid given as unstructured bounds."""
+    step = 12.0 / 8
+    bounds = np.array([-6.0 + i * step for i in range(9)])     # grid%init lin: min + (i - 1) step
+    C_ = abi.CLERK_COLLISION
+    return [
+        abi.clerk(C_, axes=[(abi.AXIS_MATERIAL, 2, 0.0, 0.0), (abi.AXIS_GROUP, 2, 0.0, 0.0)]),
+        abi.clerk(C_, axes=[abi.cell_axis([0, 1]), (abi.AXIS_GROUP, 2, 0.0, 0.0)]),
+        abi.clerk(C_, axes=[abi.cell_axis([0], undef_bin=True)]),
+        abi.clerk(C_, axes=[(abi.AXIS_X, 8, -6.0, 6.0)]),
+        abi.clerk(C_, axes=[abi.unstruct_axis(abi.AXIS_X, bounds)]),
+    ]
+
+
+def test_cell_and_unstructured_maps(oracle_mod):
+    """cellMap (Tallies/TallyMaps/Maps1D/cellMap_class.f90) and unstructured grids
+    (SharedModules/grid_class.f90 `unstruct`, binaryFloorIdxClosed): a cell map over cells that hold
+    one material each equals the material map; the rest bin holds what the listed cells do not; an
+    unstructured grid with the bounds of a lin grid bins like the lin grid."""
+    p = problems.union_cell_slab()
+    o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_ST)
+    clerks = _map_tallies()
+    a = o.upload_tally(clerks)
+    o.fixed_source_cycle(a, 20000, 4242)
+    b = o.bins(a)[:, 1]
+    mat, cell, rest, lin, uns = b[0:4], b[4:8], b[8:10], b[10:18], b[18:26]
+    assert mat.min() > 0
+    np.testing.assert_array_equal(cell, mat)
+    # material axis fastest: mat = [m1 g1, m2 g1, m1 g2, m2 g2]; rest bin = the other cell
+    np.testing.assert_allclose(rest, [mat[0] + mat[2], mat[1] + mat[3]], rtol=1e-10)
+    np.testing.assert_allclose(uns, lin, rtol=1e-10)
+    np.testing.assert_allclose(lin.sum(), mat.sum(), rtol=1e-10)
+
+
+def test_unstructured_grid_search(oracle_mod):
+    """grid%search on unstructured bounds: a value on an inner bound opens the bin above it, the
+    last bound closes the last bin, values outside the bounds map to no bin."""
+    p = problems.union_cell_slab()
+    o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_ST)
+    bounds = np.array([-1.0, 0.0, 0.5, 2.0])
+    for v, want in [(-1.0, 1), (-0.5, 1), (0.0, 2), (0.49, 2), (0.5, 3), (2.0, 3), (2.5, 0), (-1.5, 0)]:
+        assert o.grid_search(bounds, v) == want, v
