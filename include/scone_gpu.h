@@ -149,6 +149,8 @@ typedef struct sg_geometry_desc {
   const int32_t* uni_fptr;      /* [n_uni+1] into uni_fill      */
   const int32_t* uni_fill;      /* fills per local cell: matIdx or -uniIdx */
   int32_t        root_uni;      /* 0-based index of the root universe */
+  const double*  uni_rot;       /* [n_uni][3] Euler angles (phi, theta, psi) in degrees, ZXZ convention
+                                   (universe `rotation`); null: no universe is rotated */
 } sg_geometry_desc;
 
 typedef struct sg_mg_desc {     /* baseMgNeutronMaterial_class.f90:158-291, PN = P0 or P1 */

@@ -409,7 +409,25 @@ struct Coord {
   double r[3] = {0, 0, 0};
   double dir[3] = {0, 0, 0};
   int uniIdx = 0, uniRootID = 0, localID = 0, cellIdx = 0;
+  bool isRotated = false;                 // coord_class.f90:33-47
+  double rotMat[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
+
+// matmul(rotMat, v) with rotMat row-major
+static void matVec(const double m[9], const double v[3], double out[3]) {
+  for (int i = 0; i < 3; ++i) out[i] = m[3 * i + 0] * v[0] + m[3 * i + 1] * v[1] + m[3 * i + 2] * v[2];
+}
+
+// rotationMatrix (genericProcedures.f90:1098-1140): ZXZ Euler angles in degrees, row-major
+static void rotationMatrix(double phi, double theta, double psi, double m[9]) {
+  const double conv = 2.0 * 3.14159265358979323846264338327950288 / 360.0;
+  const double sf = std::sin(phi * conv), cf = std::cos(phi * conv);
+  const double st = std::sin(theta * conv), ct = std::cos(theta * conv);
+  const double sp = std::sin(psi * conv), cp = std::cos(psi * conv);
+  m[0] = cp * cf - ct * sf * sp;  m[1] = cp * sf + ct * cf * sp;   m[2] = sp * sf;
+  m[3] = -sp * cf - ct * sf * cp; m[4] = -sp * sf + ct * cf * cp;  m[5] = cp * st;
+  m[6] = st * sf;                 m[7] = -st * cf;                 m[8] = ct;
+}
 
 struct CoordList {
   int nesting = 0;
@@ -432,14 +450,22 @@ struct CoordList {
     for (int l = 0; l < n; ++l)
       for (int i = 0; i < 3; ++i) lvl[l].r[i] = lvl[l].r[i] + d * lvl[l].dir[i];
   }
-  void assignDirection(const double u[3]) {                                     // :418-434 (no rotated levels)
-    for (int l = 0; l < nesting; ++l) for (int i = 0; i < 3; ++i) lvl[l].dir[i] = u[i];
+  // the direction of levels 2..nesting from the level above (matmul by rotMat where rotated)
+  void propagateDir() {
+    for (int l = 1; l < nesting; ++l) {
+      if (lvl[l].isRotated) matVec(lvl[l].rotMat, lvl[l - 1].dir, lvl[l].dir);
+      else for (int i = 0; i < 3; ++i) lvl[l].dir[i] = lvl[l - 1].dir[i];
+    }
   }
-  void rotate(double mu, double phi) {                                          // :367-386
+  void assignDirection(const double u[3]) {                                     // :453-472
+    for (int i = 0; i < 3; ++i) lvl[0].dir[i] = u[i];
+    propagateDir();
+  }
+  void rotate(double mu, double phi) {                                          // :385-408
     double nd[3];
     rotateVector(lvl[0].dir, mu, phi, nd);
     for (int i = 0; i < 3; ++i) lvl[0].dir[i] = nd[i];
-    for (int l = 1; l < nesting; ++l) for (int i = 0; i < 3; ++i) lvl[l].dir[i] = lvl[l - 1].dir[i];
+    propagateDir();
   }
 };
 
@@ -453,6 +479,8 @@ struct distCache {   // geometry_inter.f90:21-25
 struct Universe {
   int type = 0;
   double origin[3] = {0, 0, 0};
+  bool rot = false;                       // universe_inter.f90:67-68
+  double rotMat[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   std::vector<int> ip;
   std::vector<double> dp;
   std::vector<int> fill;
@@ -587,6 +615,18 @@ struct Geometry {
       Universe& U = unis[u];
       U.type = g->uni_type[u];
       for (int i = 0; i < 3; ++i) U.origin[i] = g->uni_origin[3 * u + i];
+      if (g->uni_rot) {                                // universe%setTransform (:358-375)
+        const double* a = g->uni_rot + 3 * u;
+        if (!(a[0] == 0.0 && a[1] == 0.0 && a[2] == 0.0)) {
+          if (U.type == SG_UNI_ROOT) { err = "root universe: rotation is not supported"; return SG_ERR_BAD_ARG; }
+          if (!(a[0] >= 0.0 && a[0] < 360.0) || !(a[1] >= 0.0 && a[1] <= 180.0) || !(a[2] >= 0.0 && a[2] < 360.0)) {
+            err = "universe rotation: angles out of range";
+            return SG_ERR_BAD_ARG;
+          }
+          U.rot = true;
+          rotationMatrix(a[0], a[1], a[2], U.rotMat);
+        }
+      }
       for (int k = g->uni_iptr[u]; k < g->uni_iptr[u + 1]; ++k) U.ip.push_back(g->uni_ipar[k]);
       for (int k = g->uni_dptr[u]; k < g->uni_dptr[u + 1]; ++k) U.dp.push_back(g->uni_dpar[k]);
       for (int k = g->uni_fptr[u]; k < g->uni_fptr[u + 1]; ++k) U.fill.push_back(g->uni_fill[k]);
@@ -645,11 +685,17 @@ struct Geometry {
     return 0;
   }
 
-  // universe%enter (universe_inter.f90:400-424) with findCell; no rotation
+  // universe%enter (universe_inter.f90:400-424) with findCell
   void enter(int u, Coord& nw, const double r[3], const double dir[3]) {
     Universe& U = unis[u];
     for (int i = 0; i < 3; ++i) { nw.r[i] = r[i]; nw.dir[i] = dir[i]; }
     nw.uniIdx = u + 1;
+    nw.isRotated = U.rot;
+    if (U.rot) {
+      for (int i = 0; i < 9; ++i) nw.rotMat[i] = U.rotMat[i];
+      matVec(U.rotMat, r, nw.r);
+      matVec(U.rotMat, dir, nw.dir);
+    }
     for (int i = 0; i < 3; ++i) nw.r[i] = nw.r[i] - U.origin[i];
     findCell(u, nw.localID, nw.cellIdx, nw.r, nw.dir);
   }

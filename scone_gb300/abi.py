@@ -48,7 +48,7 @@ class GeometryDesc(C.Structure):
         ("n_cell", C.c_int32), ("cell_ptr", i32p), ("cell_surf", i32p),
         ("n_uni", C.c_int32), ("uni_type", i32p), ("uni_origin", f64p),
         ("uni_iptr", i32p), ("uni_ipar", i32p), ("uni_dptr", i32p), ("uni_dpar", f64p),
-        ("uni_fptr", i32p), ("uni_fill", i32p), ("root_uni", C.c_int32),
+        ("uni_fptr", i32p), ("uni_fill", i32p), ("root_uni", C.c_int32), ("uni_rot", f64p),
     ]
 
 
@@ -227,6 +227,8 @@ def geometry_struct(g):
     s.uni_fptr = arr("uni_fptr", np.int32)
     s.uni_fill = arr("uni_fill", np.int32)
     s.root_uni = int(g["root_uni"])
+    if g.get("uni_rot") is not None:
+        s.uni_rot = arr("uni_rot", np.float64)
     return s, keep
 
 

@@ -17,8 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsconegpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-          "-Xptxas", "-warn-spills"]
+# host code: no multiply-add contraction (gcc contracts by default on aarch64), so host-side values
+# such as rotation matrices are the same on every host and equal the oracle's
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 UNITS = {"sg_support.cu": ["-fmad=false"], "sg_host.cu": ["-fmad=false"], "sg_noalloc.cu": ["-fmad=false"],
          "sg_fission_source.cu": ["-fmad=false"], "sg_batch_host.cu": ["-fmad=false"]}
 for _op in ("st", "dt", "ht"):

@@ -396,8 +396,10 @@ __device__ __forceinline__ void surf_transform_bc(const DSurf& s, double r[3], R
 // ------------------------------------------------------------------ geometry state of one particle
 // Level 1 (the root universe, global coordinates) is held in FP64; the levels below in R: FP64 in the
 // verification form, FP32 local coordinates in the mixed form.  Levels live in registers (MAXL is a
-// compile-time bound >= the geometry's nesting); rotated universes are not supported, so every level
-// shares one direction.
+// compile-time bound >= the geometry's nesting).  One direction is kept, the global one: the
+// direction at a level below a rotated universe is the rotation matrix times the direction of the
+// level above, recomputed where it is needed, which is what SCONE stores per level and recomputes
+// after every change of the global direction (coord_class.f90:385-408,453-472).
 template <class R, int MAXL>
 struct Coords {
   double r0[3];
@@ -415,10 +417,39 @@ struct DistCache {   // geometry_inter.f90:21-25
   int lvl;
 };
 
+template <class T> struct Vec3 { T x, y, z; };
+
+// matmul(rotMat, v) of a 3x3 row-major matrix (universe%enter, universe_inter.f90:400-424), each
+// component summed left to right as gfortran's matmul does
+template <class T>
+__device__ __noinline__ Vec3<T> rot_vec(const T* m, T x, T y, T z) {
+  return Vec3<T>{m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z, m[6] * x + m[7] * y + m[8] * z};
+}
+
 template <class R, int MAXL>
 struct Geom {
   const DGeom& g;
   __device__ __forceinline__ explicit Geom(const DGeom& gg) : g(gg) {}
+
+  template <class T> __device__ __forceinline__ const T* rotm(int u) const {
+    if constexpr (sizeof(T) == 8) return g.rot + 9 * u;
+    else return g.rotf + 9 * u;
+  }
+  // direction at level l (1..MAXL-1; level 0 is the root): the global direction turned by every
+  // rotated universe entered on levels 1..l
+  __device__ __forceinline__ void level_dir(const Coords<R, MAXL>& c, int l, R d[3]) const {
+    d[0] = c.u[0]; d[1] = c.u[1]; d[2] = c.u[2];
+    if (!g.rot) return;
+#pragma unroll
+    for (int j = 1; j < MAXL; ++j) {
+      if (j > l) break;
+      const int u = c.uni[j];
+      if (g.unis[u].rot) {
+        const Vec3<R> v = rot_vec<R>(rotm<R>(u), d[0], d[1], d[2]);
+        d[0] = v.x; d[1] = v.y; d[2] = v.z;
+      }
+    }
+  }
 
   // unionCell%insideComplex (unionCell_class.f90:365-401): left to right over the evaluation array;
   // a union that is already true or an intersection that is already false ends the current bracket
@@ -609,12 +640,24 @@ struct Geom {
           for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
           return;
         }
-        double off[3];
-        cell_offset<double>(c.uni[0], c.local[0], off);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+        enter_level1(c, c.uni[1]);
       }
     }
+  }
+
+  // level-1 coordinates in universe nu entered from the root (cell offset, rotation, origin), from
+  // the FP64 global position
+  __device__ __forceinline__ void enter_level1(Coords<R, MAXL>& c, int nu) const {
+    const DUni& N = g.unis[nu];
+    double off[3];
+    cell_offset<double>(c.uni[0], c.local[0], off);
+    double t[3] = {c.r0[0] - off[0], c.r0[1] - off[1], c.r0[2] - off[2]};
+    if (g.rot && N.rot) {
+      const Vec3<double> v = rot_vec<double>(rotm<double>(nu), t[0], t[1], t[2]);
+      t[0] = v.x; t[1] = v.y; t[2] = v.z;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c.rl[0][k] = R(t[k] - N.origin[k]);
   }
 
   // level-l distance (root level in FP64 positions, lower levels in R)
@@ -622,7 +665,9 @@ struct Geom {
     if (l == 0) uni_distance<double>(c.uni[0], c.local[0], c.r0, c.u, d, s);
     else {
       if (l == 1) sync_level2(c);
-      uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], c.u, d, s);
+      R dl[3];
+      level_dir(c, l, dl);
+      uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], dl, d, s);
     }
   }
 
@@ -648,20 +693,26 @@ struct Geom {
             for (int k = 0; k < 3; ++k) c.rl[0][k] = R(c.r0[k]);
           }
         } else {
-          double off[3];
-          cell_offset<double>(c.uni[0], c.local[0], off);
-#pragma unroll
-          for (int k = 0; k < 3; ++k) c.rl[0][k] = R((c.r0[k] - off[k]) - N.origin[k]);
+          enter_level1(c, nu);
         }
       } else {
         R off[3];
         cell_offset<R>(c.uni[i], c.local[i], off);
+        R t[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) c.rl[i][k] = (c.rl[i > 0 ? i - 1 : 0][k] - off[k]) - UO<R>(N, k);
+        for (int k = 0; k < 3; ++k) t[k] = c.rl[i > 0 ? i - 1 : 0][k] - off[k];
+        if (g.rot && N.rot) {
+          const Vec3<R> v = rot_vec<R>(rotm<R>(nu), t[0], t[1], t[2]);
+          t[0] = v.x; t[1] = v.y; t[2] = v.z;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c.rl[i][k] = t[k] - UO<R>(N, k);
       }
       c.uni[i + 1] = nu;
       c.base[i + 1] = gf.y - 1;
-      c.local[i + 1] = find_cell<R>(nu, c.rl[i], c.u);
+      R dl[3];
+      level_dir(c, i + 1, dl);
+      c.local[i + 1] = find_cell<R>(nu, c.rl[i], dl);
     }
     c.mat = SG_UNDEF_MAT;
     c.nest = MAXL;
@@ -710,11 +761,17 @@ struct Geom {
   __device__ __forceinline__ void move_levels(Coords<R, MAXL>& c, int n, R d) const {
 #pragma unroll
     for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)d * (double)c.u[k];
+    R v[3] = {c.u[0], c.u[1], c.u[2]};
 #pragma unroll
     for (int l = 1; l < MAXL; ++l)
-      if (l < n)
+      if (l < n) {
+        if (g.rot && g.unis[c.uni[l]].rot) {          // this level's direction (rotated universe)
+          const Vec3<R> t = rot_vec<R>(rotm<R>(c.uni[l]), v[0], v[1], v[2]);
+          v[0] = t.x; v[1] = t.y; v[2] = t.z;
+        }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) c.rl[l - 1][k] = c.rl[l - 1][k] + d * c.u[k];
+        for (int k = 0; k < 3; ++k) c.rl[l - 1][k] = c.rl[l - 1][k] + d * v[k];
+      }
   }
 
   // move_withCache / move_noCache (geometryStd_class.f90:214-352); fields absent (fieldDist = INF).
@@ -773,11 +830,13 @@ struct Geom {
         } else {
           if (l == 1) sync_level2(c);
           R* rr = c.rl[l > 0 ? l - 1 : 0];
+          R dl[3];
+          level_dir(c, l, dl);
           if (U.type == SG_UNI_CELL) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) rr[k] = rr[k] + c.u[k] * (R)g.nudge;
+            for (int k = 0; k < 3; ++k) rr[k] = rr[k] + dl[k] * (R)g.nudge;
           }
-          c.local[l] = find_cell<R>(c.uni[l], rr, c.u);
+          c.local[l] = find_cell<R>(c.uni[l], rr, dl);
         }
       }
     }

@@ -136,6 +136,8 @@ struct sg_handle_t {
   DArr<DSurf> surfs64, surfsMx;
   DArr<DUni> unis64, unisMx;
   DArr<int> uniCells, cellPtr, cellSurf, cellComplex;
+  DArr<double> rot64;           // rotation matrices of the universes (when any is rotated)
+  DArr<float> rotF;
   DArr<double> pinRsq, pinTol64, pinTolMx;
   DArr<float> pinRsqF, pinTolF;
   DArr<int2> graph;
@@ -180,7 +182,7 @@ struct sg_handle_t {
   DArr<int> sG, sBrood, sSeq, sCursor;
   int regionCap = 0;
   DArr<int> histN, start, scanTmp, flags, pos, kbuf;
-  DArr<unsigned long long> keys, sel;
+  DArr<unsigned long long> keys, sel, winCnt, winCand;
   DArr<unsigned int> hist16;
   DArr<double> sumPart, scal;  // scal: 0 k_eff, 1 k_new, 2 start weight, 3 end weight, 4 k_end
   DArr<int> totals;            // 0 sites total, 1 kept total, 2 dup total, 3 error
@@ -224,6 +226,24 @@ struct sg_handle_t {
 namespace {
 
 unsigned long long rng_stride(unsigned long long s, long long n) { return lcg_skip(s, 152917LL * n); }
+
+// rotationMatrix (genericProcedures.f90:1098-1140): Euler angles phi, theta, psi in degrees, ZXZ
+// convention; m row-major
+void rotation_matrix(double phi, double theta, double psi, double m[9]) {
+  const double conv = 2.0 * 3.14159265358979323846264338327950288 / 360.0;
+  const double sf = std::sin(phi * conv), cf = std::cos(phi * conv);
+  const double st = std::sin(theta * conv), ct = std::cos(theta * conv);
+  const double sp = std::sin(psi * conv), cp = std::cos(psi * conv);
+  m[0] = cp * cf - ct * sf * sp;
+  m[1] = cp * sf + ct * cf * sp;
+  m[2] = sp * sf;
+  m[3] = -sp * cf - ct * sf * cp;
+  m[4] = -sp * sf + ct * cf * cp;
+  m[5] = cp * st;
+  m[6] = st * sf;
+  m[7] = -st * cf;
+  m[8] = ct;
+}
 
 // ------------------------------------------------------------------ unionCell
 // unionCell%init (Geometry/Cells/unionCell_class.f90:80-199): the token list of a cell becomes its
@@ -395,6 +415,8 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   }
   // universes
   std::vector<DUni> u64(nu), uMx(nu);
+  std::vector<double> rotM(9 * (size_t)nu, 0.0);
+  bool anyRot = false;
   std::vector<std::vector<int>> fills(nu);
   std::vector<int> uniCells;
   std::vector<double> rsq, tol64, tolMx;
@@ -470,7 +492,19 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
       default:
         return h->fail(SG_ERR_BAD_ARG, "geometry: unknown universe type");
     }
-    U.i[6] = (U.origin[0] == 0.0 && U.origin[1] == 0.0 && U.origin[2] == 0.0) ? 1 : 0;
+    if (g->uni_rot) {                            // universe%setTransform (universe_inter.f90:358-375)
+      const double* a = g->uni_rot + 3 * u;
+      if (!(a[0] == 0.0 && a[1] == 0.0 && a[2] == 0.0)) {
+        if (U.type == SG_UNI_ROOT) return h->fail(SG_ERR_BAD_ARG, "root universe: rotation is not supported");
+        if (!(a[0] >= 0.0 && a[0] < 360.0) || !(a[1] >= 0.0 && a[1] <= 180.0) || !(a[2] >= 0.0 && a[2] < 360.0))
+          return h->fail(SG_ERR_BAD_ARG, "universe rotation: angles must be phi, psi in [0,360), theta in [0,180]");
+        rotation_matrix(a[0], a[1], a[2], &rotM[9 * (size_t)u]);
+        U.rot = 1;
+        anyRot = true;
+      }
+    }
+    // level coordinates of an origin-free, unrotated universe equal those of the level above
+    U.i[6] = (!U.rot && U.origin[0] == 0.0 && U.origin[1] == 0.0 && U.origin[2] == 0.0) ? 1 : 0;
     Um = U;
     if (U.type == SG_UNI_LAT)
       for (int i = 0; i < 3; ++i) Um.d[6 + i] = U.d[i] * 0.5 - U.d[i] * SURF_TOL_M;
@@ -555,15 +589,25 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   }
   CK(h->graph.upload(graph, st));
   h->graphHost = graph;
+  if (anyRot) {
+    std::vector<float> rf(rotM.begin(), rotM.end());
+    CK(h->rot64.upload(rotM, st));
+    CK(h->rotF.upload(rf, st));
+  } else {
+    h->rot64.free();
+    h->rotF.free();
+  }
   // mixed-form tie tolerance: 16 FP32 ulps of the largest root coordinate
   double scale = 1.0;
   for (int i = 0; i < 6; ++i) scale = std::max(scale, std::fabs(h->bounds[i]));
   const double tie_abs = 16.0 * scale * 0x1p-23;
   const int* cx = anyComplex ? h->cellComplex.p : nullptr;
   h->g64 = DGeom{h->surfs64.p, h->unis64.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0, cx};
+                 h->pinTol64.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE, 0.0, cx,
+                 anyRot ? h->rot64.p : nullptr, anyRot ? h->rotF.p : nullptr};
   h->gMx = DGeom{h->surfsMx.p, h->unisMx.p, h->uniCells.p, h->cellPtr.p, h->cellSurf.p, h->pinRsq.p,
-                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs, cx};
+                 h->pinTolMx.p, h->pinRsqF.p, h->pinTolF.p, h->graph.p, g->root_uni, g->border_surf, NUDGE_M, tie_abs, cx,
+                 anyRot ? h->rot64.p : nullptr, anyRot ? h->rotF.p : nullptr};
   h->nCell = g->n_cell;
   h->hasGeom = true;
   // active materials for the majorant
@@ -837,6 +881,8 @@ int alloc_work(sg_handle h) {
   CK(h->histN.alloc(cap + 1)); CK(h->start.alloc(cap + 1)); CK(h->scanTmp.alloc(scan_tmp_size((int)cap + 1) + 16));
   CK(h->flags.alloc(cap + 1)); CK(h->pos.alloc(cap + 1)); CK(h->kbuf.alloc(4));
   CK(h->keys.alloc(cap)); CK(h->sel.alloc(2)); CK(h->hist16.alloc(65536));
+  CK(h->winCnt.alloc(2)); CK(h->winCand.alloc(WIN_CAP));
+  CK(cudaMemsetAsync(h->hist16.p, 0, 65536 * sizeof(unsigned int), h->stream));
   CK(h->sumPart.alloc(SUM_BLOCKS)); CK(h->scal.alloc(8)); CK(h->totals.alloc(8)); CK(h->ctr.alloc(1));
   if (h->cfg.record_histories) { CK(h->recColl.alloc(cap)); CK(h->recRng.alloc(cap)); }
   if (h->cfg.form == SG_FORM_EVENT) {
@@ -972,8 +1018,11 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.k_eff = d_k;
   t.acc = h->acc.p + lo;
   t.acc_n = (int)(hi - lo);
+  // Block-local FP64 score memory in shared memory for the FP64 form; the mixed form scores straight
+  // into global memory (reductions performed in L2 cost the history loop less than shared-memory
+  // FP64 atomics: 6 % on the 17x17 lattice).
   size_t smem = (size_t)t.acc_n * sizeof(double);
-  t.use_smem = (t.acc_n > 0 && smem <= 64 * 1024) ? 1 : 0;
+  t.use_smem = (sizeof(R) == 8 && t.acc_n > 0 && smem <= 64 * 1024) ? 1 : 0;
   if (!t.use_smem) smem = 0;
   t.sites = site_view(h);
   t.hist_nsites = h->histN.p;
@@ -1126,8 +1175,8 @@ int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long maste
   if (heap > 0) {
     k_rn_keys<<<((S + 31) / 32 + 127) / 128, 128, 0, s>>>(master, S, h->keys.p);
     CK(cudaGetLastError());
-    CK(radix_select(h->keys.p, S, heap, h->sel.p, h->kbuf.p, h->hist16.p, s));
-    h->launches += 9;
+    CK(quantile_select(h->keys.p, S, heap, h->sel.p, h->kbuf.p, h->hist16.p, h->winCnt.p, h->winCand.p, s));
+    h->launches += 11;
   }
   if (excess > 0) {
     CK(launch_flags(h->keys.p, S, h->sel.p, 1, h->flags.p, s));
@@ -1478,7 +1527,7 @@ int32_t sg_destroy(sg_handle h) {
   cudaStreamSynchronize(h->stream);
   for (auto& b : h->bank) b.free();
   h->surfs64.free(); h->surfsMx.free(); h->unis64.free(); h->unisMx.free(); h->uniCells.free();
-  h->cellPtr.free(); h->cellSurf.free(); h->cellComplex.free();
+  h->cellPtr.free(); h->cellSurf.free(); h->cellComplex.free(); h->rot64.free(); h->rotF.free();
   h->fsR.free(); h->fsDir.free(); h->fsWgt.free(); h->fsE.free(); h->fsG.free(); h->pinRsq.free(); h->pinTol64.free(); h->pinTolMx.free(); h->graph.free();
   h->pinRsqF.free(); h->pinTolF.free();
   for (auto& a : h->mgD) a.free();
@@ -1486,7 +1535,7 @@ int32_t sg_destroy(sg_handle h) {
   h->fissile.free(); h->acc.free(); h->bin.free(); h->csum.free(); h->csum2.free();
   h->sR.free(); h->sDir.free(); h->sWgt.free(); h->sTime.free(); h->sG.free(); h->sBrood.free(); h->sSeq.free();
   h->sCursor.free(); h->histN.free(); h->start.free(); h->scanTmp.free(); h->flags.free(); h->pos.free();
-  h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->sumPart.free(); h->scal.free();
+  h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->winCnt.free(); h->winCand.free(); h->sumPart.free(); h->scal.free();
   h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
   h->pR0.free(); h->pRl.free(); h->pU.free(); h->pW.free(); h->pW0.free(); h->pTime.free(); h->pTrack.free();
   h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();

@@ -33,6 +33,7 @@ struct DSurf {
 struct DUni {
   int type;
   int i[7];
+  int rot;         // 1: rotated (universe `rotation`); its matrix is DGeom::rot[9 * index]
   double origin[3];
   double d[9];
   float originf[3];
@@ -55,6 +56,8 @@ struct DGeom {
   double nudge;         // cellUniverse crossing nudge of the precision form
   double tie_abs;       // absolute part of the tie rule between nesting levels (0 in the FP64 form)
   const int* cell_complex;  // [n_cell] 1: unionCell with unions (cell_surf holds its evaluation array)
+  const double* rot;        // [n_uni][9] row-major rotation matrices; null when no universe is rotated
+  const float* rotf;        // FP32 copy
 };
 
 // unionCell evaluation tokens in cell_surf (surfaces are signed 1-based indices); OPEN, CLOSE and

@@ -2,6 +2,9 @@
 // fission sites by brood ID, population control (normSize_Repr), deterministic reductions and the
 // scoreMemory/tallyAdmin cycle-end update.  All are bandwidth- or latency-trivial next to the
 // history loop; they exist so that a whole eigenvalue cycle stays on the device.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include "sg_device.cuh"
 #include "sg_support.h"
 
@@ -201,8 +204,81 @@ __global__ void k_rn_keys(unsigned long long master, int S, unsigned long long* 
   }
 }
 
+// The heap threshold is first looked for in a window around its expected place: the xi are
+// uniform on (0,1), so the kth smallest of S lies within a few standard deviations
+// (sqrt(p (1 - p) / S), p = k / S) of k / S.  One pass counts the keys below the window and gathers
+// the keys inside it; one block sorts the gathered keys and picks the kth.  The result is the kth
+// smallest key itself, whichever way it is found.  When the window misses (the kth key outside it,
+// or more keys in it than the buffer holds) the radix select below runs; its kernels return at
+// once when the window found the key (ok flag).
+__global__ void k_win_gather(const unsigned long long* keys, int S, unsigned long long lo, unsigned long long hi,
+                             unsigned long long* cnt, unsigned long long* cand, int cap) {
+  __shared__ unsigned long long below_s;
+  if (threadIdx.x == 0) below_s = 0;
+  __syncthreads();
+  unsigned long long below = 0;
+  const int lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * blockDim.x; base < S; base += gridDim.x * blockDim.x) {
+    const int i = base + threadIdx.x;
+    unsigned long long k = 0;
+    bool in = false;
+    if (i < S) {
+      k = keys[i];
+      below += (k < lo) ? 1 : 0;
+      in = (k >= lo && k <= hi);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, in);
+    if (m) {
+      unsigned long long pos = 0;
+      if (lane == 0) pos = atomicAdd(cnt + 1, (unsigned long long)__popc(m));
+      pos = __shfl_sync(0xffffffffu, pos, 0);
+      if (in) {
+        const unsigned long long at = pos + __popc(m & ((1u << lane) - 1u));
+        if (at < (unsigned long long)cap) cand[at] = k;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) below += __shfl_down_sync(0xffffffffu, below, o);
+  if (lane == 0 && below) atomicAdd(&below_s, below);
+  __syncthreads();
+  if (threadIdx.x == 0 && below_s) atomicAdd(cnt, below_s);
+}
+
+// one block: bitonic sort of the gathered keys in shared memory, then the pick.  ok[0] = 1 on
+// success; otherwise the radix select's state (sel = 0, kth) is set up.
+__global__ void k_win_pick(const unsigned long long* cand, const unsigned long long* cnt, int cap, int kth,
+                           unsigned long long* sel, int* kbuf) {
+  extern __shared__ unsigned long long sk[];
+  const unsigned long long nb = cnt[0], nin = cnt[1];
+  const long long r = (long long)kth - (long long)nb;     // 1-based rank inside the window
+  const bool hit = r >= 1 && (unsigned long long)r <= nin && nin <= (unsigned long long)cap;
+  if (!hit) {
+    if (threadIdx.x == 0) { sel[0] = 0; sel[1] = 0; kbuf[0] = kth; kbuf[1] = 0; }
+    return;
+  }
+  int P = 1;
+  while (P < (int)nin) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sk[i] = (i < (int)nin) ? cand[i] : ~0ull;
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = sk[i], b = sk[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { sk[i] = b; sk[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) { sel[0] = sk[r - 1]; sel[1] = ~0ull; kbuf[0] = 1; kbuf[1] = 1; }
+}
+
 __global__ void k_radix_hist(const unsigned long long* keys, int S, const unsigned long long* sel,
-                             int shift, unsigned int* hist) {
+                             int shift, unsigned int* hist, const int* ok) {
+  if (*ok) return;
   // sel[0] = prefix, sel[1] = mask of the bits already fixed
   const unsigned long long prefix = sel[0], mask = sel[1];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S; i += gridDim.x * blockDim.x) {
@@ -213,6 +289,7 @@ __global__ void k_radix_hist(const unsigned long long* keys, int S, const unsign
 
 __global__ void k_radix_pick(unsigned int* hist, unsigned long long* sel, int* kth, int shift) {
   // single block of 1024: find the digit containing the kth (1-based) key, then clear hist
+  if (kth[1]) return;                                    // the window select found it
   __shared__ unsigned int part[1024];
   __shared__ int chosen;
   __shared__ unsigned int below;
@@ -247,13 +324,31 @@ __global__ void k_radix_pick(unsigned int* hist, unsigned long long* sel, int* k
   }
 }
 
-cudaError_t radix_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel,
-                         int* kbuf, unsigned int* hist, cudaStream_t s) {
-  cudaMemsetAsync(sel, 0, 2 * sizeof(unsigned long long), s);
-  cudaMemsetAsync(hist, 0, 65536 * sizeof(unsigned int), s);
-  cudaMemcpyAsync(kbuf, &kth, sizeof(int), cudaMemcpyHostToDevice, s);
+// kth smallest (1-based) of the S keys into sel[0].  hist (65536 counters) is zero on entry and on
+// exit; kbuf holds [kth remaining, window found]; cnt two counters; cand WIN_CAP keys.
+cudaError_t quantile_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel, int* kbuf,
+                            unsigned int* hist, unsigned long long* cnt, unsigned long long* cand, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_win_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(WIN_CAP * sizeof(unsigned long long)));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const double p = (double)kth / S;
+  const double d = 8.0 * sqrt(p * (1.0 - p) / S) + 4.0 / S;
+  const double lo = p - d, hi = p + d;
+  unsigned long long klo = 0, khi = ~0ull >> 1;
+  if (lo > 0.0) std::memcpy(&klo, &lo, sizeof(double));
+  if (hi < 1.0) std::memcpy(&khi, &hi, sizeof(double));
+  const char* off = std::getenv("SCONE_GB300_NO_WINDOW_SELECT");   // empty window: radix select only
+  if (off && off[0] == '1') { klo = 1; khi = 0; }
+  cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), s);
+  const int blocks = std::min(1216, (S + 255) / 256);
+  k_win_gather<<<blocks, 256, 0, s>>>(keys, S, klo, khi, cnt, cand, WIN_CAP);
+  k_win_pick<<<1, 1024, WIN_CAP * sizeof(unsigned long long), s>>>(cand, cnt, WIN_CAP, kth, sel, kbuf);
   for (int shift = 48; shift >= 0; shift -= 16) {
-    k_radix_hist<<<256, 256, 0, s>>>(keys, S, sel, shift, hist);
+    k_radix_hist<<<256, 256, 0, s>>>(keys, S, sel, shift, hist, kbuf + 1);
     k_radix_pick<<<1, 1024, 0, s>>>(hist, sel, kbuf, shift);
   }
   return cudaGetLastError();

@@ -31,8 +31,9 @@ cudaError_t deterministic_sum(const double* v, int n, double* part, double* out,
 
 // population control
 __global__ void k_rn_keys(unsigned long long master, int S, unsigned long long* keys);
-cudaError_t radix_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel,
-                         int* kbuf, unsigned int* hist, cudaStream_t s);
+static constexpr int WIN_CAP = 16384;   // keys the window select of the heap threshold can gather
+cudaError_t quantile_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel, int* kbuf,
+                            unsigned int* hist, unsigned long long* cnt, unsigned long long* cand, cudaStream_t s);
 cudaError_t launch_flags(const unsigned long long* keys, int S, const unsigned long long* sel, int keep,
                          int* flags, cudaStream_t s);
 cudaError_t launch_compact(const DBank& in, int S, const int* flags, const int* pos, const DBank& out,

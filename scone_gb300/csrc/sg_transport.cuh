@@ -217,6 +217,7 @@ struct Tracker {
   // keffImplicitClerk (keffImplicitClerk_class.f90:180-227)
   __device__ __forceinline__ void report_in_coll(bool virt, R trackXS) {
     const int cell = A.has_cellmap ? lowest_cell() : 0;
+    const R fluxTrack = w / trackXS;                   // collision estimator with handleVirtual
     for (int k = 0; k < A.n_clerks; ++k) {
       const DClerk& K = A.clerks[k];
       if (K.type == SG_CLERK_COLLISION) {
@@ -225,7 +226,7 @@ struct Tracker {
         int bin = map_bin(K, c.r0, G, c.mat, cell);
         if (bin == 0) continue;
         R flux;
-        if (K.handle_virtual) flux = w / trackXS;
+        if (K.handle_virtual) flux = fluxTrack;
         else if constexpr (CE) flux = w / ce_total(c.mat);
         else flux = w / xs(mg.total, c.mat, G);
         long long at = K.acc_off + (long long)K.width * (bin - 1);
@@ -233,10 +234,12 @@ struct Tracker {
       } else if (K.type == SG_CLERK_KEFF_IMPLICIT) {
         if constexpr (CE) continue;                    // rejected for CE problems at upload
         if (c.mat == SG_VOID_MAT) continue;
-        R flux = w / trackXS;
-        bool f = mg.fissile[c.mat - 1] != 0;
-        R nuF = f ? xs(mg.nuFission, c.mat, G) : R(0);
-        R absXS = xs(mg.capture, c.mat, G) + (f ? xs(mg.fission, c.mat, G) : R(0));
+        const R flux = fluxTrack;
+        // fission and nuFission are zero for non-fissile materials, so no fissile test is needed
+        // (capture + 0 is capture exactly)
+        const int xk = (c.mat - 1) * mg.nG + (G - 1);
+        const R nuF = mg.nuFission[xk];
+        const R absXS = mg.capture[xk] + mg.fission[xk];
         kprod += nuF * flux;
         kabs += absXS * flux;
       }

@@ -31,6 +31,7 @@ class GeometryBuilder:
         self.surf_type, self.surf_par = [], []
         self.cells = []
         self.unis = []          # (type, origin, ipar, dpar, fills)
+        self.rot = {}           # universe -> (phi, theta, psi) Euler angles in degrees
         self.root = None
         self.border = None
         self.bc = [0] * 6
@@ -51,6 +52,11 @@ class GeometryBuilder:
         self.unis.append((type_, list(origin), list(ipar), list(dpar), list(fills)))
         return len(self.unis) - 1
 
+    def rotate(self, uni, angles):
+        """Give universe `uni` the `rotation` (phi, theta, psi) in degrees, ZXZ Euler angles."""
+        self.rot[uni] = tuple(float(a) for a in angles)
+        return uni
+
     def root_universe(self, border_surf, fill, bc=(0, 0, 0, 0, 0, 0)):
         self.border = border_surf
         self.bc = list(bc)
@@ -60,12 +66,12 @@ class GeometryBuilder:
     def pin_universe(self, radii, fills, origin=(0.0, 0.0, 0.0)):
         return self.universe(abi.UNI_PIN, fills, dpar=sorted(radii), origin=origin)
 
-    def lattice_universe(self, shape, pitch, fills_local_order, pad_fill, offset=True):
+    def lattice_universe(self, shape, pitch, fills_local_order, pad_fill, offset=True, origin=(0.0, 0.0, 0.0)):
         return self.universe(abi.UNI_LAT, list(fills_local_order) + [pad_fill],
-                             ipar=list(shape) + [1 if offset else 0], dpar=list(pitch))
+                             ipar=list(shape) + [1 if offset else 0], dpar=list(pitch), origin=origin)
 
-    def cell_universe(self, cell_idx, fills):
-        return self.universe(abi.UNI_CELL, fills, ipar=cell_idx)
+    def cell_universe(self, cell_idx, fills, origin=(0.0, 0.0, 0.0)):
+        return self.universe(abi.UNI_CELL, fills, ipar=cell_idx, origin=origin)
 
     def arrays(self):
         def ptr(lists):
@@ -89,6 +95,8 @@ class GeometryBuilder:
             uni_dptr=ptr([u[3] for u in self.unis]), uni_dpar=cat([u[3] for u in self.unis], np.float64),
             uni_fptr=ptr([u[4] for u in self.unis]), uni_fill=cat([u[4] for u in self.unis], np.int32),
             root_uni=self.root,
+            uni_rot=(np.array([self.rot.get(i, (0.0, 0.0, 0.0)) for i in range(len(self.unis))], np.float64)
+                     if self.rot else None),
         )
 
 
@@ -471,3 +479,28 @@ def union_cell_slab(seed=41):
                                                               (abi.AXIS_GROUP, 2, 0.0, 0.0)])])
     return Problem(gb.arrays(), mg, name="union_cell_spheres", source=dict(r=(0.0, 0.0, 0.0), G=1),
                    tallies=tallies)
+
+
+def rotated_pins(seed=43):
+    """Rotated universes (universe `rotation`, ZXZ Euler angles): a vacuum box (half-width 5 cm)
+    holds a cellUniverse turned 30 degrees about z and offset to x = 0.5; its half x < 0 holds a pin
+    universe turned 90 degrees about x (the pin's axis along y of the cell universe), its other half
+    a second material; a point source and collision/track flux per material and group."""
+    rng = np.random.default_rng(seed)
+    gb = GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 5.0, 5.0, 5.0)
+    xp = gb.surface(abi.XPLANE, 0.0)
+    pin = gb.pin_universe([1.2], [1, 2])
+    gb.rotate(pin, (0.0, 90.0, 0.0))
+    left = gb.cell([-(xp + 1)])
+    right = gb.cell([xp + 1])
+    cu = gb.cell_universe([left, right], [uni_fill(pin), 3], origin=(0.5, 0.0, 0.0))
+    gb.rotate(cu, (30.0, 0.0, 0.0))
+    gb.root_universe(box, uni_fill(cu), bc=[abi.BC_VACUUM] * 6)
+    mats = [_fixed_source_xs(rng, 2) for _ in range(3)]
+    mg = mg_data(2, np.array([m[0] for m in mats]), np.array([m[1] for m in mats]),
+                 capture=np.array([m[2] for m in mats]))
+    axes = [(abi.AXIS_MATERIAL, 3, 0.0, 0.0), (abi.AXIS_GROUP, 2, 0.0, 0.0)]
+    tallies = dict(flux=[abi.clerk(abi.CLERK_COLLISION, axes=axes), abi.clerk(abi.CLERK_TRACK, axes=axes),
+                         abi.clerk(abi.CLERK_COLLISION, axes=[(abi.AXIS_X, 10, -5.0, 5.0), (abi.AXIS_Y, 10, -5.0, 5.0)])])
+    return Problem(gb.arrays(), mg, name="rotated_pins", source=dict(r=(-1.0, 0.3, 0.2), G=1), tallies=tallies)

@@ -347,3 +347,50 @@ def test_bad_map_axes_are_rejected(gpu_mod):
         with pytest.raises(gpu_mod.SconeGpuError, match=msg):
             g.upload_tally([abi.clerk(C_, axes=[ax])])
     g.close()
+
+
+def test_heap_threshold_window_and_radix_agree(gpu_mod, oracle_mod, monkeypatch):
+    """normSize_Repr's heap threshold found by the window select and by the radix select alone
+    (SCONE_GB300_NO_WINDOW_SELECT=1) gives the same cycles as the oracle."""
+    p = problems.lattice_17x17_7g()
+    o = oracle_mod.Oracle(p)
+    ko, _, _ = _eigen(o, p, 20000, 2, 2)
+    for flag in ("0", "1"):
+        monkeypatch.setenv("SCONE_GB300_NO_WINDOW_SELECT", flag)
+        g = gpu_mod.TransportOperatorGPU(p, max_bank=1 << 16)
+        kg, _, _ = _eigen(g, p, 20000, 2, 2)
+        g.close()
+        np.testing.assert_allclose(kg, ko, rtol=1e-10)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT, abi.TRANSPORT_ST_NOCACHE])
+def test_rotated_universes_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
+    """Rotated cell and pin universes (universe `rotation`): per-history bit-level agreement with the
+    oracle and equal tallies."""
+    p = problems.rotated_pins()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form)
+    n = 20000
+    bank = o.generate_source(SEED, n)
+    ag, ao = g.upload_tally(p.tallies["flux"]), o.upload_tally(p.tallies["flux"])
+    g.transport_bank(ag, bank, 97531)
+    o.transport_bank(ao, bank, 97531)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co) and np.array_equal(rg, ro)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=0)
+
+
+def test_rotated_universes_mixed_statistics(gpu_mod):
+    """The mixed form on rotated universes agrees with the FP64 form within statistics."""
+    p = problems.rotated_pins()
+    out = {}
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_ST, max_bank=1 << 18)
+        a = t.upload_tally(p.tallies["flux"])
+        t.fixed_source_cycle(a, 200000, 4321)
+        out[prec] = t.bins(a)[:, 1]
+        t.close()
+    np.testing.assert_allclose(out[abi.PREC_MIXED][:12], out[abi.PREC_FP64][:12], rtol=0.03)

@@ -546,3 +546,58 @@ def test_unstructured_grid_search(oracle_mod):
     bounds = np.array([-1.0, 0.0, 0.5, 2.0])
     for v, want in [(-1.0, 1), (-0.5, 1), (0.0, 2), (0.49, 2), (0.5, 3), (2.0, 3), (2.5, 0), (-1.5, 0)]:
         assert o.grid_search(bounds, v) == want, v
+
+
+def test_rotated_universe_enter_golden(oracle_mod):
+    """universe%enter with `rotation (90 90 90)` and `origin (2 0 0)` (the axis map x -> z,
+    y -> -y, z -> x): local positions, directions and cells as SCONE's cellUniverse test states them
+    (Geometry/Universes/Tests/cellUniverse_test.f90:28-34,150-200)."""
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 20.0, 20.0, 20.0)
+    s1 = gb.surface(abi.SPHERE, 0.0, 0.0, 0.0, 2.0)
+    s2 = gb.surface(abi.SPHERE, 4.0, 0.0, 0.0, 1.0)
+    c1 = gb.cell([-(s1 + 1)])
+    c2 = gb.cell([s1 + 1, s2 + 1])
+    uni = gb.cell_universe([c1, c2], [1, 2], origin=(2.0, 0.0, 0.0))
+    gb.rotate(uni, (90.0, 90.0, 90.0))
+    gb.root_universe(box, problems.uni_fill(uni), bc=[abi.BC_VACUUM] * 6)
+    o = oracle_mod.Oracle(problems.Problem(gb.arrays(), None))
+    cases = [((0.0, 0.0, 3.0), (0.0, 0.0, 1.0), (1.0, 0.0, 0.0), (1.0, 0.0, 0.0), 1),
+             ((2.0, 0.0, 1.0), (0.0, 1.0, 0.0), (-1.0, 0.0, 2.0), (0.0, -1.0, 0.0), 2),
+             ((0.0, 0.0, 6.5), (1.0, 0.0, 0.0), (4.5, 0.0, 0.0), (0.0, 0.0, 1.0), 3)]
+    for r, u, r_ref, u_ref, local in cases:
+        o.coords_init(r, u)
+        o.coords_place()
+        rl, ul, info = o.coords_get(1)
+        np.testing.assert_allclose(rl, r_ref, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(ul, u_ref, rtol=0, atol=1e-12)
+        assert info["local"] == local
+
+
+def test_rotation_matrix_rejections(oracle_mod):
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 5.0, 5.0, 5.0)
+    c = gb.cell([-(box + 1)])
+    uni = gb.cell_universe([c], [1])
+    gb.rotate(uni, (0.0, 200.0, 0.0))                             # theta outside [0, 180]
+    gb.root_universe(box, problems.uni_fill(uni), bc=[abi.BC_VACUUM] * 6)
+    with pytest.raises(Exception, match="rotation"):
+        oracle_mod.Oracle(problems.Problem(gb.arrays(), None))
+
+
+def test_rotated_pins_runs_and_rotation_matters(oracle_mod):
+    """The rotated-universe problem transports; turning the pin universe changes its tallies."""
+    p = problems.rotated_pins()
+    o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_ST)
+    a = o.upload_tally(p.tallies["flux"])
+    o.fixed_source_cycle(a, 5000, 1357)
+    b1 = o.bins(a)[:, 1]
+    g = dict(p.geometry)
+    g["uni_rot"] = np.zeros_like(g["uni_rot"])
+    q = problems.Problem(g, p.mg, source=p.source, tallies=p.tallies)
+    o2 = oracle_mod.Oracle(q, transport=abi.TRANSPORT_ST)
+    a2 = o2.upload_tally(q.tallies["flux"])
+    o2.fixed_source_cycle(a2, 5000, 1357)
+    b2 = o2.bins(a2)[:, 1]
+    assert b1[:6].min() > 0
+    assert not np.allclose(b1, b2)
