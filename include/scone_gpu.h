@@ -387,6 +387,34 @@ int32_t sg_transport_bank_noalloc(sg_handle h, int32_t admin, const sg_bank* dev
                                   uint64_t master_state, double k_eff, sg_bank* dev_next,
                                   int32_t next_cap, int32_t* n_next);
 
+/* ---------------------------------------------------------------- collision processor variants */
+
+/* collisionProcessor choice (CollisionOperator/CollisionProcessors): neutronMGstd / neutronCEstd
+ * (SG_COLL_STD, the default) or neutronMGimp / neutronCEimp (SG_COLL_IMP) with their options.
+ * neutronMGimp acts through weight windows only (neutronMGimp_class.f90:319-351); neutronCEimp also
+ * through implicit absorption, roulette and splitting (neutronCEimp_class.f90:160-232,406-424,
+ * 633-734).  Split particles wait in a per-history buffer and are transported after the particle
+ * that made them, last in first out, on the same RNG stream (the fixed-source and eigenvalue gen
+ * loops' `buffer`); splitting and weight windows need the history-loop form. */
+#define SG_COLL_STD 0
+#define SG_COLL_IMP 1
+typedef struct sg_collision_desc {
+  int32_t kind;                 /* SG_COLL_*                                              */
+  int32_t imp_abs;              /* `impAbs`: implicit absorption (needs roulette or windows) */
+  int32_t roulette;             /* `roulette`                                             */
+  int32_t split;                /* `split` (needs max_wgt >= 2 min_wgt)                   */
+  int32_t weight_windows;       /* `weightWindows`: use the weightWindowsField below      */
+  int32_t max_split;            /* `maxSplit` (SCONE default 1000)                        */
+  double  min_wgt, max_wgt, av_wgt;   /* `minWgt` 0.25, `maxWgt` 1.25, `avWgt` 0.5        */
+  int32_t ww_n_axes;            /* weightWindowsField (weightWindowsField_class.f90:75-111): */
+  sg_axis_desc ww_axes[3];      /*   its `map` (multiMap order)                           */
+  const double* ww_lower;       /*   `wLower`, one per map bin                            */
+  const double* ww_upper;       /*   `wUpper`, one per map bin                            */
+  double  ww_const_survival;    /*   `constSurvival` (> 1)                                */
+  int32_t buffer_depth;         /* split particles one history may hold at once (0: 32)  */
+} sg_collision_desc;
+int32_t sg_set_collision(sg_handle h, const sg_collision_desc* d);
+
 /* ---------------------------------------------------------------- event-form queue thresholds */
 
 /* No SCONE counterpart (SCONE has no event form).  The event form (SG_FORM_EVENT) alternates

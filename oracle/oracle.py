@@ -74,6 +74,7 @@ def lib():
             "or_asymptotic_scatter": (i32, [f64, f64, f64, P(f64)]),
             "or_target_velocity": (i32, [f64, P(f64), f64, f64, P(u64), P(f64)]),
             "or_grid_search": (i32, [P(f64), i32, f64]),
+            "or_set_collision": (i32, [vp, P(abi.CollisionDesc)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -158,6 +159,11 @@ class Oracle:
         n = C.c_int64()
         self._check(self.L.or_ce_union_size(self.h, C.byref(n)))
         return n.value
+
+    def set_collision(self, desc):
+        """neutronMGimp / neutronCEimp options (an abi.collision() description)."""
+        self._keep.append(desc)
+        self._check(self.L.or_set_collision(self.h, C.byref(desc)))
 
     def grid_search(self, bounds, v):
         """grid%search of an unstructured grid: 1-based bin of `v`, 0 outside."""

@@ -1317,6 +1317,8 @@ struct Particle {
   bool isDead = false;
   int fate = NO_FATE;
   int collisionN = 0, broodID = 0;
+  int splitCount = 0;                     // particle_class.f90:137
+  std::vector<PState> buffer;             // the gen loop's `buffer`: split particles, LIFO
   double k_eff = 1.0;
   RNG rng;
   double preHistWgt = 1.0, preCollWgt = 1.0;
@@ -1362,6 +1364,11 @@ struct Oracle {
   std::vector<TallyAdmin> admins;
   int transport = SG_TRANSPORT_ST;
   double htCutoff = 0.9;                             // transportOperatorHT `cutoff` (:297)
+  // neutronMGimp / neutronCEimp (SG_COLL_IMP) options and the weight-window field
+  bool collImp = false;
+  sg_collision_desc coll{};
+  Clerk wwMap;
+  std::vector<double> wwLo, wwUp;
   std::string err;
   sg_point_source_desc src{};
   std::vector<double> srcProbG;
@@ -1779,10 +1786,47 @@ struct Oracle {
     } else {
       p.isDead = true;   // capture / fission
     }
+    if (collImp) impCutoffs(p);                          // neutronMGimp cutoffs (:319-351)
     p.collisionN += 1;
     nColl++;
     reportOutColl(admin, p, MT);
     if (p.isDead) { p.fate = ABS_FATE; reportHist(admin, p); }
+  }
+
+  // neutronCEimp%cutoffs (neutronCEimp_class.f90:633-678); neutronMGimp%cutoffs acts through weight
+  // windows only (neutronMGimp_class.f90:319-351)
+  void impCutoffs(Particle& p) {
+    if (p.isDead) return;
+    if (isCE && p.E < ce.minE) { p.isDead = true; return; }
+    if (coll.weight_windows) {
+      // weightWindowsField%atP (weightWindowsField_class.f90:148-171)
+      int bin = mapState(wwMap, p.coords.lvl[0].r, p.G, p.matIdx(), p.coords.cell(), p.E, p.isMG);
+      double minW = 0.0, maxW = 0.0, avW = 0.0;
+      if (bin != 0) { minW = wwLo[bin - 1]; maxW = wwUp[bin - 1]; avW = minW * coll.ww_const_survival; }
+      if ((p.w > maxW) && (maxW != 0.0) && (p.splitCount < coll.max_split)) split(p, maxW);
+      else if (p.w < minW) russianRoulette(p, avW);
+      return;
+    }
+    if (!isCE) return;
+    if (coll.split && p.w > coll.max_wgt) split(p, coll.max_wgt);
+    else if (coll.roulette && p.w < coll.min_wgt) russianRoulette(p, coll.av_wgt);
+  }
+  // russianRoulette (neutronCEimp_class.f90:683-694)
+  void russianRoulette(Particle& p, double avWgt) {
+    if (p.rng.get() < (1.0 - p.w / avWgt)) p.isDead = true;
+    else p.w = avWgt;
+  }
+  // split (neutronCEimp_class.f90:699-734): mult - 1 copies into the history's buffer
+  void split(Particle& p, double maxWgt) {
+    int mult = (int)std::ceil(p.w / maxWgt);
+    if (mult + p.splitCount > coll.max_split) mult = coll.max_split - p.splitCount + 1;
+    PState t;
+    t.wgt = p.w / mult;
+    for (int i = 0; i < 3; ++i) { t.r[i] = p.coords.lvl[0].r[i]; t.dir[i] = p.coords.lvl[0].dir[i]; }
+    t.E = p.E; t.G = p.G; t.time = p.time; t.broodID = p.broodID;
+    for (int i = 1; i <= mult - 1; ++i) p.buffer.push_back(t);
+    p.splitCount = p.splitCount + mult;
+    p.w = p.w / mult;
   }
 
   // collisionProcessor%collide with neutronCEstd (collisionProcessor_inter.f90:114-195,
@@ -1822,7 +1866,14 @@ struct Oracle {
     if (xs > 0.0) C = C + 1;
     reportInColl(admin, p, false, trackXS);
     p.preCollWgt = p.w;
-    // implicit (:220-311): non-fissile nuclide, no sites
+    // implicit (:220-311): non-fissile nuclide, no sites; neutronCEimp implicit absorption (:406-424)
+    if (collImp && coll.imp_abs) {
+      double sig_scatter = micro[1] + micro[2];
+      double sig_tot = micro[0];
+      p.w = p.w * sig_scatter / sig_tot;
+      double totalElastic = micro[1] + micro[2];
+      C = (p.rng.get() < micro[1] / totalElastic) ? 1 : 2;
+    }
     int MT;
     if (C == 1) {                                        // elastic (:340-384)
       MT = 2;                                            // N_N_elastic
@@ -1863,7 +1914,8 @@ struct Oracle {
       MT = (C == 3) ? 101 : 18;
       p.isDead = true;
     }
-    if (p.E < ce.minE) p.isDead = true;                  // cutoffs (:434-444)
+    if (collImp) impCutoffs(p);                          // neutronCEimp cutoffs (:633-678)
+    else if (p.E < ce.minE) p.isDead = true;             // cutoffs (:434-444)
     p.collisionN += 1;
     nColl++;
     reportOutColl(admin, p, MT);
@@ -1895,10 +1947,22 @@ struct Oracle {
         if (sigmaT * majorant_inv > 1.0 - htCutoff) deltaTracking(p, admin, trackXS);
         else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_HT);
       } else surfaceTracking(p, admin, trackXS, transport == SG_TRANSPORT_ST);
-      if (p.isDead) { reportHist(admin, p); break; }
-      if (isCE) collideCE(p, admin, trackXS);
-      else collide(p, admin, trackXS, sites);
-      if (p.isDead) break;
+      if (!p.isDead) {
+        if (isCE) collideCE(p, admin, trackXS);
+        else collide(p, admin, trackXS, sites);
+        if (!p.isDead) continue;
+      } else reportHist(admin, p);
+      if (p.buffer.empty()) break;
+      // buffer%release and the restart of bufferLoop (fixedSourcePhysicsPackage_class.f90:209-216,
+      // 235-239): the last split particle, placed; the RNG stream continues
+      const PState b = p.buffer.back();
+      p.buffer.pop_back();
+      p.coords.takeAboveGeom();
+      for (int i = 0; i < 3; ++i) { p.coords.lvl[0].r[i] = b.r[i]; p.coords.lvl[0].dir[i] = b.dir[i]; }
+      p.w = b.wgt; p.G = b.G; p.E = b.E; p.time = b.time;
+      p.splitCount = 0; p.isDead = false; p.fate = NO_FATE;
+      geom.placeCoord(p.coords);
+      p.preHistWgt = p.w; p.preCollWgt = p.w;
     }
     if (recC) *recC = p.collisionN;
     if (recR) *recR = p.rng.s;
@@ -2156,6 +2220,31 @@ int32_t or_grid_search(const double* bounds, int32_t nb, double v) {
   return Oracle::binaryFloor(b, v);
 }
 
+// multiMap axes of one clerk (tallyMapFactory / grid%init / cellMap%build): grid types and steps,
+// unstructured bounds and cell bins copied out of the caller's arrays; returns the number of bins
+static int64_t setupAxes(Oracle* o, orc::Clerk& c) {
+  int64_t mul = 1;
+  for (int a = 0; a < c.d.n_axes; ++a) {
+    const sg_axis_desc& ax = c.d.axes[a];
+    int64_t nb = ax.n;
+    c.grid[a] = ax.grid != SG_GRID_DEFAULT ? ax.grid : (ax.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN);
+    if (c.grid[a] == SG_GRID_LOG) c.step[a] = std::log(ax.max / ax.min) / ax.n;   // grid_class.f90:76-90
+    else c.step[a] = (ax.max - ax.min) / ax.n;                                    // grid_class.f90:63-74
+    if (c.grid[a] == SG_GRID_UNSTRUCT && (ax.kind <= SG_AXIS_Z || ax.kind == SG_AXIS_ENERGY))
+      c.bounds[a].assign(ax.bounds, ax.bounds + ax.n + 1);
+    if (ax.kind == SG_AXIS_CELL) {                            // cellMap%build (cellMap_class.f90:87-138)
+      int rest = ax.cell_rest ? ax.n + 1 : 0;
+      c.cellBin[a].assign(o->geom.cells.size() + 1, rest);
+      for (int i = 0; i < ax.n; ++i) c.cellBin[a][ax.cells[i] + 1] = i + 1;
+      if (ax.cell_rest) nb += 1;
+    }
+    c.d.axes[a].bounds = nullptr;                             // the caller's arrays are not kept
+    c.d.axes[a].cells = nullptr;
+    c.multi[a] = mul; mul *= nb;
+  }
+  return mul;
+}
+
 int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
   Oracle* o = O(h);
   orc::TallyAdmin A;
@@ -2163,26 +2252,7 @@ int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
   for (int i = 0; i < t->n_clerks; ++i) {
     orc::Clerk c; c.d = t->clerks[i];
     c.width = c.d.n_resp > 0 ? c.d.n_resp : 1;
-    int64_t mul = 1;
-    for (int a = 0; a < c.d.n_axes; ++a) {
-      const sg_axis_desc& ax = c.d.axes[a];
-      int64_t nb = ax.n;
-      c.grid[a] = ax.grid != SG_GRID_DEFAULT ? ax.grid : (ax.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN);
-      if (c.grid[a] == SG_GRID_LOG) c.step[a] = std::log(ax.max / ax.min) / ax.n;   // grid_class.f90:76-90
-      else c.step[a] = (ax.max - ax.min) / ax.n;                                    // grid_class.f90:63-74
-      if (c.grid[a] == SG_GRID_UNSTRUCT && (ax.kind <= SG_AXIS_Z || ax.kind == SG_AXIS_ENERGY))
-        c.bounds[a].assign(ax.bounds, ax.bounds + ax.n + 1);
-      if (ax.kind == SG_AXIS_CELL) {                            // cellMap%build (cellMap_class.f90:87-138)
-        int rest = ax.cell_rest ? ax.n + 1 : 0;
-        c.cellBin[a].assign(o->geom.cells.size() + 1, rest);
-        for (int i = 0; i < ax.n; ++i) c.cellBin[a][ax.cells[i] + 1] = i + 1;
-        if (ax.cell_rest) nb += 1;
-      }
-      c.d.axes[a].bounds = nullptr;                             // the caller's arrays are not kept
-      c.d.axes[a].cells = nullptr;
-      c.multi[a] = mul; mul *= nb;
-    }
-    c.nbins = mul;
+    c.nbins = setupAxes(o, c);
     c.addr = memLoc;
     memLoc += c.size();
     A.clerks.push_back(c);
@@ -2191,6 +2261,27 @@ int32_t or_upload_tally(or_handle h, const sg_tally_desc* t, int32_t* admin) {
   if (t->norm_clerk >= 0) { A.normAddr = A.clerks[t->norm_clerk].addr; A.normVal = t->norm_val; }
   o->admins.push_back(A);
   *admin = (int32_t)o->admins.size() - 1;
+  return SG_OK;
+}
+// neutronMGimp / neutronCEimp options (neutronCEimp_class.f90:160-232) and weightWindowsField
+// (weightWindowsField_class.f90:75-111)
+int32_t or_set_collision(or_handle h, const sg_collision_desc* d) {
+  Oracle* o = O(h);
+  if (d->kind == SG_COLL_STD) { o->collImp = false; return SG_OK; }
+  if (d->split && d->max_wgt < 2 * d->min_wgt) { o->err = "upper weight bound must be at least twice the lower"; return SG_ERR_BAD_ARG; }
+  if (d->imp_abs && !d->roulette && !d->weight_windows) { o->err = "implicit absorption needs roulette or weight windows"; return SG_ERR_BAD_ARG; }
+  o->coll = *d;
+  if (d->weight_windows) {
+    orc::Clerk c{};
+    c.d.n_axes = d->ww_n_axes;
+    for (int a = 0; a < d->ww_n_axes; ++a) c.d.axes[a] = d->ww_axes[a];
+    const int64_t N = setupAxes(o, c);
+    o->wwMap = c;
+    o->wwLo.assign(d->ww_lower, d->ww_lower + N);
+    o->wwUp.assign(d->ww_upper, d->ww_upper + N);
+    if (!(d->ww_const_survival > 1.0)) { o->err = "survival constant must be bigger than one"; return SG_ERR_BAD_ARG; }
+  }
+  o->collImp = true;
   return SG_OK;
 }
 int32_t or_attach_tally(or_handle h, int32_t admin, int32_t atch) { O(h)->admins[admin].atch = atch; return SG_OK; }

@@ -254,6 +254,46 @@ def mg_struct(m):
     return s, keep
 
 
+COLL_STD, COLL_IMP = 0, 1
+
+
+class CollisionDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("imp_abs", C.c_int32), ("roulette", C.c_int32), ("split", C.c_int32),
+        ("weight_windows", C.c_int32), ("max_split", C.c_int32),
+        ("min_wgt", C.c_double), ("max_wgt", C.c_double), ("av_wgt", C.c_double),
+        ("ww_n_axes", C.c_int32), ("ww_axes", AxisDesc * 3), ("ww_lower", f64p), ("ww_upper", f64p),
+        ("ww_const_survival", C.c_double), ("buffer_depth", C.c_int32),
+    ]
+
+
+def collision(kind=COLL_IMP, imp_abs=False, roulette=False, split=False, max_split=1000, min_wgt=0.25,
+              max_wgt=1.25, av_wgt=0.5, ww_axes=None, ww_lower=None, ww_upper=None, ww_const_survival=0.0,
+              buffer_depth=0):
+    """Describe a collision processor: neutronMGstd/CEstd (COLL_STD) or neutronMGimp/CEimp (COLL_IMP)
+    with its options and defaults; weight windows when ww_axes is given (a map as for clerk())."""
+    d = CollisionDesc()
+    d.kind, d.imp_abs, d.roulette, d.split = kind, int(imp_abs), int(roulette), int(split)
+    d.max_split, d.min_wgt, d.max_wgt, d.av_wgt = max_split, min_wgt, max_wgt, av_wgt
+    d.buffer_depth = buffer_depth
+    keep = []
+    if ww_axes is not None:
+        m = clerk(CLERK_COLLISION, axes=ww_axes)
+        keep.append(m)
+        d.weight_windows = 1
+        d.ww_n_axes = m.n_axes
+        for i in range(m.n_axes):
+            d.ww_axes[i] = m.axes[i]
+        lo = np.ascontiguousarray(ww_lower, dtype=np.float64)
+        up = np.ascontiguousarray(ww_upper, dtype=np.float64)
+        keep += [lo, up]
+        d.ww_lower = lo.ctypes.data_as(f64p)
+        d.ww_upper = up.ctypes.data_as(f64p)
+        d.ww_const_survival = ww_const_survival
+    d._keep = keep
+    return d
+
+
 def unstruct_axis(kind, bounds):
     """A spaceMap / energyMap axis on an unstructured grid of ascending bounds (grid 'unstruct')."""
     b = np.ascontiguousarray(bounds, dtype=np.float64)

@@ -171,6 +171,19 @@ struct sg_handle_t {
   std::vector<DArr<float>> mapTab32;
   std::vector<DArr<int>> mapTabCell;
   int nCell = 0;                        // cells of the uploaded geometry
+  // collision processor variant (neutronMGimp / neutronCEimp) and its weight-window field
+  bool collImp = false, collBuf = false;   // collBuf: splitting or weight windows (split buffer)
+  Admin wwAdmin;                           // tables of the weight-window map
+  DArr<double> wwLo64, wwUp64;
+  DArr<float> wwLo32, wwUp32;
+  DColl<double> hColl64{};
+  DColl<float> hColl32{};
+  DArr<DColl<double>> dColl64;
+  DArr<DColl<float>> dColl32;
+  DArr<double> bufR, bufE;                 // split buffer (the handle's precision)
+  DArr<double> bufU64, bufW64, bufT64;
+  DArr<float> bufU32, bufW32, bufT32;
+  DArr<int> bufG;
   long long totalBins = 0;
   DArr<double> acc, bin, csum, csum2;
 
@@ -913,6 +926,10 @@ DPart<R> part_view(sg_handle h) {
   return p;
 }
 
+template <class R> const DColl<R>* coll_view(sg_handle h);
+template <> const DColl<double>* coll_view<double>(sg_handle h) { return h->dColl64.p; }
+template <> const DColl<float>* coll_view<float>(sg_handle h) { return h->dColl32.p; }
+
 DSites site_view(sg_handle h) {
   return DSites{h->sR.p, h->sDir.p, h->sWgt.p, h->sG.p, h->sBrood.p, h->sSeq.p, h->sTime.p, h->sCursor.p, h->regionCap};
 }
@@ -920,6 +937,33 @@ DSites site_view(sg_handle h) {
 // Bins of one map axis: cellMap has n cells plus the `undefBin` rest bin (cellMap_class.f90:129-136)
 long long axis_bins(const sg_axis_desc& x) {
   return x.kind == SG_AXIS_CELL ? (long long)x.n + (x.cell_rest ? 1 : 0) : x.n;
+}
+
+// The multiMap axes of one clerk (or of the weight-window map) as the kernels read them; tables
+// from A.tab64 / A.tab32 at [tab + axis].  Returns the number of map bins.
+template <class R>
+long long fill_axes(DClerk& K, const sg_axis_desc* axes, int n, const Admin& A, size_t tab) {
+  long long mul = 1;
+  K.n_axes = n;
+  for (int i = 0; i < n; ++i) {
+    const sg_axis_desc& x = axes[i];
+    K.ax_kind[i] = x.kind;
+    K.ax_n[i] = x.n;
+    K.ax_min[i] = x.min;
+    int grid = x.grid;
+    if (grid == SG_GRID_DEFAULT) grid = x.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN;
+    K.ax_grid[i] = grid;
+    if (grid == SG_GRID_LOG)                         // grid step (grid_class.f90:60-90)
+      K.ax_step[i] = std::log(x.max / x.min) / x.n;
+    else K.ax_step[i] = (x.max - x.min) / x.n;
+    K.ax_inv_step[i] = 1.0 / K.ax_step[i];
+    K.ax_minf[i] = (float)K.ax_min[i];
+    K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
+    K.ax_tab[i] = (sizeof(R) == 8 ? A.tab64 : A.tab32)[tab + i];
+    K.multi[i] = mul;
+    mul *= axis_bins(x);
+  }
+  return mul;
 }
 
 // clerks of admin `a` and its attachment flattened for one launch (attachment first)
@@ -957,26 +1001,9 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
       K.width = d.n_resp > 0 ? d.n_resp : 1;
       for (int i = 0; i < 4; ++i) K.resp[i] = d.resp[i];
       K.n_axes = d.n_axes;
-      long long mul = 1;
-      for (int i = 0; i < d.n_axes; ++i) {
-        const sg_axis_desc& x = d.axes[i];
-        K.ax_kind[i] = x.kind;
-        K.ax_n[i] = x.n;
-        K.ax_min[i] = x.min;
-        int grid = x.grid;
-        if (grid == SG_GRID_DEFAULT) grid = x.kind == SG_AXIS_ENERGY ? SG_GRID_LOG : SG_GRID_LIN;
-        K.ax_grid[i] = grid;
-        if (grid == SG_GRID_LOG)                       // grid step (grid_class.f90:60-90)
-          K.ax_step[i] = std::log(x.max / x.min) / x.n;
-        else K.ax_step[i] = (x.max - x.min) / x.n;
-        K.ax_inv_step[i] = 1.0 / K.ax_step[i];
-        K.ax_minf[i] = (float)K.ax_min[i];
-        K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
-        K.ax_tab[i] = (sizeof(R) == 8 ? A.tab64 : A.tab32)[3 * c + i];
-        if (x.kind == SG_AXIS_CELL) t.has_cellmap = 1;
-        K.multi[i] = mul;
-        mul *= axis_bins(x);
-      }
+      const long long mul = fill_axes<R>(K, d.axes, d.n_axes, A, 3 * c);
+      for (int i = 0; i < d.n_axes; ++i)
+        if (d.axes[i].kind == SG_AXIS_CELL) t.has_cellmap = 1;
       K.g_top = d.filter_g_top;
       K.g_low = d.filter_g_low;
       K.acc_off = A.off + (A.addr[c] - 1) - lo;
@@ -1028,6 +1055,10 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.hist_nsites = h->histN.p;
   t.rec_coll = h->cfg.record_histories ? h->recColl.p : nullptr;
   t.rec_rng = h->cfg.record_histories ? h->recRng.p : nullptr;
+  t.coll_imp = h->collImp ? 1 : 0;
+  t.coll = h->collImp ? coll_view<R>(h) : nullptr;
+  if (h->collImp && h->collBuf && h->cfg.form == SG_FORM_EVENT)
+    return h->fail(SG_ERR_BAD_ARG, "splitting and weight windows need the history-loop form");
   t.ctr = h->ctr.p;
   t.use_cache = transport_cache(h->cfg.transport);
   t.max_segments = 1000000;
@@ -1362,6 +1393,9 @@ int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<doubl
   t64->max_segments = t32->max_segments = 1000000;
   t64->ht_cutoff = h->htCutoff;
   t32->ht_cutoff = (float)h->htCutoff;
+  t64->coll_imp = t32->coll_imp = h->collImp ? 1 : 0;
+  t64->coll = h->collImp ? h->dColl64.p : nullptr;
+  t32->coll = h->collImp ? h->dColl32.p : nullptr;
   return SG_OK;
 }
 
@@ -1543,6 +1577,9 @@ int32_t sg_destroy(sg_handle h) {
   h->ceMaj64.free(); h->ceXsF.free(); h->ceAF.free(); h->ceKTF.free(); h->ceDensF.free(); h->ceMajF.free();
   h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
   h->pE.free();
+  h->wwLo64.free(); h->wwUp64.free(); h->wwLo32.free(); h->wwUp32.free(); h->dColl64.free(); h->dColl32.free();
+  h->bufR.free(); h->bufE.free(); h->bufU64.free(); h->bufW64.free(); h->bufT64.free(); h->bufU32.free();
+  h->bufW32.free(); h->bufT32.free(); h->bufG.free();
   for (auto& a : h->mapTab64) a.free();
   for (auto& a : h->mapTab32) a.free();
   for (auto& a : h->mapTabCell) a.free();
@@ -1941,6 +1978,92 @@ int32_t sg_bank_read_file(const char* path, int32_t binary, sg_bank* b, int32_t 
   }
   std::fclose(f);
   *n = c;
+  return SG_OK;
+}
+
+// neutronMGimp / neutronCEimp%init (neutronCEimp_class.f90:160-232) and weightWindowsField%init
+// (weightWindowsField_class.f90:75-111).  The split buffer is allocated here, not when a cycle runs:
+// it holds `depth` particles for every thread a persistent launch can have (SMs x threads per SM).
+int32_t sg_set_collision(sg_handle h, const sg_collision_desc* d) {
+  if (!h || !d) return SG_ERR_BAD_ARG;
+  if (d->kind == SG_COLL_STD) { h->collImp = false; h->collBuf = false; return SG_OK; }
+  if (d->kind != SG_COLL_IMP) return h->fail(SG_ERR_BAD_ARG, "collision: unknown processor");
+  if (d->max_split < 1) return h->fail(SG_ERR_BAD_ARG, "collision: maxSplit must be at least 1");
+  if (d->split && d->max_wgt < 2 * d->min_wgt)
+    return h->fail(SG_ERR_BAD_ARG, "collision: upper weight bound must be at least twice the lower weight bound");
+  if (d->imp_abs && !d->roulette && !d->weight_windows)
+    return h->fail(SG_ERR_BAD_ARG, "collision: implicit absorption needs Russian roulette or weight windows");
+  if ((d->roulette && !(d->av_wgt > 0.0)) || (d->split && !(d->max_wgt > 0.0)))
+    return h->fail(SG_ERR_BAD_ARG, "collision: weights must be positive");
+  DColl<double> c64{};
+  DColl<float> c32{};
+  c64.imp_abs = c32.imp_abs = d->imp_abs != 0;
+  c64.roulette = c32.roulette = d->roulette != 0;
+  c64.split = c32.split = d->split != 0;
+  c64.ww = c32.ww = d->weight_windows != 0;
+  c64.max_split = c32.max_split = d->max_split;
+  c64.min_wgt = d->min_wgt; c64.max_wgt = d->max_wgt; c64.av_wgt = d->av_wgt;
+  c32.min_wgt = (float)d->min_wgt; c32.max_wgt = (float)d->max_wgt; c32.av_wgt = (float)d->av_wgt;
+  if (d->weight_windows) {
+    if (d->ww_n_axes < 1 || d->ww_n_axes > 3) return h->fail(SG_ERR_BAD_ARG, "weight windows: map needs 1-3 axes");
+    if (!d->ww_lower || !d->ww_upper) return h->fail(SG_ERR_BAD_ARG, "weight windows: wLower and wUpper are required");
+    if (!(d->ww_const_survival > 1.0)) return h->fail(SG_ERR_BAD_ARG, "weight windows: survival constant must be bigger than one");
+    Admin W;
+    long long N = 1;
+    for (int a = 0; a < d->ww_n_axes; ++a) {
+      const int rc = build_axis(h, d->ww_axes[a], W);
+      if (rc) return rc;
+      N *= axis_bins(d->ww_axes[a]);
+    }
+    for (int a = d->ww_n_axes; a < 3; ++a) { W.tab64.push_back(nullptr); W.tab32.push_back(nullptr); }
+    std::vector<double> lo(d->ww_lower, d->ww_lower + N), up(d->ww_upper, d->ww_upper + N);
+    for (long long i = 0; i < N; ++i) {
+      if (lo[i] < 0.0 || up[i] < 0.0) return h->fail(SG_ERR_BAD_ARG, "weight windows: negative weights");
+      if (lo[i] * d->ww_const_survival > up[i])
+        return h->fail(SG_ERR_BAD_ARG, "weight windows: roulette survival weight above the upper weight");
+    }
+    std::vector<float> lof(lo.begin(), lo.end()), upf(up.begin(), up.end());
+    CK(h->wwLo64.upload(lo, h->stream));
+    CK(h->wwUp64.upload(up, h->stream));
+    CK(h->wwLo32.upload(lof, h->stream));
+    CK(h->wwUp32.upload(upf, h->stream));
+    fill_axes<double>(c64.ww_map, d->ww_axes, d->ww_n_axes, W, 0);
+    fill_axes<float>(c32.ww_map, d->ww_axes, d->ww_n_axes, W, 0);
+    c64.ww_lower = h->wwLo64.p; c64.ww_upper = h->wwUp64.p; c64.ww_cs = d->ww_const_survival;
+    c32.ww_lower = h->wwLo32.p; c32.ww_upper = h->wwUp32.p; c32.ww_cs = (float)d->ww_const_survival;
+    h->wwAdmin = W;
+  }
+  const bool buf = d->split || d->weight_windows;
+  if (buf) {
+    const int depth = d->buffer_depth > 0 ? d->buffer_depth : 32;
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, h->cfg.device));
+    const size_t n = (size_t)prop.multiProcessorCount * prop.maxThreadsPerMultiProcessor * depth;
+    CK(h->bufR.alloc(3 * n));
+    CK(h->bufE.alloc(n));
+    CK(h->bufG.alloc(n));
+    if (h->cfg.precision == SG_PREC_FP64) {
+      CK(h->bufU64.alloc(3 * n)); CK(h->bufW64.alloc(n)); CK(h->bufT64.alloc(n));
+      h->bufU32.free(); h->bufW32.free(); h->bufT32.free();
+    } else {
+      CK(h->bufU32.alloc(3 * n)); CK(h->bufW32.alloc(n)); CK(h->bufT32.alloc(n));
+      h->bufU64.free(); h->bufW64.free(); h->bufT64.free();
+    }
+    c64.b_r = c32.b_r = h->bufR.p;
+    c64.b_E = c32.b_E = h->bufE.p;
+    c64.b_G = c32.b_G = h->bufG.p;
+    c64.b_u = h->bufU64.p; c64.b_w = h->bufW64.p; c64.b_time = h->bufT64.p;
+    c32.b_u = h->bufU32.p; c32.b_w = h->bufW32.p; c32.b_time = h->bufT32.p;
+    c64.depth = c32.depth = depth;
+  }
+  std::vector<DColl<double>> v64(1, c64);
+  std::vector<DColl<float>> v32(1, c32);
+  CK(h->dColl64.upload(v64, h->stream));
+  CK(h->dColl32.upload(v32, h->stream));
+  h->hColl64 = c64;
+  h->hColl32 = c32;
+  h->collImp = true;
+  h->collBuf = buf;
   return SG_OK;
 }
 

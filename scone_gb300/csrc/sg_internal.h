@@ -221,6 +221,26 @@ inline bool transport_cache(int transport) {
   return transport != SG_TRANSPORT_ST_NOCACHE && transport != SG_TRANSPORT_HT_NOCACHE;
 }
 
+// neutronMGimp / neutronCEimp options and the weight-window field, in device memory (read at
+// collisions only).  The split buffer holds `depth` particles per thread of the launch.
+template <class R>
+struct DColl {
+  int imp_abs, roulette, split, ww, max_split;
+  R min_wgt, max_wgt, av_wgt;
+  DClerk ww_map;             // weightWindowsField map (axes only)
+  const R* ww_lower;         // [bins]
+  const R* ww_upper;
+  R ww_cs;                   // constSurvival
+  // split buffer: entry (thread, j) at thread * depth + j
+  double* b_r;               // [3]
+  R* b_u;                    // [3]
+  R* b_w;
+  double* b_E;
+  int* b_G;
+  R* b_time;
+  int depth;
+};
+
 template <class R>
 struct TransportArgs {
   DGeom geom;
@@ -248,6 +268,8 @@ struct TransportArgs {
   R ht_cutoff;          // transportOperatorHT `cutoff`
   DPart<R> part;        // event form: particle state
   DQueues q;            // event form: queues of the launch
+  int coll_imp;         // 1: neutronMGimp / neutronCEimp with *coll
+  const DColl<R>* coll;
 };
 
 }  // namespace sg

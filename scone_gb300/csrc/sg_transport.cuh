@@ -96,6 +96,8 @@ struct Tracker {
   // ANA_LEAK), in R; the batch sums they are added to are FP64
   R kprod, kscat, kabs, kleak;
   unsigned long long nEv, nColl;
+  int splitCount;    // particle%splitCount (neutronCEimp / neutronMGimp)
+  int nbuf;          // split particles of this history waiting in the buffer
   bool htDT;         // hybrid tracking: the current transit uses delta tracking
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
@@ -104,6 +106,8 @@ struct Tracker {
     kprod = kscat = kabs = kleak = R(0);
     nEv = nColl = 0;
     htDT = false;
+    splitCount = 0;
+    nbuf = 0;
   }
 
   __device__ __forceinline__ R xs(const R* t, int mat, int g) const { return t[(mat - 1) * mg.nG + (g - 1)]; }
@@ -337,6 +341,11 @@ struct Tracker {
     x = x - mcap;
     if (x > R(0)) C = C + 1;
     report_in_coll(false, trackXS);
+    if (A.coll_imp && A.coll->imp_abs) {                 // neutronCEimp implicit (:406-424)
+      const R scat = mel + min_;
+      w = w * scat / mt;
+      C = (rng.get() < mel / scat) ? 1 : 2;
+    }
     bool dead;
     if (C == 1) {                                        // elastic (:340-384)
       const R Anuc = ce.A[nuc], kT = ce.kT[nuc];
@@ -386,10 +395,78 @@ struct Tracker {
     } else {
       dead = true;                                       // capture / fission
     }
-    if (E < ce.minE) dead = true;                        // cutoffs (:434-444)
+    if (A.coll_imp) dead = imp_cutoffs(dead);
+    else if (E < ce.minE) dead = true;                   // cutoffs (:434-444)
     collN += 1;
     nColl += 1;
     return dead;
+  }
+
+  // ---- neutronCEimp / neutronMGimp cutoffs (neutronCEimp_class.f90:633-734,
+  // neutronMGimp_class.f90:319-407).  Returns whether the particle is dead afterwards.
+  __device__ __forceinline__ bool imp_cutoffs(bool dead) {
+    if (dead) return true;
+    const DColl<R>& K = *A.coll;
+    if constexpr (CE) { if (E < ce.minE) return true; }
+    if (K.ww) {                                          // weightWindowsField%atP (:148-171)
+      const int bin = map_bin_e(K.ww_map, c.r0, G, c.mat, lowest_cell(), E);
+      R lo = R(0), up = R(0), av = R(0);
+      if (bin > 0) { lo = K.ww_lower[bin - 1]; up = K.ww_upper[bin - 1]; av = lo * K.ww_cs; }
+      if (w > up && up != R(0) && splitCount < K.max_split) split(up);
+      else if (w < lo) return roulette(av);
+      return false;
+    }
+    if constexpr (CE) {
+      if (K.split && w > K.max_wgt) split(K.max_wgt);
+      else if (K.roulette && w < K.min_wgt) return roulette(K.av_wgt);
+    }
+    return false;
+  }
+  // russianRoulette (:683-694)
+  __device__ __forceinline__ bool roulette(R av) {
+    if (rng.get() < (R(1) - w / av)) return true;
+    w = av;
+    return false;
+  }
+  // split (:699-734): mult - 1 copies of weight w / mult into the history's buffer
+  __device__ __forceinline__ void split(R maxW) {
+    const DColl<R>& K = *A.coll;
+    int mult = (int)ceil((double)(w / maxW));
+    if (mult + splitCount > K.max_split) mult = K.max_split - splitCount + 1;
+    const R ws = w / (R)mult;
+    const long long lane = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = 1; i < mult; ++i) {
+      if (nbuf >= K.depth) { raise_error(A.ctr, SG_ERR_BANK_OVERFLOW, hist); break; }
+      const long long e = lane * K.depth + nbuf;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { K.b_r[3 * e + k] = c.r0[k]; K.b_u[3 * e + k] = c.u[k]; }
+      K.b_w[e] = ws;
+      K.b_E[e] = CE ? E : 0.0;
+      K.b_G[e] = G;
+      K.b_time[e] = time;
+      nbuf += 1;
+    }
+    splitCount += mult;
+    w = w / (R)mult;
+  }
+  // buffer%release and the restart of the gen loop's bufferLoop (fixedSourcePhysicsPackage_class.f90
+  // :209-216,235-239): the last split particle, placed, with its weight as the pre-history weight;
+  // the RNG stream continues
+  __device__ __forceinline__ void release() {
+    const DColl<R>& K = *A.coll;
+    nbuf -= 1;
+    const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * K.depth + nbuf;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { c.r0[k] = K.b_r[3 * e + k]; c.u[k] = K.b_u[3 * e + k]; }
+    w = K.b_w[e];
+    w0 = w;
+    G = K.b_G[e];
+    if constexpr (CE) set_energy(K.b_E[e]);
+    time = K.b_time[e];
+    splitCount = 0;
+    cache.lvl = 0;
+    if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist);
+    select_ht();
   }
 
   __device__ __forceinline__ void write_site(const R dir[3], int gout, R wgt) {
@@ -494,6 +571,7 @@ struct Tracker {
       MT = (C == 3) ? MT_DISAP : MT_FISSION;
       dead = true;
     }
+    if (A.coll_imp) dead = imp_cutoffs(dead);            // neutronMGimp cutoffs (:319-351)
     collN += 1;
     nColl += 1;
     if (A.keff_clerk >= 0 && MT == MT_IESCATTER) {       // keffImplicit reportOutColl (:241-268)
@@ -521,6 +599,8 @@ struct Tracker {
     collN = 0;
     nsites = 0;
     segs = 0;
+    splitCount = 0;
+    nbuf = 0;
     cache.lvl = 0;
     if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
     select_ht();
@@ -792,7 +872,10 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
     }
     if (__all_sync(FULL, !alive)) break;
     if (alive) {
-      if (T.step()) { T.finish(); alive = false; }
+      if (T.step()) {
+        if (T.nbuf > 0) T.release();                    // the history's split particles, LIFO
+        else { T.finish(); alive = false; }
+      }
     }
   }
 

@@ -39,6 +39,7 @@ def load(build=True):
         "sg_upload_mg": (i32, [vp, P(abi.MGDesc)]),
         "sg_upload_ce": (i32, [vp, P(abi.CEDesc)]),
         "sg_upload_tally": (i32, [vp, P(abi.TallyDesc), P(i32)]),
+        "sg_set_collision": (i32, [vp, P(abi.CollisionDesc)]),
         "sg_attach_tally": (i32, [vp, i32, i32]),
         "sg_set_point_source": (i32, [vp, P(abi.PointSourceDesc)]),
         "sg_generate_source": (i32, [vp, u64, i32, P(abi.Bank)]),
@@ -213,6 +214,11 @@ class TransportOperatorGPU:
         pop = C.c_int32()
         self._check(self.L.sg_eigen_get_bank(self.h, C.byref(b.struct), cap, C.byref(pop)))
         return b, pop.value
+
+    def set_collision(self, desc):
+        """neutronMGimp / neutronCEimp options (an abi.collision() description)."""
+        self._keep.append(desc)
+        self._check(self.L.sg_set_collision(self.h, C.byref(desc)))
 
     def set_file_source(self, bank):
         """fileSource: fixed-source cycles sample their particles from this host bank."""

@@ -394,3 +394,84 @@ def test_rotated_universes_mixed_statistics(gpu_mod):
         out[prec] = t.bins(a)[:, 1]
         t.close()
     np.testing.assert_allclose(out[abi.PREC_MIXED][:12], out[abi.PREC_FP64][:12], rtol=0.03)
+
+
+def _ww_sphere():
+    rng = np.random.default_rng(5)
+    p = problems.fixed_source_problem(rng, 2, "sphere", radius=6.0)
+    x = np.linspace(-6.0, 6.0, 13)
+    centres = 0.5 * (x[1:] + x[:-1])
+    lower = 0.4 / (1.0 + np.abs(centres))
+    desc = abi.collision(abi.COLL_IMP, ww_axes=[(abi.AXIS_X, 12, -6.0, 6.0)], ww_lower=lower,
+                         ww_upper=5.0 * lower, ww_const_survival=2.5, buffer_depth=64)
+    return p, desc
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_weight_windows_mg_fp64_history_parity(gpu_mod, oracle_mod, transport):
+    """neutronMGimp with weight windows (splitting into the history's buffer, roulette) on the device
+    against the oracle: per-history collision counts and final RNG states, and tallies."""
+    p, desc = _ww_sphere()
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=abi.FORM_HISTORY)
+    g.set_collision(desc)
+    o.set_collision(desc)
+    n = 20000
+    bank = o.generate_source(SEED, n)
+    ag, ao = g.upload_tally(p.tallies["flux"]), o.upload_tally(p.tallies["flux"])
+    g.transport_bank(ag, bank, 8642)
+    o.transport_bank(ao, bank, 8642)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co) and np.array_equal(rg, ro)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_ce_imp_fp64_history_parity(gpu_mod, oracle_mod, form):
+    """neutronCEimp with implicit absorption and roulette (and splitting in the history-loop form)
+    on the CE slab: per-history agreement with the oracle and equal tallies."""
+    p = problems.ce_slab_3layer(points=(2000, 4000))
+    desc = abi.collision(abi.COLL_IMP, imp_abs=True, roulette=True, split=(form == abi.FORM_HISTORY),
+                         min_wgt=0.25, max_wgt=1.25, av_wgt=0.5)
+    g, o = make_pair(gpu_mod, oracle_mod, p, abi.TRANSPORT_DT, form=form)
+    g.set_collision(desc)
+    o.set_collision(desc)
+    n = 5000
+    bank = o.generate_source(SEED, n)
+    ag, ao = g.upload_tally(p.tallies["flux"]), o.upload_tally(p.tallies["flux"])
+    g.transport_bank(ag, bank, 1122)
+    o.transport_bank(ao, bank, 1122)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co) and np.array_equal(rg, ro)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=0)
+
+
+def test_weight_windows_mixed_statistics(gpu_mod):
+    """Mixed form with weight windows against the FP64 form and against analog transport."""
+    p, desc = _ww_sphere()
+    out = {}
+    for key, prec, imp in (("f64", abi.PREC_FP64, True), ("mx", abi.PREC_MIXED, True), ("std", abi.PREC_FP64, False)):
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_ST, max_bank=1 << 18)
+        if imp:
+            t.set_collision(desc)
+        a = t.upload_tally(p.tallies["flux"])
+        t.fixed_source_cycle(a, 200000, 55)
+        out[key] = t.bins(a)[:, 1]
+        t.close()
+    np.testing.assert_allclose(out["mx"], out["f64"], rtol=0.02)
+    np.testing.assert_allclose(out["f64"], out["std"], rtol=0.02)
+
+
+def test_splitting_needs_history_form(gpu_mod):
+    p, desc = _ww_sphere()
+    t = gpu_mod.TransportOperatorGPU(p, max_bank=1 << 12, form=abi.FORM_EVENT)
+    t.set_collision(desc)
+    a = t.upload_tally(p.tallies["flux"])
+    with pytest.raises(gpu_mod.SconeGpuError, match="history-loop"):
+        t.fixed_source_cycle(a, 1000, 1)
+    t.close()

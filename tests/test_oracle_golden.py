@@ -601,3 +601,64 @@ def test_rotated_pins_runs_and_rotation_matters(oracle_mod):
     b2 = o2.bins(a2)[:, 1]
     assert b1[:6].min() > 0
     assert not np.allclose(b1, b2)
+
+
+def _ww_sphere():
+    """A 2-group homogeneous sphere (radius 6 cm) and weight windows over x that rise toward the
+    centre: particles moving out split, particles moving in are rouletted."""
+    rng = np.random.default_rng(5)
+    p = problems.fixed_source_problem(rng, 2, "sphere", radius=6.0)
+    x = np.linspace(-6.0, 6.0, 13)
+    centres = 0.5 * (x[1:] + x[:-1])
+    lower = 0.4 / (1.0 + np.abs(centres))
+    upper = 5.0 * lower
+    desc = abi.collision(abi.COLL_IMP, ww_axes=[(abi.AXIS_X, 12, -6.0, 6.0)], ww_lower=lower, ww_upper=upper,
+                         ww_const_survival=2.5, buffer_depth=64)
+    return p, desc
+
+
+def test_weight_windows_mg_unbiased(oracle_mod):
+    """neutronMGimp with weight windows (weightWindowsField: split above wUpper, roulette below
+    wLower to wLower * constSurvival) leaves the flux estimate unbiased against neutronMGstd."""
+    p, desc = _ww_sphere()
+    n = 20000
+    res = {}
+    for imp in (False, True):
+        o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_ST)
+        if imp:
+            o.set_collision(desc)
+        a = o.upload_tally(p.tallies["flux"])
+        o.fixed_source_cycle(a, n, 2024)
+        res[imp] = o.bins(a)[:, 1]
+    std, ww = res[False], res[True]
+    assert std.min() > 0
+    np.testing.assert_allclose(ww, std, rtol=0.05)
+    assert not np.allclose(ww, std, rtol=1e-9)                 # the game did act
+
+
+def test_ce_implicit_absorption_roulette_unbiased(oracle_mod):
+    """neutronCEimp with implicit absorption, roulette and splitting: the flux tally agrees with
+    neutronCEstd within statistics on the 3-layer CE slab."""
+    p = problems.ce_slab_3layer(points=(2000, 4000))
+    n = 4000
+    res = {}
+    for imp in (False, True):
+        o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_DT)
+        if imp:
+            o.set_collision(abi.collision(abi.COLL_IMP, imp_abs=True, roulette=True, split=True,
+                                          min_wgt=0.25, max_wgt=1.25, av_wgt=0.5))
+        a = o.upload_tally(p.tallies["flux"])
+        o.fixed_source_cycle(a, n, 777)
+        res[imp] = o.bins(a)[:, 1]
+    std, imp = res[False], res[True]
+    ok = std > 0.05 * std.max()
+    np.testing.assert_allclose(imp[ok].sum(), std[ok].sum(), rtol=0.05)
+
+
+def test_collision_options_rejected(oracle_mod):
+    p, _ = _ww_sphere()
+    o = oracle_mod.Oracle(p)
+    with pytest.raises(Exception, match="roulette"):
+        o.set_collision(abi.collision(abi.COLL_IMP, imp_abs=True))
+    with pytest.raises(Exception, match="twice"):
+        o.set_collision(abi.collision(abi.COLL_IMP, split=True, min_wgt=1.0, max_wgt=1.5))
