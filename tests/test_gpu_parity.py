@@ -456,7 +456,8 @@ def test_weight_windows_mixed_statistics(gpu_mod):
     p, desc = _ww_sphere()
     out = {}
     for key, prec, imp in (("f64", abi.PREC_FP64, True), ("mx", abi.PREC_MIXED, True), ("std", abi.PREC_FP64, False)):
-        t = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_ST, max_bank=1 << 18)
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_ST, max_bank=1 << 18,
+                                         form=abi.FORM_HISTORY)
         if imp:
             t.set_collision(desc)
         a = t.upload_tally(p.tallies["flux"])
