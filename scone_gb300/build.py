@@ -94,6 +94,15 @@ def build(force=False, verbose=False, extra=()):
         running.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     while running:
         wait_one()
+    # a unit that failed while many compilers ran is compiled once more on its own (nvcc has been seen
+    # to crash under load); a real compile error fails again and is reported
+    retry = [(u, c) for u, c in cmds if u in failed]
+    failed.clear()
+    for unit, cmd in retry:
+        p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if p.returncode != 0:
+            failed.append(unit)
+            sys.stderr.write(p.stdout.decode(errors="replace"))
     if failed:
         raise RuntimeError("nvcc failed for " + ", ".join(failed))
     tmp = LIB + ".tmp"
