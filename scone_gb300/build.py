@@ -50,6 +50,17 @@ def up_to_date():
     return all(os.path.getmtime(s) <= t for s in sources())
 
 
+def _big_stack():
+    """Compilers inherit the largest stack the hard limit allows: the front end recurses deeply on the
+    biggest units, and an 8 MB stack has made it crash on aarch64 hosts."""
+    try:
+        import resource
+        soft, hard = resource.getrlimit(resource.RLIMIT_STACK)
+        resource.setrlimit(resource.RLIMIT_STACK, (hard, hard))
+    except (ImportError, ValueError, OSError):
+        pass
+
+
 def build(force=False, verbose=False, extra=()):
     if not force and up_to_date():
         return LIB
@@ -91,15 +102,20 @@ def build(force=False, verbose=False, extra=()):
             wait_one()
         if verbose:
             print(" ".join(cmd), flush=True)
-        running.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        running.append((unit, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                                               preexec_fn=_big_stack)))
     while running:
         wait_one()
-    # a unit that failed while many compilers ran is compiled once more on its own (nvcc has been seen
-    # to crash under load); a real compile error fails again and is reported
+    # a unit that failed while many compilers ran is compiled again on its own, up to three times (the
+    # compiler has been seen to crash with SIGSEGV on aarch64 hosts, now and then, on units it
+    # compiles cleanly otherwise); a real compile error fails every time and is reported
     retry = [(u, c) for u, c in cmds if u in failed]
     failed.clear()
     for unit, cmd in retry:
-        p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        for attempt in range(3):
+            p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, preexec_fn=_big_stack)
+            if p.returncode == 0:
+                break
         if p.returncode != 0:
             failed.append(unit)
             sys.stderr.write(p.stdout.decode(errors="replace"))
