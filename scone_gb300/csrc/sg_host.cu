@@ -1045,11 +1045,12 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.k_eff = d_k;
   t.acc = h->acc.p + lo;
   t.acc_n = (int)(hi - lo);
-  // Block-local FP64 score memory in shared memory for the FP64 form; the mixed form scores straight
-  // into global memory (reductions performed in L2 cost the history loop less than shared-memory
-  // FP64 atomics: 6 % on the 17x17 lattice).
+  // Few bins: block-local score memory in shared memory (global reductions on a handful of
+  // addresses serialise in L2: 2.5-6x slower on the 2-group infinite medium).  Many bins: straight
+  // into global memory (L2 reductions spread over the bins cost less than shared-memory FP64
+  // atomics: 7 % on the 2 023-bin lattice mesh).
   size_t smem = (size_t)t.acc_n * sizeof(double);
-  t.use_smem = (sizeof(R) == 8 && t.acc_n > 0 && smem <= 64 * 1024) ? 1 : 0;
+  t.use_smem = (t.acc_n > 0 && t.acc_n < 1024) ? 1 : 0;
   if (!t.use_smem) smem = 0;
   t.sites = site_view(h);
   t.hist_nsites = h->histN.p;

@@ -847,7 +847,6 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
   Tracker<R, MAXL, OP, CE> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
   bool alive = false, done = false;
-  bool coll = false;           // the lane's particle waits for its collision
   int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
 
   while (true) {
@@ -872,20 +871,18 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
       need &= ~__ballot_sync(FULL, mine);
     }
     if (__all_sync(FULL, !alive)) break;
-    // Collisions wait until at least half of the warp's live lanes have one, and are then processed
-    // together: lanes keep flying meanwhile, so the long, branchy collision code runs with more
-    // lanes active (7-10 % on the 17x17 lattice).  Each history keeps its own RNG stream, so the
-    // results do not depend on this order.
-    bool ended = false;
-    if (alive && !coll) {
+    // One flight per live lane, then the warp meets again (the vote) before the lanes whose flight
+    // ended in a real collision process it: the collision code then starts with every colliding lane
+    // together (7 % faster on the 17x17 lattice than flight and collision in one branch).  Making
+    // lanes wait until half the warp has a collision was no faster with delta tracking and 8 %
+    // slower with surface tracking.
+    bool ended = false, coll = false;
+    if (alive) {
       const int e = T.segment();
-      if (e == SEG_COLLIDE) coll = true;
-      else ended = (e == SEG_END);
+      coll = (e == SEG_COLLIDE);
+      ended = (e == SEG_END);
     }
-    const unsigned cm = __ballot_sync(FULL, coll);
-    const unsigned lm = __ballot_sync(FULL, alive && !ended);
-    if (2 * __popc(cm) >= __popc(lm) && coll) {
-      coll = false;
+    if (__any_sync(FULL, coll) && coll) {
       ended = T.collide(T.trackXS);
       if (!ended) T.select_ht();
     }
