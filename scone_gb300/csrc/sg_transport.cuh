@@ -155,10 +155,15 @@ struct Tracker {
   // the cell the particle is in at its lowest level, as a 1-based index of the geometry's cells; 0
   // when that level is not a cellUniverse (coord%cell, coord_class.f90:419-425)
   __device__ __forceinline__ int lowest_cell() const {
-    const int l = c.nest - 1;
-    const DUni& U = geom.g.unis[c.uni[l]];
-    if (U.type != SG_UNI_CELL || c.local[l] > U.i[1]) return 0;   // local n+1: no cell of the universe
-    return geom.g.uni_cells[U.i[0] + c.local[l] - 1] + 1;
+    // the lowest level's universe and local cell, selected with compile-time indices only (a
+    // runtime index would put the level arrays in local memory for the whole kernel)
+    int u = c.uni[0], loc = c.local[0];
+#pragma unroll
+    for (int l = 1; l < MAXL; ++l)
+      if (l < c.nest) { u = c.uni[l]; loc = c.local[l]; }
+    const DUni& U = geom.g.unis[u];
+    if (U.type != SG_UNI_CELL || loc > U.i[1]) return 0;   // local n+1: no cell of the universe
+    return geom.g.uni_cells[U.i[0] + loc - 1] + 1;
   }
 
   // binaryFloorIdxClosed (genericProcedures.f90:132-166) on an unstructured grid of nb ascending
