@@ -75,6 +75,7 @@ def lib():
             "or_target_velocity": (i32, [f64, P(f64), f64, f64, P(u64), P(f64)]),
             "or_grid_search": (i32, [P(f64), i32, f64]),
             "or_set_collision": (i32, [vp, P(abi.CollisionDesc)]),
+            "or_map_point": (i32, [vp, P(abi.AxisDesc), i32, P(f64), i32, i32, i32, f64, i32, P(i32)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -164,6 +165,15 @@ class Oracle:
         """neutronMGimp / neutronCEimp options (an abi.collision() description)."""
         self._keep.append(desc)
         self._check(self.L.or_set_collision(self.h, C.byref(desc)))
+
+    def map_point(self, axes, r=(0.0, 0.0, 0.0), G=1, mat=1, cell=0, E=0.0, mg=True):
+        """Bin (1-based, 0 outside) of one particle state in the multiMap of `axes` (as for abi.clerk)."""
+        c = abi.clerk(abi.CLERK_COLLISION, axes=axes)
+        _, pr = _d(r)
+        b = C.c_int32()
+        self._check(self.L.or_map_point(self.h, c.axes, c.n_axes, pr, G, mat, cell, float(E), 1 if mg else 0,
+                                        C.byref(b)))
+        return b.value
 
     def grid_search(self, bounds, v):
         """grid%search of an unstructured grid: 1-based bin of `v`, 0 outside."""

@@ -2215,6 +2215,21 @@ int32_t or_target_velocity(double E, const double* dir, double A, double kT, uin
   return SG_OK;
 }
 
+static int64_t setupAxes(Oracle* o, orc::Clerk& c);
+
+// one particle state through a multiMap of the given axes (tallyMap%map): 1-based bin, 0 outside
+int32_t or_map_point(or_handle h, const sg_axis_desc* axes, int32_t n_axes, const double* r, int32_t G,
+                     int32_t mat, int32_t cell, double E, int32_t isMG, int32_t* bin) {
+  Oracle* o = O(h);
+  orc::Clerk c{};
+  c.d.n_axes = n_axes;
+  for (int a = 0; a < n_axes; ++a) c.d.axes[a] = axes[a];
+  setupAxes(o, c);
+  if (cell < 0 || cell > (int)o->geom.cells.size()) return SG_ERR_BAD_ARG;
+  *bin = o->mapState(c, r, G, mat, cell, E, isMG != 0);
+  return SG_OK;
+}
+
 int32_t or_grid_search(const double* bounds, int32_t nb, double v) {
   std::vector<double> b(bounds, bounds + nb);
   return Oracle::binaryFloor(b, v);

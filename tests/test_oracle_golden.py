@@ -662,3 +662,46 @@ def test_collision_options_rejected(oracle_mod):
         o.set_collision(abi.collision(abi.COLL_IMP, imp_abs=True))
     with pytest.raises(Exception, match="twice"):
         o.set_collision(abi.collision(abi.COLL_IMP, split=True, min_wgt=1.0, max_wgt=1.5))
+
+
+def test_map_golden_vectors(oracle_mod):
+    """spaceMap, energyMap and cellMap against the known answers of SCONE's own map tests
+    (Tallies/TallyMaps/Maps1D/Tests/spaceMap_test.f90:88-140, energyMap_test.f90:25-181,
+    cellMap_test.f90:28-128)."""
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 5.0, 5.0, 5.0)
+    z = [gb.surface(abi.ZPLANE, v) for v in (-1.3, 0.0, 1.0)]
+    cells = [gb.cell([-(z[0] + 1), z[2] + 1]), gb.cell([-(z[0] + 1), -(z[2] + 1), z[1] + 1]),
+             gb.cell([-(z[1] + 1), z[0] + 1]), gb.cell([-(z[0] + 1)])]   # the test's ids 2, 1, 5, 3
+    uni = gb.cell_universe(cells, [1, 1, 1, 1])
+    gb.root_universe(box, problems.uni_fill(uni), bc=[abi.BC_VACUUM] * 6)
+    o = oracle_mod.Oracle(problems.Problem(gb.arrays(), None))
+    # spaceMap: lin -10..10 in 20 bins, unstructured on [-10, -8, ..., 10]
+    div = [-10.0, -8.0, -6.0, -4.0, -2.0, 0.0, 2.0, 4.0, 6.0, 8.0, 10.0]
+    for ax in (abi.AXIS_X, abi.AXIS_Y, abi.AXIS_Z):
+        for pos, lin, uns in ((0.5, 11, 6), (-10.1, 0, 0)):
+            r = [0.0, 0.0, 0.0]
+            r[ax - abi.AXIS_X] = pos
+            assert o.map_point([(ax, 20, -10.0, 10.0)], r=r) == lin
+            assert o.map_point([abi.unstruct_axis(ax, div)], r=r) == uns
+    # energyMap: lin 0.01..10 (20), log 1e-7..10 (20), unstructured (25 bins)
+    E_lin = [7.5774, 9.3652, 3.9223, 6.5548, 1.7119, 20.0]
+    E_log = [0.0445008907555061, 1.79747463687278e-07, 1.64204055725811e-05, 2.34083673923110e-07,
+             5.98486350302033e-07, 20.0]
+    E_uns = [0.0761191517392624, 0.00217742635754091, 6.38548311340975e-08, 2.52734532533842,
+             2.59031729968032e-11, 20.0]
+    grid = [1e-11, 3e-8, 5.8e-8, 1.4e-7, 2.8e-7, 3.5e-7, 6.25e-7, 9.72e-7, 1.02e-6, 1.097e-6, 1.15e-6,
+            1.855e-6, 4e-6, 9.877e-6, 1.5968e-5, 1.48728e-4, 5.53e-3, 9.118e-3, 0.111, 0.5, 0.821, 1.353,
+            2.231, 3.679, 6.0655, 10.0]
+    lin_ax = (abi.AXIS_ENERGY, 20, 0.01, 10.0, abi.GRID_LIN)
+    log_ax = (abi.AXIS_ENERGY, 20, 1.0e-7, 10.0, abi.GRID_LOG)
+    uns_ax = abi.unstruct_axis(abi.AXIS_ENERGY, grid)
+    for ax, Es, want in ((lin_ax, E_lin, [16, 19, 8, 14, 4, 0]), (log_ax, E_log, [15, 1, 6, 1, 2, 0]),
+                         (uns_ax, E_uns, [18, 16, 3, 23, 1, 0])):
+        assert [o.map_point([ax], E=e, mg=False) for e in Es] == want
+        assert o.map_point([ax], E=Es[0], mg=True) == 0              # MG particles map to no bin
+    # cellMap over cells (2 5 3) by id, i.e. indices 0, 2, 3: cellIdx 1..4, and 0 (in no cell)
+    no_undef = abi.cell_axis([0, 2, 3])
+    undef = abi.cell_axis([0, 2, 3], undef_bin=True)
+    assert [o.map_point([no_undef], cell=c) for c in (1, 2, 3, 4, 0)] == [1, 0, 2, 3, 0]
+    assert [o.map_point([undef], cell=c) for c in (1, 2, 3, 4, 0)] == [1, 4, 2, 3, 4]
