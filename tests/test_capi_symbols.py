@@ -72,3 +72,40 @@ def test_bank_file_round_trip(tmp_path):
             np.testing.assert_array_equal(c[k], b[k])
         np.testing.assert_array_equal(c["G"], b["G"])
         np.testing.assert_array_equal(c["brood_id"], b["brood_id"])
+
+
+STRUCTS = {"GeometryDesc": "sg_geometry_desc", "MGDesc": "sg_mg_desc", "CEDesc": "sg_ce_desc",
+           "AxisDesc": "sg_axis_desc", "ClerkDesc": "sg_clerk_desc", "TallyDesc": "sg_tally_desc",
+           "PointSourceDesc": "sg_point_source_desc", "Config": "sg_config", "Bank": "sg_bank",
+           "CycleStats": "sg_cycle_stats", "CollisionDesc": "sg_collision_desc", "EventTuning": "sg_event_tuning",
+           "BatchConfig": "sg_batch_config", "ProblemDesc": "sg_problem_desc", "BatchTuning": "sg_batch_tuning",
+           "BatchStats": "sg_batch_stats"}
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """Every ctypes mirror in scone_gb300/abi.py has the size and field offsets of its struct in
+    include/scone_gpu.h (a C program built with the host compiler prints them)."""
+    import shutil
+    import subprocess
+    from scone_gb300 import abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "scone_gpu.h"', 'int main(void) {']
+    for py, c in STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(abi, py)._fields_:
+            lines.append(f'  printf("{py} {name} %zu\\n", offsetof({c}, {name}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for py in STRUCTS:
+        cls = getattr(abi, py)
+        assert got[(py, "size")] == ctypes.sizeof(cls), py
+        for name, _ in cls._fields_:
+            assert got[(py, name)] == getattr(cls, name).offset, (py, name)
