@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
       if (__all_sync(FULL, done)) break;
       continue;
     }
-    // (deferring collisions as k_transport does measured 2 % slower on the uneven batch)
+    // flight and collision in one branch: deferring collisions measured 2 % slower on the uneven
+    // batch, and a warp vote between flight and collision (as k_transport has) no faster
     if (alive) {
       if (T.step()) { T.finish(); alive = false; }
     }
