@@ -705,3 +705,18 @@ def test_map_golden_vectors(oracle_mod):
     undef = abi.cell_axis([0, 2, 3], undef_bin=True)
     assert [o.map_point([no_undef], cell=c) for c in (1, 2, 3, 4, 0)] == [1, 0, 2, 3, 0]
     assert [o.map_point([undef], cell=c) for c in (1, 2, 3, 4, 0)] == [1, 4, 2, 3, 4]
+
+
+def test_multimap_golden_vectors(oracle_mod):
+    """multiMap of three unstructured spaceMaps, first axis fastest: the known answers of SCONE's
+    multiMap test (Tallies/TallyMaps/Tests/multiMap_test.f90:26-85)."""
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 100.0, 100.0, 100.0)
+    gb.root_universe(box, 1, bc=[abi.BC_VACUUM] * 6)
+    o = oracle_mod.Oracle(problems.Problem(gb.arrays(), None))
+    axes = [abi.unstruct_axis(abi.AXIS_X, [0.0, 1.0, 2.0]), abi.unstruct_axis(abi.AXIS_Y, [0.0, 2.0, 4.0, 6.0]),
+            abi.unstruct_axis(abi.AXIS_Z, [0.0, 3.0, 6.0])]
+    assert [abi.axis_bins(a) for a in axes] == [2, 3, 2]
+    for r, want in (((0.1, 0.1, 0.1), 1), ((1.1, 5.1, 5.1), 12), ((1.1, 3.1, 2.1), 4),
+                    ((-1.1, 5.1, 5.1), 0), ((1.1, 50.1, 5.1), 0), ((1.1, 5.1, -5.1), 0)):
+        assert o.map_point(axes, r=r) == want, r
