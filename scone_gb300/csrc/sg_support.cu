@@ -328,12 +328,15 @@ __global__ void k_radix_pick(unsigned int* hist, unsigned long long* sel, int* k
 // exit; kbuf holds [kth remaining, window found]; cnt two counters; cand WIN_CAP keys.
 cudaError_t quantile_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel, int* kbuf,
                             unsigned int* hist, unsigned long long* cnt, unsigned long long* cand, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_win_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(WIN_CAP * sizeof(unsigned long long)));
+  static int attrDevice = -1;                     // the attribute is set once per device
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev != attrDevice) {
+    e = cudaFuncSetAttribute(k_win_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(WIN_CAP * sizeof(unsigned long long)));
     if (e != cudaSuccess) return e;
-    attr = true;
+    attrDevice = dev;
   }
   const double p = (double)kth / S;
   const double d = 8.0 * sqrt(p * (1.0 - p) / S) + 4.0 / S;
