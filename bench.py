@@ -410,7 +410,7 @@ def batched_section(a, local):
         tuning = out["tuning"]
         B.close()
         B = None
-        for name, rate, efrac in (("config4_2000rps", 2000.0, 0.05),
+        for name, rate, efrac in (("mix_2000rps_5pct_eigen", 2000.0, 0.05),
                                   ("half_capacity", 0.5 * cap / mean_hist, 0.0)):
             Bs, cat = load(abi.PREC_MIXED)
             Bs.set_tuning(**tuning)
@@ -530,7 +530,7 @@ def main():
                "h2d_bytes_per_step": pop * (24 + 24 + 8 + 4 + 8),
                "d2h_bytes_per_step": int(d2h / a.steps), "ms_per_step": 1e3 * we / a.steps}
 
-    # the other transport operator of config 1 ("surface tracking vs delta tracking"), same K steps
+    # the other transport operator on the lattice workload (surface tracking vs delta tracking), same K steps
     alt = None
     if not a.no_alt and world == 1:
         tr2 = abi.TRANSPORT_ST if tr == abi.TRANSPORT_DT else abi.TRANSPORT_DT
