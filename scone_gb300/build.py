@@ -1,10 +1,11 @@
 """Builds libsconegpu.so in-tree (scone_gb300/_build/) with nvcc for sm_103a.
 
-Translation units compile in parallel, one per (nuclear data, precision form, transport operator)
-for the transport kernels and one per (precision, operator) for the batched kernel.  The FP64
-verification units and the support kernels are compiled with -fmad=false (every multiply and add
-rounded separately, as SCONE's gfortran build does on x86-64); the mixed-precision units keep FMA
-contraction.
+Translation units compile in parallel: four per (nuclear data, precision form, transport operator)
+for the transport kernels (sg_tr_unit.cu with the SG_* macros: history loop and event kernels, each
+for nesting bounds 2 and 4), one per (precision, operator) for the batched kernel, and the host and
+support units.  The FP64 verification units and the support kernels are compiled with -fmad=false
+(every multiply and add rounded separately, as SCONE's gfortran build does on x86-64); the
+mixed-precision units keep FMA contraction.
 """
 import os
 import shutil
@@ -21,14 +22,17 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # such as rotation matrices are the same on every host and equal the oracle's
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-UNITS = {"sg_support.cu": ["-fmad=false"], "sg_host.cu": ["-fmad=false"], "sg_noalloc.cu": ["-fmad=false"],
-         "sg_fission_source.cu": ["-fmad=false"], "sg_batch_host.cu": ["-fmad=false"]}
+# (object name, source, flags)
+UNITS = [(u.replace(".cu", ""), u, ["-fmad=false"])
+         for u in ("sg_support.cu", "sg_host.cu", "sg_noalloc.cu", "sg_fission_source.cu", "sg_batch_host.cu")]
 for _op in ("st", "dt", "ht"):
-    for _data in ("mg", "ce"):
-        UNITS[f"sg_tr_{_data}_fp64_{_op}.cu"] = ["-fmad=false"]
-        UNITS[f"sg_tr_{_data}_mixed_{_op}.cu"] = []
-    UNITS[f"sg_batch_fp64_{_op}.cu"] = ["-fmad=false"]
-    UNITS[f"sg_batch_mixed_{_op}.cu"] = []
+    for _prec, _R, _fl in (("fp64", "double", ["-fmad=false"]), ("mixed", "float", [])):
+        for _data, _ce in (("mg", 0), ("ce", 1)):
+            for _part in range(4):
+                UNITS.append((f"sg_tr_{_data}_{_prec}_{_op}_p{_part}", "sg_tr_unit.cu",
+                              _fl + [f"-DSG_R={_R}", f"-DSG_CE={_ce}", f"-DSG_OP=OP_{_op.upper()}",
+                                     f"-DSG_PART={_part}"]))
+        UNITS.append((f"sg_batch_{_prec}_{_op}", f"sg_batch_{_prec}_{_op}.cu", _fl))
 
 
 def nvcc():
@@ -68,12 +72,14 @@ def build(force=False, verbose=False, extra=()):
     cc = nvcc()
     objs = []
     cmds = []
-    for unit, flags in UNITS.items():
-        obj = os.path.join(OUT, unit.replace(".cu", ".o"))
-        cmds.append((unit, [cc, *ARCH, *COMMON, *flags, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]))
+    for unit, src, flags in UNITS:
+        obj = os.path.join(OUT, unit + ".o")
+        cmds.append((unit, [cc, *ARCH, *COMMON, *flags, *extra, "-c", os.path.join(CSRC, src), "-o", obj]))
         objs.append(obj)
-    # the long transport units first, at most one compiler per host core
-    cmds.sort(key=lambda c: (not c[0].startswith("sg_tr_"), not c[0].startswith("sg_batch_")))
+    # the long units first (history loops and event kernels of the hybrid operator, then the rest of
+    # the transport parts, then the batched kernels), at most one compiler per host core
+    cmds.sort(key=lambda c: (not c[0].endswith("_ht_p2") and not c[0].endswith("_ht_p3"),
+                             not c[0].startswith("sg_tr_"), not c[0].startswith("sg_batch_")))
     jobs = max(1, os.cpu_count() or 1)
     failed = []
     running = []

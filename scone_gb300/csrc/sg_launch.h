@@ -1,5 +1,7 @@
-// sg_launch.h -- host-callable launch wrappers of the kernels.  Each transport-kernel translation
-// unit (sg_tr_<data>_<precision>_<operator>.cu) defines one launch_kind_op specialisation.
+// sg_launch.h -- host-callable launch wrappers of the kernels.  The transport kernels of one
+// (precision, data, operator) combination are compiled in four parts, each its own translation unit
+// (sg_tr_unit.cu built with the SG_* macros): part 0 the history loop for nesting bound 2, part 1
+// the event kernels for bound 2, parts 2 and 3 the same for bound 4.
 #pragma once
 #include "sg_internal.h"
 
@@ -8,11 +10,20 @@ namespace sg {
 // kernel kinds of the history loop and of the event form
 enum { K_HISTORY = 0, K_EV_START = 1, K_EV_TRANSIT = 2, K_EV_COLLIDE = 3, K_EV_TAIL = 4, K_KINDS = 5 };
 
+// one part's launch (defined by that part's translation unit)
+template <class R, bool CE, int OP, int PART>
+cudaError_t launch_part(int kind, const TransportArgs<R>& a, size_t smem, cudaStream_t s, int* grid_out);
+
 // launch of kernel `kind` for working precision R, data kind CE (continuous energy) and transport
 // operator OP; maxl is the geometry's nesting bound (2 or 4 compiled)
 template <class R, bool CE, int OP>
-cudaError_t launch_kind_op(int kind, const TransportArgs<R>& a, int maxl, size_t smem, cudaStream_t s,
-                           int* grid_out);
+inline cudaError_t launch_kind_op(int kind, const TransportArgs<R>& a, int maxl, size_t smem, cudaStream_t s,
+                                  int* grid_out) {
+  const bool ev = kind != K_HISTORY;
+  if (maxl <= 2)
+    return ev ? launch_part<R, CE, OP, 1>(kind, a, smem, s, grid_out) : launch_part<R, CE, OP, 0>(kind, a, smem, s, grid_out);
+  return ev ? launch_part<R, CE, OP, 3>(kind, a, smem, s, grid_out) : launch_part<R, CE, OP, 2>(kind, a, smem, s, grid_out);
+}
 
 template <class R, bool CE>
 inline cudaError_t launch_kind_data(int kind, const TransportArgs<R>& a, int maxl, int op, size_t smem,
