@@ -183,13 +183,21 @@ def poisson_run(server, templates, rate, duration, seed=1, eigen_fraction=0.0, e
 
 
 def latency_summary(reqs, wall, offered_histories):
+    """Completed requests, latency percentiles over all of them and per request kind (fixed-source
+    requests take milliseconds, eigenvalue requests seconds), and the achieved history rate."""
     lat = np.array([r.latency for r in reqs]) if reqs else np.zeros(1)
     hist = float(sum(r.histories for r in reqs))
+    by_kind = {}
+    for kind in sorted({r.kind for r in reqs}):
+        lk = np.array([r.latency for r in reqs if r.kind == kind])
+        by_kind[kind] = {"completed": int(lk.size), "p50_ms": float(np.percentile(lk, 50) * 1e3),
+                         "p99_ms": float(np.percentile(lk, 99) * 1e3)}
     return {
         "completed": len(reqs),
         "p50_ms": float(np.percentile(lat, 50) * 1e3),
         "p99_ms": float(np.percentile(lat, 99) * 1e3),
         "mean_ms": float(lat.mean() * 1e3),
+        "by_kind": by_kind,
         "histories_per_s": hist / wall if wall > 0 else 0.0,
         "offered_histories_per_s": offered_histories,
         "wall_s": wall,

@@ -82,3 +82,16 @@ def test_poisson_driver_offers_the_rate():
     assert len(done) == n
     s = serve.latency_summary(done, wall, 500.0 * 200)
     assert s["completed"] == n and s["p99_ms"] >= s["p50_ms"] > 0
+    assert s["by_kind"]["fixed"]["completed"] == n
+
+
+def test_latency_summary_by_kind():
+    reqs = []
+    for i in range(10):
+        r = serve.Request(i, "fixed" if i < 8 else "eigen", 0, 10, 1, i, arrival=0.0)
+        r.latency = 0.01 if i < 8 else 2.0
+        reqs.append(r)
+    s = serve.latency_summary(reqs, 1.0, 0.0)
+    assert s["by_kind"]["fixed"] == {"completed": 8, "p50_ms": 10.0, "p99_ms": 10.0}
+    assert s["by_kind"]["eigen"]["completed"] == 2 and abs(s["by_kind"]["eigen"]["p50_ms"] - 2000.0) < 1e-9
+    assert s["p99_ms"] > 1000.0                       # the overall tail is the eigenvalue requests
