@@ -306,7 +306,9 @@ int32_t sg_generate_source(sg_handle h, uint64_t master_state, int32_t n, sg_ban
  * history n (1-based) of `in` starts with RNG master + stride(n), is placed, transported and
  * collided until death, scoring into tally admin `admin` (and its attachment).
  * Fission sites are returned in `next` sorted by brood ID (the order normSize_Repr sorts to);
- * `next_cap` is its capacity.  `k_eff` is the k used for fission-site weights. */
+ * `next_cap` is its capacity.  `k_eff` is the k used for fission-site weights.  An input bank in
+ * page-locked host memory that the device can address is read in place by the kernels (no staging
+ * copy); other host memory is copied first. */
 int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t n,
                           uint64_t master_state, double k_eff,
                           sg_bank* next, int32_t next_cap, sg_cycle_stats* stats);
@@ -350,6 +352,18 @@ int32_t sg_eigen_init(sg_handle h, int32_t pop, uint64_t master_state, double k0
  * (eigenPhysicsPackage_class.f90:203-338).  `admin` is the cycle's tally admin; the
  * k estimate is read from attachment `atch`. */
 int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats* stats);
+/* The same whole cycle for a caller that keeps its dungeons in host memory: the body of
+ * eigenPhysicsPackage%cycles (eigenPhysicsPackage_class.f90:203-338) with thisCycle in `in` (pop
+ * particles), the package's pRNG in *master_state, thisCycle%k_eff in *k_eff and nextCycle%k_eff in
+ * k_end.  The gen loop, cleanPop, stride(pop+1), reportCycleEnd, normSize_Repr to pop, stride(1) and
+ * the k estimate of attachment `atch` run on the device; `out` receives the normalised next-cycle
+ * bank (pop particles, in brood order), *master_state the strided pRNG and *k_eff the new k.  A bank
+ * in page-locked host memory that the device can address (cudaHostAlloc, or cudaHostRegister with
+ * mapping) is read by the kernels in place across the host link while they run; other host memory
+ * is copied to the device first.  Replaces the resident run of sg_eigen_init. */
+int32_t sg_eigen_cycle_bank(sg_handle h, int32_t admin, int32_t atch, const sg_bank* in, int32_t pop,
+                            uint64_t* master_state, double* k_eff, double k_end, sg_bank* out,
+                            sg_cycle_stats* stats);
 /* current master RNG state and k of the resident eigen run */
 int32_t sg_eigen_state(sg_handle h, uint64_t* master_state, double* k);
 /* copy the resident "this cycle" bank to the host (pop particles) */
@@ -374,13 +388,18 @@ int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t share, i
  * to a pool reserved up front (cudaMalloc would go around it or fail once the pool holds the GPU),
  * and real-time sections that must stay out of the driver's allocator, whose calls can block.  The banks are the
  * caller's device arrays (dev_in: r, dir, wgt, G, time; dev_next: every array, capacity next_cap);
- * the handle must already hold the geometry, data and tallies.  It calls no cudaMalloc/cudaFree:
- * its scratch (site staging, per-history counts, scan sums, counters, k) is one static device array
- * of 3 MiB that every GPU loading the library holds until exit, which limits a call to
- * SG_NOALLOC_MAX_HISTORIES histories and SG_NOALLOC_MAX_SITES fission sites (larger n is rejected
- * with SG_ERR_BAD_ARG).  The first call on a device looks up that array's device address, so make
- * it before any stream capture.  All calls share the array: calls that overlap on the GPU race.
- * Returns the number of sites written in *n_next; results are those of sg_transport_bank. */
+ * the handle must already hold the geometry, multigroup data and tallies.  Multigroup handles only:
+ * a continuous-energy handle is refused with SG_ERR_STATE.  It always runs the history-loop kernel,
+ * whatever the handle's form.  It calls no cudaMalloc/cudaFree: its scratch (site staging,
+ * per-history counts, scan sums, counters, k) is one static device array of 3 MiB that every GPU
+ * loading the library holds until exit, which limits a call to SG_NOALLOC_MAX_HISTORIES histories
+ * (larger n is rejected with SG_ERR_BAD_ARG before anything runs) and SG_NOALLOC_MAX_SITES fission
+ * sites in total (a call that makes more fails with SG_ERR_BANK_OVERFLOW; the scores it made before
+ * stopping stay in the tallies, as with sg_transport_bank).  The first call on a device looks up
+ * that array's device address, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  Returns the number of sites written in *n_next; the sites
+ * and the scores are those of sg_transport_bank on the same bank (the fission bank identical, the
+ * bins equal up to the order of the floating-point sums). */
 #define SG_NOALLOC_MAX_HISTORIES 16384
 #define SG_NOALLOC_MAX_SITES     32768
 int32_t sg_transport_bank_noalloc(sg_handle h, int32_t admin, const sg_bank* dev_in, int32_t n,

@@ -50,15 +50,17 @@ __device__ __forceinline__ bool stage_problem_warp(BatchProblem<R>* dst, const B
 
 // pointSource%sampleParticle (pointSource_class.f90:189-270), then the particle enters the gen loop
 // as thisCycle%copy + placeCoord would leave it.
+// s_src / s_tr: the source and transport RNG states of this history, master_c + stride(n) and
+// master_c + stride(pop + n)
 template <class R, int MAXL, int OP>
-__device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, const BatchProblem<R>& P, int f) {
+__device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, const BatchProblem<R>& P, int f,
+                                              unsigned long long s_src, unsigned long long s_tr) {
   const int c = f / P.pop;
   const int n = f - c * P.pop + 1;
-  const long long base = 2LL * P.pop * c;
   // the source direction in the working precision: FP64 as SCONE in the verification form; FP32
   // in the mixed form (the direction is kept in FP32 there, and FP64 is scarce on this GPU)
   Rng<R> rs;
-  rs.s = lcg_skip(P.master, RNG_STRIDE * (base + n));
+  rs.s = s_src;
   R d0 = (R)P.src_dir[0], d1 = (R)P.src_dir[1], d2 = (R)P.src_dir[2];
   if (P.src_isotropic) {
     const R mu = R(2) * rs.get() - R(1);
@@ -86,7 +88,7 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
   T.w0 = R(1);
   T.G = g;
   T.time = R(0);
-  T.rng.s = lcg_skip(P.master, RNG_STRIDE * (base + P.pop + n));
+  T.rng.s = s_tr;
   T.collN = 0;
   T.nsites = 0;
   T.segs = 0;
@@ -97,9 +99,12 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
 }
 
 template <class R, int MAXL, int OP>
-__global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaunch L) {
+__global__ void __launch_bounds__(128, (history_min_blocks<R, false, OP>())) k_batch(const __grid_constant__ BatchLaunch L) {
   __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
   __shared__ __align__(8) unsigned long long s_bar[BATCH_MAX_WARPS];
+  __shared__ RngJump s_jump;
+  rng_jump_table(s_jump);
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   BatchProblem<R>& P = *reinterpret_cast<BatchProblem<R>*>(s_rec[threadIdx.x >> 5]);
   unsigned long long* bar = &s_bar[threadIdx.x >> 5];
@@ -119,6 +124,10 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
   int cur = -1;                     // slot of the staged problem (warp-uniform)
   int pend = -1;                    // claimed item of another problem, waiting for the warp to drain
   int q_next = 0, q_end = 0;        // warp-uniform range of flat histories of the current item
+  // the chunk being started: at most 32 histories of one cycle of the item, from flat history
+  // ch_base, whose source and transport RNG states are s_src / s_tr (warp-uniform)
+  int ch_base = 0, ch_end = 0;
+  unsigned long long s_src = 0, s_tr = 0;
   bool alive = false, done = false;
   bool stopped = false;             // warp-uniform: a record copy timed out
 
@@ -150,11 +159,24 @@ __global__ void __launch_bounds__(128) k_batch(const __grid_constant__ BatchLaun
         pend = -1;
         q_next = wi.first;
         q_end = wi.first + wi.count;
+        ch_end = q_next;
       }
-      const int avail = q_end - q_next;
+      if (q_next >= ch_end) {                         // a new chunk: one skip for the warp
+        const int c = q_next / P.pop;
+        const int n = q_next - c * P.pop + 1;
+        ch_base = q_next;
+        ch_end = min(min(q_next + 32, q_end), (c + 1) * P.pop);
+        s_src = lcg_skip(P.master, RNG_STRIDE * (2LL * P.pop * c + n));
+        s_tr = lcg_skip(s_src, RNG_STRIDE * (long long)P.pop);
+      }
+      const int avail = ch_end - q_next;
       const int rank = __popc(need & ((1u << lane) - 1u));
       const bool mine = ((need >> lane) & 1u) && rank < avail;
-      if (mine) { start_batched<R, MAXL, OP>(T, P, q_next + rank); alive = true; }
+      if (mine) {
+        const int off = q_next + rank - ch_base;
+        start_batched<R, MAXL, OP>(T, P, q_next + rank, rng_jump(s_jump, off, s_src), rng_jump(s_jump, off, s_tr));
+        alive = true;
+      }
       q_next += min(__popc(need), avail);
       need &= ~__ballot_sync(FULL, mine);
     }

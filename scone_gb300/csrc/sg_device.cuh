@@ -517,7 +517,10 @@ struct Geom {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
           const T pitch = UD<T>(U, i), corner = UD<T>(U, 3 + i);
-          ijk[i] = (int)floor((r[i] - corner) / pitch) + 1;
+          // FP64 form: SCONE's division; mixed form: the reciprocal pitch (a cell boundary within an
+          // ulp is then settled by the tolerance test below, as any FP32 rounding is)
+          if constexpr (sizeof(T) == 8) ijk[i] = (int)floor((r[i] - corner) / pitch) + 1;
+          else ijk[i] = (int)floorf((r[i] - corner) * U.invf[i]) + 1;
           T r_bar = r[i] - corner - ijk[i] * pitch + T(0.5) * pitch;
           if (fabs(r_bar) > UD<T>(U, 6 + i) && r_bar * (T)dir[i] > T(0)) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
           if (ijk[i] <= 0 || ijk[i] > U.i[i]) out = true;
@@ -527,13 +530,22 @@ struct Geom {
     }
   }
 
-  __device__ __forceinline__ static void get_ijk(int localID, const int* sizeN, int ijk[3]) {
+  // floor(t / n) for 0 <= t < 2^24 and n >= 1 from the FP32 reciprocal inv ~ 1/n: the estimate is
+  // off by at most one and corrected exactly, so the quotient equals the integer division's
+  __device__ __forceinline__ static int quot(int t, int n, float inv) {
+    int q = __float2int_rz(__int2float_rn(t) * inv);
+    const int r = t - q * n;
+    if (r < 0) q -= 1;
+    else if (r >= n) q += 1;
+    return q;
+  }
+  __device__ __forceinline__ static void get_ijk(int localID, const DUni& U, int ijk[3]) {
     int temp = localID - 1;                                      // latUniverse_class.f90:489-506
-    int base = temp / sizeN[0];
-    ijk[0] = temp - sizeN[0] * base + 1;
+    int base = quot(temp, U.i[0], U.invn[0]);
+    ijk[0] = temp - U.i[0] * base + 1;
     temp = base;
-    base = temp / sizeN[1];
-    ijk[1] = temp - sizeN[1] * base + 1;
+    base = quot(temp, U.i[1], U.invn[1]);
+    ijk[1] = temp - U.i[1] * base + 1;
     ijk[2] = base + 1;
   }
 
@@ -590,7 +602,7 @@ struct Geom {
           return;
         }
         int ijk[3];
-        get_ijk(localID, U.i, ijk);
+        get_ijk(localID, U, ijk);
         d = INF_R;
         int ax = 0;
 #pragma unroll
@@ -620,7 +632,7 @@ struct Geom {
     off[0] = off[1] = off[2] = T(0);
     if (U.type == SG_UNI_LAT && U.i[5] != 0 && localID != U.i[3]) {
       int ijk[3];
-      get_ijk(localID, U.i, ijk);
+      get_ijk(localID, U, ijk);
 #pragma unroll
       for (int i = 0; i < 3; ++i) off[i] = (ijk[i] - T(0.5)) * UD<T>(U, i) + UD<T>(U, 3 + i);
     }
@@ -747,8 +759,9 @@ struct Geom {
 
   // geometryStd%teleport (geometryStd_class.f90:492-514)
   __device__ __forceinline__ bool teleport(Coords<R, MAXL>& c, R dist) const {
+    // the step in the working precision, accumulated in FP64 (in the FP64 form the same products)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)dist * (double)c.u[k];
+    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)(dist * c.u[k]);
     bool ok = place(c);
     if (c.mat == 0) {
       surf_transform_bc<R>(g.surfs[g.border], c.r0, c.u);
@@ -760,7 +773,7 @@ struct Geom {
   // moveLocal over levels 1..n (coord_class.f90:346-356)
   __device__ __forceinline__ void move_levels(Coords<R, MAXL>& c, int n, R d) const {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)d * (double)c.u[k];
+    for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)(d * c.u[k]);
     R v[3] = {c.u[0], c.u[1], c.u[2]};
 #pragma unroll
     for (int l = 1; l < MAXL; ++l)
@@ -801,7 +814,7 @@ struct Geom {
     }
     if (surfIdx == g.border + 1 && level == 1) {                  // domain boundary
 #pragma unroll
-      for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)dist * (double)c.u[k];
+      for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)(dist * c.u[k]);
       maxDist = dist;
       cache.lvl = 0;
       surf_explicit_bc<R>(g.surfs[g.border], c.r0, c.u);

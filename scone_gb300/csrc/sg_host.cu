@@ -213,6 +213,7 @@ struct sg_handle_t {
   long long launches = 0;      // kernels launched since the last reset (cycle stats)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float lastTransportMs = 0.f;
+  sg_cycle_stats lastStats{};   // the last eigenvalue cycle's statistics
 
   // point source
   bool hasSource = false;
@@ -523,6 +524,10 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
       for (int i = 0; i < 3; ++i) Um.d[6 + i] = U.d[i] * 0.5 - U.d[i] * SURF_TOL_M;
     for (int i = 0; i < 3; ++i) { U.originf[i] = (float)U.origin[i]; Um.originf[i] = (float)Um.origin[i]; }
     for (int i = 0; i < 9; ++i) { U.f[i] = (float)U.d[i]; Um.f[i] = (float)Um.d[i]; }
+    if (U.type == SG_UNI_LAT) {
+      for (int i = 0; i < 3; ++i) U.invf[i] = Um.invf[i] = (float)(1.0 / U.d[i]);
+      for (int i = 0; i < 2; ++i) U.invn[i] = Um.invn[i] = (float)(1.0 / U.i[i]);
+    }
     u64[u] = U;
     uMx[u] = Um;
     fills[u] = f;
@@ -931,7 +936,8 @@ template <> const DColl<double>* coll_view<double>(sg_handle h) { return h->dCol
 template <> const DColl<float>* coll_view<float>(sg_handle h) { return h->dColl32.p; }
 
 DSites site_view(sg_handle h) {
-  return DSites{h->sR.p, h->sDir.p, h->sWgt.p, h->sG.p, h->sBrood.p, h->sSeq.p, h->sTime.p, h->sCursor.p, h->regionCap};
+  return DSites{h->sR.p, h->sDir.p, h->sWgt.p, h->sG.p, h->sBrood.p, h->sSeq.p, h->sTime.p, h->sCursor.p, h->regionCap,
+                SITE_REGIONS - 1};
 }
 
 // Bins of one map axis: cellMap has n cells plus the `undefBin` rest bin (cellMap_class.f90:129-136)
@@ -1045,12 +1051,8 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.k_eff = d_k;
   t.acc = h->acc.p + lo;
   t.acc_n = (int)(hi - lo);
-  // Few bins: block-local score memory in shared memory (global reductions on a handful of
-  // addresses serialise in L2: 2.5-6x slower on the 2-group infinite medium).  Many bins: straight
-  // into global memory (L2 reductions spread over the bins cost less than shared-memory FP64
-  // atomics: 7 % on the 2 023-bin lattice mesh).
   size_t smem = (size_t)t.acc_n * sizeof(double);
-  t.use_smem = (t.acc_n > 0 && t.acc_n < 1024) ? 1 : 0;
+  t.use_smem = scores_in_shared_memory(t.acc_n) ? 1 : 0;
   if (!t.use_smem) smem = 0;
   t.sites = site_view(h);
   t.hist_nsites = h->histN.p;
@@ -1278,6 +1280,28 @@ int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
   return SG_OK;
 }
 
+// A host bank in page-locked memory that the device can address (cudaHostAlloc / cudaHostRegister
+// with mapping, the default under unified addressing) is read by the kernels in place, across the
+// C2C link of a Grace-Blackwell node, while they run: no staging copy before the gen loop.  True and
+// the device view when every array the gen loop reads (r, dir, wgt, G, time; E for CE) is such
+// memory; false otherwise (the bank is then copied).
+bool mapped_host_bank(sg_handle h, const sg_bank* b, DBank* d) {
+  auto dev = [](const void* p, void** out) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+    *out = a.devicePointer;
+    return true;
+  };
+  void *r, *dir, *wgt, *G, *time, *E = nullptr;
+  if (!dev(b->r, &r) || !dev(b->dir, &dir) || !dev(b->wgt, &wgt) || !dev(b->time, &time)) return false;
+  if (h->hasCE) { if (!dev(b->E, &E)) return false; G = nullptr; }
+  else if (!dev(b->G, &G)) return false;
+  *d = DBank{(double*)r, (double*)dir, (double*)wgt, (int*)G, nullptr, (double*)time, (double*)E};
+  return true;
+}
+
 // Checks one map axis and uploads its table: the bounds of an unstructured grid (grid%init_unstruct,
 // grid_class.f90:100-113: sorted, at least 2 bounds) or the bin of every cell for a cellMap
 // (cellMap%build, cellMap_class.f90:87-138: listed cells take bins 1..n in order, every other cell
@@ -1363,12 +1387,59 @@ int build_admin(sg_handle h, const sg_tally_desc* t, Admin& A) {
   return SG_OK;
 }
 
+// One whole eigenvalue cycle (eigenPhysicsPackage_class.f90:203-338) on device banks: `in` is
+// thisCycle (h->pop particles), the fission sites go to `sites` in brood order, normSize_Repr writes
+// the next-cycle bank to `out` (which may be `in`).  h->master and h->k advance; the k used is in
+// scal[0] and end%k_eff in scal[4].  The caller recorded ev[2] at its start.
+int eigen_cycle_core(sg_handle h, int admin, int atch, DBank A, DBank B, DBank out, sg_cycle_stats* stats) {
+  cudaStream_t s = h->stream;
+  const int n = h->pop;
+  CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, s));       // popWeight(thisCycle)
+  h->launches += 2;
+  int rc = cycle_start(h, admin, h->scal.p + 2, 0.0);
+  if (rc) return rc;
+  int S = 0;
+  sg_cycle_stats st{};
+  rc = gen_loop(h, admin, A, n, h->master, h->scal.p + 0, B, h->cap, &S, &st);
+  if (rc) return rc;
+  h->master = rng_stride(h->master, (long long)h->pop + 1);              // :257
+  CK(deterministic_sum(B.wgt, S, h->sumPart.p, h->scal.p + 3, s));       // popWeight(nextCycle)
+  h->launches += 2;
+  rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, atch, h->scal.p + 1);
+  if (rc) return rc;
+  rc = norm_size(h, B, S, h->pop, h->master, out, n);                    // :269
+  if (rc) return rc;
+  h->master = rng_stride(h->master, 1);                                  // :275
+  CK(cudaMemcpyAsync(h->scal.p + 0, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->scal.p + 4, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  double sc[5];
+  CK(cudaMemcpyAsync(sc, h->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->ev[3], s));
+  CK(cudaStreamSynchronize(s));
+  float cyc = 0.f;
+  CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
+  double kUsed = h->k;
+  h->k = sc[1];
+  st.start_weight = sc[2];
+  st.end_weight = sc[3];
+  st.k_eff = kUsed;
+  st.k_new = sc[1];
+  st.cycle_ms = cyc;
+  st.n_kernels = h->launches;
+  h->lastStats = st;
+  if (stats) *stats = st;
+  return SG_OK;
+}
+
 }  // namespace
 
 // Bridge for sg_transport_bank_noalloc (sg_noalloc.cu): the launch arguments that do not depend on
 // the call.  Reads the handle only; allocates nothing.
 int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<double>* t64, TransportArgs<float>* t32,
                      long long* lo) {
+  if (h->hasCE)
+    return h->fail(SG_ERR_STATE, "sg_transport_bank_noalloc: multigroup handles only (this handle holds "
+                                 "continuous-energy data; use sg_transport_bank)");
   if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "upload geometry and MG data first");
   if (admin < 0 || admin >= (int)h->admins.size()) return h->fail(SG_ERR_BAD_ARG, "bad tally admin");
   v->stream = h->stream;
@@ -1675,8 +1746,12 @@ int32_t sg_transport_bank(sg_handle h, int32_t admin, const sg_bank* in, int32_t
   DBank A = h->bank[0].view(), B = h->bank[1].view();
   h->launches = 0;
   CK(cudaEventRecord(h->ev[2], h->stream));
-  int rc = h2d_bank(h, in, n, A);
-  if (rc) return rc;
+  int rc = SG_OK;
+  if (!mapped_host_bank(h, in, &A)) {
+    A = h->bank[0].view();
+    rc = h2d_bank(h, in, n, A);
+    if (rc) return rc;
+  }
   CK(cudaMemcpyAsync(h->scal.p + 0, &k_eff, sizeof(double), cudaMemcpyHostToDevice, h->stream));
   // popWeight of the bank given (particleDungeon_class.f90:358-375), summed on the device
   CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, h->stream));
@@ -1788,45 +1863,52 @@ int32_t sg_eigen_init(sg_handle h, int32_t pop, uint64_t master_state, double k0
 int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats* stats) {
   if (!h || !h->eigenReady) return h ? h->fail(SG_ERR_STATE, "call sg_eigen_init first") : SG_ERR_BAD_ARG;
   if (admin < 0 || admin >= (int)h->admins.size() || atch < 0 || atch >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  h->launches = 0;
+  CK(cudaEventRecord(h->ev[2], h->stream));
+  DBank A = h->bank[h->cur].view();
+  return eigen_cycle_core(h, admin, atch, A, h->bank[1 - h->cur].view(), A, stats);
+}
+
+int32_t sg_eigen_cycle_bank(sg_handle h, int32_t admin, int32_t atch, const sg_bank* in, int32_t pop,
+                            uint64_t* master_state, double* k_eff, double k_end, sg_bank* out,
+                            sg_cycle_stats* stats) {
+  if (!h || !in || !out || !master_state || !k_eff || pop <= 0 || pop > h->cap) return SG_ERR_BAD_ARG;
+  if (admin < 0 || admin >= (int)h->admins.size() || atch < 0 || atch >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "eigenvalue cycles need geometry and fissile MG data");
+  if (!out->r || !out->dir || !out->wgt || !out->G)
+    return h->fail(SG_ERR_BAD_ARG, "sg_eigen_cycle_bank: the output bank needs r, dir, wgt and G");
   cudaStream_t s = h->stream;
-  DBank A = h->bank[h->cur].view(), B = h->bank[1 - h->cur].view();
-  const int n = h->pop;
   h->launches = 0;
   CK(cudaEventRecord(h->ev[2], s));
-  CK(deterministic_sum(A.wgt, n, h->sumPart.p, h->scal.p + 2, s));       // popWeight(thisCycle)
-  h->launches += 2;
-  int rc = cycle_start(h, admin, h->scal.p + 2, 0.0);
+  // thisCycle: read in place from mapped host memory, else staged in bank 0; the fission sites go to
+  // bank 1 and the normalised next-cycle bank to bank 0 (the staged input is consumed by then)
+  DBank res = h->bank[0].view(), in_d;
+  if (!mapped_host_bank(h, in, &in_d)) {
+    in_d = res;
+    int rc = h2d_bank(h, in, pop, in_d);
+    if (rc) return rc;
+  }
+  double kk[2] = {*k_eff, k_end};                    // k used this cycle, end%k_eff
+  CK(cudaMemcpyAsync(h->scal.p + 0, &kk[0], sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(h->scal.p + 4, &kk[1], sizeof(double), cudaMemcpyHostToDevice, s));
+  h->pop = pop;
+  h->master = *master_state;
+  h->k = *k_eff;
+  h->cur = 0;
+  int rc = eigen_cycle_core(h, admin, atch, in_d, h->bank[1].view(), res, nullptr);
+  h->eigenReady = false;   // the device banks hold no resident run for sg_eigen_cycle
   if (rc) return rc;
-  int S = 0;
-  sg_cycle_stats st{};
-  rc = gen_loop(h, admin, A, n, h->master, h->scal.p + 0, B, h->cap, &S, &st);
+  rc = d2h_bank(h, res, pop, out);
   if (rc) return rc;
-  h->master = rng_stride(h->master, (long long)h->pop + 1);              // :257
-  CK(deterministic_sum(B.wgt, S, h->sumPart.p, h->scal.p + 3, s));       // popWeight(nextCycle)
-  h->launches += 2;
-  rc = cycle_end(h, admin, h->scal.p + 3, h->scal.p + 4, atch, h->scal.p + 1);
-  if (rc) return rc;
-  rc = norm_size(h, B, S, h->pop, h->master, A, n);                      // :269, result in A
-  if (rc) return rc;
-  h->master = rng_stride(h->master, 1);                                  // :275
-  CK(cudaMemcpyAsync(h->scal.p + 0, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(h->scal.p + 4, h->scal.p + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
-  double sc[5];
-  CK(cudaMemcpyAsync(sc, h->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(h->ev[3], s));
   CK(cudaStreamSynchronize(s));
-  float cyc = 0.f;
-  CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
-  double kUsed = h->k;
-  h->k = sc[1];
+  *master_state = h->master;
+  *k_eff = h->k;
   if (stats) {
-    *stats = st;
-    stats->start_weight = sc[2];
-    stats->end_weight = sc[3];
-    stats->k_eff = kUsed;
-    stats->k_new = sc[1];
+    *stats = h->lastStats;
+    float cyc = 0.f;
+    CK(cudaEventElapsedTime(&cyc, h->ev[2], h->ev[3]));
     stats->cycle_ms = cyc;
-    stats->n_kernels = h->launches;
   }
   return SG_OK;
 }

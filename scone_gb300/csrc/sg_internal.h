@@ -28,7 +28,8 @@ struct DSurf {
 //   CELL: i0 first entry in uni_cells, i1 number of cells
 //   PIN : i0 first annulus in pin_rsq/pin_tol, i1 number of annuli (last one has radius 1.1*INF)
 //   LAT : i0..i2 sizeN, i3 outLocalID, i4 outline surface, i5 offset flag;
-//         d0..2 pitch, d3..5 corner, d6..8 a_bar (half pitch reduced by the surface tolerance)
+//         d0..2 pitch, d3..5 corner, d6..8 a_bar (half pitch reduced by the surface tolerance);
+//         invf0..2 1 / pitch and invn0..1 1 / sizeN (FP32)
 //   all : i6 = 1 when the origin is (0, 0, 0)
 struct DUni {
   int type;
@@ -38,6 +39,8 @@ struct DUni {
   double d[9];
   float originf[3];
   float f[9];      // FP32 copy of d
+  float invf[3];   // lattice: 1 / pitch (mixed-form cell search)
+  float invn[2];   // lattice: 1 / sizeN[0], 1 / sizeN[1] (local ID -> ijk)
 };
 
 struct DGeom {
@@ -159,8 +162,10 @@ struct DBank {
 };
 
 // Fission sites produced by one gen loop before they are ordered by brood ID.  The buffer is split
-// into NREG regions, each filled through its own atomic cursor, so the append rate is not limited
-// by one contended counter.
+// into up to SITE_REGIONS regions, each filled through its own atomic cursor, so the append rate is
+// not limited by one contended counter.  A warp appends to region (warp index & region_mask):
+// region_mask = SITE_REGIONS - 1 spreads the appends over every region, 0 puts every site in
+// region 0 (one cursor, the whole buffer as its capacity).
 static constexpr int SITE_REGIONS = 64;
 struct DSites {
   double* r;
@@ -172,6 +177,7 @@ struct DSites {
   double* time;
   int* cursor;          // [SITE_REGIONS]
   int region_cap;
+  int region_mask;      // SITE_REGIONS - 1, or 0 for a single region
 };
 
 // Per-launch counters written by the transport kernel
@@ -271,5 +277,12 @@ struct TransportArgs {
   int coll_imp;         // 1: neutronMGimp / neutronCEimp with *coll
   const DColl<R>* coll;
 };
+
+// Where the history loop scores map clerks.  Few bins: a block-local copy of score memory in shared
+// memory, flushed once per block (global reductions on a handful of addresses serialise in L2:
+// 2.5-6x slower on the 2-group infinite medium).  Many bins: straight into global memory (L2
+// reductions spread over the bins cost less than shared-memory FP64 atomics: 7 % on the 2 023-bin
+// lattice mesh).
+inline bool scores_in_shared_memory(long long acc_n) { return acc_n > 0 && acc_n < 1024; }
 
 }  // namespace sg

@@ -4,14 +4,17 @@
 // Some callers cannot call cudaMalloc at the point where they run a cycle: host programs whose
 // device memory is owned by another allocator or by a pool reserved up front (a cudaMalloc would
 // bypass it, or fail once the pool holds the GPU's memory), and real-time sections that must not
-// enter the driver's allocator, whose calls can block.  For them this entry point runs the history-loop kernel on banks the caller
-// already holds in device memory and keeps all of its per-call scratch (fission-site staging,
-// per-history site counts, scan partial sums, counters, k) in one file-scope static __device__
-// array.  The handle (geometry, nuclear data, tallies) must have been set up beforehand.
+// enter the driver's allocator, whose calls can block.  For them this entry point runs the
+// history-loop kernel on banks the caller already holds in device memory and keeps all of its
+// per-call scratch (fission-site staging, per-history site counts, scan partial sums, counters, k)
+// in one file-scope static __device__ array.  The handle (geometry, multigroup data, tallies) must
+// have been set up beforehand; continuous-energy handles are refused.
 //
 // Limits: at most SG_NOALLOC_MAX_HISTORIES histories and SG_NOALLOC_MAX_SITES fission sites per
 // call (3 MiB of device memory, held on every GPU that loads this library until the process exits).
-// All calls share the array: calls that overlap on the GPU (different streams or threads) race.
+// Every site goes to one region of the staging buffer, so the site limit is the call's total, however
+// the sites fall over the warps.  All calls share the array: calls that overlap on the GPU
+// (different streams or threads) race.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -25,7 +28,6 @@ namespace {
 
 constexpr int NA_MAX_HIST = SG_NOALLOC_MAX_HISTORIES;
 constexpr int NA_MAX_SITES = SG_NOALLOC_MAX_SITES;
-constexpr int NA_REGION_CAP = NA_MAX_SITES / sg::SITE_REGIONS;
 constexpr size_t NA_SCRATCH_BYTES = 3u << 20;
 
 // byte layout of the scratch array (offsets 256-byte aligned)
@@ -96,7 +98,8 @@ int run_noalloc(const sg::NoAllocView& v, sg::TransportArgs<R> t, unsigned char*
   t.sites = DSites{reinterpret_cast<double*>(S + OFF_R), reinterpret_cast<double*>(S + OFF_DIR),
                    reinterpret_cast<double*>(S + OFF_WGT), reinterpret_cast<int*>(S + OFF_G),
                    reinterpret_cast<int*>(S + OFF_BROOD), reinterpret_cast<int*>(S + OFF_SEQ),
-                   reinterpret_cast<double*>(S + OFF_TIME), reinterpret_cast<int*>(S + OFF_CURSOR), NA_REGION_CAP};
+                   reinterpret_cast<double*>(S + OFF_TIME), reinterpret_cast<int*>(S + OFF_CURSOR), NA_MAX_SITES,
+                   0 /* one region: the site limit is the total */};
   int* histN = reinterpret_cast<int*>(S + OFF_HISTN);
   int* start = reinterpret_cast<int*>(S + OFF_START);
   int* scanTmp = reinterpret_cast<int*>(S + OFF_SCAN);
@@ -106,7 +109,7 @@ int run_noalloc(const sg::NoAllocView& v, sg::TransportArgs<R> t, unsigned char*
   t.rec_rng = nullptr;
   t.ctr = reinterpret_cast<DCounters*>(S + OFF_CTR);
   size_t smem = (size_t)t.acc_n * sizeof(double);
-  t.use_smem = (t.acc_n > 0 && smem <= 64 * 1024) ? 1 : 0;
+  t.use_smem = scores_in_shared_memory(t.acc_n) ? 1 : 0;
   if (!t.use_smem) smem = 0;
   // the scratch keeps the previous call's contents: clear what must start at zero
   cudaError_t e;
@@ -130,10 +133,15 @@ int run_noalloc(const sg::NoAllocView& v, sg::TransportArgs<R> t, unsigned char*
     return fail(SG_ERR_CUDA, cudaGetErrorString(e));
   if (c.err_code) {
     char m[160];
-    std::snprintf(m, sizeof(m), "transport: error %d raised in history %d", c.err_code, c.err_hist);
+    if (c.err_code == SG_ERR_BANK_OVERFLOW)
+      std::snprintf(m, sizeof(m), "sg_transport_bank_noalloc: more than SG_NOALLOC_MAX_SITES (%d) fission sites "
+                    "(history %d); this call's partial scores stay in the tallies", NA_MAX_SITES, c.err_hist);
+    else
+      std::snprintf(m, sizeof(m), "transport: error %d raised in history %d", c.err_code, c.err_hist);
     return fail(c.err_code, m);
   }
-  if (tot[3] || tot[0] > next_cap) return fail(SG_ERR_BANK_OVERFLOW, "next bank capacity too small");
+  if (tot[3] || tot[0] > next_cap)
+    return fail(SG_ERR_BANK_OVERFLOW, "sg_transport_bank_noalloc: next bank capacity too small");
   *n_next = tot[0];
   return SG_OK;
 }

@@ -61,6 +61,29 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   return false;
 }
 
+// Start states of the histories of a warp's chunk.  History h starts from master + stride(h)
+// (RNG_class.f90:251-316), i.e. T^(152917 h)(master) with T the LCG step s -> g s + 1 mod 2^63, an
+// affine map; powers of one affine map compose in any order, so for h = b + off the state is
+// T^(152917 off) applied to T^(152917 b)(master).  The table holds (A, C) of T^(152917 off) for
+// off = 0..31 (A = g^(152917 off), C = T^(152917 off)(0)); a warp then makes one full skip per chunk
+// of 32 histories and each history one multiply-add, bit for bit the states of lcg_skip.
+struct RngJump {
+  unsigned long long a[32], c[32];
+};
+// fills the table (the block's first warp; the caller synchronises the block afterwards)
+__device__ __forceinline__ void rng_jump_table(RngJump& J) {
+  if (threadIdx.x < 32) {
+    const long long k = RNG_STRIDE * (long long)threadIdx.x;
+    const unsigned long long c = lcg_skip(0ULL, k);
+    J.c[threadIdx.x] = c;
+    J.a[threadIdx.x] = (lcg_skip(1ULL, k) - c) & RNG_MASK;
+  }
+}
+// T^(152917 off)(s), off in 0..31
+__device__ __forceinline__ unsigned long long rng_jump(const RngJump& J, int off, unsigned long long s) {
+  return (J.a[off] * s + J.c[off]) & RNG_MASK;
+}
+
 template <class R, int MAXL, int OP, bool CE>
 struct Tracker {
   const TransportArgs<R>& A;
@@ -475,7 +498,7 @@ struct Tracker {
   }
 
   __device__ __forceinline__ void write_site(const R dir[3], int gout, R wgt) {
-    int region = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (SITE_REGIONS - 1);
+    int region = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & A.sites.region_mask;
     int slot = atomicAdd(&A.sites.cursor[region], 1);
     if (slot >= A.sites.region_cap) { raise_error(A.ctr, SG_ERR_BANK_OVERFLOW, hist); return; }
     long long i = (long long)region * A.sites.region_cap + slot;
@@ -586,7 +609,9 @@ struct Tracker {
     return dead;
   }
 
-  __device__ __forceinline__ void start(int h) {
+  __device__ __forceinline__ void start(int h) { start_from(h, lcg_skip(A.master, RNG_STRIDE * (long long)h)); }
+  // history h of the bank, its RNG already at master + stride(h)
+  __device__ __forceinline__ void start_from(int h, unsigned long long s0) {
     hist = h;
     const int i = h - 1;
     c.r0[0] = A.in.r[3 * i + 0];
@@ -600,7 +625,7 @@ struct Tracker {
     G = CE ? 0 : A.in.G[i];
     if constexpr (CE) set_energy(A.in.E[i]);
     time = (R)A.in.time[i];
-    rng.s = lcg_skip(A.master, RNG_STRIDE * (long long)h);
+    rng.s = s0;
     collN = 0;
     nsites = 0;
     segs = 0;
@@ -841,18 +866,28 @@ __device__ __forceinline__ int warp_append(int* counter) {
   return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// Blocks per SM the history loop is compiled for (0: ptxas' choice).  The multigroup delta-tracking
+// kernels are held to 72 registers (7 blocks of 128 threads) in the mixed form and 80 (6 blocks) in
+// the FP64 form: left alone, ptxas picks 64 registers and spills more, which measured slower on the
+// lattice.
+template <class R, bool CE, int OP>
+constexpr int history_min_blocks() { return (CE || OP != OP_DT) ? 0 : (sizeof(R) == 4 ? 7 : 6); }
+
 template <class R, int MAXL, int OP, bool CE>
-__global__ void __launch_bounds__(128) k_transport(const __grid_constant__ TransportArgs<R> A) {
+__global__ void __launch_bounds__(128, (history_min_blocks<R, CE, OP>())) k_transport(const __grid_constant__ TransportArgs<R> A) {
   extern __shared__ double s_acc[];
+  __shared__ RngJump s_jump;
   const bool smem = A.use_smem != 0;
-  if (smem) {
+  if (smem)
     for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) s_acc[i] = 0.0;
-    __syncthreads();
-  }
+  rng_jump_table(s_jump);
+  __syncthreads();
   Tracker<R, MAXL, OP, CE> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
   bool alive = false, done = false;
   int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
+  int q_base = 0;              // first history (0-based) of the warp's chunk
+  unsigned long long s_base = 0;   // master + stride(q_base + 1), warp-uniform
 
   while (true) {
     unsigned need = __ballot_sync(FULL, !alive && !done);
@@ -867,11 +902,17 @@ __global__ void __launch_bounds__(128) k_transport(const __grid_constant__ Trans
         }
         q_next = base;
         q_end = min(base + 32, A.n);
+        q_base = base;
+        s_base = lcg_skip(A.master, RNG_STRIDE * (long long)(base + 1));
       }
       const int avail = q_end - q_next;
       const int rank = __popc(need & ((1u << lane) - 1u));
       const bool mine = ((need >> lane) & 1u) && rank < avail;
-      if (mine) { T.start(q_next + rank + 1); alive = true; }
+      if (mine) {
+        const int h0 = q_next + rank;
+        T.start_from(h0 + 1, rng_jump(s_jump, h0 - q_base, s_base));
+        alive = true;
+      }
       q_next += min(__popc(need), avail);
       need &= ~__ballot_sync(FULL, mine);
     }

@@ -49,6 +49,8 @@ def load(build=True):
         "sg_get_keff": (i32, [vp, i32, P(f64), P(f64)]),
         "sg_eigen_init": (i32, [vp, i32, u64, f64]), "sg_eigen_cycle": (i32, [vp, i32, i32, P(abi.CycleStats)]),
         "sg_eigen_state": (i32, [vp, P(u64), P(f64)]), "sg_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
+        "sg_eigen_cycle_bank": (i32, [vp, i32, i32, P(abi.Bank), i32, P(u64), P(f64), f64, P(abi.Bank),
+                                      P(abi.CycleStats)]),
         "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_set_file_source": (i32, [vp, P(abi.Bank), i32]),
@@ -203,6 +205,15 @@ class TransportOperatorGPU:
         st = abi.CycleStats()
         self._check(self.L.sg_eigen_cycle(self.h, admin, atch, C.byref(st)))
         return st
+
+    def eigen_cycle_bank(self, admin, atch, bank, pop, master, k_eff, k_end, out):
+        """One whole eigenvalue cycle on host banks (thisCycle `bank`, normalised next bank into
+        `out`); returns (master, k_new, stats)."""
+        m, k = C.c_uint64(master), C.c_double(k_eff)
+        st = abi.CycleStats()
+        self._check(self.L.sg_eigen_cycle_bank(self.h, admin, atch, C.byref(bank.struct), pop, C.byref(m), C.byref(k),
+                                               k_end, C.byref(out.struct), C.byref(st)))
+        return m.value, k.value, st
 
     def eigen_state(self):
         m, k = C.c_uint64(), C.c_double()
