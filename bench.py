@@ -2,30 +2,40 @@
 """Benchmark of the SCONE particle-tracking cycle on GB300.
 
 Workload: the 17x17 pin-lattice k-eigenvalue problem (7 groups, seeded synthetic XS, pitch 1.26 cm,
-pin radius 0.54 cm, reflective box), 1e6 particles per cycle, surface tracking, FP32 XS/distances
-with FP64 positions and tally sums.  One step = one active eigenvalue cycle: the gen loop over the
-bank, fission-site ordering, tally cycle end (17x17x7 mesh flux + implicit k), normSize_Repr and
-k feedback, all resident on the device.
+pin radius 0.54 cm, reflective box), 1e6 particles per cycle, delta tracking (surface tracking
+measured beside it), FP32 XS/distances with FP64 positions and tally sums.  One step = one active
+eigenvalue cycle on a converged bank: the gen loop over the bank, fission-site ordering, tally cycle
+end (17x17x7 mesh flux + implicit k), normSize_Repr and k feedback.
 
   value  histories/s of the device-resident cycle (CUDA events on the library's stream)
-  e2e    histories/s through the C ABI with host banks (sg_transport_bank + tally cycle calls),
-         host->device bank copy and device->host fission bank copy inside every step
-  roofline  the history-loop kernel: algorithmic bytes (128 B per event, mixed form) / kernel time
-  cpu_baseline  the CPU restatement of SCONE (oracle/) on the host cores, bounded sample
+  e2e    histories/s of the same cycle through the C ABI with host banks (sg_eigen_cycle_bank): the
+         bank in page-locked host memory, read by the kernels across the host link, and the
+         normalised next bank copied back to the host, inside every step
+  roofline  the history-loop kernel: algorithmic bytes (128 B per event, mixed form) / kernel time,
+         with the compute-side counters of its committed ncu capture
+  cpu_baseline  the same eigenvalue cycle of SCONE's algorithm on the host cores (the oracle's OpenMP
+         cycle, the code `--impl reference` times), bounded sample
 
-Beside the lattice line, the same JSON line carries the uneven batch (4096 independent fixed-source
-problems of 1-16 groups, spheres and multi-slabs, 1e3-1e6 histories each, 5.9e8 histories in all):
+Beside the lattice line, the same JSON line carries config 1's k and mesh-flux deviation of the
+mixed form from the all-FP64 form (50 inactive + 100 active cycles of 1e6), the infinite medium and
+the CE slab (each with its tally deviation from FP64), and the uneven batch (4096 independent
+fixed-source problems of 1-16 groups, spheres and multi-slabs, 1e3-1e6 histories each, 5.9e8
+histories in all):
 
   batched   histories/s of the batched form (every cycle of every problem in one persistent launch,
             one CUDA graph), mixed precision, delta tracking, launch shape from the autotuner
   plain     histories/s of the plain form over the same batch: one problem per launch sequence
-            (sg_fixed_source_cycle per cycle), event-based and history-loop kernels
+            (sg_fixed_source_cycle per cycle), event-based and history-loop kernels; compared
+            device time with device time and wall clock with wall clock
   tally error  per-bin relative errors of the batched mixed form against the all-FP64 batched form
+  cpu_baseline  a stratified, timed sample of the 4096 problems run one after another through the
+            oracle (OpenMP over histories), extrapolated to the whole batch
   serving   Poisson arrivals of requests drawn from the batch (plus 5 % lattice eigenvalue
-            requests), continuous batching: p50/p99 latency, achieved and offered histories/s
+            requests), continuous batching: p50/p99 latency, achieved and offered histories/s,
+            per-request tally error against the all-FP64 form
 
 `--impl reference` times SCONE's algorithm on the host cores instead (the oracle restatement: SCONE
-itself is Fortran and cannot be built here), on the same workload and metric.
+itself is Fortran and cannot be built here), on the same workload, step and metric.
 Multi-GPU (torchrun): independent replicas, one per rank, each with its own RNG offset (the path
 shards over histories with no exchange inside a cycle); value sums all ranks.
 """
@@ -52,7 +62,7 @@ def args_():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--pop", type=int, default=1_000_000)
+    ap.add_argument("--pop", type=int, default=None, help="particles per cycle (default 1e6; 1e5 with --profile)")
     ap.add_argument("--transport", default="dt", choices=["st", "dt", "st-nocache"])
     ap.add_argument("--no-alt", action="store_true", help="skip the second transport operator measurement")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -64,17 +74,19 @@ def args_():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / plain / served measurements")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-problem-per-launch forms")
     ap.add_argument("--no-fp64-batch", action="store_true", help="skip the all-FP64 batched reference run")
-    ap.add_argument("--serve-seconds", type=float, default=15.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--wave-histories", type=int, default=1 << 23, help="histories per serving wave")
     ap.add_argument("--serve-item", type=int, default=256, help="histories per work item while serving")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape of the batch")
     ap.add_argument("--no-configs", action="store_true", help="skip the infinite-medium and CE-slab lines")
     a = ap.parse_args()
-    if a.profile:   # a short run for ncu: lattice cycles and one small batch, nothing else
+    if a.profile:   # a reduced run for ncu captures: lattice cycles, one small batch and one CE cycle
         a.no_cpu_baseline = a.no_e2e = a.no_alt = a.no_plain = a.no_fp64_batch = a.no_serve = True
         a.no_autotune = a.no_configs = True
         a.batch_problems = min(a.batch_problems, 256)
+    if a.pop is None:
+        a.pop = 100_000 if a.profile else 1_000_000
     return a
 
 
@@ -158,117 +170,205 @@ def lattice_setup(t, p):
     return inact, ia, act, aa
 
 
-def cpu_rate(p, pop_bank, threads, target_s=10.0, max_hist=2_000_000, transport=None):
-    """Histories/s of the oracle's OpenMP gen loop on the host cores over a bounded sample: the
-    bank is transported repeatedly (fresh RNG streams) until about target_s seconds have passed."""
-    from oracle import oracle
+def transport_code(a):
     from scone_gb300 import abi
-    o = oracle.Oracle(p, transport=abi.TRANSPORT_ST if transport is None else transport)
-    adm = o.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
-    n = min(max_hist, len(pop_bank["wgt"]))
-    bank = abi.HostBank(n, {k: v[:n] for k, v in pop_bank.items()})
-    hist = ev = 0
-    t0 = time.perf_counter()
-    rep = 0
+    return {"st": abi.TRANSPORT_ST, "dt": abi.TRANSPORT_DT, "st-nocache": abi.TRANSPORT_ST_NOCACHE}[a.transport]
+
+
+def workload_config(a, world):
+    """The workload and step both arms time, as one dict (the reference arm prints the same one)."""
+    return {"workload": "lattice_17x17_7g_eigen", "particles_per_cycle": a.pop, "groups": 7,
+            "lattice": "17x17 pins r=0.54 cm pitch=1.26 cm, reflective box", "transport": a.transport.upper(),
+            "step": "one active eigenvalue cycle on a converged bank: gen loop, fission-site order, tally cycle "
+                    "end, normSize_Repr, k feedback",
+            "warmup_cycles": "inactive cycles (keff analog tally) before the timed active cycles",
+            "tally": "17x17x7 mesh flux (collision estimator) + implicit k",
+            "l2": "per-step working set exceeds L2 (bank 72 MB in, ~80 MB sites, 72 MB ordered, 72 MB normalised)",
+            "parallelism": f"replicas{world}"}
+
+
+def cpu_eigen_cycles(p, pop, transport, threads, inactive, active=None, target_s=None):
+    """SCONE's eigenvalue cycle on the host cores: the oracle's OpenMP cycle (histories over threads,
+    thread-private score memory summed at the cycle end, sites ordered by brood, cycle end,
+    normSize_Repr and k feedback on the master thread) after `inactive` cycles from the fission
+    source; then `active` timed cycles, or as many as fit in target_s seconds.
+    Returns (seconds per timed cycle, events per timed cycle, histories per cycle)."""
+    from oracle import oracle
+    o = oracle.Oracle(p, transport=transport)
+    inact, ia, act, aa = lattice_setup(o, p)
+    o.eigen_init(pop, SEED)
+    for _ in range(inactive):
+        o.eigen_cycle_omp(inact, ia, threads)
+    secs, evs = [], []
+    t_start = time.perf_counter()
     while True:
-        nh, e = o.timed_gen_loop(adm, bank, 12345 + 7919 * rep, 1.0, threads)
-        hist += nh
-        ev += e
-        rep += 1
-        dt = time.perf_counter() - t0
-        if dt >= target_s:
+        t0 = time.perf_counter()
+        st = o.eigen_cycle_omp(act, aa, threads)
+        secs.append(time.perf_counter() - t0)
+        evs.append(st.n_events)
+        if active is not None and len(secs) >= active:
             break
-    return hist / dt, ev / dt, hist, dt
+        if target_s is not None and time.perf_counter() - t_start >= target_s:
+            break
+    o.close()
+    return secs, evs, pop
 
 
 def host_bank_dict(b, n):
     return {k: b[k][:n].copy() for k in ("wgt", "r", "dir", "G", "time", "brood_id")}
 
 
+def pinned_bank(src, n, cap):
+    """A HostBank in page-locked host memory (cudaHostAlloc through torch), filled from src."""
+    import torch
+    from scone_gb300 import abi
+    arrs = {}
+    for k, shape, dt in (("wgt", (cap,), torch.float64), ("r", (cap, 3), torch.float64),
+                         ("dir", (cap, 3), torch.float64), ("G", (cap,), torch.int32),
+                         ("time", (cap,), torch.float64), ("brood_id", (cap,), torch.int32)):
+        t = torch.zeros(shape, dtype=dt).pin_memory()
+        if src is not None:
+            t[:n].copy_(torch.from_numpy(src[k][:n].copy()))
+        arrs[k] = t
+    hb = abi.HostBank(cap, {k: v.numpy() for k, v in arrs.items()})
+    hb.pinned = arrs
+    return hb
+
+
 def reference_arm(a, p):
-    """SCONE's algorithm on the host cores (oracle restatement), same workload and metric."""
+    """SCONE's algorithm on the host cores (the oracle's OpenMP eigenvalue cycle), same workload,
+    step and metric as the GPU arm: the same number of inactive cycles, then K timed active cycles."""
     rank, world, _ = dist_env()
     if rank != 0:
         return None
-    from oracle import oracle
-    from scone_gb300 import abi
     threads = os.cpu_count() or 1
-    tr = {"st": abi.TRANSPORT_ST, "dt": abi.TRANSPORT_DT, "st-nocache": abi.TRANSPORT_ST_NOCACHE}[a.transport]
-    o = oracle.Oracle(p, transport=tr)
-    o.eigen_init(a.pop, SEED)
-    bank, pop = o.eigen_bank(a.pop)
-    bd = host_bank_dict(bank, pop)
-    # one step = a bounded sample of one cycle's gen loop (the bank of `pop` histories)
-    n = pop
-    adm = o.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
-    hb = abi.HostBank(n, {k: v[:n] for k, v in bd.items()})
-    for _ in range(a.warmup):
-        o.timed_gen_loop(adm, hb, 777, 1.0, threads)
-    tot, ev = 0.0, 0
-    for s in range(a.steps):
-        t0 = time.perf_counter()
-        nh, e = o.timed_gen_loop(adm, hb, 1000 + s, 1.0, threads)
-        tot += time.perf_counter() - t0
-        ev += e
+    warm = max(3, a.warmup)
+    secs, evs, n = cpu_eigen_cycles(p, a.pop, transport_code(a), threads, warm, active=a.steps)
+    tot = sum(secs)
     value = a.steps * n / tot
     line = {
         "impl": "reference", "metric": "histories/s", "value": value, "unit": "histories/s",
-        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps,
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": warm, "ms_per_step": 1e3 * tot / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "events_per_s": ev / tot,
-        "config": {"workload": "lattice_17x17_7g_eigen", "particles_per_cycle": n, "groups": 7,
-                   "lattice": "17x17 pins r=0.54 pitch=1.26", "transport": a.transport.upper(),
-                   "reference": "C++ restatement of SCONE's algorithm (oracle/); SCONE is Fortran and no "
-                                "Fortran compiler exists here"},
+        "events_per_s": sum(evs) / tot,
+        "config": workload_config(a, world),
+        "reference": "C++ restatement of SCONE's algorithm (oracle/), OpenMP over histories as SCONE's OpenMP "
+                     "build; SCONE is Fortran and no Fortran compiler exists here",
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: the gen loop over the {n}-particle initial fission bank, "
+                         "sample": f"{warm} inactive + {a.steps} timed active cycles of {n} particles, "
                                    f"OpenMP over histories on {threads} threads"},
         "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
 
 
-def lattice_k_section(a, local):
-    """Lattice k of the mixed form against the all-FP64 form: the same inactive and active cycles
-    (1e5 particles, 10 + 20 cycles, delta tracking) in both; z = difference over the combined sigma."""
+def tally_deviation(b64, b32, n_batches):
+    """Per-bin deviation of a mixed-form tally from the all-FP64 one (scoreMemory bins(N,3) of both,
+    n_batches batches): z = mean difference / combined sigma, and the ratio of the relative
+    standard errors (mixed / FP64)."""
+    import numpy as np
+    n = n_batches
+    m1, m2 = b64[:, 1] / n, b32[:, 1] / n
+    v1 = np.maximum(b64[:, 2] / n - m1 ** 2, 0) / (n - 1)
+    v2 = np.maximum(b32[:, 2] / n - m2 ** 2, 0) / (n - 1)
+    ok = (v1 > 0) & (v2 > 0) & (m1 > 0) & (m2 > 0)
+    if not ok.any():
+        return {"bins": 0}
+    z = (m2[ok] - m1[ok]) / np.sqrt(v1[ok] + v2[ok])
+    ratio = (np.sqrt(v2[ok]) / m2[ok]) / (np.sqrt(v1[ok]) / m1[ok])
+    dev = np.abs(ratio - 1.0)
+    return {"bins": int(ok.sum()), "z_mean": float(z.mean()), "z_std": float(z.std()),
+            "max_abs_z": float(np.abs(z).max()), "chi2_per_bin": float(np.mean(z ** 2)),
+            "rel_err_ratio_median_abs_dev": float(np.median(dev)), "rel_err_ratio_p99_abs_dev": float(np.percentile(dev, 99)),
+            "frac_rel_err_within_10pct": float(np.mean(dev < 0.10)),
+            "note": "both forms draw the same RNG streams, so most histories follow the same path and the "
+                    "differences are far smaller than independent runs would show"}
+
+
+def lattice_k_section(a, local, inactive=50, active=100, pop=1_000_000, replicas=6):
+    """Config 1 as stated: k and the 17x17x7 mesh flux of the mixed form against the all-FP64 form,
+    each from `replicas` independent runs (different seeds) of `inactive` + `active` cycles of 1e6
+    particles (delta tracking).  The spread of the replicas' results is the uncertainty: the
+    cycle-to-cycle sigma of one run underestimates it, because the fission source of an eigenvalue
+    run is correlated from cycle to cycle (the ratio of the two is reported)."""
+    import numpy as np
     from scone_gb300 import abi, gpu, problems
     p = problems.lattice_17x17_7g()
     res = {}
     for name, prec in (("mixed", abi.PREC_MIXED), ("fp64", abi.PREC_FP64)):
-        t = gpu.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_DT, max_bank=300000, device=local,
-                                     form=abi.FORM_HISTORY)
-        inact, ia, act, aa = lattice_setup(t, p)
-        t.eigen_init(100000, SEED)
-        for _ in range(10):
-            t.eigen_cycle(inact, ia)
-        for _ in range(20):
-            t.eigen_cycle(act, aa)
-        res[name] = t.keff(aa)
+        t = gpu.TransportOperatorGPU(p, precision=prec, transport=abi.TRANSPORT_DT, max_bank=int(2.5 * pop) + 4096,
+                                     device=local, form=abi.FORM_HISTORY)
+        ks, sds, mesh = [], [], []
+        t0 = time.perf_counter()
+        for r in range(replicas):
+            inact, ia, act, aa = lattice_setup(t, p)
+            t.eigen_init(pop, gpu.rng_skip(SEED, 7919 * 152917 * (r + 1) * pop))
+            for _ in range(inactive):
+                t.eigen_cycle(inact, ia)
+            for _ in range(active):
+                t.eigen_cycle(act, aa)
+            k, sd = t.keff(aa)
+            ks.append(k)
+            sds.append(sd)
+            mesh.append(t.bins(act))
+        res[name] = (np.array(ks), np.array(sds), np.array(mesh), time.perf_counter() - t0)
         t.close()
-    (km, sm), (kd, sd) = res["mixed"], res["fp64"]
-    return {"k_mixed": km, "sigma_mixed": sm, "k_fp64": kd, "sigma_fp64": sd,
-            "z": (km - kd) / (sm * sm + sd * sd) ** 0.5, "cycles": "10 inactive + 20 active, 1e5 particles"}
+    (km, sm, mm, wm), (kd, sd, md, wd) = res["mixed"], res["fp64"]
+    se_m, se_d = km.std(ddof=1) / np.sqrt(replicas), kd.std(ddof=1) / np.sqrt(replicas)
+    z = (km.mean() - kd.mean()) / np.sqrt(se_m ** 2 + se_d ** 2)
+    # relative standard error of each bin within one run (100 active cycles), averaged over the
+    # replicas: the quantity the 10 % criterion compares
+    def rel_err(b):
+        m = b[:, :, 1] / active
+        v = np.maximum(b[:, :, 2] / active - m ** 2, 0) / (active - 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return np.where(m > 0, np.sqrt(v) / m, np.nan).mean(axis=0)
+    re_m, re_d = rel_err(mm), rel_err(md)
+    # mesh flux: per bin, replica means and their standard errors
+    mm, md = mm[:, :, 1] / active, md[:, :, 1] / active
+    mmean, dmean = mm.mean(axis=0), md.mean(axis=0)
+    mse, dse = mm.std(axis=0, ddof=1) / np.sqrt(replicas), md.std(axis=0, ddof=1) / np.sqrt(replicas)
+    ok = (mse > 0) & (dse > 0) & (dmean > 0)
+    zb = (mmean[ok] - dmean[ok]) / np.sqrt(mse[ok] ** 2 + dse[ok] ** 2)
+    ratio = re_m[ok] / re_d[ok]
+    return {"k_mixed": float(km.mean()), "se_mixed": float(se_m), "k_fp64": float(kd.mean()), "se_fp64": float(se_d),
+            "z": float(z), "within_3_sigma": bool(abs(z) < 3.0),
+            "replicas": replicas, "k_replicas": {"mixed": km.tolist(), "fp64": kd.tolist()},
+            "sigma_ratio_replicas_over_within_run": float(np.sqrt((km.var(ddof=1) + kd.var(ddof=1)) / 2) /
+                                                          np.mean(np.concatenate([sm, sd]))),
+            "cycles": f"{replicas} independent runs per form of {inactive} inactive + {active} active cycles, "
+                      f"{pop} particles, DT", "wall_s": {"mixed": wm, "fp64": wd},
+            "mesh_flux_vs_fp64": {"bins": int(ok.sum()), "z_mean": float(zb.mean()), "z_std": float(zb.std()),
+                                  "max_abs_z": float(np.abs(zb).max()), "chi2_per_bin": float(np.mean(zb ** 2)),
+                                  "rel_err_ratio_median_abs_dev": float(np.median(np.abs(ratio - 1))),
+                                  "frac_rel_err_within_10pct": float(np.mean(np.abs(ratio - 1) < 0.10)),
+                                  "note": "z from the replica spread per bin; the relative-error ratio (mixed / "
+                                          "FP64) from each run's cycle-to-cycle estimate, averaged over the "
+                                          "replicas"}}
 
 
 def configs_section(a, local):
     """The other two workloads, each through sg_fixed_source_cycle on its own handle (device-resident
     source, gen loop and batch close) and through the oracle on the host cores:
     infinite homogeneous medium, 2 groups, 1e5 histories; continuous-energy 3-layer slab, 1e7
-    histories (10 cycles of 1e6), FP32 tables with FP64 energy and position."""
+    histories (10 cycles of 1e6), FP32 tables with FP64 energy and position.  Each carries the
+    deviation of its tally in the mixed form from the all-FP64 form (same cycles, same seeds)."""
     from oracle import oracle
     from scone_gb300 import abi, gpu, problems
     threads = os.cpu_count() or 1
     out = {}
-    cases = [("infinite_medium_2g", problems.infinite_medium_2g(), "flux", 100000, 1, abi.TRANSPORT_ST),
-             ("ce_slab_3layer", problems.ce_slab_3layer(), "current", 1000000, 10, abi.TRANSPORT_DT)]
-    for name, p, tally, pop, cycles, tr in cases:
+    cases = [("infinite_medium_2g", problems.infinite_medium_2g(), "flux", 100000, 1, 10, abi.TRANSPORT_ST),
+             ("ce_slab_3layer", problems.ce_slab_3layer(), "current", 1000000, 10, 10, abi.TRANSPORT_DT)]
+    for name, p, tally, pop, cycles, dev_cycles, tr in cases:
         res = {"histories": pop * cycles, "transport": "ST" if tr == abi.TRANSPORT_ST else "DT"}
+        bins = {}
         for prec_name, prec in (("mixed", abi.PREC_MIXED), ("fp64", abi.PREC_FP64)):
             t = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=pop + 4096, device=local,
                                          form=abi.FORM_HISTORY)
+            warm_adm = t.upload_tally(p.tallies[tally])
             adm = t.upload_tally(p.tallies[tally])
+            t.fixed_source_cycle(warm_adm, min(pop, 10000), SEED)          # warm-up (own tally)
             m = SEED
-            t.fixed_source_cycle(adm, min(pop, 10000), m)                # warm-up
             ms = ev = 0.0
             for _ in range(cycles):
                 m, st = t.fixed_source_cycle(adm, pop, m)
@@ -276,7 +376,16 @@ def configs_section(a, local):
                 ev += st.n_events
             res[prec_name] = {"value": pop * cycles / (ms / 1e3), "unit": "histories/s",
                               "events_per_s": ev / (ms / 1e3), "ms": ms}
+            # tally deviation: dev_cycles batches (more than the timed cycles when those are fewer)
+            if dev_cycles > cycles:
+                adm = t.upload_tally(p.tallies[tally])
+                m = SEED
+                for _ in range(dev_cycles):
+                    m, _ = t.fixed_source_cycle(adm, pop, m)
+            bins[prec_name] = t.bins(adm)
             t.close()
+        res["tally_vs_fp64"] = tally_deviation(bins["fp64"], bins["mixed"], max(cycles, dev_cycles))
+        res["tally_vs_fp64"]["tally"] = tally
         # the oracle on the host cores, a bounded sample (about 10 s)
         o = oracle.Oracle(p, transport=tr)
         adm = o.upload_tally(p.tallies[tally])
@@ -299,8 +408,59 @@ def configs_section(a, local):
     return out
 
 
+def batch_cpu_baseline(batch, threads, target_s=20.0, strata=8, seed=5):
+    """The uneven batch on the host cores, as separate runs one after another (the plain CPU analogue
+    of the batch): a stratified, timed sample.  Problems are sorted by history count into `strata`
+    strata of equal size; from each, problems drawn at random (seeded) run through the oracle -- set
+    up (geometry, data, tally), then every cycle: the point source and the gen loop with OpenMP over
+    histories -- until the stratum has used its share of target_s.  The whole batch's time is
+    estimated as the sum over strata of (mean seconds per sampled problem) x (problems in it)."""
+    import numpy as np
+    from oracle import oracle
+    from scone_gb300 import abi
+    hist = np.array([pop * c for _, pop, c, _ in batch], dtype=np.float64)
+    groups = np.array_split(np.argsort(hist, kind="stable"), strata)
+    rng = np.random.default_rng(seed)
+    est = 0.0
+    n_sampled = 0
+    h_sampled = 0.0
+    t_sampled = 0.0
+    per_stratum = []
+    for g in groups:
+        times = []
+        t_s = time.perf_counter()
+        for i in rng.permutation(g):
+            p, pop, cycles, master = batch[int(i)]
+            t0 = time.perf_counter()
+            o = oracle.Oracle(p, transport=abi.TRANSPORT_DT)
+            adm = o.upload_tally(p.tallies["flux"])
+            m = master
+            for c in range(cycles):
+                bank = o.generate_source(m, pop)
+                o.timed_gen_loop(adm, bank, m + 1, 1.0, threads)
+                m = oracle.rng_skip(m, 2 * 152917 * pop)
+            o.close()
+            times.append(time.perf_counter() - t0)
+            h_sampled += hist[int(i)]
+            if time.perf_counter() - t_s >= target_s / strata:
+                break
+        est += float(np.mean(times)) * len(g)
+        n_sampled += len(times)
+        t_sampled += float(np.sum(times))
+        per_stratum.append({"problems": len(g), "sampled": len(times), "histories_min": float(hist[g].min()),
+                            "histories_max": float(hist[g].max()), "mean_s_per_problem": float(np.mean(times))})
+    return {"value": float(hist.sum()) / est, "unit": "histories/s", "cores": threads, "kind": "port",
+            "estimated_batch_s": est,
+            "sample": f"{n_sampled} of {len(batch)} problems ({h_sampled:.3g} histories, {t_sampled:.1f} s), "
+                      f"{strata} strata by history count, each problem a separate oracle run (setup + cycles of "
+                      f"point source and OpenMP gen loop on {threads} threads); batch time = sum over strata of "
+                      f"mean time per problem x problems",
+            "strata": per_stratum}
+
+
 def batched_section(a, local):
-    """The uneven batch: batched form vs the plain forms, tally error vs all-FP64, and serving."""
+    """The uneven batch: batched form vs the plain forms, tally error vs all-FP64, CPU baseline and
+    serving."""
     import numpy as np
     from scone_gb300 import abi, gpu, problems, serve
     out = {"workload": f"batched_uneven_{a.batch_problems}", "precision": "mixed", "transport": "DT"}
@@ -311,7 +471,7 @@ def batched_section(a, local):
 
     def load(prec):
         B = gpu.BatchGPU(precision=prec, transport=abi.TRANSPORT_DT, device=local, max_problems=2 * len(batch),
-                         arena_bytes=4 << 30, max_work_items=1 << 21)
+                         arena_bytes=(1 << 30) if a.profile else (4 << 30), max_work_items=1 << 21)
         return B, [B.add(p, pop, c, m) for p, pop, c, m in batch]
 
     B, slots = load(abi.PREC_MIXED)
@@ -323,15 +483,18 @@ def batched_section(a, local):
     for s in slots:
         B.clear_tally(s)
     steps = max(1, min(a.steps, 3))
-    ms = []
+    ms, walls = [], []
     ev = 0
     for _ in range(steps):
+        w0 = time.perf_counter()
         st = B.run(slots)
+        walls.append(time.perf_counter() - w0)
         ms.append(st.run_ms)
         ev = st.n_events
     mean_ms = sum(ms) / len(ms)
     out["value"] = total / (mean_ms / 1e3)
     out["unit"] = "histories/s"
+    out["wall_value"] = total / (sum(walls) / len(walls))
     out["events_per_s"] = ev / (mean_ms / 1e3)
     out["ms_per_step"] = mean_ms
     out["gpu_launches_per_step"] = 2
@@ -356,7 +519,12 @@ def batched_section(a, local):
     out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                        "peak_source": kind, "kernel": "k_batch (batched history loop)",
                        "traffic": bpe_dram * ev if bpe_dram else None, "bytes_per_event": BYTES_PER_EVENT_MIXED,
-                       "events_per_launch": ev, "launch_ms": mean_ms}
+                       "events_per_launch": ev, "launch_ms": mean_ms,
+                       "launch_ms_spans": "the run graph (work-list copy, counter reset, k_batch, k_batch_close), "
+                                          "CUDA events on the batch stream; k_batch is ~100 % of it"}
+    comp = committed_compute("k_batch_uneven")
+    if comp:
+        out["roofline"]["compute"] = comp
     if not a.no_plain:
       try:
         # the event form's queue thresholds tuned on a sample (every 64th problem), as the batch's
@@ -371,11 +539,15 @@ def batched_section(a, local):
             st = B.run_plain(slots, form=form)
             w = time.perf_counter() - t0
             out[name] = {"value": total / w, "unit": "histories/s", "wall_s": w, "kernels": int(st.n_kernels),
+                         "device_value": total / (st.run_ms / 1e3), "run_ms": st.run_ms,
                          "transport_kernel_ms": st.kernel_ms}
-        out["speedup_vs_plain_event"] = out["value"] / out["plain_event"]["value"]
-        out["speedup_vs_plain_history"] = out["value"] / out["plain_history"]["value"]
+        # like with like: wall clock against wall clock, device time against device time
+        for name in ("plain_event", "plain_history"):
+            out[f"speedup_vs_{name}"] = {"wall": out["wall_value"] / out[name]["value"],
+                                         "device": out["value"] / out[name]["device_value"]}
       except Exception as e:
         out["plain_error"] = repr(e)
+    B64 = s64 = None
     if not a.no_fp64_batch:
       try:
         B64, s64 = load(abi.PREC_FP64)
@@ -397,9 +569,14 @@ def batched_section(a, local):
                                           "p99_abs_dev": float(np.percentile(r, 99)),
                                           "frac_within_10pct": float(np.mean(r < 0.10)),
                                           "max_abs_z": float(np.max(np.abs(zs)))}
-        B64.close()
       except Exception as e:
         out["fp64_error"] = repr(e)
+    if not a.no_cpu_baseline:
+      try:
+        out["cpu_baseline"] = batch_cpu_baseline(batch, os.cpu_count() or 1)
+        out["speedup_vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
+      except Exception as e:
+        out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
     if not a.no_serve and a.serve_seconds > 0:
       try:
         templates = [(pop, c) for _, pop, c, _ in batch]
@@ -410,34 +587,92 @@ def batched_section(a, local):
         tuning = out["tuning"]
         B.close()
         B = None
-        for name, rate, efrac in (("mix_2000rps_5pct_eigen", 2000.0, 0.05),
-                                  ("half_capacity", 0.5 * cap / mean_hist, 0.0)):
+        for name, rate, efrac, secs in (("mix_2000rps_5pct_eigen", 2000.0, 0.05, a.serve_seconds),
+                                        ("half_capacity", 0.5 * cap / mean_hist, 0.0, min(a.serve_seconds, 20.0))):
             Bs, cat = load(abi.PREC_MIXED)
             Bs.set_tuning(**tuning)
-            pool = serve.EigenPool(lat, 4, abi.PREC_MIXED, abi.TRANSPORT_DT, 100000) if efrac > 0 else None
-            S = serve.SolveServer(Bs, cat, wave_histories=a.wave_histories, item_histories=a.serve_item, eigen=pool)
+            pool = serve.EigenPool(lat, 2, abi.PREC_MIXED, abi.TRANSPORT_DT, 100000) if efrac > 0 else None
+            S = serve.SolveServer(Bs, cat, wave_histories=a.wave_histories, item_histories=a.serve_item, eigen=pool,
+                                  eigen_queue_max=4 if efrac > 0 else None,
+                                  defer_backlog=2 * a.wave_histories if efrac > 0 else None)
             offered = rate * ((1 - efrac) * mean_hist + efrac * 100000 * 60)
-            done, wall, n = serve.poisson_run(S, templates, rate, a.serve_seconds, seed=7, eigen_fraction=efrac,
-                                              drain=(efrac == 0), max_drain_s=30.0)
+            qlog = []
+            done, wall, n = serve.poisson_run(S, templates, rate, secs, seed=7, eigen_fraction=efrac,
+                                              drain=(efrac == 0), max_drain_s=30.0, queue_log=qlog)
             S.stop()
             sh, se = Bs.serve_counts()
             summ = serve.latency_summary(done, wall, offered)
             summ["fixed_source_events_per_s"] = se / wall
             summ["roofline_frac"] = se * BYTES_PER_EVENT_MIXED / wall / 1e9 / measured_peaks()[0]
-            summ.update({"arrival_rate": rate, "arrived": n, "eigen_fraction": efrac,
-                         "eigen_completed": sum(1 for r in done if r.kind == "eigen"),
-                         "waves": Bs.serve_status()[2]})
+            summ.update({"arrival_rate": rate, "arrived": n, "eigen_fraction": efrac, "seconds": secs,
+                         "eigen_completed": sum(1 for r in done if r.kind == "eigen" and r.status == "done"),
+                         "waves": Bs.serve_status()[2], "queues": serve.queue_growth(qlog)})
+            if efrac > 0:
+                summ["eigen_policy"] = {"pool": 2, "queue_max": 4, "defer_backlog_histories": 2 * a.wave_histories,
+                                        "deferred_turns": S.deferred_turns, "shed": S.shed,
+                                        "rule": "at most 2 eigenvalue requests run; an arrival finding 4 waiting is "
+                                                "shed; eigenvalue cycles wait while fixed-source requests wait for "
+                                                "memory or more than 2 waves of histories are queued"}
+            # per-request tally error against the all-FP64 form: a sample of completed fixed-source
+            # requests re-run as FP64 instances with the same sizes and seeds
+            if B64 is not None:
+                fixed = [r for r in done if r.kind == "fixed" and r.bins is not None]
+                rng = np.random.default_rng(11)
+                pick = [fixed[i] for i in rng.choice(len(fixed), size=min(256, len(fixed)), replace=False)]
+                inst = [B64.instance(s64[r.template], r.pop, r.cycles, r.master) for r in pick]
+                B64.run(inst)
+                per = []
+                for r, sl in zip(pick, inst):
+                    d = tally_deviation(B64.bins(sl), r.bins, r.cycles)
+                    if d["bins"]:
+                        per.append((d["max_abs_z"], d["frac_rel_err_within_10pct"], d["rel_err_ratio_median_abs_dev"]))
+                    B64.remove(sl)
+                if per:
+                    per = np.array(per)
+                    summ["per_request_tally_vs_fp64"] = {
+                        "requests": int(per.shape[0]), "max_abs_z_median": float(np.median(per[:, 0])),
+                        "max_abs_z_p99": float(np.percentile(per[:, 0], 99)),
+                        "frac_bins_rel_err_within_10pct_mean": float(per[:, 1].mean()),
+                        "frac_requests_all_bins_within_10pct": float(np.mean(per[:, 1] == 1.0)),
+                        "rel_err_ratio_median_abs_dev_median": float(np.median(per[:, 2])),
+                        "how": "sampled completed requests re-run as all-FP64 batch instances (same template, "
+                               "population, cycles, seed); per bin z and relative-error ratio"}
             res[name] = summ
             if pool:
-                for t, _ in pool.free:
-                    t.close()
+                for t_, _ in pool.free:
+                    t_.close()
             Bs.close()
         out["serving"] = res
       except Exception as e:
         out["serving_error"] = repr(e)
+    if B64 is not None:
+        B64.close()
     if B is not None:
         B.close()
     return out
+
+
+def profile_ce_cycle(local, pop=200_000):
+    """For ncu captures: two fixed-source cycles of the continuous-energy 3-layer slab (mixed form,
+    delta tracking), the second one the captured launch."""
+    from scone_gb300 import abi, gpu, problems
+    p = problems.ce_slab_3layer()
+    t = gpu.TransportOperatorGPU(p, precision=abi.PREC_MIXED, transport=abi.TRANSPORT_DT, max_bank=pop + 4096,
+                                 device=local, form=abi.FORM_HISTORY)
+    adm = t.upload_tally(p.tallies["current"])
+    m = SEED
+    for _ in range(2):
+        m, _st = t.fixed_source_cycle(adm, pop, m)
+    t.close()
+
+
+def committed_compute(kernel):
+    """Compute-side counters of `kernel` from its committed ncu capture (profiles/compute.json)."""
+    p = os.path.join(ROOT, "profiles", "compute.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    return None
 
 
 def main():
@@ -461,7 +696,7 @@ def main():
     from scone_gb300 import gpu
 
     prec = abi.PREC_MIXED if a.precision == "mixed" else abi.PREC_FP64
-    tr = {"st": abi.TRANSPORT_ST, "dt": abi.TRANSPORT_DT, "st-nocache": abi.TRANSPORT_ST_NOCACHE}[a.transport]
+    tr = transport_code(a)
     cap = int(2.5 * a.pop) + 4096
     form = abi.FORM_EVENT if a.form == "event" else abi.FORM_HISTORY
     t = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=cap, device=local, form=form)
@@ -497,38 +732,63 @@ def main():
         pg.barrier()
     clocks = sampler.stop()
 
-    # e2e: the same cycles through the host-bank C ABI (what a Fortran physicsPackage calls)
+    # e2e: the same cycle through the C ABI with host banks (sg_eigen_cycle_bank: what a Fortran
+    # eigenPhysicsPackage that keeps its dungeons in host memory calls once per cycle), starting from
+    # the converged bank and pRNG of the run above; the bank is page-locked host memory that the
+    # kernels read in place, and the normalised next bank is copied back every step
     e2e = None
+    e2e_gen = None
     if not a.no_e2e:
-        bank, pop = t.eigen_bank(a.pop)
-        pin = {k: torch.from_numpy(v).pin_memory() for k, v in host_bank_dict(bank, pop).items()}
-        hb = abi.HostBank(pop, {k: v.numpy() for k, v in pin.items()})
-        nxt_cap = cap
-        pin_next = {k: torch.empty((nxt_cap, 3) if k in ("r", "dir") else (nxt_cap,),
-                                   dtype=torch.float64 if k in ("wgt", "r", "dir", "time") else torch.int32).pin_memory()
-                    for k in ("wgt", "r", "dir", "G", "time", "brood_id")}
-        nb = abi.HostBank(nxt_cap, {k: v.numpy() for k, v in pin_next.items()})
         import ctypes as C
-        adm_e2e = t.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
-        for w_ in range(2):
-            st = abi.CycleStats()
-            t._check(t.L.sg_transport_bank(t.h, adm_e2e, C.byref(hb.struct), pop, C.c_uint64(55 + w_), 1.0,
-                                           C.byref(nb.struct), nxt_cap, C.byref(st)))
+        bank, pop = t.eigen_bank(a.pop)
+        master, k = t.eigen_state()
+        b_in, b_out = pinned_bank(bank, pop, pop), pinned_bank(None, 0, pop)
+        e_act = t.upload_tally(p.tallies["mesh"])
+        e_aa = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        t.attach_tally(e_act, e_aa)
+        k_end = k
+        for _ in range(2):                                             # warm-up
+            master, k, _st = t.eigen_cycle_bank(e_act, e_aa, b_in, pop, master, k, k_end, b_out)
+            k_end = k
+            b_in, b_out = b_out, b_in
         torch.cuda.synchronize()
         w0 = time.perf_counter()
-        d2h = 0
-        for s in range(a.steps):
-            t.tally_cycle_start(adm_e2e, float(pop))
-            st = abi.CycleStats()
-            t._check(t.L.sg_transport_bank(t.h, adm_e2e, C.byref(hb.struct), pop, C.c_uint64(1000 + s), ks[-1],
-                                           C.byref(nb.struct), nxt_cap, C.byref(st)))
-            t.tally_cycle_end(adm_e2e, float(st.n_next), ks[-1])
-            d2h += st.n_next * (24 + 24 + 8 + 4 + 8 + 4)
+        for _ in range(a.steps):
+            master, k, _st = t.eigen_cycle_bank(e_act, e_aa, b_in, pop, master, k, k_end, b_out)
+            k_end = k
+            b_in, b_out = b_out, b_in
         torch.cuda.synchronize()
         we = time.perf_counter() - w0
         e2e = {"value": a.steps * pop / we, "unit": "histories/s",
                "h2d_bytes_per_step": pop * (24 + 24 + 8 + 4 + 8),
-               "d2h_bytes_per_step": int(d2h / a.steps), "ms_per_step": 1e3 * we / a.steps}
+               "d2h_bytes_per_step": pop * (24 + 24 + 8 + 4 + 8 + 4), "ms_per_step": 1e3 * we / a.steps,
+               "call": "sg_eigen_cycle_bank (one whole cycle per call, host dungeons)",
+               "h2d": "page-locked host bank read in place by the kernels across the host link (no staging copy)",
+               "d2h": "normalised next-cycle bank, cudaMemcpyAsync after the cycle"}
+        # the gen loop alone through sg_transport_bank (a shim that keeps normSize_Repr in Fortran)
+        nxt_cap = cap
+        b_next = pinned_bank(None, 0, nxt_cap)
+        adm_e2e = t.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        for w_ in range(2):
+            st = abi.CycleStats()
+            t._check(t.L.sg_transport_bank(t.h, adm_e2e, C.byref(b_in.struct), pop, C.c_uint64(55 + w_), 1.0,
+                                           C.byref(b_next.struct), nxt_cap, C.byref(st)))
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        d2h = 0
+        for s_ in range(a.steps):
+            t.tally_cycle_start(adm_e2e, float(pop))
+            st = abi.CycleStats()
+            t._check(t.L.sg_transport_bank(t.h, adm_e2e, C.byref(b_in.struct), pop, C.c_uint64(1000 + s_), ks[-1],
+                                           C.byref(b_next.struct), nxt_cap, C.byref(st)))
+            t.tally_cycle_end(adm_e2e, float(st.n_next), ks[-1])
+            d2h += st.n_next * (24 + 24 + 8 + 4 + 8 + 4)
+        torch.cuda.synchronize()
+        we = time.perf_counter() - w0
+        e2e_gen = {"value": a.steps * pop / we, "unit": "histories/s", "h2d_bytes_per_step": pop * 68,
+                   "d2h_bytes_per_step": int(d2h / a.steps), "ms_per_step": 1e3 * we / a.steps,
+                   "call": "sg_tally_cycle_start + sg_transport_bank + sg_tally_cycle_end (gen loop and site "
+                           "order only; normSize_Repr left to the caller)"}
 
     # the other transport operator on the lattice workload (surface tracking vs delta tracking), same K steps
     alt = None
@@ -578,19 +838,24 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": peak_kind, "kernel": ("event loop: k_ev_start + k_ev_transit + k_ev_collide + k_ev_transit<tail>"
                        if a.form == "event" else "k_transport (history loop)"),
-            "bytes_per_event": bpe, "events_per_launch": ev_per_launch, "launch_ms": launch_ms}
+            "bytes_per_event": bpe, "events_per_launch": ev_per_launch, "launch_ms": launch_ms,
+            "launch_ms_spans": "the history-loop kernel alone: CUDA events recorded on the library's stream "
+                               "directly before and after its one launch per cycle (an active cycle, with the "
+                               "mesh tally)"}
+    comp = committed_compute("k_transport_lattice")
+    if comp:
+        roof["compute"] = comp
 
     cpu = None
     if not a.no_cpu_baseline:
         try:
-            bank, pop = t.eigen_bank(min(a.pop, 400000))
-            bd = host_bank_dict(bank, min(pop, 400000))
             threads = os.cpu_count() or 1
-            rate, erate, n, dt = cpu_rate(p, bd, threads, transport=tr)
-            cpu = {"value": rate, "unit": "histories/s", "cores": threads, "kind": "port",
-                   "sample": f"{n} histories (lattice bank of {min(pop, 400000)} transported repeatedly), "
-                             f"{dt:.1f} s, OpenMP over histories",
-                   "events_per_s": erate}
+            cpu_pop = a.pop
+            secs, evs, n = cpu_eigen_cycles(p, cpu_pop, tr, threads, 3, target_s=10.0)
+            cpu = {"value": len(secs) * n / sum(secs), "unit": "histories/s", "cores": threads, "kind": "port",
+                   "sample": f"3 inactive + {len(secs)} timed active eigenvalue cycles of {n} particles "
+                             f"({sum(secs):.1f} s), OpenMP over histories: the code --impl reference times",
+                   "events_per_s": sum(evs) / sum(secs)}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
@@ -605,6 +870,8 @@ def main():
             configs["lattice_k_vs_fp64"] = lattice_k_section(a, local)
         except Exception as e:
             configs["lattice_k_error"] = repr(e)
+    if a.profile and world == 1:
+        profile_ce_cycle(local)
     batched = None
     if not a.no_batch and world == 1:
         try:
@@ -616,15 +883,11 @@ def main():
         "metric": "histories/s", "value": hist / sec, "unit": "histories/s", "n_gpus": world,
         "steps": a.steps, "warmup": warm, "ms_per_step": 1e3 * sec / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == abi.PREC_MIXED else "f64",
-        "data": "synthetic",
-        "config": {"workload": "lattice_17x17_7g_eigen", "particles_per_cycle": a.pop, "groups": 7,
-                   "lattice": "17x17 pins r=0.54 cm pitch=1.26 cm, reflective box", "transport": a.transport.upper(),
-                   "precision": a.precision, "form": a.form, "step": "one active eigenvalue cycle (gen loop + site order + "
-                   "tally close + normSize_Repr + k feedback)", "tally": "17x17x7 mesh flux + implicit k",
-                   "l2": "per-step working set exceeds L2 (bank 72 MB in, ~80 MB sites, 72 MB ordered, 72 MB normalised)",
-                   "parallelism": f"replicas{world}"},
+        "data": "synthetic", "precision": a.precision, "form": a.form,
+        "config": workload_config(a, world),
         "events_per_s": events / sec, "k_eff": ks[-1], "wall_ms_per_step": 1e3 * wall / a.steps,
-        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "e2e_gen_loop_only": e2e_gen, "clocks": clocks,
         "other_transport": alt, "batched": batched, "other_configs": configs,
     }
     print(json.dumps(line), flush=True)

@@ -52,6 +52,7 @@ def lib():
             "or_get_keff": (i32, [vp, i32, P(f64), P(f64)]),
             "or_get_history_records": (i32, [vp, P(i32), P(u64), i32]),
             "or_eigen_init": (i32, [vp, i32, u64, f64]), "or_eigen_cycle": (i32, [vp, i32, i32, P(abi.CycleStats)]),
+            "or_eigen_cycle_omp": (i32, [vp, i32, i32, i32, P(abi.CycleStats)]),
             "or_eigen_state": (i32, [vp, P(u64), P(f64)]), "or_eigen_get_bank": (i32, [vp, P(abi.Bank), i32, P(i32)]),
             "or_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
             "or_rng_draws": (i32, [P(u64), P(f64), i32]), "or_rng_skip": (u64, [u64, i64]),
@@ -240,6 +241,12 @@ class Oracle:
     def eigen_cycle(self, admin, atch):
         st = abi.CycleStats()
         self._check(self.L.or_eigen_cycle(self.h, admin, atch, C.byref(st)))
+        return st
+
+    def eigen_cycle_omp(self, admin, atch, threads=0):
+        """The same cycle with OpenMP over histories (SCONE's OpenMP build): the CPU baseline."""
+        st = abi.CycleStats()
+        self._check(self.L.or_eigen_cycle_omp(self.h, admin, atch, threads, C.byref(st)))
         return st
 
     def eigen_state(self):

@@ -2388,6 +2388,86 @@ int32_t or_eigen_cycle(or_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
   }
   return SG_OK;
 }
+// The same eigenvalue cycle as SCONE's OpenMP build runs it (eigenPhysicsPackage_class.f90:203-338):
+// the gen loop over histories with dynamic scheduling on `threads` threads, each with private
+// operators and private score memory (scoreMemory's per-thread parallelBins, scoreMemory_class.f90
+// :215-233, summed into the shared bins at the cycle end), fission sites detained per thread and
+// then ordered by brood ID (particleDungeon%sortByBroodID, particleDungeon_class.f90:923-981); the
+// rest of the cycle (reportCycleEnd, normSize_Repr, k feedback) on the master thread.  The banks,
+// RNG states and k equal or_eigen_cycle's; the tally sums differ only in their order.  CPU
+// baseline of the bench, not used by the parity tests.
+int32_t or_eigen_cycle_omp(or_handle h, int32_t admin, int32_t atch, int32_t threads, sg_cycle_stats* st) {
+  Oracle* o = O(h);
+  double startW = 0; for (auto& s : o->thisCycle) startW += s.wgt;
+  o->reportCycleStart(admin, startW);
+  const int n = (int)o->thisCycle.size();
+  std::vector<orc::PState> bank;
+  bank.swap(o->thisCycle);                            // kept out of the thread-private copies
+  o->recColl.clear(); o->recRng.clear();
+  const uint64_t master = o->master.s;
+  const double k = o->k_new;
+  std::vector<int> count(n + 1, 0);
+  std::vector<std::vector<int>> tHist;
+  std::vector<std::vector<orc::PState>> tSites;
+  int64_t ev = 0, coll = 0;
+  std::string err;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel reduction(+:ev, coll)
+  {
+    Oracle local = *o;
+    for (auto& A : local.admins) std::fill(A.mem.parallel.begin(), A.mem.parallel.end(), 0.0);
+    local.nEvents = 0; local.nColl = 0;
+    std::vector<int> myHist;
+    std::vector<orc::PState> mySites;
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < n; ++i) {
+      std::vector<orc::PState> s;
+      local.runHistory(bank[i], i + 1, master, k, admin, &s, nullptr, nullptr);
+      for (auto& x : s) { myHist.push_back(i + 1); mySites.push_back(x); }
+    }
+    ev += local.nEvents;
+    coll += local.nColl;
+#pragma omp critical
+    {
+      for (size_t a = 0; a < o->admins.size(); ++a) {
+        auto& P = o->admins[a].mem.parallel;
+        const auto& Q = local.admins[a].mem.parallel;
+        for (size_t i = 0; i < P.size(); ++i) P[i] += Q[i];
+      }
+      if (!local.err.empty()) err = local.err;
+      tHist.emplace_back(std::move(myHist));
+      tSites.emplace_back(std::move(mySites));
+    }
+  }
+  o->nEvents = ev; o->nColl = coll;
+  if (!err.empty()) { o->err = err; bank.swap(o->thisCycle); return SG_ERR_LOST; }
+  // sortByBroodID: a counting sort by history, each history's sites in their detain order
+  for (const auto& v : tHist) for (int b : v) count[b] += 1;
+  std::vector<int> pos(n + 2, 0);
+  for (int i = 1; i <= n; ++i) pos[i + 1] = pos[i] + count[i];
+  std::vector<orc::PState> next((size_t)pos[n + 1]);
+  for (size_t t = 0; t < tHist.size(); ++t)
+    for (size_t j = 0; j < tHist[t].size(); ++j) next[pos[tHist[t][j]]++] = tSites[t][j];
+  o->master.stride(o->pop + 1);                       // :257
+  double endW = 0; for (auto& s : next) endW += s.wgt;
+  o->reportCycleEnd(admin, endW, o->nextK);            // :261
+  if (next.empty()) { o->err = "empty fission bank"; return SG_ERR_STATE; }
+  o->normSizeRepr(next, o->pop, o->master);            // :269
+  o->master.stride(1);                                 // :275
+  o->thisCycle.swap(next);
+  double kn = o->k_new, sd = 0.0;
+  o->getKeff(atch, kn, sd);                            // :289-298
+  double kUsed = o->k_new;
+  o->k_new = kn;
+  o->nextK = kn;
+  if (st) {
+    st->n_histories = n; st->n_events = ev; st->n_collisions = coll; st->n_next = (int64_t)o->thisCycle.size();
+    st->start_weight = startW; st->end_weight = endW; st->k_eff = kUsed; st->k_new = kn;
+  }
+  return SG_OK;
+}
 int32_t or_eigen_state(or_handle h, uint64_t* master, double* k) { *master = O(h)->master.s; *k = O(h)->k_new; return SG_OK; }
 int32_t or_eigen_get_bank(or_handle h, sg_bank* out, int32_t cap, int32_t* pop) {
   Oracle* o = O(h);

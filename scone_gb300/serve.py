@@ -11,6 +11,10 @@ their latency (arrival to device completion of their last wave).
 
 Eigenvalue requests (the lattice k-eigenvalue problem) run on a small pool of resident
 TransportOperatorGPU handles, one cycle per loop turn, on their own CUDA streams beside the waves.
+Their admission policy protects the fixed-source requests under overload: at most the pool's size
+run at once; an arrival that finds `eigen_queue_max` requests already waiting is shed (completed at
+once with status "shed"); and while the fixed-source backlog (histories queued on the device) exceeds
+`defer_backlog`, no eigenvalue cycle is launched that turn (the running ones are deferred).
 """
 import collections
 import math
@@ -22,7 +26,7 @@ from . import abi, gpu
 
 class Request:
     __slots__ = ("rid", "kind", "template", "pop", "cycles", "master", "arrival", "slot", "submitted",
-                 "latency", "bins", "k", "handle", "cycle", "histories")
+                 "latency", "bins", "k", "handle", "cycle", "histories", "status")
 
     def __init__(self, rid, kind, template, pop, cycles, master, arrival):
         self.rid, self.kind, self.template = rid, kind, template
@@ -30,6 +34,7 @@ class Request:
         self.slot = self.submitted = self.latency = self.bins = self.k = self.handle = None
         self.cycle = 0
         self.histories = pop * cycles
+        self.status = "queued"
 
 
 class EigenPool:
@@ -61,7 +66,7 @@ class SolveServer:
     EigenPool (eigenvalue requests)."""
 
     def __init__(self, batch, catalogue, wave_histories=1 << 23, item_histories=256, eigen=None,
-                 eigen_cycles=(20, 40), eigen_share=2):
+                 eigen_cycles=(20, 40), eigen_share=2, eigen_queue_max=None, defer_backlog=None):
         self.B = batch
         self.catalogue = catalogue            # resident slots that requests instantiate
         self.waiting = collections.deque()    # fixed-source requests not yet admitted (arena full)
@@ -72,11 +77,21 @@ class SolveServer:
         self.eigen_running = []
         self.done = []
         self.eigen_share = eigen_share        # blocks per SM the waves leave free while eigen requests run
+        self.eigen_queue_max = eigen_queue_max  # eigen arrivals beyond this many waiting are shed (None: never)
+        self.defer_backlog = defer_backlog    # fixed-source histories queued above which eigen cycles wait
+        self.shed = 0
+        self.deferred_turns = 0
         self.B.serve_start(wave_histories, item_histories)
 
     # ---- requests
     def submit(self, req):
         if req.kind == "eigen":
+            if self.eigen_queue_max is not None and len(self.eigen_waiting) >= self.eigen_queue_max:
+                req.status = "shed"                    # rejected at arrival: the eigen queue is full
+                req.latency = 0.0
+                self.shed += 1
+                self.done.append(req)
+                return
             self.eigen_waiting.append(req)
         else:
             self.waiting.append(req)
@@ -91,6 +106,7 @@ class SolveServer:
             self.waiting.popleft()
             r.slot = slot
             r.submitted = self.B.clock()
+            r.status = "running"
             self.B.submit(slot)
             self.running[slot] = r
         while self.eigen_waiting and self.eigen is not None:
@@ -102,6 +118,7 @@ class SolveServer:
             t.eigen_init(r.pop, r.master)
             r.handle = h
             r.submitted = self.B.clock()
+            r.status = "running"
             self.eigen_running.append(r)
 
     def _eigen_step(self):
@@ -118,6 +135,7 @@ class SolveServer:
             if r.cycle >= sum(self.eigen_cycles):
                 r.latency = self.B.clock() - r.arrival
                 r.k = t.keff(aa)
+                r.status = "done"
                 self.eigen.give(r.handle)
                 r.handle = None
                 self.done.append(r)
@@ -131,10 +149,14 @@ class SolveServer:
             r = self.running.pop(slot)
             r.latency = lat + (r.submitted - r.arrival)
             r.bins = self.B.bins(slot)
+            r.status = "done"
             self.B.remove(slot)
             self.done.append(r)
         if self.eigen_running:
-            self._eigen_step()
+            if self.defer_backlog is not None and (self.waiting or self.B.serve_status()[0] > self.defer_backlog):
+                self.deferred_turns += 1               # fixed-source backlog: eigen cycles wait a turn
+            else:
+                self._eigen_step()
         self._admit()
         if self.eigen is not None and hasattr(self.B, "serve_share"):
             self.B.serve_share(self.eigen_share, bool(self.eigen_running))
@@ -144,16 +166,23 @@ class SolveServer:
     def outstanding(self):
         return len(self.waiting) + len(self.running) + len(self.eigen_waiting) + len(self.eigen_running)
 
+    def queue_state(self):
+        """(fixed-source requests waiting for memory, histories queued on the device, fixed-source
+        requests running, eigenvalue requests waiting, eigenvalue requests running)."""
+        return (len(self.waiting), int(self.B.serve_status()[0]), len(self.running), len(self.eigen_waiting),
+                len(self.eigen_running))
+
     def stop(self):
         self.B.serve_stop()
 
 
 def poisson_run(server, templates, rate, duration, seed=1, eigen_fraction=0.0, eigen_pop=100000,
-                drain=True, max_drain_s=120.0):
+                drain=True, max_drain_s=120.0, queue_log=None, log_every=0.5):
     """Drives `server` with a Poisson arrival stream of `rate` requests/s for `duration` seconds.
     templates: [(pop, cycles)] of the catalogue entries (fixed-source requests copy their entry's
     size); a fraction `eigen_fraction` of requests are eigenvalue requests.  Returns the completed
-    requests and the wall time."""
+    requests and the wall time.  With a list `queue_log`, (seconds since start, *server.queue_state())
+    is appended every `log_every` seconds."""
     rng = np.random.default_rng(seed)
     clock = server.B.clock
     t0 = clock()
@@ -161,8 +190,12 @@ def poisson_run(server, templates, rate, duration, seed=1, eigen_fraction=0.0, e
     rid = 0
     finished = []
     end = t0 + duration
+    next_log = t0
     while True:
         now = clock()
+        if queue_log is not None and now >= next_log:
+            queue_log.append((now - t0,) + server.queue_state())
+            next_log += log_every
         while next_at <= now and next_at < end:
             if eigen_fraction > 0 and rng.uniform() < eigen_fraction:
                 cyc = sum(server.eigen_cycles)
@@ -185,6 +218,8 @@ def poisson_run(server, templates, rate, duration, seed=1, eigen_fraction=0.0, e
 def latency_summary(reqs, wall, offered_histories):
     """Completed requests, latency percentiles over all of them and per request kind (fixed-source
     requests take milliseconds, eigenvalue requests seconds), and the achieved history rate."""
+    shed = [r for r in reqs if r.status == "shed"]
+    reqs = [r for r in reqs if r.status != "shed"]
     lat = np.array([r.latency for r in reqs]) if reqs else np.zeros(1)
     hist = float(sum(r.histories for r in reqs))
     by_kind = {}
@@ -201,4 +236,24 @@ def latency_summary(reqs, wall, offered_histories):
         "histories_per_s": hist / wall if wall > 0 else 0.0,
         "offered_histories_per_s": offered_histories,
         "wall_s": wall,
+        "shed": len(shed),
+        "shed_histories": float(sum(r.histories for r in shed)),
     }
+
+
+def queue_growth(log):
+    """Summary of a queue log of poisson_run: the largest and last value of each queue and the
+    growth rate (per second, least squares) of the fixed-source device backlog and of the waiting
+    requests over the second half of the run."""
+    if len(log) < 4:
+        return {}
+    a = np.array(log, dtype=np.float64)
+    names = ["fixed_waiting_for_memory", "device_backlog_histories", "fixed_running", "eigen_waiting", "eigen_running"]
+    out = {"samples": int(a.shape[0])}
+    half = a[a[:, 0] >= a[-1, 0] / 2]
+    for i, n in enumerate(names):
+        col = a[:, i + 1]
+        out[n] = {"max": float(col.max()), "last": float(col[-1])}
+        if half.shape[0] >= 2 and n in ("fixed_waiting_for_memory", "device_backlog_histories", "eigen_waiting"):
+            out[n]["growth_per_s_second_half"] = float(np.polyfit(half[:, 0], half[:, i + 1], 1)[0])
+    return out

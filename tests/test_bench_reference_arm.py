@@ -1,5 +1,6 @@
-"""bench.py's reference arm (the oracle's gen loop on the host cores) prints one JSON line with the
-fields the bench contract asks of it; a small population keeps it to seconds.  No GPU is used."""
+"""bench.py's reference arm (the oracle's OpenMP eigenvalue cycle on the host cores) prints one JSON
+line with the fields the bench contract asks of it, and names the same workload and step as the GPU
+arm's config; a small population keeps it to seconds.  No GPU is used."""
 import json
 import os
 import subprocess
@@ -20,3 +21,8 @@ def test_reference_arm_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["config"]["workload"] == "lattice_17x17_7g_eigen"
+    # the GPU arm prints the same config dict for the same arguments
+    sys.path.insert(0, ROOT)
+    import bench
+    ns = type("A", (), {"pop": 20000, "transport": "dt"})()
+    assert d["config"] == bench.workload_config(ns, 1)

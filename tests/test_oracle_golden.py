@@ -720,3 +720,30 @@ def test_multimap_golden_vectors(oracle_mod):
     for r, want in (((0.1, 0.1, 0.1), 1), ((1.1, 5.1, 5.1), 12), ((1.1, 3.1, 2.1), 4),
                     ((-1.1, 5.1, 5.1), 0), ((1.1, 50.1, 5.1), 0), ((1.1, 5.1, -5.1), 0)):
         assert o.map_point(axes, r=r) == want, r
+
+
+def test_openmp_eigen_cycle_equals_serial(oracle_mod):
+    """The CPU baseline's eigenvalue cycle (OpenMP over histories, thread-private score memory, sites
+    ordered by brood) gives the serial oracle's banks, master RNG state and k (tally sums to
+    round-off: they are added in another order)."""
+    p = problems.lattice_17x17_7g()
+    res = []
+    for omp in (False, True):
+        o = oracle_mod.Oracle(p, transport=abi.TRANSPORT_DT)
+        inact, act = o.upload_tally([]), o.upload_tally(p.tallies["mesh"])
+        ia = o.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+        aa = o.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        o.attach_tally(inact, ia)
+        o.attach_tally(act, aa)
+        o.eigen_init(5000, 0x5C3A84C9)
+        ks = []
+        for c in range(5):
+            adm, atch = (inact, ia) if c < 2 else (act, aa)
+            ks.append((o.eigen_cycle_omp(adm, atch, 4) if omp else o.eigen_cycle(adm, atch)).k_new)
+        b, pop = o.eigen_bank(5000)
+        res.append((np.array(ks), o.eigen_state()[0], b["r"][:pop].copy(), b["G"][:pop].copy(), o.bins(act)))
+    (k0, m0, r0, g0, b0), (k1, m1, r1, g1, b1) = res
+    np.testing.assert_allclose(k1, k0, rtol=1e-11)
+    assert m0 == m1
+    assert np.array_equal(r0, r1) and np.array_equal(g0, g1)
+    np.testing.assert_allclose(b1, b0, rtol=1e-10, atol=1e-300)
