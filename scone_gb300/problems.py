@@ -257,6 +257,57 @@ def scone_test_lat():
     return gb.arrays(), dict(water=water, mox43=mox43, uox=uox)
 
 
+def scone_test_lat_problem(seed=13, n_g=4):
+    """A transport problem on SCONE's test_lat geometry: the squareCylinder root with reflective x and
+    periodic y boundaries (BC 1 1 2 2 0 0, z unbounded), a 2x2 lattice of a cylindrical pin and a
+    square pin in a cellUniverse.  n_g groups of seeded synthetic data (water non-fissile, mox43 and
+    uox fissile, as the lattice workload's regions); an isotropic point source in group 1 at
+    (0.3, -0.2, 0); collision mesh flux (4x4 over the root) per group, track flux per material."""
+    g, mats = scone_test_lat()
+    rng = np.random.default_rng(seed)
+    regions = [_lattice_xs(rng, n_g, False), _lattice_xs(rng, n_g, True), _lattice_xs(rng, n_g, True)]
+    chi = np.zeros((3, n_g))
+    for m in (1, 2):
+        x = rng.uniform(0.1, 1.0, size=n_g) * np.exp(-np.arange(n_g))
+        chi[m] = x / x.sum()
+    mg = mg_data(n_g, np.array([r[0] for r in regions]), np.array([r[1] for r in regions]),
+                 capture=np.array([r[2] for r in regions]), fission=np.array([r[3] for r in regions]),
+                 nu=np.array([r[4] for r in regions]), chi=chi)
+    tallies = dict(flux=[abi.clerk(abi.CLERK_COLLISION, axes=[(abi.AXIS_X, 4, -1.26, 1.26), (abi.AXIS_Y, 4, -1.26, 1.26),
+                                                              (abi.AXIS_GROUP, n_g, 0.0, 0.0)]),
+                         abi.clerk(abi.CLERK_TRACK, axes=[(abi.AXIS_MATERIAL, 3, 0.0, 0.0)])])
+    return Problem(g, mg, name="scone_test_lat", source=dict(r=(0.3, -0.2, 0.0), G=1), tallies=tallies,
+                   meta=dict(mats=mats, seed=seed))
+
+
+def plane_cells(seed=47):
+    """General planes (plane_class.f90) and the box's periodic boundary: a box (half-width 4 cm) with
+    periodic x, reflective y and vacuum z faces holds a cellUniverse of four cells cut by two tilted
+    planes (normals (1, 2, 0.5) and (-0.3, 1, 1.5), offsets 0.7 and -0.4) and a sphere (r 1.5 cm at
+    (1, 0, 0)), two materials alternating; 2 groups (synthetic XS as in the infinite-medium workload),
+    a point source at the origin, collision flux per material and group and a track-length x mesh
+    over [-4.5, 4.5] (its bin edges stay off the periodic faces, where a track that starts right after
+    a periodic translation would be binned by the last bit of its position)."""
+    rng = np.random.default_rng(seed)
+    gb = GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 4.0, 4.0, 4.0)
+    p1 = gb.surface(abi.PLANE, 1.0, 2.0, 0.5, 0.7)
+    p2 = gb.surface(abi.PLANE, -0.3, 1.0, 1.5, -0.4)
+    sph = gb.surface(abi.SPHERE, 1.0, 0.0, 0.0, 1.5)
+    cells = [gb.cell([-(sph + 1), -(p1 + 1)]), gb.cell([-(sph + 1), p1 + 1]),
+             gb.cell([sph + 1, -(p2 + 1)]), gb.cell([sph + 1, p2 + 1])]
+    uni = gb.cell_universe(cells, [1, 2, 2, 1])
+    gb.root_universe(box, uni_fill(uni), bc=[abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_REFLECTIVE,
+                                             abi.BC_REFLECTIVE, abi.BC_VACUUM, abi.BC_VACUUM])
+    mats = [_fixed_source_xs(rng, 2), _fixed_source_xs(rng, 2)]
+    mg = mg_data(2, np.array([m[0] for m in mats]), np.array([m[1] for m in mats]),
+                 capture=np.array([m[2] for m in mats]))
+    tallies = dict(flux=[abi.clerk(abi.CLERK_COLLISION, axes=[(abi.AXIS_MATERIAL, 2, 0.0, 0.0),
+                                                              (abi.AXIS_GROUP, 2, 0.0, 0.0)]),
+                         abi.clerk(abi.CLERK_TRACK, axes=[(abi.AXIS_X, 8, -4.5, 4.5)])])
+    return Problem(gb.arrays(), mg, name="plane_cells", source=dict(r=(0.0, 0.0, 0.0), G=1), tallies=tallies)
+
+
 # ----------------------------------------------------------------------------- CE data
 KT_293K = 2.53e-8          # kT at 293.6 K [MeV]
 

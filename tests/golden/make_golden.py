@@ -10,15 +10,21 @@ Contents
                table in IntegrationTestFiles/1001JEF311.ace, the H-1 data that
                NuclearData/ceNeutronData/aceDatabase/Tests/aceNeutronDatabase_iTest.f90 reads.
 
-Run from the repository root with the SCONE sources at $SCONE_REF (default /root/reference); the
-committed JSON is what the tests read, so the sources are only needed to regenerate it.
+Beside the JSON it writes tests/golden/scone_h1_1001_03c.ace: that 1001.03c table as it stands in
+the file (header, NXS/JXS and its XSS lines, 12 + ceil(NXS(1)/4) lines from the line testLib
+gives), so the tests read SCONE's own H-1 table without the SCONE tree.
+
+Run from the repository root with $SCONE_REF naming a SCONE source tree; the committed files are
+what the tests read, so the sources are only needed to regenerate them.  Without $SCONE_REF the
+fields taken from SCONE are carried over from the committed JSON.
 """
 import json
 import os
 import re
 
-REF = os.environ.get("SCONE_REF", "/root/reference")
+REF = os.environ.get("SCONE_REF", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "scone_golden.json")
+H1_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "scone_h1_1001_03c.ace")
 
 G = 2806196910506780709
 MASK = (1 << 63) - 1
@@ -84,6 +90,14 @@ def parse_ace_esz(path, first_line):
                 elastic=blk(3))
 
 
+def ace_table_lines(path, first_line):
+    """The lines of the ACE type-1 table that starts at 1-based line `first_line`: the header (2
+    lines), IZ/AW (4), NXS and JXS (6), then NXS(1) XSS values four to a line."""
+    lines = open(path).read().splitlines(keepends=True)[first_line - 1:]
+    nxs1 = int(" ".join(lines[6:12]).split()[0])
+    return lines[:12 + (nxs1 + 3) // 4]
+
+
 def main():
     seed = 0x5C3A84C9
     xs, st = lcg_draws(seed, 1000)
@@ -94,13 +108,16 @@ def main():
                 "skip": {k: str(v) for k, v in skips.items()}, "skip_negative": {k: str(v) for k, v in neg.items()}},
     }
     tbl = os.path.join(REF, "RandomNumbers", "RNG_class.f90")
-    if os.path.exists(tbl):
+    if REF and os.path.exists(tbl):
         gold["pow_of_gsq"] = [str(v) for v in parse_table(tbl)]
         gold["mgMat1"] = parse_mg(os.path.join(REF, "IntegrationTestFiles", "mgMat1"))
         gold["mgMat2"] = parse_mg(os.path.join(REF, "IntegrationTestFiles", "mgMat2"))
         lib = open(os.path.join(REF, "IntegrationTestFiles", "testLib")).read()
         line = int(re.search(r"1001\.03c;\s*(\d+);", lib).group(1))
         gold["h1_ace"] = parse_ace_esz(os.path.join(REF, "IntegrationTestFiles", "1001JEF311.ace"), line)
+        with open(H1_OUT, "w") as f:
+            f.writelines(ace_table_lines(os.path.join(REF, "IntegrationTestFiles", "1001JEF311.ace"), line))
+        print("wrote", H1_OUT)
     elif os.path.exists(OUT):
         old = json.load(open(OUT))
         for k in ("pow_of_gsq", "mgMat1", "mgMat2", "h1_ace"):

@@ -1,18 +1,18 @@
 """ACE type-1 tables (scone_gb300/ace.py): synthetic nuclides written and read back, several tables
-in one file, and, when SCONE_REF names a SCONE source tree, its H-1 table read as aceCard reads it
+in one file, and SCONE's own H-1 table (IntegrationTestFiles/1001JEF311.ace, the 1001.03c table cut
+out by tests/golden/make_golden.py into tests/golden/scone_h1_1001_03c.ace) read as aceCard reads it
 (NuclearData/DataDecks/ACE/aceCard_class.f90:1454-1530) and run through the oracle to the cross
 sections of aceNeutronDatabase_iTest.f90:183-197.  No GPU is used."""
 import json
 import os
-import re
 
 import numpy as np
 import pytest
 
 from scone_gb300 import abi, ace, problems
 
-REF = os.environ.get("SCONE_REF", "")
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scone_golden.json")))
+H1_TABLE = os.path.join(os.path.dirname(__file__), "golden", "scone_h1_1001_03c.ace")
 
 
 def test_synthetic_round_trip(tmp_path):
@@ -57,12 +57,9 @@ def test_rejects_malformed_tables(tmp_path):
         ace.write_table(str(tmp_path / "x.ace"), "1.00c", 1.0, 1e-8, [1.0, 0.5], [1, 1], [1, 1], [0, 0])
 
 
-@pytest.mark.skipif(not REF or not os.path.exists(os.path.join(REF, "IntegrationTestFiles", "1001JEF311.ace")),
-                    reason="SCONE_REF does not name a SCONE tree")
 def test_reads_scone_h1_table(oracle_mod):
-    lib = open(os.path.join(REF, "IntegrationTestFiles", "testLib")).read()
-    line = int(re.search(r"1001\.03c;\s*(\d+);", lib).group(1))
-    r = ace.nuclide(os.path.join(REF, "IntegrationTestFiles", "1001JEF311.ace"), line)
+    r = ace.nuclide(H1_TABLE)
+    assert r["zaid"] == "1001.03c"
     g = GOLD["h1_ace"]
     assert np.array_equal(r["e"], g["e"]) and np.array_equal(r["xs"][:, 0], g["total"])
     assert np.array_equal(r["xs"][:, 1], g["elastic"]) and np.array_equal(r["xs"][:, 3], g["absorption"])

@@ -144,3 +144,68 @@ def test_ce_mixed_matches_fp64_statistically(gpu_mod, slab_full):
     z = (c64 - cmx) * N / np.sqrt(2.0 * np.maximum((c64 + cmx) * N, 1.0))   # counts, 2x for re-crossings
     assert np.all(np.abs(z) < 5.0), z
     assert np.all(cmx[c64 == 0] == 0)
+
+
+def _history_parity(gpu_mod, oracle_mod, p, transport, n, tally, master=2468):
+    g = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_FP64, transport=transport, max_bank=max(n, 4096),
+                                     record_histories=True, form=abi.FORM_HISTORY)
+    o = oracle_mod.Oracle(p, transport=transport)
+    bank = o.generate_source(SEED, n)
+    out = []
+    for t in (g, o):
+        a = t.upload_tally(tally)
+        _, st = t.transport_bank(a, bank, master)
+        t.tally_cycle_end(a, float(n))
+        out.append((t.history_records(n), t.bins(a), st))
+    ((hg, rg), bg, sg), ((ho, ro), bo, so) = out
+    assert np.array_equal(hg, ho) and np.array_equal(rg, ro)
+    assert sg.n_events == so.n_events
+    np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=0)
+    g.close()
+    return bg
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_ace_tables_drive_the_ce_kernels(gpu_mod, oracle_mod, transport, tmp_path):
+    """The CE slab's ten nuclides written as ACE type-1 tables into one library file, read back as
+    aceNeutronDatabase reads them (aceNeutronNuclide%init, aceNeutronNuclide_class.f90:737) and
+    uploaded: GPU histories equal the oracle's on the same tables, per history, FP64."""
+    from scone_gb300 import ace
+    slab = problems.ce_slab_3layer(scale=0.05)
+    ce = slab.ce
+    path = str(tmp_path / "slab.ace")
+    nucs = []
+    for k in range(len(ce["A"])):
+        a, b = int(ce["nuc_ptr"][k]), int(ce["nuc_ptr"][k + 1])
+        e, xs = ce["e"][a:b], ce["xs"][a:b]
+        line = ace.write_table(path, f"{1001 + 1000 * k}.90c", float(ce["A"][k]), float(ce["kT"][k]), e, xs[:, 0],
+                               xs[:, 1], xs[:, 3], ext_mode="a")
+        r = ace.nuclide(path, line)
+        np.testing.assert_allclose(r["xs"], xs, rtol=1e-10, atol=0)
+        nucs.append(dict(e=r["e"], xs=r["xs"], A=r["A"], kT=r["kT"]))
+    mats = [[(int(ce["mat_nuc"][j]), float(ce["mat_dens"][j])) for j in range(ce["mat_ptr"][m], ce["mat_ptr"][m + 1])]
+            for m in range(len(ce["mat_ptr"]) - 1)]
+    p = problems.Problem(slab.geometry, None, ce=problems.ce_data(nucs, mats), source=slab.source,
+                         tallies=slab.tallies)
+    bins = _history_parity(gpu_mod, oracle_mod, p, transport, 4000, p.tallies["current"])
+    assert bins[:, 1].sum() > 0
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_scone_h1_table_on_the_device(gpu_mod, oracle_mod, transport):
+    """SCONE's own H-1 table (IntegrationTestFiles/1001JEF311.ace, 1001.03c, committed under
+    tests/golden) uploaded to the device: hydrogen in an all-reflective box, a 1 MeV source slowing
+    down to thermal energies through free-gas scattering (A < 1 always samples a moving target,
+    neutronCEstd_class.f90:340-384): per-history FP64 parity with the oracle and equal spectra."""
+    import os
+    from scone_gb300 import ace
+    r = ace.nuclide(os.path.join(os.path.dirname(__file__), "golden", "scone_h1_1001_03c.ace"))
+    assert r["zaid"] == "1001.03c" and r["A"] < 1.0
+    ce = problems.ce_data([dict(e=r["e"], xs=r["xs"], A=r["A"], kT=r["kT"])], [[(0, 0.0669)]])
+    gb = problems.GeometryBuilder()
+    box = gb.surface(abi.BOX, 0.0, 0.0, 0.0, 50.0, 50.0, 50.0)
+    gb.root_universe(box, 1, bc=[abi.BC_REFLECTIVE] * 6)
+    ax = [(abi.AXIS_ENERGY, 60, 1.0e-11, 2.0)]
+    p = problems.Problem(gb.arrays(), None, ce=ce, source=dict(r=(0.0, 0.0, 0.0), E=1.0))
+    bins = _history_parity(gpu_mod, oracle_mod, p, transport, 1500, [abi.clerk(abi.CLERK_COLLISION, axes=ax)])
+    assert (bins[:, 1] > 0).sum() > 30                         # the spectrum spans the slowing-down range

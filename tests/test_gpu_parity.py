@@ -476,3 +476,198 @@ def test_splitting_needs_history_form(gpu_mod):
     with pytest.raises(gpu_mod.SconeGpuError, match="history-loop"):
         t.fixed_source_cycle(a, 1000, 1)
     t.close()
+
+
+def _fixed_bank_parity(gpu_mod, oracle_mod, p, transport, form, n, master, k_eff=1.0, tally="flux"):
+    """One gen loop over the same source bank on the device and in the oracle, FP64: per-history
+    collision counts and end RNG states identical, fission banks identical (when fissile), tallies
+    equal to round-off.  Returns the device bins."""
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=form, max_bank=max(1 << 18, 4 * n))
+    bank = o.generate_source(SEED, n)
+    ag, ao = g.upload_tally(p.tallies[tally]), o.upload_tally(p.tallies[tally])
+    ng, sg = g.transport_bank(ag, bank, master, k_eff=k_eff)
+    no, so = o.transport_bank(ao, bank, master, k_eff=k_eff)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(rg, ro)
+    assert sg.n_events == so.n_events and sg.n_collisions == so.n_collisions
+    assert sg.n_next == so.n_next
+    m = so.n_next
+    for k in ("G", "wgt", "brood_id"):
+        assert np.array_equal(ng[k][:m], no[k][:m]), k
+    np.testing.assert_allclose(ng["r"][:m], no["r"][:m], rtol=0, atol=1e-9)
+    g.tally_cycle_end(ag, float(n))
+    o.tally_cycle_end(ao, float(n))
+    bg, bo = g.bins(ag), o.bins(ao)
+    np.testing.assert_allclose(bg, bo, rtol=1e-10, atol=1e-300)
+    g.close()
+    return bg, so
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", ALL_TRANSPORTS)
+def test_scone_test_lat_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
+    """SCONE's own test_lat geometry (IntegrationTestFiles/Geometry/test_lat, geometryStd_iTest.f90):
+    squareCylinder root with reflective x and periodic y boundaries, a pin and a square pin in a 2x2
+    lattice; fissile regions give fission sites.  Per-history and bank parity with the oracle."""
+    p = problems.scone_test_lat_problem()
+    bins, st = _fixed_bank_parity(gpu_mod, oracle_mod, p, transport, form, 20000, 97531, k_eff=1.1)
+    assert st.n_next > 0
+    assert (bins[:, 1] > 0).sum() >= 60                          # every mesh cell of every group is reached
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("transport", ALL_TRANSPORTS)
+def test_plane_cells_periodic_box_fp64_history_parity(gpu_mod, oracle_mod, transport, form):
+    """General planes (plane_class.f90:144-186) cutting a cellUniverse, inside a box with periodic x
+    faces (box_class.f90 explicitBC / transformBC periodic branches): per-history parity."""
+    p = problems.plane_cells()
+    bins, _ = _fixed_bank_parity(gpu_mod, oracle_mod, p, transport, form, 20000, 86420)
+    assert bins[:4, 1].min() > 0                                   # both materials, both groups
+
+
+@pytest.mark.parametrize("problem", ["scone_test_lat", "plane_cells"])
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_scone_geometries_mixed_statistics(gpu_mod, problem, transport):
+    """The mixed form on squareCylinder/periodic and general-plane geometries agrees with the FP64
+    form within statistics: per-bin z-scores of 10 cycles of 20 000 histories (the gen loop over the
+    same point-source bank, fission sites discarded)."""
+    p = problems.scone_test_lat_problem() if problem == "scone_test_lat" else problems.plane_cells()
+    out = {}
+    n, cycles = 20000, 10
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED):
+        t = gpu_mod.TransportOperatorGPU(p, precision=prec, transport=transport, max_bank=1 << 18,
+                                         form=abi.FORM_HISTORY)
+        a = t.upload_tally(p.tallies["flux"])
+        bank = t.generate_source(SEED, n)
+        for c in range(cycles):
+            t.transport_bank(a, bank, 2468 + 7919 * c, k_eff=1.1, next_cap=1 << 18)
+            t.tally_cycle_end(a, float(n), 1.1)
+        out[prec] = t.bins(a)
+        t.close()
+    b64, b32 = out[abi.PREC_FP64], out[abi.PREC_MIXED]
+    m64, m32 = b64[:, 1] / cycles, b32[:, 1] / cycles
+    v64 = np.maximum(b64[:, 2] / cycles - m64 ** 2, 0) / (cycles - 1)
+    v32 = np.maximum(b32[:, 2] / cycles - m32 ** 2, 0) / (cycles - 1)
+    ok = (v64 + v32) > 0
+    z = (m64[ok] - m32[ok]) / np.sqrt(v64[ok] + v32[ok])
+    assert ok.sum() >= 4                                      # DT scores no track-length bins
+    assert np.abs(z).max() < 5.0 and abs(z.mean()) < 0.5, (z.mean(), np.abs(z).max())
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_lattice_fp64_parity_large_population(gpu_mod, oracle_mod, transport):
+    """FP64 per-history parity on 1e5 lattice histories (a converged-shape fission bank, the mesh
+    tally and k-implicit clerks): every history's collision count and end RNG state, the fission
+    bank and the bins."""
+    p = problems.lattice_17x17_7g()
+    n = 100000
+    g, o = make_pair(gpu_mod, oracle_mod, p, transport, form=abi.FORM_HISTORY, max_bank=1 << 19)
+    o.eigen_init(n, SEED)
+    bank, pop = o.eigen_bank(n)
+    assert pop == n
+    clerks = p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)]
+    ag, ao = g.upload_tally(clerks), o.upload_tally(clerks)
+    ng, sg = g.transport_bank(ag, bank, 5551212, k_eff=1.07, next_cap=1 << 19)
+    no, so = o.transport_bank(ao, bank, 5551212, k_eff=1.07, next_cap=1 << 19)
+    cg, rg = g.history_records(n)
+    co, ro = o.history_records(n)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(rg, ro)
+    assert sg.n_events == so.n_events and sg.n_next == so.n_next > 0
+    m = so.n_next
+    for k in ("G", "wgt", "brood_id"):
+        assert np.array_equal(ng[k][:m], no[k][:m]), k
+    np.testing.assert_allclose(ng["r"][:m], no["r"][:m], rtol=0, atol=1e-9)
+    g.tally_cycle_end(ag, float(m), 1.07)
+    o.tally_cycle_end(ao, float(m), 1.07)
+    np.testing.assert_allclose(g.bins(ag), o.bins(ao), rtol=1e-10, atol=1e-300)
+    g.close()
+
+
+def _pinned_bank(src, n, cap=None):
+    """A HostBank whose arrays live in page-locked host memory (torch pin_memory), filled from src."""
+    import torch
+    cap = cap or n
+    arrs = {}
+    for k, shape, dt in (("wgt", (cap,), torch.float64), ("r", (cap, 3), torch.float64),
+                         ("dir", (cap, 3), torch.float64), ("G", (cap,), torch.int32),
+                         ("time", (cap,), torch.float64), ("brood_id", (cap,), torch.int32)):
+        t = torch.zeros(shape, dtype=dt).pin_memory()
+        if src is not None:
+            t[:n].copy_(torch.from_numpy(np.ascontiguousarray(src[k][:n])))
+        arrs[k] = t
+    hb = abi.HostBank(cap, {k: v.numpy() for k, v in arrs.items()})
+    hb._pinned = arrs                                      # keeps the page-locked memory alive
+    return hb
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_eigen_cycle_bank_equals_resident_cycles(gpu_mod, pinned):
+    """sg_eigen_cycle_bank (host dungeons: bank in, normalised bank out, pRNG and k passed through)
+    gives the device-resident sg_eigen_cycle's k, pRNG and banks, FP64, cycle after cycle; with
+    page-locked banks the kernels read the input in place."""
+    p = problems.lattice_17x17_7g()
+    pop = 5000
+    res = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_FP64, max_bank=1 << 16, form=abi.FORM_HISTORY)
+    host = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_FP64, max_bank=1 << 16, form=abi.FORM_HISTORY)
+    adm = {}
+    for t in (res, host):
+        inact, act = t.upload_tally([]), t.upload_tally(p.tallies["mesh"])
+        ia = t.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+        aa = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        t.attach_tally(inact, ia)
+        t.attach_tally(act, aa)
+        adm[id(t)] = (inact, ia, act, aa)
+    res.eigen_init(pop, SEED)
+    b0, _ = res.eigen_bank(pop)
+    master, k = res.eigen_state()
+    k_end = 1.0
+    mk = (lambda src, n, cap=None: _pinned_bank(src, n, cap)) if pinned else \
+        (lambda src, n, cap=None: abi.HostBank(cap or n) if src is None else abi.HostBank(n, src.head(n)))
+    bank = mk(b0, pop)
+    out = mk(None, pop, pop)
+    for c in range(6):
+        inact, ia, act, aa = adm[id(res)]
+        st_r = res.eigen_cycle(inact if c < 3 else act, ia if c < 3 else aa)
+        inact, ia, act, aa = adm[id(host)]
+        master, k_new, st_h = host.eigen_cycle_bank(inact if c < 3 else act, ia if c < 3 else aa, bank, pop,
+                                                    master, k, k_end, out)
+        k_end = k = k_new
+        # k sums scores added atomically in another order: equal to round-off
+        assert abs(st_h.k_new - st_r.k_new) <= 1e-12 * st_r.k_new and st_h.n_next == st_r.n_next, c
+        assert st_h.n_events == st_r.n_events
+        mr, kr = res.eigen_state()
+        assert master == mr and abs(k - kr) <= 1e-12 * kr
+        br, _ = res.eigen_bank(pop)
+        for key in ("G", "brood_id", "wgt", "r", "dir"):
+            assert np.array_equal(out[key][:pop], br[key][:pop]), (c, key)
+        bank, out = out, bank
+    np.testing.assert_allclose(host.bins(adm[id(host)][2]), res.bins(adm[id(res)][2]), rtol=1e-12, atol=1e-300)
+    res.close()
+    host.close()
+
+
+def test_transport_bank_reads_page_locked_banks_in_place(gpu_mod, oracle_mod):
+    """sg_transport_bank on a page-locked host bank (read in place by the kernels) and on the same
+    bank in pageable memory (copied first): identical fission banks and bins."""
+    p = problems.lattice_17x17_7g()
+    n = 20000
+    o = oracle_mod.Oracle(p)
+    o.eigen_init(n, SEED)
+    bank, _ = o.eigen_bank(n)
+    out = []
+    for pinned in (False, True):
+        g = gpu_mod.TransportOperatorGPU(p, precision=abi.PREC_MIXED, transport=abi.TRANSPORT_DT, max_bank=1 << 17,
+                                         form=abi.FORM_HISTORY)
+        a = g.upload_tally(p.tallies["mesh"] + [abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+        b = _pinned_bank(bank, n) if pinned else abi.HostBank(n, bank.head(n))
+        nxt, st = g.transport_bank(a, b, 31337, k_eff=1.02, next_cap=1 << 17)
+        g.tally_cycle_end(a, float(st.n_next), 1.02)
+        out.append((nxt.head(st.n_next), g.bins(a)))
+        g.close()
+    (b0, t0), (b1, t1) = out
+    for k in ("G", "brood_id", "wgt", "r", "dir", "time"):
+        assert np.array_equal(b0[k], b1[k]), k
+    np.testing.assert_allclose(t1, t0, rtol=1e-10, atol=1e-300)
