@@ -369,13 +369,29 @@ def configs_section(a, local):
             adm = t.upload_tally(p.tallies[tally])
             t.fixed_source_cycle(warm_adm, min(pop, 10000), SEED)          # warm-up (own tally)
             m = SEED
-            ms = ev = 0.0
+            ms = ev = kms = 0.0
             for _ in range(cycles):
                 m, st = t.fixed_source_cycle(adm, pop, m)
                 ms += st.cycle_ms
+                kms += st.transport_ms
                 ev += st.n_events
             res[prec_name] = {"value": pop * cycles / (ms / 1e3), "unit": "histories/s",
-                              "events_per_s": ev / (ms / 1e3), "ms": ms}
+                              "events_per_s": ev / (ms / 1e3), "ms": ms, "transport_kernel_ms": kms}
+            if name.startswith("ce") and prec == abi.PREC_MIXED:
+                # CE bytes per event: state 176 B + FP64 energy 16 B + per nuclide (hash bin, two grid
+                # energies, two totals) 28 B x 10 + the sampled nuclide's pair 16 B
+                peak, kind = measured_peaks()
+                bpe = 176 + 16 + 28 * 10 + 16
+                ach = ev * bpe / (kms / 1e3) / 1e9
+                bpe_dram = committed_traffic("k_transport_ce_slab")
+                res["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                                   "peak_source": kind, "kernel": "k_transport<float, 2, DT, CE> (history loop)",
+                                   "bytes_per_event": bpe, "events_per_launch": ev / cycles,
+                                   "launch_ms": kms / cycles,
+                                   "traffic": bpe_dram * ev / cycles if bpe_dram else None}
+                comp = committed_compute("k_transport_ce_slab")
+                if comp:
+                    res["roofline"]["compute"] = comp
             # tally deviation: dev_cycles batches (more than the timed cycles when those are fewer)
             if dev_cycles > cycles:
                 adm = t.upload_tally(p.tallies[tally])
@@ -753,8 +769,11 @@ def main():
             b_in, b_out = b_out, b_in
         torch.cuda.synchronize()
         w0 = time.perf_counter()
+        e_tr = e_cyc = 0.0
         for _ in range(a.steps):
             master, k, _st = t.eigen_cycle_bank(e_act, e_aa, b_in, pop, master, k, k_end, b_out)
+            e_tr += _st.transport_ms
+            e_cyc += _st.cycle_ms
             k_end = k
             b_in, b_out = b_out, b_in
         torch.cuda.synchronize()
@@ -764,7 +783,8 @@ def main():
                "d2h_bytes_per_step": pop * (24 + 24 + 8 + 4 + 8 + 4), "ms_per_step": 1e3 * we / a.steps,
                "call": "sg_eigen_cycle_bank (one whole cycle per call, host dungeons)",
                "h2d": "page-locked host bank read in place by the kernels across the host link (no staging copy)",
-               "d2h": "normalised next-cycle bank, cudaMemcpyAsync after the cycle"}
+               "d2h": "normalised next-cycle bank, cudaMemcpyAsync after the cycle",
+               "transport_kernel_ms_per_step": e_tr / a.steps, "call_device_ms_per_step": e_cyc / a.steps}
         # the gen loop alone through sg_transport_bank (a shim that keeps normSize_Repr in Fortran)
         nxt_cap = cap
         b_next = pinned_bank(None, 0, nxt_cap)
@@ -810,6 +830,29 @@ def main():
         alt = {"transport": "ST" if tr2 == abi.TRANSPORT_ST else "DT", "value": h2 / (c2 / 1e3),
                "unit": "histories/s", "events_per_s": e2 / (c2 / 1e3), "ms_per_step": c2 / a.steps, "k_eff": k2}
         t2.close()
+
+    # the lattice in the other execution form (the event-based plain form against the history loop),
+    # same K steps: the measurement behind keeping the history loop as the fast form
+    other_form = None
+    if not a.no_alt and world == 1:
+        f2 = abi.FORM_HISTORY if form == abi.FORM_EVENT else abi.FORM_EVENT
+        t3 = gpu.TransportOperatorGPU(p, precision=prec, transport=tr, max_bank=cap, device=local, form=f2)
+        i3, ia3, a3, aa3 = lattice_setup(t3, p)
+        t3.eigen_init(a.pop, master0)
+        for _ in range(warm):
+            t3.eigen_cycle(i3, ia3)
+        c3 = tk3 = h3 = 0.0
+        n3 = 0
+        for _ in range(a.steps):
+            st = t3.eigen_cycle(a3, aa3)
+            c3 += st.cycle_ms
+            tk3 += st.transport_ms
+            h3 += st.n_histories
+            n3 += st.n_kernels
+        other_form = {"form": "event" if f2 == abi.FORM_EVENT else "history", "value": h3 / (c3 / 1e3),
+                      "unit": "histories/s", "ms_per_step": c3 / a.steps, "transport_ms_per_step": tk3 / a.steps,
+                      "kernels_per_step": n3 / a.steps}
+        t3.close()
 
     # max over ranks of the device time; histories summed over ranks
     sec = cyc_ms / 1e3
@@ -888,7 +931,7 @@ def main():
         "events_per_s": events / sec, "k_eff": ks[-1], "wall_ms_per_step": 1e3 * wall / a.steps,
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "e2e_gen_loop_only": e2e_gen, "clocks": clocks,
-        "other_transport": alt, "batched": batched, "other_configs": configs,
+        "other_transport": alt, "other_form": other_form, "batched": batched, "other_configs": configs,
     }
     print(json.dumps(line), flush=True)
     if pg:

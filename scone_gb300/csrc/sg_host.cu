@@ -148,8 +148,8 @@ struct sg_handle_t {
   bool hasMG = false;
   bool anyFissile = false;
   int nMat = 0, nG = 0;
-  DArr<double> mgD[10];
-  DArr<float> mgF[10];
+  DArr<double> mgD[11];
+  DArr<float> mgF[11];
   DArr<int> fissile;
   DMG<double> mg64{};
   DMG<float> mgMx{};
@@ -706,10 +706,22 @@ int build_mg(sg_handle h, const sg_mg_desc* d) {
   }
   CK(h->fissile.upload(fis, st));
   double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
+  // 1 / max(majorant, collisionXS) per group, the delta-tracking flight's inverse majorant: the same
+  // IEEE division the kernel would make, in each precision
+  std::vector<double> majInv(nG);
+  std::vector<float> majInvF(nG);
+  for (int g = 0; g < nG; ++g) {
+    majInv[g] = 1.0 / std::max(maj[g], cxs);
+    majInvF[g] = 1.0f / std::max((float)maj[g], (float)cxs);
+  }
+  CK(h->mgD[10].upload(majInv, st));
+  CK(h->mgF[10].upload(majInvF, st));
   h->mg64 = DMG<double>{M, nG, h->mgD[0].p, h->mgD[1].p, h->mgD[2].p, h->mgD[3].p, h->mgD[4].p, h->mgD[5].p,
-                        h->mgD[6].p, h->mgD[7].p, h->fissile.p, h->mgD[8].p, cxs, d->p1 ? h->mgD[9].p : nullptr};
+                        h->mgD[6].p, h->mgD[7].p, h->fissile.p, h->mgD[8].p, cxs, d->p1 ? h->mgD[9].p : nullptr,
+                        h->mgD[10].p};
   h->mgMx = DMG<float>{M, nG, h->mgF[0].p, h->mgF[1].p, h->mgF[2].p, h->mgF[3].p, h->mgF[4].p, h->mgF[5].p,
-                       h->mgF[6].p, h->mgF[7].p, h->fissile.p, h->mgF[8].p, (float)cxs, d->p1 ? h->mgF[9].p : nullptr};
+                       h->mgF[6].p, h->mgF[7].p, h->fissile.p, h->mgF[8].p, (float)cxs, d->p1 ? h->mgF[9].p : nullptr,
+                       h->mgF[10].p};
   h->hasMG = true;
   return SG_OK;
 }

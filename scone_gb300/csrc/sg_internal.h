@@ -85,6 +85,7 @@ struct DMG {
   const R* majorant;
   R collisionXS;
   const R* P1n;         // [mat][Gin][Gout] 3 P1/P0 (multiScatterP1MG), null for P0 scattering
+  const R* majInv;      // [G] 1 / max(majorant, collisionXS)
 };
 
 // Continuous-energy neutron data (aceNeutronNuclide mainData / eGrid, ceNeutronMaterial composition,

@@ -247,9 +247,12 @@ struct Tracker {
 
   // tallyAdmin%reportInColl -> collisionClerk (collisionClerk_class.f90:192-242) and
   // keffImplicitClerk (keffImplicitClerk_class.f90:180-227)
-  __device__ __forceinline__ void report_in_coll(bool virt, R trackXS) {
+  // invTrack = 1 / trackXS: the mixed form multiplies by it; the FP64 form divides, as SCONE does
+  __device__ __forceinline__ void report_in_coll(bool virt, R trackXS, R invTrack) {
     const int cell = A.has_cellmap ? lowest_cell() : 0;
-    const R fluxTrack = w / trackXS;                   // collision estimator with handleVirtual
+    R fluxTrack;                                       // collision estimator with handleVirtual
+    if constexpr (sizeof(R) == 4) fluxTrack = w * invTrack;
+    else fluxTrack = w / trackXS;
     for (int k = 0; k < A.n_clerks; ++k) {
       const DClerk& K = A.clerks[k];
       if (K.type == SG_CLERK_COLLISION) {
@@ -368,7 +371,7 @@ struct Tracker {
     if (x > R(0)) C = C + 1;
     x = x - mcap;
     if (x > R(0)) C = C + 1;
-    report_in_coll(false, trackXS);
+    report_in_coll(false, trackXS, R(1) / trackXS);
     if (A.coll_imp && A.coll->imp_abs) {                 // neutronCEimp implicit (:406-424)
       const R scat = mel + min_;
       w = w * scat / mt;
@@ -548,7 +551,7 @@ struct Tracker {
     if (x > R(0)) C = C + 1;
     x = x - capture;
     if (x > R(0)) C = C + 1;
-    report_in_coll(false, trackXS);
+    report_in_coll(false, trackXS, R(1) / trackXS);
     const R preCollW = w;
     if (fiss) {                                          // implicit (:134-201)
       R rand1 = rng.get();
@@ -657,10 +660,9 @@ struct Tracker {
   // in void).  No random number is drawn.
   __device__ __forceinline__ void select_ht() {
     if constexpr (OP == OP_HT) {
-      R maj, sigT;
-      if constexpr (CE) maj = fmax(ce_major(), ce.collisionXS);
-      else maj = fmax(mg.majorant[G - 1], mg.collisionXS);
-      const R majInv = R(1) / maj;
+      R sigT, majInv;
+      if constexpr (CE) majInv = R(1) / fmax(ce_major(), ce.collisionXS);
+      else majInv = mg.majInv[G - 1];
       if (c.mat == SG_VOID_MAT) sigT = R(0);
       else if constexpr (CE) sigT = ce_total(c.mat);
       else sigT = xs(mg.total, c.mat, G);
@@ -707,7 +709,7 @@ struct Tracker {
           trackXS = sigmaTrack;
           return SEG_COLLIDE;
         }
-        report_in_coll(true, sigmaTrack);
+        report_in_coll(true, sigmaTrack, invSig);
       }
       return SEG_MORE;
     }
@@ -717,10 +719,9 @@ struct Tracker {
     int mat = c.mat;
     {
       // deltaTracking (transportOperatorDT_class.f90:47-131)
-      R maj;
-      if constexpr (CE) maj = fmax(ce_major(), ce.collisionXS);
-      else maj = fmax(mg.majorant[G - 1], mg.collisionXS);
-      const R majInv = R(1) / maj;
+      R maj, majInv;
+      if constexpr (CE) { maj = fmax(ce_major(), ce.collisionXS); majInv = R(1) / maj; }
+      else { maj = fmax(mg.majorant[G - 1], mg.collisionXS); majInv = mg.majInv[G - 1]; }
       const R dist = -dlog<R>(rng.get()) * majInv;
       double rpre[3];
       R u0[3];
@@ -737,7 +738,7 @@ struct Tracker {
       mat = c.mat;
       if (A.has_current) report_current(rpre, matPre, cellPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
-      if (mat == SG_VOID_MAT) { report_in_coll(true, maj); return SEG_MORE; }
+      if (mat == SG_VOID_MAT) { report_in_coll(true, maj, majInv); return SEG_MORE; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
         return SEG_END;
@@ -746,7 +747,7 @@ struct Tracker {
       if constexpr (CE) sigT = ce_total(mat);
       else sigT = xs(mg.total, mat, G);
       if (rng.get() < sigT * majInv) { trackXS = maj; return SEG_COLLIDE; }
-      report_in_coll(true, maj);
+      report_in_coll(true, maj, majInv);
       return SEG_MORE;
     }
   }
@@ -1021,8 +1022,28 @@ __global__ void __launch_bounds__(128) k_ev_transit(const __grid_constant__ Tran
   flush_counters(T, A, lane);
 }
 
+// Block-level stream compaction of one round's flags: a ballot per warp, the warps' counts scanned in
+// shared memory, one atomic per block for the block's base in the queue; returns this thread's
+// position (meaningful where flag is set).  Every thread of the block calls it.
+__device__ __forceinline__ int block_append(bool flag, int* counter, int* s_cnt) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned m = __ballot_sync(FULL, flag);
+  if (lane == 0) s_cnt[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < nw; ++w) { const int c = s_cnt[w]; s_cnt[w] = tot; tot += c; }
+    s_cnt[nw] = tot ? atomicAdd(counter, tot) : 0;
+  }
+  __syncthreads();
+  const int pos = s_cnt[nw] + s_cnt[warp] + __popc(m & ((1u << lane) - 1u));
+  __syncthreads();                                      // the counts are rewritten next round
+  return pos;
+}
+
 template <class R, int MAXL, int OP, bool CE>
 __global__ void __launch_bounds__(128) k_ev_collide(const __grid_constant__ TransportArgs<R> A) {
+  __shared__ int s_cnt[4 + 1];
   Tracker<R, MAXL, OP, CE> T(A, A.acc);
   const int nIn = *A.q.n_in;
   const int stride = gridDim.x * blockDim.x;
@@ -1030,15 +1051,20 @@ __global__ void __launch_bounds__(128) k_ev_collide(const __grid_constant__ Tran
   const int rounds = (nIn + stride - 1) / stride;      // uniform trip count keeps warps convergent
   for (int r = 0; r < rounds; ++r) {
     const int idx = first + r * stride;
+    int slot = -1;
+    bool survivor = false;
     if (idx < nIn) {
-      const int slot = A.q.in[idx];
+      slot = A.q.in[idx];
       T.load(A.part, slot);
       if (T.collide(T.trackXS)) T.finish();
       else {
         T.store(A.part, slot);
-        A.q.out[warp_append(A.q.n_out)] = slot;
+        survivor = true;
       }
     }
+    // the survivors go back to the transit queue, compacted per block (contiguous writes)
+    const int pos = block_append(survivor, A.q.n_out, s_cnt);
+    if (survivor) A.q.out[pos] = slot;
   }
   flush_counters(T, A, threadIdx.x & 31);
 }
