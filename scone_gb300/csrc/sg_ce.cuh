@@ -13,18 +13,24 @@ namespace sg {
 // Floor index (0-based lower point) of E in e[0..n-1], or -1 when E lies outside [e[0], e[n-1]].
 // `b` is the hash bin of E; h[b] brackets it (e[lo] <= E < e[hi] for every E of the bin).  A
 // bracket that does not hold (E outside the hashed range) falls back to the whole grid.
+// Grid energies are positive, and for non-negative IEEE doubles the order of the values is the order
+// of their bit patterns read as signed 64-bit integers; so every comparison here is an integer one
+// (the integer pipe instead of the FP64 pipe, which this GPU issues at a small fraction of its
+// FP32 rate) with the same outcome.  A negative or NaN E compares outside the grid, as before.
 __device__ __forceinline__ int ce_search(const double* __restrict__ e, int n, const int2* __restrict__ h, int b,
                                          double E) {
-  if (!(E >= e[0] && E <= e[n - 1])) return -1;
-  if (E == e[n - 1]) return n - 2;
+  const long long* __restrict__ k = reinterpret_cast<const long long*>(e);
+  const long long x = __double_as_longlong(E);
+  if (!(x >= k[0] && x <= k[n - 1])) return -1;
+  if (x == k[n - 1]) return n - 2;
   int lo = 0, hi = n - 1;
   if (h) {
     const int2 br = h[b];
-    if (e[br.x] <= E && E < e[br.y]) { lo = br.x; hi = br.y; }
+    if (k[br.x] <= x && x < k[br.y]) { lo = br.x; hi = br.y; }
   }
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (e[mid] <= E) lo = mid;
+    if (k[mid] <= x) lo = mid;
     else hi = mid;
   }
   return lo;

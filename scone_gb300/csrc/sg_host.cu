@@ -975,7 +975,8 @@ long long fill_axes(DClerk& K, const sg_axis_desc* axes, int n, const Admin& A, 
       K.ax_step[i] = std::log(x.max / x.min) / x.n;
     else K.ax_step[i] = (x.max - x.min) / x.n;
     K.ax_inv_step[i] = 1.0 / K.ax_step[i];
-    K.ax_minf[i] = (float)K.ax_min[i];
+    // the FP32 copy of a log grid holds log(min): the mixed form bins log(E) - log(min) directly
+    K.ax_minf[i] = grid == SG_GRID_LOG ? (float)std::log(x.min) : (float)K.ax_min[i];
     K.ax_inv_stepf[i] = (float)K.ax_inv_step[i];
     K.ax_tab[i] = (sizeof(R) == 8 ? A.tab64 : A.tab32)[tab + i];
     K.multi[i] = mul;
@@ -1245,12 +1246,13 @@ int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long maste
     h->launches += (heap > 0 ? 5 : 4);
     (void)n_hist;
   } else {
-    CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(out.dir, in.dir, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(out.wgt, in.wgt, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(out.time, in.time, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(out.G, in.G, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(out.brood, in.brood, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
+    // (the destination may be a caller's page-locked host bank: the copy kind follows the pointers)
+    CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.dir, in.dir, 3 * sizeof(double) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.wgt, in.wgt, sizeof(double) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.time, in.time, sizeof(double) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.G, in.G, sizeof(int) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.brood, in.brood, sizeof(int) * S, cudaMemcpyDefault, s));
   }
   return SG_OK;
 }
@@ -1311,6 +1313,21 @@ bool mapped_host_bank(sg_handle h, const sg_bank* b, DBank* d) {
   if (h->hasCE) { if (!dev(b->E, &E)) return false; G = nullptr; }
   else if (!dev(b->G, &G)) return false;
   *d = DBank{(double*)r, (double*)dir, (double*)wgt, (int*)G, nullptr, (double*)time, (double*)E};
+  return true;
+}
+
+// The same for a bank the device writes (the normalised next-cycle bank of sg_eigen_cycle_bank):
+// every array written (r, dir, wgt, G, time, brood_id) must be such memory; the kernels that build
+// the bank then write it in place across the host link, with no device copy and no copy back.
+bool mapped_host_out(sg_handle h, const sg_bank* b, DBank* d) {
+  if (h->hasCE) return false;
+  DBank m;
+  if (!mapped_host_bank(h, b, &m) || !b->brood_id) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, b->brood_id) != cudaSuccess) { cudaGetLastError(); return false; }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+  m.brood = (int*)a.devicePointer;
+  *d = m;
   return true;
 }
 
@@ -1907,11 +1924,16 @@ int32_t sg_eigen_cycle_bank(sg_handle h, int32_t admin, int32_t atch, const sg_b
   h->master = *master_state;
   h->k = *k_eff;
   h->cur = 0;
-  int rc = eigen_cycle_core(h, admin, atch, in_d, h->bank[1].view(), res, nullptr);
+  // nextCycle: written in place into the caller's page-locked bank when the device can address it
+  DBank out_d;
+  const bool outMapped = mapped_host_out(h, out, &out_d);
+  int rc = eigen_cycle_core(h, admin, atch, in_d, h->bank[1].view(), outMapped ? out_d : res, nullptr);
   h->eigenReady = false;   // the device banks hold no resident run for sg_eigen_cycle
   if (rc) return rc;
-  rc = d2h_bank(h, res, pop, out);
-  if (rc) return rc;
+  if (!outMapped) {
+    rc = d2h_bank(h, res, pop, out);
+    if (rc) return rc;
+  }
   CK(cudaEventRecord(h->ev[3], s));
   CK(cudaStreamSynchronize(s));
   *master_state = h->master;

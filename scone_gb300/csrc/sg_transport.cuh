@@ -224,7 +224,7 @@ struct Tracker {
         } else if (grid == SG_GRID_LOG) {
           if (!(v > 0.0)) return 0;
           if constexpr (sizeof(R) == 8) b = (int)floor(log(v / K.ax_min[a]) / K.ax_step[a]) + 1;
-          else b = (int)floorf(__logf((float)(v / K.ax_min[a])) * K.ax_inv_stepf[a]) + 1;
+          else b = (int)floorf((__logf((float)v) - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;   // ax_minf: log(min)
         } else {
           if constexpr (sizeof(R) == 8) b = (int)floor((v - K.ax_min[a]) / K.ax_step[a]) + 1;
           else b = (int)floorf(((float)v - K.ax_minf[a]) * K.ax_inv_stepf[a]) + 1;
@@ -322,8 +322,10 @@ struct Tracker {
     ep = ce_point<R>(ce, En);
     ceTotMat = -1;
     ceMajOK = false;
-    // particle_class.f90:481-503: speed = sqrt(2E/m) c
-    invSpeed = (R)(1.0 / (sqrt(2.0 * En / 939.56542194) * 2.99792458e10));
+    // particle_class.f90:481-503: speed = sqrt(2E/m) c; the mixed form keeps time in FP32 and takes
+    // 1/speed from an FP32 reciprocal square root
+    if constexpr (sizeof(R) == 8) invSpeed = 1.0 / (sqrt(2.0 * En / 939.56542194) * 2.99792458e10);
+    else invSpeed = rsqrtf((float)(En * (2.0 / 939.56542194))) * (1.0f / 2.99792458e10f);
   }
   __device__ __forceinline__ R ce_total(int mat) {
     if (mat != ceTotMat) {
@@ -386,15 +388,25 @@ struct Tracker {
         R mu = R(2) * rng.get() - R(1);
         R sp, cp;
         sincos_phi<R>(rng.get(), sp, cp);
-        const double Ad = (double)Anuc, mud = (double)mu;
-        const double inv_Ap1 = 1.0 / (Ad + 1.0);
-        Eout = (1.0 + Ad * Ad + 2 * Ad * mud) * E * inv_Ap1 * inv_Ap1;
-        R muL = (R)((Ad * mud + 1) * sqrt(E / Eout) * inv_Ap1);
+        R muL;
+        if constexpr (sizeof(R) == 8) {
+          const double Ad = (double)Anuc, mud = (double)mu;
+          const double inv_Ap1 = 1.0 / (Ad + 1.0);
+          Eout = (1.0 + Ad * Ad + 2 * Ad * mud) * E * inv_Ap1 * inv_Ap1;
+          muL = (R)((Ad * mud + 1) * sqrt(E / Eout) * inv_Ap1);
+        } else {                                         // the same kinematics with an FP32 ratio
+          const float inv_Ap1 = 1.0f / (Anuc + 1.0f);
+          const float ratio = (1.0f + Anuc * Anuc + 2.0f * Anuc * mu) * inv_Ap1 * inv_Ap1;   // Eout / E
+          Eout = E * (double)ratio;
+          muL = (Anuc * mu + 1.0f) * rsqrtf(ratio) * inv_Ap1;
+        }
         if (muL > R(1)) muL = R(1);
         rotate_vector<R>(c.u[0], c.u[1], c.u[2], muL, sp, cp);
       } else {                                           // scatterFromMoving (:495-585)
         const R d0 = c.u[0], d1 = c.u[1], d2 = c.u[2];
-        const R sE = (R)sqrt(E);
+        R sE;
+        if constexpr (sizeof(R) == 8) sE = sqrt(E);
+        else sE = sqrtf((float)E);
         R Vn[3] = {d0 * sE, d1 * sE, d2 * sE};
         R Vt[3], Vcm[3];
         bool bad = false;
