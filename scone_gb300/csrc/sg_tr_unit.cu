@@ -12,12 +12,16 @@
 #if !defined(SG_R) || !defined(SG_CE) || !defined(SG_OP) || !defined(SG_PART)
 #error "sg_tr_unit.cu needs SG_R, SG_CE, SG_OP and SG_PART"
 #endif
+// nesting bound of parts 2 and 3 (deeper geometries than 2 levels)
+#ifndef SG_MAXL_HI
+#define SG_MAXL_HI 4
+#endif
 
 namespace sg {
 template <>
 cudaError_t launch_part<SG_R, (SG_CE != 0), SG_OP, SG_PART>(int kind, const TransportArgs<SG_R>& a, size_t smem,
                                                            cudaStream_t s, int* grid_out) {
-  return launch_one<SG_R, (SG_PART < 2 ? 2 : 4), SG_OP, (SG_CE != 0), ((SG_PART & 1) != 0)>(kind, a, smem, s,
+  return launch_one<SG_R, (SG_PART < 2 ? 2 : SG_MAXL_HI), SG_OP, (SG_CE != 0), ((SG_PART & 1) != 0)>(kind, a, smem, s,
                                                                                         grid_out);
 }
 }  // namespace sg
