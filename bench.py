@@ -882,9 +882,11 @@ def main():
             "traffic": traffic, "peak_source": peak_kind, "kernel": ("event loop: k_ev_start + k_ev_transit + k_ev_collide + k_ev_transit<tail>"
                        if a.form == "event" else "k_transport (history loop)"),
             "bytes_per_event": bpe, "events_per_launch": ev_per_launch, "launch_ms": launch_ms,
-            "launch_ms_spans": "the history-loop kernel alone: CUDA events recorded on the library's stream "
-                               "directly before and after its one launch per cycle (an active cycle, with the "
-                               "mesh tally)"}
+            "launch_ms_spans": ("the gen loop's event kernels (start, transit and collision rounds, tail) between "
+                                "CUDA events on the library's stream" if a.form == "event" else
+                                "the history-loop kernel alone: CUDA events recorded on the library's stream "
+                                "directly before and after its one launch per cycle (an active cycle, with the "
+                                "mesh tally)")}
     comp = committed_compute("k_transport_lattice")
     if comp:
         roof["compute"] = comp

@@ -359,9 +359,8 @@ int32_t sg_eigen_cycle(sg_handle h, int32_t admin, int32_t atch, sg_cycle_stats*
  * the k estimate of attachment `atch` run on the device; `out` receives the normalised next-cycle
  * bank (pop particles, in brood order), *master_state the strided pRNG and *k_eff the new k.  A bank
  * in page-locked host memory that the device can address (cudaHostAlloc, or cudaHostRegister with
- * mapping) is read by the kernels in place across the host link while they run, and an output bank
- * in such memory (every array, brood_id included) is written in place by the kernels that build it;
- * other host memory is copied to or from the device.  Replaces the resident run of sg_eigen_init. */
+ * mapping) is read by the kernels in place across the host link while they run; other host memory
+ * is copied to the device first.  Replaces the resident run of sg_eigen_init. */
 int32_t sg_eigen_cycle_bank(sg_handle h, int32_t admin, int32_t atch, const sg_bank* in, int32_t pop,
                             uint64_t* master_state, double* k_eff, double k_end, sg_bank* out,
                             sg_cycle_stats* stats);

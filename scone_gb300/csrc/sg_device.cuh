@@ -338,11 +338,14 @@ __device__ __forceinline__ bool surf_going(const DSurf& s, const T r[3], const R
   }
 }
 
+// dirTol: SCONE's rule for a point within the surface tolerance -- the side the direction points
+// to (surface_inter.f90:363-378).  Without it the sign of the surface function decides (mixed form,
+// points not on a surface; see Geom::place).
 template <class R, class T>
-__device__ __forceinline__ bool surf_halfspace(const DSurf& s, const T r[3], const R u[3]) {
-  T c = surf_evaluate<T>(s, r);   // surface_inter.f90:363-378
+__device__ __forceinline__ bool surf_halfspace(const DSurf& s, const T r[3], const R u[3], bool dirTol = true) {
+  T c = surf_evaluate<T>(s, r);
   bool hs = c > T(0);
-  if (fabs(c) < STOL<T>(s)) hs = surf_going<R, T>(s, r, u);
+  if (dirTol && fabs(c) < STOL<T>(s)) hs = surf_going<R, T>(s, r, u);
   return hs;
 }
 
@@ -455,14 +458,14 @@ struct Geom {
   // a union that is already true or an intersection that is already false ends the current bracket
   // (shortCircuit, :406-422) or, at depth 0, the whole cell
   template <class T>
-  __device__ __forceinline__ bool inside_complex(int cell, const T r[3], const R dir[3]) const {
+  __device__ __forceinline__ bool inside_complex(int cell, const T r[3], const R dir[3], bool dirTol = true) const {
     bool isIt = true;
     int depth = 0;
     const int end = g.cell_ptr[cell + 1];
     for (int i = g.cell_ptr[cell]; i < end; ++i) {
       const int el = g.cell_surf[i];
       if (!cell_is_op(el)) {
-        const bool hs = surf_halfspace<R, T>(g.surfs[abs(el) - 1], r, dir);
+        const bool hs = surf_halfspace<R, T>(g.surfs[abs(el) - 1], r, dir, dirTol);
         isIt = (hs == (el > 0));
       } else if ((el == CELL_UNION && isIt) || (el == CELL_INTERSECT && !isIt)) {
         if (depth == 0) return isIt;
@@ -478,24 +481,25 @@ struct Geom {
     return isIt;
   }
 
-  // universe%findCell for the universe `u` at local position r
+  // universe%findCell for the universe `u` at local position r; dirTol as in surf_halfspace (the
+  // pin and lattice searches' direction-dependent tolerances follow it too)
   template <class T>
-  __device__ __forceinline__ int find_cell(int u, const T r[3], const R dir[3]) const {
+  __device__ __forceinline__ int find_cell(int u, const T r[3], const R dir[3], bool dirTol = true) const {
     const DUni& U = g.unis[u];
     switch (U.type) {
       case SG_UNI_ROOT:                                          // rootUniverse_class.f90:127-145
-        return surf_halfspace<R, T>(g.surfs[U.i[0]], r, dir) ? 2 : 1;
+        return surf_halfspace<R, T>(g.surfs[U.i[0]], r, dir, dirTol) ? 2 : 1;
       case SG_UNI_CELL: {                                        // cellUniverse_class.f90:203-246
         int nc = U.i[1];
         for (int c = 0; c < nc; ++c) {
           int cell = g.uni_cells[U.i[0] + c];
           bool isIt = false;
-          if (g.cell_complex && g.cell_complex[cell]) isIt = inside_complex<T>(cell, r, dir);
+          if (g.cell_complex && g.cell_complex[cell]) isIt = inside_complex<T>(cell, r, dir, dirTol);
           else
             for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
               int ss = g.cell_surf[k];
               if (cell_is_op(ss)) continue;                    // brackets of an all-intersection cell
-              bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir);
+              bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir, dirTol);
               isIt = (hs == (ss > 0));
               if (!isIt) break;
             }
@@ -505,7 +509,7 @@ struct Geom {
       }
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:150-173
         T rsq = r[0] * r[0] + r[1] * r[1];
-        T mul = ((T)(r[0] * (T)dir[0] + r[1] * (T)dir[1]) >= T(0)) ? T(-1) : T(1);
+        T mul = !dirTol ? T(0) : (((T)(r[0] * (T)dir[0] + r[1] * (T)dir[1]) >= T(0)) ? T(-1) : T(1));
         int N = U.i[1];
         for (int l = 1; l <= N; ++l)
           if (rsq < PIN_RSQ<T>(g, U.i[0] + l - 1) + mul * PIN_TOL<T>(g, U.i[0] + l - 1)) return l;
@@ -522,7 +526,7 @@ struct Geom {
           if constexpr (sizeof(T) == 8) ijk[i] = (int)floor((r[i] - corner) / pitch) + 1;
           else ijk[i] = (int)floorf((r[i] - corner) * U.invf[i]) + 1;
           T r_bar = r[i] - corner - ijk[i] * pitch + T(0.5) * pitch;
-          if (fabs(r_bar) > UD<T>(U, 6 + i) && r_bar * (T)dir[i] > T(0)) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
+          if (dirTol && fabs(r_bar) > UD<T>(U, 6 + i) && r_bar * (T)dir[i] > T(0)) ijk[i] += (dir[i] < R(0)) ? -1 : 1;
           if (ijk[i] <= 0 || ijk[i] > U.i[i]) out = true;
         }
         return out ? U.i[3] : ijk[0] + U.i[0] * (ijk[1] - 1 + U.i[1] * (ijk[2] - 1));
@@ -685,7 +689,8 @@ struct Geom {
 
   // geometryStd%diveToMat (geometryStd_class.f90:565-619); returns false on nesting overflow.
   // rf: float(r0) when the caller has it (mixed form), so an origin-free level 2 reuses it
-  __device__ __forceinline__ bool dive(Coords<R, MAXL>& c, int start, const float* rf = nullptr) const {
+  __device__ __forceinline__ bool dive(Coords<R, MAXL>& c, int start, const float* rf = nullptr,
+                                       bool dirTol = true) const {
 #pragma unroll
     for (int i = 0; i < MAXL; ++i) {
       if (i < start) continue;
@@ -724,7 +729,7 @@ struct Geom {
       c.base[i + 1] = gf.y - 1;
       R dl[3];
       level_dir(c, i + 1, dl);
-      c.local[i + 1] = find_cell<R>(nu, c.rl[i], dl);
+      c.local[i + 1] = find_cell<R>(nu, c.rl[i], dl, dirTol);
     }
     c.mat = SG_UNDEF_MAT;
     c.nest = MAXL;
@@ -736,7 +741,14 @@ struct Geom {
   // Mixed form: the root border test is first made in FP32 at float(r0); only a value within the
   // surface's filter margin (tolerance plus the FP32 error bound) goes to the FP64 test, so the side
   // found is always the FP64 one.
-  __device__ __forceinline__ bool place(Coords<R, MAXL>& c) const {
+  // onSurface: the point may lie on a surface (a boundary hit), so SCONE's direction-dependent
+  // tolerance rule decides it.  Points reached by a flight, a history start or a split release are
+  // not on a surface; in the mixed form they are classified by the sign of each surface function.
+  // There the tolerances are sized to FP32 crossing accuracy (~4e-6 cm), and the rule would assign
+  // a shell of that thickness around every surface by flight direction: with the net current out
+  // of fuel pins it shrank the fuel the flights saw and lowered k by 1.5e-5 (correlated runs of the
+  // two forms).  The FP64 form applies the rule everywhere, as SCONE does.
+  __device__ __forceinline__ bool place(Coords<R, MAXL>& c, bool onSurface = true) const {
     c.uni[0] = g.root;
     c.base[0] = 0;
     int loc = 0;
@@ -748,10 +760,11 @@ struct Geom {
         if (v > S.filt) loc = 2;
         else if (v < -S.filt) loc = 1;
       }
-      if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u);
+      if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u, onSurface);
       c.local[0] = loc;
-      return dive(c, 0, rf);
+      return dive(c, 0, rf, onSurface);
     }
+    (void)onSurface;
     if (loc == 0) loc = find_cell<double>(g.root, c.r0, c.u);
     c.local[0] = loc;
     return dive(c, 0);
@@ -762,10 +775,10 @@ struct Geom {
     // the step in the working precision, accumulated in FP64 (in the FP64 form the same products)
 #pragma unroll
     for (int k = 0; k < 3; ++k) c.r0[k] = c.r0[k] + (double)(dist * c.u[k]);
-    bool ok = place(c);
+    bool ok = place(c, false);
     if (c.mat == 0) {
       surf_transform_bc<R>(g.surfs[g.border], c.r0, c.u);
-      ok = place(c);
+      ok = place(c, false);
     }
     return ok;
   }

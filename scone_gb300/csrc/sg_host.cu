@@ -212,6 +212,8 @@ struct sg_handle_t {
   int lastN = 0;
   long long launches = 0;      // kernels launched since the last reset (cycle stats)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t copyStream = nullptr;   // second stream of the bank copies back to the host
+  cudaEvent_t copyEv[2] = {nullptr, nullptr};
   float lastTransportMs = 0.f;
   sg_cycle_stats lastStats{};   // the last eigenvalue cycle's statistics
 
@@ -1246,13 +1248,12 @@ int norm_size(sg_handle h, DBank in, int S, int totPop, unsigned long long maste
     h->launches += (heap > 0 ? 5 : 4);
     (void)n_hist;
   } else {
-    // (the destination may be a caller's page-locked host bank: the copy kind follows the pointers)
-    CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDefault, s));
-    CK(cudaMemcpyAsync(out.dir, in.dir, 3 * sizeof(double) * S, cudaMemcpyDefault, s));
-    CK(cudaMemcpyAsync(out.wgt, in.wgt, sizeof(double) * S, cudaMemcpyDefault, s));
-    CK(cudaMemcpyAsync(out.time, in.time, sizeof(double) * S, cudaMemcpyDefault, s));
-    CK(cudaMemcpyAsync(out.G, in.G, sizeof(int) * S, cudaMemcpyDefault, s));
-    CK(cudaMemcpyAsync(out.brood, in.brood, sizeof(int) * S, cudaMemcpyDefault, s));
+    CK(cudaMemcpyAsync(out.r, in.r, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.dir, in.dir, 3 * sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.wgt, in.wgt, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.time, in.time, sizeof(double) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.G, in.G, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(out.brood, in.brood, sizeof(int) * S, cudaMemcpyDeviceToDevice, s));
   }
   return SG_OK;
 }
@@ -1280,16 +1281,22 @@ int h2d_bank(sg_handle h, const sg_bank* b, int n, DBank d) {
   return SG_OK;
 }
 
+// The arrays go back in two halves on two streams, so two copy engines share the transfer (the
+// second stream waits for the bank to be complete and the first waits for the second's copies).
 int d2h_bank(sg_handle h, DBank d, int n, const sg_bank* b) {
-  cudaStream_t s = h->stream;
+  cudaStream_t s = h->stream, s2 = h->copyStream;
   if (n <= 0) return SG_OK;
+  CK(cudaEventRecord(h->copyEv[0], s));
+  CK(cudaStreamWaitEvent(s2, h->copyEv[0], 0));
   if (b->r) CK(cudaMemcpyAsync(b->r, d.r, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  if (b->dir) CK(cudaMemcpyAsync(b->dir, d.dir, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->dir) CK(cudaMemcpyAsync(b->dir, d.dir, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s2));
   if (b->wgt) CK(cudaMemcpyAsync(b->wgt, d.wgt, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-  if (b->G) CK(cudaMemcpyAsync(b->G, d.G, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-  if (b->time) CK(cudaMemcpyAsync(b->time, d.time, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (b->G) CK(cudaMemcpyAsync(b->G, d.G, sizeof(int) * n, cudaMemcpyDeviceToHost, s2));
+  if (b->time) CK(cudaMemcpyAsync(b->time, d.time, sizeof(double) * n, cudaMemcpyDeviceToHost, s2));
   if (b->brood_id) CK(cudaMemcpyAsync(b->brood_id, d.brood, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
   if (b->E && d.E) CK(cudaMemcpyAsync(b->E, d.E, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(h->copyEv[1], s2));
+  CK(cudaStreamWaitEvent(s, h->copyEv[1], 0));
   CK(cudaStreamSynchronize(s));
   return SG_OK;
 }
@@ -1313,21 +1320,6 @@ bool mapped_host_bank(sg_handle h, const sg_bank* b, DBank* d) {
   if (h->hasCE) { if (!dev(b->E, &E)) return false; G = nullptr; }
   else if (!dev(b->G, &G)) return false;
   *d = DBank{(double*)r, (double*)dir, (double*)wgt, (int*)G, nullptr, (double*)time, (double*)E};
-  return true;
-}
-
-// The same for a bank the device writes (the normalised next-cycle bank of sg_eigen_cycle_bank):
-// every array written (r, dir, wgt, G, time, brood_id) must be such memory; the kernels that build
-// the bank then write it in place across the host link, with no device copy and no copy back.
-bool mapped_host_out(sg_handle h, const sg_bank* b, DBank* d) {
-  if (h->hasCE) return false;
-  DBank m;
-  if (!mapped_host_bank(h, b, &m) || !b->brood_id) return false;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, b->brood_id) != cudaSuccess) { cudaGetLastError(); return false; }
-  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
-  m.brood = (int*)a.devicePointer;
-  *d = m;
   return true;
 }
 
@@ -1653,6 +1645,9 @@ int32_t sg_create(const sg_config* cfg, sg_handle* out) {
   if (rc) { delete h; return rc; }
   for (auto& e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) { delete h; return SG_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return SG_ERR_CUDA; }
+  for (auto& e : h->copyEv)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { delete h; return SG_ERR_CUDA; }
   *out = h;
   return SG_OK;
 }
@@ -1685,6 +1680,8 @@ int32_t sg_destroy(sg_handle h) {
   for (auto& a : h->mapTab32) a.free();
   for (auto& a : h->mapTabCell) a.free();
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+  for (auto& e : h->copyEv) if (e) cudaEventDestroy(e);
+  if (h->copyStream) cudaStreamDestroy(h->copyStream);
   cudaStreamDestroy(h->stream);
   delete h;
   return SG_OK;
@@ -1924,16 +1921,11 @@ int32_t sg_eigen_cycle_bank(sg_handle h, int32_t admin, int32_t atch, const sg_b
   h->master = *master_state;
   h->k = *k_eff;
   h->cur = 0;
-  // nextCycle: written in place into the caller's page-locked bank when the device can address it
-  DBank out_d;
-  const bool outMapped = mapped_host_out(h, out, &out_d);
-  int rc = eigen_cycle_core(h, admin, atch, in_d, h->bank[1].view(), outMapped ? out_d : res, nullptr);
+  int rc = eigen_cycle_core(h, admin, atch, in_d, h->bank[1].view(), res, nullptr);
   h->eigenReady = false;   // the device banks hold no resident run for sg_eigen_cycle
   if (rc) return rc;
-  if (!outMapped) {
-    rc = d2h_bank(h, res, pop, out);
-    if (rc) return rc;
-  }
+  rc = d2h_bank(h, res, pop, out);
+  if (rc) return rc;
   CK(cudaEventRecord(h->ev[3], s));
   CK(cudaStreamSynchronize(s));
   *master_state = h->master;

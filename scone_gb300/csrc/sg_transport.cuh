@@ -508,7 +508,7 @@ struct Tracker {
     time = K.b_time[e];
     splitCount = 0;
     cache.lvl = 0;
-    if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist);
+    if (!geom.place(c, false)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist);
     select_ht();
   }
 
@@ -647,7 +647,7 @@ struct Tracker {
     splitCount = 0;
     nbuf = 0;
     cache.lvl = 0;
-    if (!geom.place(c)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
+    if (!geom.place(c, false)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
     select_ht();
   }
 
