@@ -1,8 +1,8 @@
 """Builds libsconegpu.so in-tree (scone_gb300/_build/) with nvcc for sm_103a.
 
-Translation units compile in parallel: four per (nuclear data, precision form, transport operator)
+Translation units compile in parallel: six per (nuclear data, precision form, transport operator)
 for the transport kernels (sg_tr_unit.cu with the SG_* macros: history loop and event kernels, each
-for nesting bounds 2 and 4), one per (precision, operator) for the batched kernel, and the host and
+for nesting bounds 2, 3 and 4), one per (precision, operator) for the batched kernel, and the host and
 support units.  The FP64 verification units and the support kernels are compiled with -fmad=false
 (every multiply and add rounded separately, as SCONE's gfortran build does on x86-64); the
 mixed-precision units keep FMA contraction.
@@ -28,7 +28,7 @@ UNITS = [(u.replace(".cu", ""), u, ["-fmad=false"])
 for _op in ("st", "dt", "ht"):
     for _prec, _R, _fl in (("fp64", "double", ["-fmad=false"]), ("mixed", "float", [])):
         for _data, _ce in (("mg", 0), ("ce", 1)):
-            for _part in range(4):
+            for _part in range(6):
                 UNITS.append((f"sg_tr_{_data}_{_prec}_{_op}_p{_part}", "sg_tr_unit.cu",
                               _fl + [f"-DSG_R={_R}", f"-DSG_CE={_ce}", f"-DSG_OP=OP_{_op.upper()}",
                                      f"-DSG_PART={_part}"]))

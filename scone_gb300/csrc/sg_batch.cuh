@@ -93,6 +93,7 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
   T.nsites = 0;
   T.segs = 0;
   T.cache.lvl = 0;
+  T.onSurf = false;
   T.acc = P.t.acc + (long long)c * P.n_bins;
   if (!T.geom.place(T.c, false)) raise_error(P.t.ctr, SG_ERR_UNDEF_MAT, n);
   T.select_ht();

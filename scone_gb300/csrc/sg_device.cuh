@@ -217,9 +217,12 @@ __device__ __forceinline__ T surf_evaluate(const DSurf& s, const T r[3]) {
 }
 
 // box/squareCylinder slab intersection (box_class.f90:168-237, squareCylinder_class.f90:212-270)
+// onSurf: the particle may sit on a surface (it has just crossed or hit one), so a point within the
+// surface tolerance takes SCONE's on-surface branches; false: the plain intersection (mixed form,
+// after a collision or a placement; see Geom::place)
 template <class R, class T>
 __device__ __forceinline__ R slab_distance(const DSurf& s, const T r[3], const R u[3], int nax,
-                                           int ax0, int ax1, int ax2) {
+                                           int ax0, int ax1, int ax2, bool onSurf = true) {
   const R FP_MISS_TOL = (sizeof(R) == 8) ? R(1.0 + 10.0 * 2.220446049250313e-16) : R(1.0f + 10.0f * 1.1920929e-7f);
   const R HUGE_R = (sizeof(R) == 8) ? R(1.7976931348623157e308) : R(3.4028234663852886e38f);
   const R INF_R = R(D_INF);
@@ -245,20 +248,20 @@ __device__ __forceinline__ R slab_distance(const DSurf& s, const T r[3], const R
   }
   R d;
   if (far <= near * FP_MISS_TOL) d = INF_R;
-  else if (fabs(surf_evaluate<T>(s, r)) < STOL<T>(s)) d = (fabs(far) >= fabs(near)) ? far : near;
+  else if (onSurf && fabs(surf_evaluate<T>(s, r)) < STOL<T>(s)) d = (fabs(far) >= fabs(near)) ? far : near;
   else d = (near <= R(0)) ? far : near;
   if (d <= R(0) || d > INF_R) d = INF_R;
   return d;
 }
 
 template <class R, class T>
-__device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R u[3]) {
+__device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R u[3], bool onSurf = true) {
   const R INF_R = R(D_INF);
   switch (s.type) {
     case SG_SURF_XPLANE: case SG_SURF_YPLANE: case SG_SURF_ZPLANE: {   // aPlane_class.f90:157-181
       T ra = SP<T>(s, 0) - at3(r, s.axis);
       R ua = at3(u, s.axis), d;
-      if (fabs(ra) < STOL<T>(s)) d = INF_R;
+      if (onSurf && fabs(ra) < STOL<T>(s)) d = INF_R;
       else if (ua != R(0)) d = R(ra) / ua;
       else d = INF_R;
       if (d <= R(0) || d > INF_R) d = INF_R;
@@ -268,7 +271,7 @@ __device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R
       R k = u[0] * R(SP<T>(s, 0)) + u[1] * R(SP<T>(s, 1)) + u[2] * R(SP<T>(s, 2));
       T c = surf_evaluate<T>(s, r);
       R d;
-      if (k == R(0) || fabs(c) < STOL<T>(s)) d = INF_R;
+      if (k == R(0) || (onSurf && fabs(c) < STOL<T>(s))) d = INF_R;
       else { d = -R(c) / k; if (d <= R(0) || d > INF_R) d = INF_R; }
       return d;
     }
@@ -278,7 +281,7 @@ __device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R
       R a = R(1) - at3(u, s.axis) * at3(u, s.axis);
       R delta = k * k - a * R(c), d;
       if (delta < R(0) || a == R(0)) d = INF_R;
-      else if (fabs(c) < STOL<T>(s)) {
+      else if (onSurf && fabs(c) < STOL<T>(s)) {
         if (k >= R(0)) d = INF_R;
         else { d = -k + dsqrt<R>(delta); d = d / a; }
       } else if (c < T(0)) { d = -k + dsqrt<R>(delta); d = d / a; }
@@ -290,15 +293,15 @@ __device__ __forceinline__ R surf_distance(const DSurf& s, const T r[3], const R
       R k = R(r[0] - SP<T>(s, 0)) * u[0] + R(r[1] - SP<T>(s, 1)) * u[1] + R(r[2] - SP<T>(s, 2)) * u[2];
       R delta = k * k - R(c), d;
       if (delta < R(0)) d = INF_R;
-      else if (fabs(c) < STOL<T>(s)) { if (k >= R(0)) d = INF_R; else d = -k + dsqrt<R>(delta); }
+      else if (onSurf && fabs(c) < STOL<T>(s)) { if (k >= R(0)) d = INF_R; else d = -k + dsqrt<R>(delta); }
       else if (c < T(0)) d = -k + dsqrt<R>(delta);
       else { d = -k - dsqrt<R>(delta); if (d <= R(0)) d = INF_R; }
       return d;
     }
     case SG_SURF_BOX:
-      return slab_distance<R, T>(s, r, u, 3, 0, 1, 2);
+      return slab_distance<R, T>(s, r, u, 3, 0, 1, 2, onSurf);
     default:
-      return slab_distance<R, T>(s, r, u, 2, s.pl0, s.pl1, 0);
+      return slab_distance<R, T>(s, r, u, 2, s.pl0, s.pl1, 0, onSurf);
   }
 }
 
@@ -555,14 +558,14 @@ struct Geom {
 
   // pin annulus k: zCylinder at the origin (pinUniverse_class.f90:114-118)
   template <class T>
-  __device__ __forceinline__ R pin_cyl(const DUni& U, int k, const T r[3], const R u[3]) const {
+  __device__ __forceinline__ R pin_cyl(const DUni& U, int k, const T r[3], const R u[3], bool onSurf) const {
     const R INF_R = R(D_INF);
     T c = (r[0] * r[0] + r[1] * r[1]) - PIN_RSQ<T>(g, U.i[0] + k);
     R kk = R(r[0]) * u[0] + R(r[1]) * u[1];
     R a = R(1) - u[2] * u[2];
     R delta = kk * kk - a * R(c), d;
     if (delta < R(0) || a == R(0)) d = INF_R;
-    else if (fabs(c) < PIN_TOL<T>(g, U.i[0] + k)) {
+    else if (onSurf && fabs(c) < PIN_TOL<T>(g, U.i[0] + k)) {
       if (kk >= R(0)) d = INF_R;
       else { d = -kk + dsqrt<R>(delta); d = d / a; }
     } else if (c < T(0)) { d = -kk + dsqrt<R>(delta); d = d / a; }
@@ -570,16 +573,16 @@ struct Geom {
     return fmin(d, INF_R);
   }
 
-  // universe%distance
+  // universe%distance; onSurf as in surf_distance
   template <class T>
   __device__ __forceinline__ void uni_distance(int u, int localID, const T r[3], const R dir[3],
-                                               R& d, int& surfIdx) const {
+                                               R& d, int& surfIdx, bool onSurf = true) const {
     const R INF_R = R(D_INF);
     const DUni& U = g.unis[u];
     switch (U.type) {
       case SG_UNI_ROOT:                                          // rootUniverse_class.f90:152-162
         surfIdx = U.i[0] + 1;
-        d = surf_distance<R, T>(g.surfs[U.i[0]], r, dir);
+        d = surf_distance<R, T>(g.surfs[U.i[0]], r, dir, onSurf);
         return;
       case SG_UNI_CELL: {                                        // simpleCell_class.f90:120-141
         int cell = g.uni_cells[U.i[0] + localID - 1];
@@ -587,22 +590,22 @@ struct Geom {
         for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // unionCell :426-443 alike
           int ss = g.cell_surf[k];
           if (cell_is_op(ss)) continue;
-          R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir);
+          R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir, onSurf);
           if (td < d) { d = td; surfIdx = abs(ss); }
         }
         return;
       }
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:185-226
         int N = U.i[1];
-        R d_out = (localID > N) ? INF_R : pin_cyl<T>(U, localID - 1, r, dir);
-        R d_in = (localID == 1) ? INF_R : pin_cyl<T>(U, localID - 2, r, dir);
+        R d_out = (localID > N) ? INF_R : pin_cyl<T>(U, localID - 1, r, dir, onSurf);
+        R d_in = (localID == 1) ? INF_R : pin_cyl<T>(U, localID - 2, r, dir, onSurf);
         if (d_in < d_out) { surfIdx = -1; d = d_in; } else { surfIdx = -2; d = d_out; }
         return;
       }
       default: {                                                 // latUniverse_class.f90:319-373
         if (localID == U.i[3]) {
           surfIdx = -7;
-          d = surf_distance<R, T>(g.surfs[U.i[4]], r, dir);     // outline box
+          d = surf_distance<R, T>(g.surfs[U.i[4]], r, dir, onSurf);     // outline box
           return;
         }
         int ijk[3];
@@ -677,13 +680,13 @@ struct Geom {
   }
 
   // level-l distance (root level in FP64 positions, lower levels in R)
-  __device__ __forceinline__ void level_distance(Coords<R, MAXL>& c, int l, R& d, int& s) const {
-    if (l == 0) uni_distance<double>(c.uni[0], c.local[0], c.r0, c.u, d, s);
+  __device__ __forceinline__ void level_distance(Coords<R, MAXL>& c, int l, R& d, int& s, bool onSurf = true) const {
+    if (l == 0) uni_distance<double>(c.uni[0], c.local[0], c.r0, c.u, d, s, onSurf);
     else {
       if (l == 1) sync_level2(c);
       R dl[3];
       level_dir(c, l, dl);
-      uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], dl, d, s);
+      uni_distance<R>(c.uni[l], c.local[l], c.rl[l > 0 ? l - 1 : 0], dl, d, s, onSurf);
     }
   }
 
@@ -802,8 +805,11 @@ struct Geom {
 
   // move_withCache / move_noCache (geometryStd_class.f90:214-352); fields absent (fieldDist = INF).
   // Returns the event; maxDist is replaced by the distance moved.
+  // onSurf: whether the particle may sit on a surface (it reached this point by a crossing or a
+  // boundary hit); the FP64 form always takes SCONE's on-surface branches
   __device__ __forceinline__ int move(Coords<R, MAXL>& c, R& maxDist, R cdist[MAXL], int csurf[MAXL],
-                                      DistCache& cache, bool useCache) const {
+                                      DistCache& cache, bool useCache, bool onSurf = true) const {
+    if constexpr (sizeof(R) == 8) onSurf = true;
     R dist = R(D_INF);
     int surfIdx = 0, level = 0;
     if (!useCache) cache.lvl = 0;
@@ -811,7 +817,7 @@ struct Geom {
     for (int l = 0; l < MAXL; ++l) {
       if (l < c.nest) {
         if (cache.lvl < l + 1) {
-          level_distance(c, l, cdist[l], csurf[l]);
+          level_distance(c, l, cdist[l], csurf[l], onSurf);
           cache.lvl += 1;
         }
         R td = cdist[l];

@@ -562,7 +562,7 @@ int build_geometry(sg_handle h, const sg_geometry_desc* g) {
   };
   int dep = depth(g->root_uni, 1);
   if (dep > 4) return h->fail(SG_ERR_BAD_ARG, "geometry: nesting deeper than 4 levels is not supported");
-  h->maxl = dep <= 2 ? 2 : 4;
+  h->maxl = dep <= 2 ? 2 : (dep == 3 ? 3 : 4);
   // bounds (geometryStd_class.f90:186-205)
   {
     const DSurf& b = s64[g->border_surf];

@@ -3,8 +3,9 @@
 //            coincidence tests and tally sums) or double (FP64 verification form)
 //   SG_CE    0 multigroup data (neutronMGstd / neutronMGimp), 1 continuous energy (neutronCEstd / CEimp)
 //   SG_OP    OP_ST, OP_DT or OP_HT (transportOperatorST / DT / HT)
-//   SG_PART  0 history loop, nesting bound 2; 1 event kernels, bound 2; 2 and 3 the same, bound 4
-// Splitting each combination four ways keeps every translation unit small enough to compile in
+//   SG_PART  0 history loop, nesting bound 2; 1 event kernels, bound 2; 2 and 3 the same, bound 3;
+//            4 and 5 the same, bound 4
+// Splitting each combination six ways keeps every translation unit small enough to compile in
 // parallel in a minute or two.
 #include <algorithm>
 #include "sg_dispatch.cuh"
@@ -12,16 +13,13 @@
 #if !defined(SG_R) || !defined(SG_CE) || !defined(SG_OP) || !defined(SG_PART)
 #error "sg_tr_unit.cu needs SG_R, SG_CE, SG_OP and SG_PART"
 #endif
-// nesting bound of parts 2 and 3 (deeper geometries than 2 levels)
-#ifndef SG_MAXL_HI
-#define SG_MAXL_HI 4
-#endif
+
 
 namespace sg {
 template <>
 cudaError_t launch_part<SG_R, (SG_CE != 0), SG_OP, SG_PART>(int kind, const TransportArgs<SG_R>& a, size_t smem,
                                                            cudaStream_t s, int* grid_out) {
-  return launch_one<SG_R, (SG_PART < 2 ? 2 : SG_MAXL_HI), SG_OP, (SG_CE != 0), ((SG_PART & 1) != 0)>(kind, a, smem, s,
+  return launch_one<SG_R, (SG_PART < 2 ? 2 : (SG_PART < 4 ? 3 : 4)), SG_OP, (SG_CE != 0), ((SG_PART & 1) != 0)>(kind, a, smem, s,
                                                                                         grid_out);
 }
 }  // namespace sg

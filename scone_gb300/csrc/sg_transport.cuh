@@ -122,6 +122,7 @@ struct Tracker {
   int splitCount;    // particle%splitCount (neutronCEimp / neutronMGimp)
   int nbuf;          // split particles of this history waiting in the buffer
   bool htDT;         // hybrid tracking: the current transit uses delta tracking
+  bool onSurf;       // the particle reached its position by a surface crossing or boundary hit
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
       : A(a), geom(a.geom), mg(a.mg), ce(a.ce), acc(accp) {
@@ -129,6 +130,7 @@ struct Tracker {
     kprod = kscat = kabs = kleak = R(0);
     nEv = nColl = 0;
     htDT = false;
+    onSurf = false;
     splitCount = 0;
     nbuf = 0;
   }
@@ -508,6 +510,7 @@ struct Tracker {
     time = K.b_time[e];
     splitCount = 0;
     cache.lvl = 0;
+    onSurf = false;
     if (!geom.place(c, false)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist);
     select_ht();
   }
@@ -647,6 +650,7 @@ struct Tracker {
     splitCount = 0;
     nbuf = 0;
     cache.lvl = 0;
+    onSurf = false;
     if (!geom.place(c, false)) raise_error(A.ctr, SG_ERR_UNDEF_MAT, h);
     select_ht();
   }
@@ -703,7 +707,8 @@ struct Tracker {
       const R u0[3] = {c.u[0], c.u[1], c.u[2]};
       const int matPre = mat;
       const int cellPre = A.has_cellmap ? lowest_cell() : 0;
-      const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0);
+      const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0, onSurf);
+      onSurf = (ev != 1);                                // a crossing or boundary hit leaves it on a surface
       if constexpr (CE) time = time + dist * invSpeed;
       else time = time + dist;
       nEv += 1;
@@ -743,6 +748,7 @@ struct Tracker {
       }
       const int matPre = mat;
       const int cellPre = (A.has_cellmap && A.has_current) ? lowest_cell() : 0;
+      onSurf = false;
       if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return SEG_END; }
       if constexpr (CE) time = time + dist * invSpeed;
       else time = time + dist;
@@ -833,6 +839,7 @@ struct Tracker {
     nsites = P.ints[3 * cap + i];
     segs = P.ints[4 * cap + i];
     cache.lvl = 0;
+    onSurf = false;                                    // stored particles sit at a collision point or a start
     if constexpr (CE) set_energy(P.E[i]);
     select_ht();
   }

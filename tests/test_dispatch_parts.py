@@ -1,5 +1,5 @@
 """The launch of a transport kernel reaches the part (translation unit) that holds it: the history
-loop or the event kernels, for nesting bound 2 or 4 (scone_gb300/csrc/sg_launch.h).  A host program
+loop or the event kernels, for nesting bound 2, 3 or 4 (scone_gb300/csrc/sg_launch.h).  A host program
 built with the host compiler replaces the parts with recorders; no GPU is used."""
 import os
 import shutil
@@ -15,7 +15,8 @@ namespace sg {
 static int last = -1;
 #define PART(R, CE, OP, P) template <> cudaError_t launch_part<R, CE, OP, P>(int, const TransportArgs<R>&, size_t, \
     cudaStream_t, int*) { last = 1000 * (sizeof(R) == 8) + 100 * CE + 10 * OP + P; return cudaSuccess; }
-#define PARTS(R, CE, OP) PART(R, CE, OP, 0) PART(R, CE, OP, 1) PART(R, CE, OP, 2) PART(R, CE, OP, 3)
+#define PARTS(R, CE, OP) PART(R, CE, OP, 0) PART(R, CE, OP, 1) PART(R, CE, OP, 2) PART(R, CE, OP, 3) \
+    PART(R, CE, OP, 4) PART(R, CE, OP, 5)
 #define OPS(R, CE) PARTS(R, CE, OP_ST) PARTS(R, CE, OP_DT) PARTS(R, CE, OP_HT)
 OPS(float, false) OPS(float, true) OPS(double, false) OPS(double, true)
 }
@@ -23,7 +24,7 @@ int main() {
   sg::TransportArgs<float> a{};
   sg::TransportArgs<double> b{};
   const int kinds[5] = {sg::K_HISTORY, sg::K_EV_START, sg::K_EV_TRANSIT, sg::K_EV_COLLIDE, sg::K_EV_TAIL};
-  for (int maxl : {2, 4})
+  for (int maxl : {2, 3, 4})
     for (int op : {sg::OP_ST, sg::OP_DT, sg::OP_HT})
       for (int kind : kinds) {
         sg::launch_kind_data<float, false>(kind, a, maxl, op, 0, nullptr, nullptr);
@@ -53,8 +54,8 @@ def test_launch_reaches_its_part(tmp_path):
             continue
         prec, ce, maxl, op, kind, got = r.split()
         maxl, op, kind, got = int(maxl), int(op), int(kind), int(got)
-        part = (0 if maxl <= 2 else 2) + (0 if kind == 0 else 1)
+        part = (0 if maxl <= 2 else (2 if maxl == 3 else 4)) + (0 if kind == 0 else 1)
         want = 1000 * (prec == "d") + 100 * int(ce) + 10 * op + part
         assert got == want, r
         seen += 1
-    assert seen == 2 * 3 * 5 * 2
+    assert seen == 3 * 3 * 5 * 2
