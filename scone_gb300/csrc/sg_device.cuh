@@ -19,6 +19,13 @@
 #include <cuda_runtime.h>
 #include "sg_internal.h"
 
+// How the cell-universe search and distance are compiled: inlined (default) or as one out-of-line
+// copy (-DSG_CELL_SEARCH=__noinline__), which keeps their surface loops out of the code of the
+// geometries that have no cell universes
+#ifndef SG_CELL_SEARCH
+#define SG_CELL_SEARCH __forceinline__
+#endif
+
 namespace sg {
 
 // ------------------------------------------------------------------ constants
@@ -484,6 +491,29 @@ struct Geom {
     return isIt;
   }
 
+  // cellUniverse%findCell (cellUniverse_class.f90:203-246): the first cell of the universe whose
+  // simpleCell / unionCell test holds, n + 1 if none.  SG_CELL_SEARCH sets how it is compiled
+  // (inlined into every level's search, or one out-of-line copy).
+  template <class T>
+  __device__ SG_CELL_SEARCH int find_cell_cells(const DUni& U, const T r[3], const R dir[3], bool dirTol) const {
+    const int nc = U.i[1];
+    for (int c = 0; c < nc; ++c) {
+      const int cell = g.uni_cells[U.i[0] + c];
+      bool isIt = false;
+      if (g.cell_complex && g.cell_complex[cell]) isIt = inside_complex<T>(cell, r, dir, dirTol);
+      else
+        for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
+          const int ss = g.cell_surf[k];
+          if (cell_is_op(ss)) continue;                        // brackets of an all-intersection cell
+          const bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir, dirTol);
+          isIt = (hs == (ss > 0));
+          if (!isIt) break;
+        }
+      if (isIt) return c + 1;
+    }
+    return nc + 1;
+  }
+
   // universe%findCell for the universe `u` at local position r; dirTol as in surf_halfspace (the
   // pin and lattice searches' direction-dependent tolerances follow it too)
   template <class T>
@@ -492,24 +522,8 @@ struct Geom {
     switch (U.type) {
       case SG_UNI_ROOT:                                          // rootUniverse_class.f90:127-145
         return surf_halfspace<R, T>(g.surfs[U.i[0]], r, dir, dirTol) ? 2 : 1;
-      case SG_UNI_CELL: {                                        // cellUniverse_class.f90:203-246
-        int nc = U.i[1];
-        for (int c = 0; c < nc; ++c) {
-          int cell = g.uni_cells[U.i[0] + c];
-          bool isIt = false;
-          if (g.cell_complex && g.cell_complex[cell]) isIt = inside_complex<T>(cell, r, dir, dirTol);
-          else
-            for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // simpleCell :90-111
-              int ss = g.cell_surf[k];
-              if (cell_is_op(ss)) continue;                    // brackets of an all-intersection cell
-              bool hs = surf_halfspace<R, T>(g.surfs[abs(ss) - 1], r, dir, dirTol);
-              isIt = (hs == (ss > 0));
-              if (!isIt) break;
-            }
-          if (isIt) return c + 1;
-        }
-        return nc + 1;
-      }
+      case SG_UNI_CELL:
+        return find_cell_cells<T>(U, r, dir, dirTol);
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:150-173
         T rsq = r[0] * r[0] + r[1] * r[1];
         T mul = !dirTol ? T(0) : (((T)(r[0] * (T)dir[0] + r[1] * (T)dir[1]) >= T(0)) ? T(-1) : T(1));
@@ -573,6 +587,22 @@ struct Geom {
     return fmin(d, INF_R);
   }
 
+  // simpleCell%distance (simpleCell_class.f90:120-141; unionCell :426-443 alike): the nearest of the
+  // cell's surfaces; compiled as SG_CELL_SEARCH says
+  template <class T>
+  __device__ SG_CELL_SEARCH void cell_distance(const DUni& U, int localID, const T r[3], const R dir[3], R& d,
+                                               int& surfIdx, bool onSurf) const {
+    const int cell = g.uni_cells[U.i[0] + localID - 1];
+    d = R(D_INF);
+    surfIdx = 0;
+    for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {
+      const int ss = g.cell_surf[k];
+      if (cell_is_op(ss)) continue;
+      const R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir, onSurf);
+      if (td < d) { d = td; surfIdx = abs(ss); }
+    }
+  }
+
   // universe%distance; onSurf as in surf_distance
   template <class T>
   __device__ __forceinline__ void uni_distance(int u, int localID, const T r[3], const R dir[3],
@@ -584,17 +614,9 @@ struct Geom {
         surfIdx = U.i[0] + 1;
         d = surf_distance<R, T>(g.surfs[U.i[0]], r, dir, onSurf);
         return;
-      case SG_UNI_CELL: {                                        // simpleCell_class.f90:120-141
-        int cell = g.uni_cells[U.i[0] + localID - 1];
-        d = INF_R; surfIdx = 0;
-        for (int k = g.cell_ptr[cell]; k < g.cell_ptr[cell + 1]; ++k) {   // unionCell :426-443 alike
-          int ss = g.cell_surf[k];
-          if (cell_is_op(ss)) continue;
-          R td = surf_distance<R, T>(g.surfs[abs(ss) - 1], r, dir, onSurf);
-          if (td < d) { d = td; surfIdx = abs(ss); }
-        }
+      case SG_UNI_CELL:
+        cell_distance<T>(U, localID, r, dir, d, surfIdx, onSurf);
         return;
-      }
       case SG_UNI_PIN: {                                         // pinUniverse_class.f90:185-226
         int N = U.i[1];
         R d_out = (localID > N) ? INF_R : pin_cyl<T>(U, localID - 1, r, dir, onSurf);
