@@ -381,6 +381,28 @@ int32_t sg_fixed_source_cycle(sg_handle h, int32_t admin, int32_t n, uint64_t* m
 int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t share, int32_t total,
                                     uint64_t* master_state, sg_cycle_stats* stats);
 
+/* One process's part of particleDungeon%normSize_Repr when the population is split over processes
+ * (particleDungeon_class.f90:431-605, MPI branches).  `sites` holds this process's n fission sites
+ * sorted by brood ID (as sg_transport_bank returns them); sites_before is the number of sites of the
+ * processes before this one and tot_sites the number over all processes (the gathered popSizes);
+ * master_state is the master process's RNG state at the call (:469-494: its draws number the sites
+ * of all processes in process order).  Every process finds the same threshold (the heap threshold
+ * over all tot_sites draws, computed on the device from master_state alone: there is nothing to
+ * broadcast) and keeps, or duplicates, its own sites with the draws that fall to them (:500-586).
+ * The result, sorted by brood ID, goes to `out` (capacity out_cap), its size to n_out.  The sizes
+ * summed over processes equal tot_pop; loadBalancing (:593-700) is the caller's exchange. */
+int32_t sg_normalise_shard(sg_handle h, const sg_bank* sites, int32_t n, int64_t sites_before,
+                           int64_t tot_sites, int32_t tot_pop, uint64_t master_state,
+                           sg_bank* out, int32_t out_cap, int32_t* n_out);
+
+/* The running-batch scores of one admin (n_bins values, the sum over threads of scoreMemory's
+ * parallelBins, scoreMemory_class.f90:215-233): read, and written back after a sum over processes.
+ * That sum is the MPI reduction of a tally with mpiSync (scoreMemory%reduceBins, :403-432), which
+ * the k attachment of an eigenvalue calculation uses (eigenPhysicsPackage_class.f90:607-630); call
+ * both between sg_transport_bank and sg_tally_cycle_end of the batch's last cycle. */
+int32_t sg_tally_get_scores(sg_handle h, int32_t admin, double* scores, int64_t n_bins);
+int32_t sg_tally_set_scores(sg_handle h, int32_t admin, const double* scores, int64_t n_bins);
+
 /* ---------------------------------------------------------------- gen loop without allocation */
 
 /* No counterpart in SCONE.  The gen loop of sg_transport_bank for callers that cannot allocate

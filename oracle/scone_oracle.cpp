@@ -2089,6 +2089,46 @@ struct Oracle {
       sortByBroodID(b);
     }
   }
+  // normSize_Repr on one rank of an MPI run (the same routine, :431-590): popSizes gathered to the
+  // master (:466), which draws one number per site of every rank in rank order into the heap and
+  // records the state each rank's draws start from (:477-494); threshold, excess and seeds are
+  // broadcast (:497-501) and the rank keeps or duplicates its own sites with its seed (:507-586).
+  // `before` is the number of sites of the ranks below, `totSites` the sum of popSizes; `b` holds
+  // this rank's sites.  loadBalancing (:593-700) is left to the caller.
+  void normSizeReprRank(std::vector<PState>& b, int64_t before, int64_t totSites, int totPop, const RNG& rand) {
+    sortByBroodID(b);
+    const int64_t excess = totSites - totPop;
+    int64_t heapSize = excess < 0 ? (-excess) % totSites : excess;
+    double threshold = 1.0;
+    uint64_t seed = 0;
+    if (heapSize != 0) {                              // master: the heap over all ranks' draws
+      RNG mr = rand;
+      std::vector<double> rn((size_t)totSites);
+      for (int64_t j = 0; j < totSites; ++j) {
+        if (j == before) seed = mr.s;                 // seeds(rank + 1)
+        rn[(size_t)j] = mr.get();
+      }
+      if (before == totSites) seed = mr.s;
+      std::nth_element(rn.begin(), rn.begin() + (heapSize - 1), rn.end());
+      threshold = rn[(size_t)(heapSize - 1)];
+    }
+    RNG rr; rr.s = seed;                              // rankRand%init(seeds(rank + 1))
+    const int pop = (int)b.size();
+    if (excess > 0) {
+      std::vector<PState> keep;
+      for (int i = 0; i < pop; ++i) if (rr.get() > threshold) keep.push_back(b[i]);
+      b.swap(keep);
+    } else if (excess < 0) {
+      const int64_t n_copies = (-excess) / totSites;
+      const int64_t n_duplicates = (-excess) % totSites;
+      std::vector<PState> out(b);
+      for (int64_t c = 0; c < n_copies; ++c) out.insert(out.end(), b.begin(), b.begin() + pop);
+      if (n_duplicates != 0)
+        for (int i = 0; i < pop; ++i) if (rr.get() <= threshold) out.push_back(b[i]);
+      b.swap(out);
+      sortByBroodID(b);
+    }
+  }
 };
 
 }  // namespace orc
@@ -2339,6 +2379,45 @@ int32_t or_tally_size(or_handle h, int32_t admin, int64_t* n) { *n = O(h)->admin
 int32_t or_get_bins(or_handle h, int32_t admin, double* bins, int64_t n) {
   orc::ScoreMemory& m = O(h)->admins[admin].mem;
   for (int64_t i = 0; i < n && i < m.N; ++i) { bins[i] = m.bin[i]; bins[n + i] = m.csum[i]; bins[2 * n + i] = m.csum2[i]; }
+  return SG_OK;
+}
+int32_t or_normalise_shard(or_handle h, const sg_bank* sites, int32_t n, int64_t before, int64_t tot_sites,
+                           int32_t tot_pop, uint64_t master, sg_bank* out, int32_t cap, int32_t* n_out) {
+  if (n < 0 || before < 0 || tot_sites < before + n || tot_pop <= 0) return SG_ERR_BAD_ARG;
+  if (tot_sites == 0) return SG_ERR_STATE;
+  std::vector<orc::PState> v;
+  bankToStates(sites, n, v);
+  orc::RNG r; r.s = master;
+  O(h)->normSizeReprRank(v, before, tot_sites, tot_pop, r);
+  *n_out = (int32_t)v.size();
+  if ((int)v.size() > cap) return SG_ERR_BANK_OVERFLOW;
+  statesToBank(v, out, cap);
+  return SG_OK;
+}
+// normSize_Repr of a single-process run on a bank given by the caller (the sites sorted by brood)
+int32_t or_normalise(or_handle h, const sg_bank* sites, int32_t n, int32_t tot_pop, uint64_t master, sg_bank* out,
+                     int32_t cap, int32_t* n_out) {
+  if (n <= 0 || tot_pop <= 0) return SG_ERR_BAD_ARG;
+  std::vector<orc::PState> v;
+  bankToStates(sites, n, v);
+  orc::RNG r; r.s = master;
+  O(h)->normSizeRepr(v, tot_pop, r);
+  *n_out = (int32_t)v.size();
+  if ((int)v.size() > cap) return SG_ERR_BANK_OVERFLOW;
+  statesToBank(v, out, cap);
+  return SG_OK;
+}
+// the running batch (parallelBins summed over threads), read and written around a sum over ranks
+int32_t or_tally_get_scores(or_handle h, int32_t admin, double* s, int64_t n) {
+  orc::ScoreMemory& m = O(h)->admins[admin].mem;
+  if (n < m.N) return SG_ERR_BAD_ARG;
+  for (int64_t i = 0; i < m.N; ++i) s[i] = m.parallel[i];
+  return SG_OK;
+}
+int32_t or_tally_set_scores(or_handle h, int32_t admin, const double* s, int64_t n) {
+  orc::ScoreMemory& m = O(h)->admins[admin].mem;
+  if (n < m.N) return SG_ERR_BAD_ARG;
+  for (int64_t i = 0; i < m.N; ++i) m.parallel[i] = s[i];
   return SG_OK;
 }
 int32_t or_get_keff(or_handle h, int32_t admin, double* k, double* sd) {

@@ -359,6 +359,20 @@ __device__ __forceinline__ bool surf_halfspace(const DSurf& s, const T r[3], con
   return hs;
 }
 
+// The reduced half-width below which a coordinate is "well inside" for the boundary transforms.
+// FP64 form: SCONE's halfwidth * (1 - surfTol) with the relative SURF_TOL (box_class.f90:393,440).
+// Mixed form, whose tolerance is an absolute length of a few FP32 ulps of the geometry: the explicit
+// BC (applied on a boundary hit, where the hit coordinates sit on their faces only to FP32 accuracy)
+// takes the half-width less that length; the transform BC after a delta-tracking flight takes the
+// half-width itself, so that it transforms exactly the coordinates that the sign classification of
+// the flight's end point put outside.  (A wider band reflects a coordinate that was inside next to
+// another face and leaves the point outside: the history would end as a leak.)
+template <class R>
+__device__ __forceinline__ double bc_inner(const DSurf& s, int ax, bool transform) {
+  if constexpr (sizeof(R) == 8) return s.p[3 + ax] * (1.0 - s.tol);
+  else return transform ? s.p[3 + ax] : s.p[3 + ax] - s.tol;
+}
+
 // explicitBC (box_class.f90:380-420, squareCylinder_class.f90:430-472); root level, FP64 positions
 template <class R>
 __device__ __forceinline__ void surf_explicit_bc(const DSurf& s, double r[3], R u[3]) {
@@ -368,7 +382,11 @@ __device__ __forceinline__ void surf_explicit_bc(const DSurf& s, double r[3], R 
     bool active = (s.type == SG_SURF_BOX) || ax == s.pl0 || ax == s.pl1;
     if (!active) continue;
     double r0 = r[ax] - s.p[ax];
-    if (fabs(r0) <= s.p[3 + ax] * (1.0 - s.tol)) continue;
+    if (fabs(r0) <= bc_inner<R>(s, ax, false)) continue;
+    // mixed form: of the coordinates within that band of their faces only those heading out (the
+    // hit one, and a second one at a corner hit); one heading in keeps its direction, where a
+    // reflection would turn it outward on its face and the placement would put it outside
+    if constexpr (sizeof(R) == 4) { if ((double)u[ax] * r0 <= 0.0) continue; }
     int b = (r0 < 0.0) ? s.bc[2 * ax] : s.bc[2 * ax + 1];
     if (b == SG_BC_REFLECTIVE) u[ax] = -u[ax];
     else if (b == SG_BC_PERIODIC) r[ax] = r[ax] - 2.0 * sgn(s.p[3 + ax], r0);
@@ -383,7 +401,7 @@ __device__ __forceinline__ void surf_transform_bc(const DSurf& s, double r[3], R
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
     bool active = (s.type == SG_SURF_BOX) || ax == s.pl0 || ax == s.pl1;
-    double a_bar = s.p[3 + ax] * (1.0 - s.tol);
+    double a_bar = bc_inner<R>(s, ax, true);
     Ri[ax] = active ? ((int)ceil(fabs(r[ax] - s.p[ax]) / a_bar)) / 2 : 0;
   }
 #pragma unroll

@@ -2,6 +2,7 @@
 // nuclear data, one transport operator and one nesting bound (included by sg_tr_unit.cu, which is
 // compiled once per such part).
 #pragma once
+#include <mutex>
 #include "sg_transport.cuh"
 #include "sg_launch.h"
 
@@ -23,11 +24,14 @@ const void* kernel_ptr(int kind) {
   }
 }
 
-// persistent grid: SM count x resident blocks of 128 threads (occupancy calculator)
+// persistent grid: SM count x resident blocks of 128 threads (occupancy calculator); the cache is
+// shared by every handle, so it is locked for callers that drive handles from several threads
 template <class R, int MAXL, int OP, bool CE, bool EV>
 int persistent_grid(int kind, size_t smem) {
+  static std::mutex mu;
   static int cached[K_KINDS] = {0};
   static size_t cached_smem = 0;
+  std::lock_guard<std::mutex> lock(mu);
   if (kind == K_HISTORY && smem != cached_smem) { cached[K_HISTORY] = 0; cached_smem = smem; }
   if (!cached[kind]) {
     int dev = 0, sms = 0, per = 0;

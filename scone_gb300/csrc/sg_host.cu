@@ -196,6 +196,7 @@ struct sg_handle_t {
   int regionCap = 0;
   DArr<int> histN, start, scanTmp, flags, pos, kbuf;
   DArr<unsigned long long> keys, sel, winCnt, winCand;
+  DArr<unsigned long long> shardKeys;   // sg_normalise_shard: the draws of all processes' sites
   DArr<unsigned int> hist16;
   DArr<double> sumPart, scal;  // scal: 0 k_eff, 1 k_new, 2 start weight, 3 end weight, 4 k_end
   DArr<int> totals;            // 0 sites total, 1 kept total, 2 dup total, 3 error
@@ -1665,7 +1666,7 @@ int32_t sg_destroy(sg_handle h) {
   h->fissile.free(); h->acc.free(); h->bin.free(); h->csum.free(); h->csum2.free();
   h->sR.free(); h->sDir.free(); h->sWgt.free(); h->sTime.free(); h->sG.free(); h->sBrood.free(); h->sSeq.free();
   h->sCursor.free(); h->histN.free(); h->start.free(); h->scanTmp.free(); h->flags.free(); h->pos.free();
-  h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->winCnt.free(); h->winCand.free(); h->sumPart.free(); h->scal.free();
+  h->kbuf.free(); h->keys.free(); h->sel.free(); h->hist16.free(); h->winCnt.free(); h->winCand.free(); h->shardKeys.free(); h->sumPart.free(); h->scal.free();
   h->totals.free(); h->ctr.free(); h->recColl.free(); h->recRng.free(); h->probG.free();
   h->pR0.free(); h->pRl.free(); h->pU.free(); h->pW.free(); h->pW0.free(); h->pTime.free(); h->pTrack.free();
   h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();
@@ -2020,6 +2021,94 @@ int32_t sg_fixed_source_cycle_shard(sg_handle h, int32_t admin, int32_t n, int32
     stats->cycle_ms = cyc;
     stats->n_kernels = h->launches;
   }
+  return SG_OK;
+}
+
+// particleDungeon%normSize_Repr, one process's part (particleDungeon_class.f90:431-590 with MPI).
+// The keys of all tot_sites sites are the master stream's draws in process order (:469-494), so
+// every process generates them all and finds the same heap threshold; its own sites take the keys
+// from sites_before on (the seed the master would have broadcast, :497-500).
+int32_t sg_normalise_shard(sg_handle h, const sg_bank* sites, int32_t n, int64_t sites_before, int64_t tot_sites,
+                           int32_t tot_pop, uint64_t master_state, sg_bank* out, int32_t out_cap, int32_t* n_out) {
+  if (!h || !sites || !out || !n_out) return SG_ERR_BAD_ARG;
+  if (!h->hasGeom || !h->hasMG) return h->fail(SG_ERR_STATE, "sg_normalise_shard: multigroup eigenvalue banks only");
+  if (n < 0 || n > h->cap || sites_before < 0 || tot_sites < sites_before + n || tot_sites > INT32_MAX || tot_pop <= 0)
+    return h->fail(SG_ERR_BAD_ARG, "sg_normalise_shard: bad sizes");
+  if (tot_sites == 0) return h->fail(SG_ERR_STATE, "normSize: empty fission bank");
+  if (n > 0 && (!sites->r || !sites->dir || !sites->G || !sites->brood_id))
+    return h->fail(SG_ERR_BAD_ARG, "sg_normalise_shard: the sites need r, dir, G and brood_id");
+  if (!out->r || !out->dir || !out->wgt || !out->G)
+    return h->fail(SG_ERR_BAD_ARG, "sg_normalise_shard: the output bank needs r, dir, wgt and G");
+  for (int i = 0; i < n; ++i)
+    if (sites->brood_id[i] < 1 || sites->brood_id[i] > h->cap || (i > 0 && sites->brood_id[i] < sites->brood_id[i - 1]))
+      return h->fail(SG_ERR_BAD_ARG, "sg_normalise_shard: brood IDs must be sorted and within 1..max_bank");
+  const int S = (int)tot_sites;
+  const long long excess = tot_sites - tot_pop;
+  const int heap = excess > 0 ? (int)excess : (excess < 0 ? (int)((-excess) % tot_sites) : 0);
+  const int n_copies = excess < 0 ? (int)((-excess) / tot_sites) : 0;
+  cudaStream_t s = h->stream;
+  h->eigenReady = false;   // the device banks are used as scratch
+  DBank in = h->bank[1].view(), res = h->bank[0].view();
+  *n_out = 0;
+  if (n > 0) {
+    int rc = h2d_bank(h, sites, n, in);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(in.brood, sites->brood_id, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  }
+  if (heap > 0) {
+    if (h->shardKeys.n < (size_t)S) CK(h->shardKeys.alloc(S));
+    k_rn_keys<<<((S + 31) / 32 + 127) / 128, 128, 0, s>>>(master_state, S, h->shardKeys.p);
+    CK(cudaGetLastError());
+    CK(quantile_select(h->shardKeys.p, S, heap, h->sel.p, h->kbuf.p, h->hist16.p, h->winCnt.p, h->winCand.p, s));
+  }
+  const unsigned long long* keys = heap > 0 ? h->shardKeys.p + sites_before : nullptr;
+  int m = n;
+  if (n > 0 && excess > 0) {
+    CK(launch_flags(keys, n, h->sel.p, 1, h->flags.p, s));
+    CK(cudaMemsetAsync(h->flags.p + n, 0, sizeof(int), s));
+    CK(exclusive_scan(h->flags.p, n + 1, h->pos.p, h->scanTmp.p, h->totals.p + 1, s));
+    CK(launch_compact(in, n, h->flags.p, h->pos.p, res, s));
+    CK(cudaMemcpyAsync(&m, h->totals.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  } else if (n > 0 && excess < 0) {
+    if (heap > 0) CK(launch_flags(keys, n, h->sel.p, 0, h->flags.p, s));
+    else CK(cudaMemsetAsync(h->flags.p, 0, (size_t)n * sizeof(int), s));
+    CK(cudaMemsetAsync(h->flags.p + n, 0, sizeof(int), s));
+    CK(exclusive_scan(h->flags.p, n + 1, h->pos.p, h->scanTmp.p, h->totals.p + 2, s));
+    int dups = 0;
+    CK(cudaMemcpyAsync(&dups, h->totals.p + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if ((long long)n * (n_copies + 1) + dups > h->cap) return h->fail(SG_ERR_BANK_OVERFLOW, "normSize: bank overflow");
+    m = n * (n_copies + 1) + dups;
+    CK(launch_brood_starts(in.brood, n, sites->brood_id[n - 1], h->start.p, s));
+    CK(launch_replicate(in, n, h->flags.p, h->pos.p, h->start.p, n_copies, res, s));
+  } else if (n > 0) {
+    res = in;
+  }
+  if (m > out_cap) return h->fail(SG_ERR_BANK_OVERFLOW, "sg_normalise_shard: output bank too small");
+  int rc = d2h_bank(h, res, m, out);
+  if (rc) return rc;
+  *n_out = m;
+  return SG_OK;
+}
+
+int32_t sg_tally_get_scores(sg_handle h, int32_t admin, double* scores, int64_t n) {
+  if (!h || !scores || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  const Admin& A = h->admins[admin];
+  if (n < A.N) return h->fail(SG_ERR_BAD_ARG, "get_scores: buffer smaller than the tally");
+  if (A.N == 0) return SG_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(scores, h->acc.p + A.off, A.N * sizeof(double), cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+int32_t sg_tally_set_scores(sg_handle h, int32_t admin, const double* scores, int64_t n) {
+  if (!h || !scores || admin < 0 || admin >= (int)h->admins.size()) return SG_ERR_BAD_ARG;
+  const Admin& A = h->admins[admin];
+  if (n < A.N) return h->fail(SG_ERR_BAD_ARG, "set_scores: buffer smaller than the tally");
+  if (A.N == 0) return SG_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(h->acc.p + A.off, scores, A.N * sizeof(double), cudaMemcpyHostToDevice));
   return SG_OK;
 }
 

@@ -2,6 +2,7 @@
 // fission sites by brood ID, population control (normSize_Repr), deterministic reductions and the
 // scoreMemory/tallyAdmin cycle-end update.  All are bandwidth- or latency-trivial next to the
 // history loop; they exist so that a whole eigenvalue cycle stays on the device.
+#include <atomic>
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -328,15 +329,15 @@ __global__ void k_radix_pick(unsigned int* hist, unsigned long long* sel, int* k
 // exit; kbuf holds [kth remaining, window found]; cnt two counters; cand WIN_CAP keys.
 cudaError_t quantile_select(const unsigned long long* keys, int S, int kth, unsigned long long* sel, int* kbuf,
                             unsigned int* hist, unsigned long long* cnt, unsigned long long* cand, cudaStream_t s) {
-  static int attrDevice = -1;                     // the attribute is set once per device
+  static std::atomic<int> attrDevice{-1};         // the attribute is set once per device
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev != attrDevice) {
+  if (dev != attrDevice.load()) {
     e = cudaFuncSetAttribute(k_win_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(WIN_CAP * sizeof(unsigned long long)));
     if (e != cudaSuccess) return e;
-    attrDevice = dev;
+    attrDevice.store(dev);
   }
   const double p = (double)kth / S;
   const double d = 8.0 * sqrt(p * (1.0 - p) / S) + 4.0 / S;
@@ -409,6 +410,25 @@ cudaError_t launch_compact(const DBank& in, int S, const int* flags, const int* 
 cudaError_t launch_replicate(const DBank& in, int S, const int* flags, const int* dpos, const int* start,
                              int n_copies, const DBank& out, cudaStream_t s) {
   k_replicate<<<(S + 255) / 256, 256, 0, s>>>(in, S, flags, dpos, start, n_copies, out);
+  return cudaGetLastError();
+}
+
+// The brood offsets k_replicate reads, for a bank sorted by brood that did not come from this
+// handle's gen loop: start[b] = the first index whose brood exceeds b, b = 0..nb (a lower-bound
+// search per entry).
+__global__ void k_brood_starts(const int* brood, int S, int nb, int* start) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += gridDim.x * blockDim.x) {
+    int lo = 0, hi = S;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (brood[mid] <= b) lo = mid + 1;
+      else hi = mid;
+    }
+    start[b] = lo;
+  }
+}
+cudaError_t launch_brood_starts(const int* brood, int S, int nb, int* start, cudaStream_t s) {
+  k_brood_starts<<<(nb + 1 + 255) / 256, 256, 0, s>>>(brood, S, nb, start);
   return cudaGetLastError();
 }
 

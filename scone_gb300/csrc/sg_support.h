@@ -40,6 +40,7 @@ cudaError_t launch_compact(const DBank& in, int S, const int* flags, const int* 
                            cudaStream_t s);
 cudaError_t launch_replicate(const DBank& in, int S, const int* flags, const int* dpos, const int* start,
                              int n_copies, const DBank& out, cudaStream_t s);
+cudaError_t launch_brood_starts(const int* brood, int S, int nb, int* start, cudaStream_t s);
 
 struct TallyCloseArgs {
   double* acc;

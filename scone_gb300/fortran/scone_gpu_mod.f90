@@ -337,7 +337,8 @@ module scone_gpu_mod
       integer(c_int32_t) :: sg_eigen_cycle
     end function sg_eigen_cycle
 
-    function sg_eigen_cycle_bank(h, admin, atch, in, pop, master_state, k_eff, k_end, out, stats) bind(C, name="sg_eigen_cycle_bank")
+    function sg_eigen_cycle_bank(h, admin, atch, in, pop, master_state, k_eff, k_end, out, stats) &
+        bind(C, name="sg_eigen_cycle_bank")
       import
       type(c_ptr), value :: h
       integer(c_int32_t), value :: admin
@@ -390,7 +391,42 @@ module scone_gpu_mod
       integer(c_int32_t) :: sg_fixed_source_cycle_shard
     end function sg_fixed_source_cycle_shard
 
-    function sg_transport_bank_noalloc(h, admin, dev_in, n, master_state, k_eff, dev_next, next_cap, n_next) bind(C, name="sg_transport_bank_noalloc")
+    function sg_normalise_shard(h, sites, n, sites_before, tot_sites, tot_pop, master_state, out, out_cap, n_out) &
+        bind(C, name="sg_normalise_shard")
+      import
+      type(c_ptr), value :: h
+      type(sg_bank), intent(in) :: sites
+      integer(c_int32_t), value :: n
+      integer(c_int64_t), value :: sites_before
+      integer(c_int64_t), value :: tot_sites
+      integer(c_int32_t), value :: tot_pop
+      integer(c_int64_t), value :: master_state
+      type(sg_bank), intent(inout) :: out
+      integer(c_int32_t), value :: out_cap
+      integer(c_int32_t), intent(inout) :: n_out
+      integer(c_int32_t) :: sg_normalise_shard
+    end function sg_normalise_shard
+
+    function sg_tally_get_scores(h, admin, scores, n_bins) bind(C, name="sg_tally_get_scores")
+      import
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: admin
+      real(c_double), dimension(*), intent(inout) :: scores
+      integer(c_int64_t), value :: n_bins
+      integer(c_int32_t) :: sg_tally_get_scores
+    end function sg_tally_get_scores
+
+    function sg_tally_set_scores(h, admin, scores, n_bins) bind(C, name="sg_tally_set_scores")
+      import
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: admin
+      real(c_double), dimension(*), intent(in) :: scores
+      integer(c_int64_t), value :: n_bins
+      integer(c_int32_t) :: sg_tally_set_scores
+    end function sg_tally_set_scores
+
+    function sg_transport_bank_noalloc(h, admin, dev_in, n, master_state, k_eff, dev_next, next_cap, n_next) &
+        bind(C, name="sg_transport_bank_noalloc")
       import
       type(c_ptr), value :: h
       integer(c_int32_t), value :: admin

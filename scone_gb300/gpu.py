@@ -53,6 +53,8 @@ def load(build=True):
                                       P(abi.CycleStats)]),
         "sg_fixed_source_cycle": (i32, [vp, i32, i32, P(u64), P(abi.CycleStats)]),
         "sg_fixed_source_cycle_shard": (i32, [vp, i32, i32, i32, P(u64), P(abi.CycleStats)]),
+        "sg_normalise_shard": (i32, [vp, P(abi.Bank), i32, i64, i64, i32, u64, P(abi.Bank), i32, P(i32)]),
+        "sg_tally_get_scores": (i32, [vp, i32, P(f64), i64]), "sg_tally_set_scores": (i32, [vp, i32, P(f64), i64]),
         "sg_set_file_source": (i32, [vp, P(abi.Bank), i32]),
         "sg_bank_write_file": (i32, [C.c_char_p, P(abi.Bank), i32, i32]),
         "sg_bank_count_file": (i32, [C.c_char_p, i32, P(i64)]),
@@ -185,6 +187,32 @@ class TransportOperatorGPU:
         out = np.zeros(3 * max(n.value, 1))
         self._check(self.L.sg_get_bins(self.h, admin, out.ctypes.data_as(C.POINTER(C.c_double)), n.value))
         return out[:3 * n.value].reshape(3, n.value).T.copy()
+
+    def normalise_shard(self, sites, n, before, tot_sites, tot_pop, master, cap):
+        """This process's part of normSize_Repr over a population split over processes
+        (sg_normalise_shard): returns (bank, n_out)."""
+        out = abi.HostBank(max(cap, 1))
+        m = C.c_int32()
+        self._check(self.L.sg_normalise_shard(self.h, C.byref(sites.struct), n, before, tot_sites, tot_pop,
+                                                C.c_uint64(master), C.byref(out.struct), cap, C.byref(m)))
+        return out, m.value
+
+    def _tally_n(self, admin):
+        n = C.c_int64()
+        self._check(self.L.sg_tally_size(self.h, admin, C.byref(n)))
+        return n.value
+
+    def get_scores(self, admin):
+        """The running-batch scores of an admin (summed over processes for a synchronised tally)."""
+        out = np.zeros(max(self._tally_n(admin), 1))
+        self._check(self.L.sg_tally_get_scores(self.h, admin, out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out[:self._tally_n(admin)].copy()
+
+    def set_scores(self, admin, scores):
+        s = np.ascontiguousarray(scores, dtype=np.float64)
+        if s.size < self._tally_n(admin):
+            raise ValueError("set_scores: fewer values than the tally has bins")
+        self._check(self.L.sg_tally_set_scores(self.h, admin, s.ctypes.data_as(C.POINTER(C.c_double)), s.size))
 
     def keff(self, admin):
         k, s = C.c_double(), C.c_double()

@@ -98,7 +98,7 @@ def header_prototypes():
 
 
 def fortran_interfaces():
-    text = open(MOD).read()
+    text = re.sub(r"&[ \t]*\n[ \t]*", "", open(MOD).read())        # join continued lines
     out = {}
     for name, args, body in re.findall(r'function (sg_\w+)\(([^)]*)\) bind\(C, name="\1"\)\n(.*?)end function \1', text, re.S):
         names = [a.strip() for a in args.split(",") if a.strip()]
@@ -140,3 +140,10 @@ def test_every_entry_point_has_a_matching_interface():
                 assert spec.startswith(C2F[ty]) and "value" not in spec, (name, spec)   # by reference
             else:
                 assert spec == f"{C2F[ty]}, value", (name, spec)
+
+
+def test_fortran_lines_fit_free_form():
+    """Free-form Fortran allows 132 characters a line (gfortran's default)."""
+    for path in (MOD, os.path.join(os.path.dirname(MOD), "transportOperatorGPU_class.f90")):
+        for i, line in enumerate(open(path).read().splitlines(), 1):
+            assert len(line) <= 132, (os.path.basename(path), i, len(line))

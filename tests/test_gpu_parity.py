@@ -153,7 +153,10 @@ def test_lattice_mixed_vs_fp64_statistics(gpu_mod, form, transport):
     v32 = (b32[:, 2] / n - m32 ** 2) / (n - 1)
     ok = (v64 + v32) > 0
     z = (m64[ok] - m32[ok]) / np.sqrt(v64[ok] + v32[ok])
-    assert abs(z.mean()) < 0.2 and z.std() < 1.3, (z.mean(), z.std())
+    # the variances come from consecutive cycles, whose fission sources are correlated (strongly in
+    # this reflective lattice), so they understate the true variance and z spreads wider than 1 for
+    # equal distributions; a bias shows in the mean
+    assert abs(z.mean()) < 0.2 and z.std() < 1.6, (z.mean(), z.std())
 
 
 @pytest.mark.parametrize("form", FORMS)
@@ -671,3 +674,28 @@ def test_transport_bank_reads_page_locked_banks_in_place(gpu_mod, oracle_mod):
     for k in ("G", "brood_id", "wgt", "r", "dir", "time"):
         assert np.array_equal(b0[k], b1[k]), k
     np.testing.assert_allclose(t1, t0, rtol=1e-10, atol=1e-300)
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("form,transport", [(abi.FORM_HISTORY, abi.TRANSPORT_DT), (abi.FORM_HISTORY, abi.TRANSPORT_ST),
+                                            (abi.FORM_HISTORY, abi.TRANSPORT_HT), (abi.FORM_EVENT, abi.TRANSPORT_DT)])
+def test_reflective_box_never_leaks(gpu_mod, precision, form, transport):
+    """The 17x17 lattice sits in an all-reflective box, so no history may end as a leak: the
+    k-implicit clerk's leakage bin stays exactly zero over 1e6 histories.  (Delta-tracking flights
+    that leave the box are brought back by the transform BC; a transform that also reflected a
+    coordinate lying just inside another face would leave the point outside, which the mixed form
+    then scored as a leak about once per 1e5 histories.)"""
+    p = problems.lattice_17x17_7g()
+    n = 1000000
+    t = gpu_mod.TransportOperatorGPU(p, precision=precision, transport=transport, max_bank=1 << 21, form=form)
+    t.eigen_init(n, SEED)
+    bank, pop = t.eigen_bank(n)
+    assert pop == n
+    a = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+    nxt, st = t.transport_bank(a, bank, 8675309, k_eff=1.08, next_cap=1 << 21)
+    assert st.n_next > 0.9 * n
+    t.tally_cycle_end(a, float(st.n_next), 1.08)
+    b = t.bins(a)
+    assert b[3, 1] == 0.0, b[:, 1]                        # bins: prod, scatter prod, abs, leak, k
+    assert b[2, 1] > 0.0
+    t.close()
