@@ -699,3 +699,42 @@ def test_reflective_box_never_leaks(gpu_mod, precision, form, transport):
     assert b[3, 1] == 0.0, b[:, 1]                        # bins: prod, scatter prod, abs, leak, k
     assert b[2, 1] > 0.0
     t.close()
+
+
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_DT, abi.TRANSPORT_ST])
+def test_lattice_mixed_k_unbiased_correlated(gpu_mod, transport):
+    """Correlated sampling: both precision forms transport the same converged 1e6 bank with the
+    same RNG streams, cycle after cycle, so most histories follow the same path and k_mixed - k_FP64
+    has a standard error of a few 1e-7: a bias of the mixed form shows far below the statistical
+    error of either k.  (A boundary transform that leaked a few histories per 1e5 moved it by
+    -1.6e-5.)"""
+    p = problems.lattice_17x17_7g()
+    pop = 1000000
+    ops = {prec: gpu_mod.TransportOperatorGPU(p, precision=prec, transport=transport, max_bank=3 * pop,
+                                              form=abi.FORM_HISTORY)
+           for prec in (abi.PREC_FP64, abi.PREC_MIXED)}
+    fp = ops[abi.PREC_FP64]
+    inact = fp.upload_tally([])
+    ia = fp.upload_tally([abi.clerk(abi.CLERK_KEFF_ANALOG)])
+    fp.attach_tally(inact, ia)
+    fp.eigen_init(pop, SEED)
+    for _ in range(20):
+        fp.eigen_cycle(inact, ia)
+    bank, n = fp.eigen_bank(pop)
+    k0 = fp.eigen_state()[1]
+    dk = []
+    for c in range(8):
+        ks = {}
+        for prec, t in ops.items():
+            a = t.upload_tally([abi.clerk(abi.CLERK_KEFF_IMPLICIT)])
+            _, st = t.transport_bank(a, bank, 1000003 * (c + 1), k_eff=k0, next_cap=3 * pop)
+            t.tally_cycle_end(a, float(st.n_next), k0)
+            b = t.bins(a)
+            assert b[3, 1] == 0.0                               # no leakage from a reflective box
+            ks[prec] = b[4, 1]
+        dk.append(ks[abi.PREC_MIXED] - ks[abi.PREC_FP64])
+    dk = np.array(dk)
+    se = dk.std(ddof=1) / np.sqrt(len(dk))
+    assert abs(dk.mean()) < 4.0 * se + 2e-6, (dk.mean(), se)
+    for t in ops.values():
+        t.close()
