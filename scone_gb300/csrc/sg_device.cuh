@@ -4,13 +4,14 @@
 //   R = double : all-FP64 verification form.  Compiled with -fmad=false so every multiply and add is
 //                rounded separately, in SCONE's operation order; per-history results then match the
 //                CPU restatement exactly (collision counts, end-of-history RNG states, bin indices).
-//   R = float  : mixed form.  Cross sections, distances, sampling and direction arithmetic in FP32;
-//                positions (every level), the surface-coincidence tests, tally sums and k in FP64.
-//                Geometric tolerances are widened to the FP32 distance accuracy (see Tol<float>).
+//   R = float  : mixed form.  Cross sections, distances, sampling, directions and the coordinates
+//                below the root (local to their universe) in FP32; the global position, the tests
+//                against root-level surfaces, tally sums and k in FP64.  Geometric tolerances are
+//                widened to the FP32 distance accuracy (see Tol<float> and the host's surface records).
 //
 // Data layout in HBM (all flat, read-only during a launch, resident across cycles):
-//   surfaces  DSurf[n]           64 B records (type, bc, params, tolerance)
-//   universes DUni[n]            128 B records; pin radii, cell lists and the geometry graph are
+//   surfaces  DSurf[n]           136 B records (type, axes, bc, FP64 params and tolerance, FP32 copies)
+//   universes DUni[n]            208 B records; pin radii, cell lists and the geometry graph are
 //                                separate int/double arrays indexed from the record
 //   MG data   [mat][G] SoA arrays of R, P0/prod as [mat][Gin][Gout]
 //   banks     SoA: r (3 x FP64), dir (3 x FP64), wgt, G, brood -- see sg_internal.h
