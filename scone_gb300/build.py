@@ -28,7 +28,7 @@ UNITS = [(u.replace(".cu", ""), u, ["-fmad=false"])
 for _op in ("st", "dt", "ht"):
     for _prec, _R, _fl in (("fp64", "double", ["-fmad=false"]), ("mixed", "float", [])):
         for _data, _ce in (("mg", 0), ("ce", 1)):
-            for _part in range(6):
+            for _part in range(9 if _ce == 0 else 6):    # 6-8: the lean history loop, multigroup only
                 UNITS.append((f"sg_tr_{_data}_{_prec}_{_op}_p{_part}", "sg_tr_unit.cu",
                               _fl + [f"-DSG_R={_R}", f"-DSG_CE={_ce}", f"-DSG_OP=OP_{_op.upper()}",
                                      f"-DSG_PART={_part}"]))

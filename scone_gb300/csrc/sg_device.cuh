@@ -459,10 +459,12 @@ __device__ __noinline__ Vec3<T> rot_vec(const T* m, T x, T y, T z) {
   return Vec3<T>{m[0] * x + m[1] * y + m[2] * z, m[3] * x + m[4] * y + m[5] * z, m[6] * x + m[7] * y + m[8] * z};
 }
 
-template <class R, int MAXL>
+// LEAN: compiled for geometries without rotated universes (the rotation code is left out).
+template <class R, int MAXL, bool LEAN = false>
 struct Geom {
   const DGeom& g;
   __device__ __forceinline__ explicit Geom(const DGeom& gg) : g(gg) {}
+  __device__ __forceinline__ bool rotated() const { return !LEAN && g.rot != nullptr; }
 
   template <class T> __device__ __forceinline__ const T* rotm(int u) const {
     if constexpr (sizeof(T) == 8) return g.rot + 9 * u;
@@ -472,7 +474,7 @@ struct Geom {
   // rotated universe entered on levels 1..l
   __device__ __forceinline__ void level_dir(const Coords<R, MAXL>& c, int l, R d[3]) const {
     d[0] = c.u[0]; d[1] = c.u[1]; d[2] = c.u[2];
-    if (!g.rot) return;
+    if (!rotated()) return;
 #pragma unroll
     for (int j = 1; j < MAXL; ++j) {
       if (j > l) break;
@@ -713,7 +715,7 @@ struct Geom {
     double off[3];
     cell_offset<double>(c.uni[0], c.local[0], off);
     double t[3] = {c.r0[0] - off[0], c.r0[1] - off[1], c.r0[2] - off[2]};
-    if (g.rot && N.rot) {
+    if (rotated() && N.rot) {
       const Vec3<double> v = rot_vec<double>(rotm<double>(nu), t[0], t[1], t[2]);
       t[0] = v.x; t[1] = v.y; t[2] = v.z;
     }
@@ -763,7 +765,7 @@ struct Geom {
         R t[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) t[k] = c.rl[i > 0 ? i - 1 : 0][k] - off[k];
-        if (g.rot && N.rot) {
+        if (rotated() && N.rot) {
           const Vec3<R> v = rot_vec<R>(rotm<R>(nu), t[0], t[1], t[2]);
           t[0] = v.x; t[1] = v.y; t[2] = v.z;
         }
@@ -836,7 +838,7 @@ struct Geom {
 #pragma unroll
     for (int l = 1; l < MAXL; ++l)
       if (l < n) {
-        if (g.rot && g.unis[c.uni[l]].rot) {          // this level's direction (rotated universe)
+        if (rotated() && g.unis[c.uni[l]].rot) {          // this level's direction (rotated universe)
           const Vec3<R> t = rot_vec<R>(rotm<R>(c.uni[l]), v[0], v[1], v[2]);
           v[0] = t.x; v[1] = t.y; v[2] = t.z;
         }

@@ -1046,6 +1046,14 @@ int build_clerks(sg_handle h, int a, TransportArgs<R>& t, long long& lo, long lo
   return SG_OK;
 }
 
+// Whether a launch can run the lean history loop: multigroup data and none of rotated universes,
+// cell maps, surface-current clerks, neutronMGimp or P1 scattering.
+template <class R>
+bool lean_launch(sg_handle h, const TransportArgs<R>& t) {
+  return !h->hasCE && t.geom.rot == nullptr && !t.has_cellmap && !t.has_current && !t.coll_imp &&
+         t.mg.P1n == nullptr;
+}
+
 // The gen loop over `n` histories of bank `in` on the device; fission sites are written into bank
 // `out` in brood order.  Returns SG_OK and the number of sites.
 template <class R>
@@ -1082,6 +1090,7 @@ int gen_loop_t(sg_handle h, int admin, DBank in, int n, unsigned long long maste
   t.use_cache = transport_cache(h->cfg.transport);
   t.max_segments = 1000000;
   t.ht_cutoff = (R)h->htCutoff;
+  t.lean = lean_launch(h, t) ? 1 : 0;
   CK(cudaMemsetAsync(h->ctr.p, 0, sizeof(DCounters), s));
   CK(cudaMemsetAsync(h->sCursor.p, 0, SITE_REGIONS * sizeof(int), s));
   CK(cudaMemsetAsync(h->histN.p, 0, (size_t)(n + 1) * sizeof(int), s));
@@ -1490,6 +1499,8 @@ int sg::noalloc_view(sg_handle h, int admin, NoAllocView* v, TransportArgs<doubl
   t64->coll_imp = t32->coll_imp = h->collImp ? 1 : 0;
   t64->coll = h->collImp ? h->dColl64.p : nullptr;
   t32->coll = h->collImp ? h->dColl32.p : nullptr;
+  t64->lean = lean_launch(h, *t64) ? 1 : 0;
+  t32->lean = lean_launch(h, *t32) ? 1 : 0;
   return SG_OK;
 }
 

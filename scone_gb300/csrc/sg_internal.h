@@ -277,6 +277,8 @@ struct TransportArgs {
   DQueues q;            // event form: queues of the launch
   int coll_imp;         // 1: neutronMGimp / neutronCEimp with *coll
   const DColl<R>* coll;
+  int lean;             // 1: no rotated universe, cell map, current clerk, coll_imp or P1 scattering
+                        // (multigroup): the history loop runs its lean instantiation
 };
 
 // Where the history loop scores map clerks.  Few bins: a block-local copy of score memory in shared

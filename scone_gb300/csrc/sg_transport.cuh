@@ -84,10 +84,13 @@ __device__ __forceinline__ unsigned long long rng_jump(const RngJump& J, int off
   return (J.a[off] * s + J.c[off]) & RNG_MASK;
 }
 
-template <class R, int MAXL, int OP, bool CE>
+// LEAN: the history loop compiled for launches without rotated universes, cell maps, surface-current
+// clerks, neutronMGimp / neutronCEimp or P1 scattering (TransportArgs::lean): their uniform branches
+// are left out, which shortens the loop the instruction caches have to hold.
+template <class R, int MAXL, int OP, bool CE, bool LEAN = false>
 struct Tracker {
   const TransportArgs<R>& A;
-  const Geom<R, MAXL> geom;
+  const Geom<R, MAXL, LEAN> geom;
   const DMG<R>& mg;
   const DCE<R>& ce;
   double* acc;
@@ -123,6 +126,10 @@ struct Tracker {
   int nbuf;          // split particles of this history waiting in the buffer
   bool htDT;         // hybrid tracking: the current transit uses delta tracking
   bool onSurf;       // the particle reached its position by a surface crossing or boundary hit
+
+  __device__ __forceinline__ bool imp() const { return !LEAN && A.coll_imp; }
+  __device__ __forceinline__ bool current() const { return !LEAN && A.has_current; }
+  __device__ __forceinline__ bool cellmap() const { return !LEAN && A.has_cellmap; }
 
   __device__ __forceinline__ Tracker(const TransportArgs<R>& a, double* accp)
       : A(a), geom(a.geom), mg(a.mg), ce(a.ce), acc(accp) {
@@ -251,7 +258,7 @@ struct Tracker {
   // keffImplicitClerk (keffImplicitClerk_class.f90:180-227)
   // invTrack = 1 / trackXS: the mixed form multiplies by it; the FP64 form divides, as SCONE does
   __device__ __forceinline__ void report_in_coll(bool virt, R trackXS, R invTrack) {
-    const int cell = A.has_cellmap ? lowest_cell() : 0;
+    const int cell = cellmap() ? lowest_cell() : 0;
     R fluxTrack;                                       // collision estimator with handleVirtual
     if constexpr (sizeof(R) == 4) fluxTrack = w * invTrack;
     else fluxTrack = w / trackXS;
@@ -376,7 +383,7 @@ struct Tracker {
     x = x - mcap;
     if (x > R(0)) C = C + 1;
     report_in_coll(false, trackXS, R(1) / trackXS);
-    if (A.coll_imp && A.coll->imp_abs) {                 // neutronCEimp implicit (:406-424)
+    if (imp() && A.coll->imp_abs) {                 // neutronCEimp implicit (:406-424)
       const R scat = mel + min_;
       w = w * scat / mt;
       C = (rng.get() < mel / scat) ? 1 : 2;
@@ -440,7 +447,7 @@ struct Tracker {
     } else {
       dead = true;                                       // capture / fission
     }
-    if (A.coll_imp) dead = imp_cutoffs(dead);
+    if (imp()) dead = imp_cutoffs(dead);
     else if (E < ce.minE) dead = true;                   // cutoffs (:434-444)
     collN += 1;
     nColl += 1;
@@ -603,7 +610,7 @@ struct Tracker {
       }
       if (go > mg.nG) go = walk_failed(row, 1);
       R mu;                                              // multiScatterP1MG%sampleOut (:69-85)
-      if (mg.P1n) mu = sample_legendre_p1<R>(mg.P1n[(long long)k * mg.nG + (go - 1)], rng);
+      if (!LEAN && mg.P1n) mu = sample_legendre_p1<R>(mg.P1n[(long long)k * mg.nG + (go - 1)], rng);
       else mu = R(2) * rng.get() - R(1);
       R sp, cp;
       sincos_phi<R>(rng.get(), sp, cp);
@@ -617,7 +624,7 @@ struct Tracker {
       MT = (C == 3) ? MT_DISAP : MT_FISSION;
       dead = true;
     }
-    if (A.coll_imp) dead = imp_cutoffs(dead);            // neutronMGimp cutoffs (:319-351)
+    if (imp()) dead = imp_cutoffs(dead);            // neutronMGimp cutoffs (:319-351)
     collN += 1;
     nColl += 1;
     if (A.keff_clerk >= 0 && MT == MT_IESCATTER) {       // keffImplicit reportOutColl (:241-268)
@@ -706,7 +713,7 @@ struct Tracker {
       const double rpre[3] = {c.r0[0], c.r0[1], c.r0[2]};
       const R u0[3] = {c.u[0], c.u[1], c.u[2]};
       const int matPre = mat;
-      const int cellPre = A.has_cellmap ? lowest_cell() : 0;
+      const int cellPre = cellmap() ? lowest_cell() : 0;
       const int ev = geom.move(c, dist, cdist, csurf, cache, A.use_cache != 0, onSurf);
       onSurf = (ev != 1);                                // a crossing or boundary hit leaves it on a surface
       if constexpr (CE) time = time + dist * invSpeed;
@@ -714,7 +721,7 @@ struct Tracker {
       nEv += 1;
       report_path(rpre, matPre, cellPre, dist);
       mat = c.mat;
-      if (A.has_current) report_current(rpre, matPre, cellPre, u0, mat == 0);
+      if (current()) report_current(rpre, matPre, cellPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
         raise_error(A.ctr, mat == SG_UNDEF_MAT ? SG_ERR_UNDEF_MAT : SG_ERR_OVERLAP, hist);
@@ -742,19 +749,19 @@ struct Tracker {
       const R dist = -dlog<R>(rng.get()) * majInv;
       double rpre[3];
       R u0[3];
-      if (A.has_current) {
+      if (current()) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) { rpre[i] = c.r0[i]; u0[i] = c.u[i]; }
       }
       const int matPre = mat;
-      const int cellPre = (A.has_cellmap && A.has_current) ? lowest_cell() : 0;
+      const int cellPre = (cellmap() && current()) ? lowest_cell() : 0;
       onSurf = false;
       if (!geom.teleport(c, dist)) { raise_error(A.ctr, SG_ERR_UNDEF_MAT, hist); return SEG_END; }
       if constexpr (CE) time = time + dist * invSpeed;
       else time = time + dist;
       nEv += 1;
       mat = c.mat;
-      if (A.has_current) report_current(rpre, matPre, cellPre, u0, mat == 0);
+      if (current()) report_current(rpre, matPre, cellPre, u0, mat == 0);
       if (mat == 0) { leak(); return SEG_END; }
       if (mat == SG_VOID_MAT) { report_in_coll(true, maj, majInv); return SEG_MORE; }
       if (mat == SG_UNDEF_MAT || mat == SG_OVERLAP_MAT) {
@@ -851,8 +858,8 @@ struct Tracker {
 
 
 // k-implicit partial sums and event counters of a warp, reduced and added to global memory
-template <class R, int MAXL, int OP, bool CE>
-__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, OP, CE>& T, const TransportArgs<R>& A, int lane) {
+template <class R, int MAXL, int OP, bool CE, bool LEAN>
+__device__ __forceinline__ void flush_counters(Tracker<R, MAXL, OP, CE, LEAN>& T, const TransportArgs<R>& A, int lane) {
   if (A.keff_clerk >= 0) {
     double v[4] = {(double)T.kprod, (double)T.kscat, (double)T.kabs, (double)T.kleak};
 #pragma unroll
@@ -893,7 +900,7 @@ __device__ __forceinline__ int warp_append(int* counter) {
 template <class R, bool CE, int OP>
 constexpr int history_min_blocks() { return (CE || OP != OP_DT) ? 0 : (sizeof(R) == 4 ? 7 : 6); }
 
-template <class R, int MAXL, int OP, bool CE>
+template <class R, int MAXL, int OP, bool CE, bool LEAN = false>
 __global__ void __launch_bounds__(128, (history_min_blocks<R, CE, OP>())) k_transport(const __grid_constant__ TransportArgs<R> A) {
   extern __shared__ double s_acc[];
   __shared__ RngJump s_jump;
@@ -902,7 +909,7 @@ __global__ void __launch_bounds__(128, (history_min_blocks<R, CE, OP>())) k_tran
     for (int i = threadIdx.x; i < A.acc_n; i += blockDim.x) s_acc[i] = 0.0;
   rng_jump_table(s_jump);
   __syncthreads();
-  Tracker<R, MAXL, OP, CE> T(A, smem ? s_acc : A.acc);
+  Tracker<R, MAXL, OP, CE, LEAN> T(A, smem ? s_acc : A.acc);
   const int lane = threadIdx.x & 31;
   bool alive = false, done = false;
   int q_next = 0, q_end = 0;   // warp-uniform range of histories taken from the global counter
@@ -953,7 +960,7 @@ __global__ void __launch_bounds__(128, (history_min_blocks<R, CE, OP>())) k_tran
       if (!ended) T.select_ht();
     }
     if (ended) {
-      if (T.nbuf > 0) T.release();                      // the history's split particles, LIFO
+      if (!LEAN && T.nbuf > 0) T.release();             // the history's split particles, LIFO
       else { T.finish(); alive = false; }
     }
   }
