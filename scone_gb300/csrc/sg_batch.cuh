@@ -52,8 +52,8 @@ __device__ __forceinline__ bool stage_problem_warp(BatchProblem<R>* dst, const B
 // as thisCycle%copy + placeCoord would leave it.
 // s_src / s_tr: the source and transport RNG states of this history, master_c + stride(n) and
 // master_c + stride(pop + n)
-template <class R, int MAXL, int OP>
-__device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, const BatchProblem<R>& P, int f,
+template <class R, int MAXL, int OP, bool LEAN>
+__device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false, LEAN>& T, const BatchProblem<R>& P, int f,
                                               unsigned long long s_src, unsigned long long s_tr) {
   const int c = f / P.pop;
   const int n = f - c * P.pop + 1;
@@ -99,7 +99,9 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false>& T, co
   T.select_ht();
 }
 
-template <class R, int MAXL, int OP>
+// LEAN: every problem of the launch runs without rotated universes, cell maps, current clerks or P1
+// scattering (BatchLaunch::lean), so the lean Tracker is compiled
+template <class R, int MAXL, int OP, bool LEAN = false>
 __global__ void __launch_bounds__(128, (history_min_blocks<R, false, OP>())) k_batch(const __grid_constant__ BatchLaunch L) {
   __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
   __shared__ __align__(8) unsigned long long s_bar[BATCH_MAX_WARPS];
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(128, (history_min_blocks<R, false, OP>())) k_b
     P.t.acc = nullptr;
   }
   __syncwarp();
-  Tracker<R, MAXL, OP, false> T(P.t, nullptr);
+  Tracker<R, MAXL, OP, false, LEAN> T(P.t, nullptr);
   const int nItems = *L.n_items;
   int cur = -1;                     // slot of the staged problem (warp-uniform)
   int pend = -1;                    // claimed item of another problem, waiting for the warp to drain
@@ -204,7 +206,8 @@ __global__ void __launch_bounds__(128, (history_min_blocks<R, false, OP>())) k_b
 namespace sg {
 
 template <class R, int OP>
-const void* batch_kernel_ptr(int maxl) {
+const void* batch_kernel_ptr(int maxl, bool lean) {
+  if (lean) return maxl <= 2 ? (const void*)k_batch<R, 2, OP, true> : (const void*)k_batch<R, 4, OP, true>;
   return maxl <= 2 ? (const void*)k_batch<R, 2, OP> : (const void*)k_batch<R, 4, OP>;
 }
 
@@ -213,13 +216,13 @@ template <class R, int OP>
 cudaError_t launch_batch_unit(const BatchLaunch& L, int grid, int block, cudaStream_t s) {
   if (block < 32 || block > 32 * BATCH_MAX_WARPS || block % 32) return cudaErrorInvalidValue;
   void* args[] = {(void*)&L};
-  return cudaLaunchKernel(batch_kernel_ptr<R, OP>(L.maxl), dim3(grid), dim3(block), args, 0, s);
+  return cudaLaunchKernel(batch_kernel_ptr<R, OP>(L.maxl, L.lean != 0), dim3(grid), dim3(block), args, 0, s);
 }
 
 template <class R, int OP>
-int batch_occupancy_unit(int maxl, int block) {
+int batch_occupancy_unit(int maxl, bool lean, int block) {
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel_ptr<R, OP>(maxl), block, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel_ptr<R, OP>(maxl, lean), block, 0) != cudaSuccess)
     return 1;
   return per < 1 ? 1 : per;
 }

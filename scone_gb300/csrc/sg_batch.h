@@ -57,13 +57,14 @@ struct BatchLaunch {
   DCounters* ctr;
   const double* k_one;          // 1.0: the k of fixed-source collisions
   int maxl;
+  int lean;                     // 1: every problem of the launch can run the lean history loop
 };
 
 // the batched kernel for precision R and transport operator OP (one translation unit each)
 template <class R, int OP>
 cudaError_t launch_batch_op(const BatchLaunch& L, int grid, int block, cudaStream_t s);
 template <class R, int OP>
-int batch_occupancy_op(int maxl, int block);
+int batch_occupancy_op(int maxl, int lean, int block);
 
 template <class R>
 inline cudaError_t launch_batch(const BatchLaunch& L, int op, int grid, int block, cudaStream_t s) {
@@ -72,10 +73,10 @@ inline cudaError_t launch_batch(const BatchLaunch& L, int op, int grid, int bloc
   return launch_batch_op<R, OP_ST>(L, grid, block, s);
 }
 template <class R>
-inline int batch_occupancy(int maxl, int op, int block) {
-  if (op == OP_DT) return batch_occupancy_op<R, OP_DT>(maxl, block);
-  if (op == OP_HT) return batch_occupancy_op<R, OP_HT>(maxl, block);
-  return batch_occupancy_op<R, OP_ST>(maxl, block);
+inline int batch_occupancy(int maxl, int lean, int op, int block) {
+  if (op == OP_DT) return batch_occupancy_op<R, OP_DT>(maxl, lean, block);
+  if (op == OP_HT) return batch_occupancy_op<R, OP_HT>(maxl, lean, block);
+  return batch_occupancy_op<R, OP_ST>(maxl, lean, block);
 }
 
 // scoreMemory%closeCycle for every cycle of the listed problems, in cycle order (sg_batch_host.cu)

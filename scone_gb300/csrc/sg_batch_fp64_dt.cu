@@ -8,5 +8,7 @@ cudaError_t launch_batch_op<double, OP_DT>(const BatchLaunch& L, int grid, int b
   return launch_batch_unit<double, OP_DT>(L, grid, block, s);
 }
 template <>
-int batch_occupancy_op<double, OP_DT>(int maxl, int block) { return batch_occupancy_unit<double, OP_DT>(maxl, block); }
+int batch_occupancy_op<double, OP_DT>(int maxl, int lean, int block) {
+  return batch_occupancy_unit<double, OP_DT>(maxl, lean != 0, block);
+}
 }  // namespace sg

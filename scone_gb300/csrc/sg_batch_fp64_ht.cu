@@ -8,5 +8,7 @@ cudaError_t launch_batch_op<double, OP_HT>(const BatchLaunch& L, int grid, int b
   return launch_batch_unit<double, OP_HT>(L, grid, block, s);
 }
 template <>
-int batch_occupancy_op<double, OP_HT>(int maxl, int block) { return batch_occupancy_unit<double, OP_HT>(maxl, block); }
+int batch_occupancy_op<double, OP_HT>(int maxl, int lean, int block) {
+  return batch_occupancy_unit<double, OP_HT>(maxl, lean != 0, block);
+}
 }  // namespace sg

@@ -144,7 +144,7 @@ struct sg_batch_t {
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t itemsCopy = nullptr, closeCopy = nullptr;
     sg_batch_tuning tune{};
-  } graph[2][2][2];               // [mirror][nesting class][SMs reserved for other streams]
+  } graph[2][4][2];               // [mirror][kernel class: nesting 2 or 4, + 2 lean][SMs reserved for other streams]
   int reserve = 0;                 // blocks per SM the serving waves leave to other streams' kernels
   int reserving = 0;               // reserve in force (serving with other work on the device)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -223,10 +223,17 @@ int check_slot(sg_batch b, int slot) {
   return SG_OK;
 }
 
-int grid_for(sg_batch b, int maxl) {
+// Whether a problem can run the lean history loop: no rotated universe, cell map, surface-current
+// clerk or P1 scattering (the batched form runs the standard collision processors).
+bool slot_lean(const Slot& S) {
+  const auto& t = S.sp.t64;
+  return t.geom.rot == nullptr && !t.has_cellmap && !t.has_current && !t.coll_imp && t.mg.P1n == nullptr;
+}
+
+int grid_for(sg_batch b, int maxl, int lean) {
   const int dt = transport_op(b->cfg.transport);
-  const int occ = fp64(b) ? batch_occupancy<double>(maxl, dt, b->tune.block_threads)
-                          : batch_occupancy<float>(maxl, dt, b->tune.block_threads);
+  const int occ = fp64(b) ? batch_occupancy<double>(maxl, lean, dt, b->tune.block_threads)
+                          : batch_occupancy<float>(maxl, lean, dt, b->tune.block_threads);
   int per = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, occ) : occ;
   if (b->reserving) per -= b->reserve;
   return b->sms * std::max(per, 1);
@@ -238,7 +245,8 @@ void drop_graph(sg_batch_t::Graph& G) {
   G = sg_batch_t::Graph();
 }
 
-// The transport graph of mirror set m and nesting class x (0: maxl 2, 1: maxl 4): copies of the
+// The transport graph of mirror set m and kernel class x (bit 0: maxl 4 instead of 2; bit 1: the
+// lean history loop, for launches whose problems all allow it): copies of the
 // work list, the count block and the close list from pinned memory, counter reset and the batched
 // kernel.  The two list copies are resized to the current counts before each launch; the kernels
 // read the counts from device memory.  The cycle closes run after it (run_closes).
@@ -248,7 +256,8 @@ int build_graph(sg_batch b, int m, int x) {
     if (std::memcmp(&G.tune, &b->tune, sizeof(G.tune)) == 0) return SG_OK;
     drop_graph(G);
   }
-  const int maxl = x ? 4 : 2;
+  const int maxl = (x & 1) ? 4 : 2;
+  const int lean = x >> 1;
   cudaStream_t s = b->stream;
   const int dt = transport_op(b->cfg.transport);
   BatchLaunch L;
@@ -259,7 +268,8 @@ int build_graph(sg_batch b, int m, int x) {
   L.ctr = b->dCtr[m];
   L.k_one = b->dOne;
   L.maxl = maxl;
-  const int grid = grid_for(b, maxl);
+  L.lean = lean;
+  const int grid = grid_for(b, maxl, lean);
   BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   auto step = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
@@ -362,8 +372,8 @@ int clear_tally(sg_batch b, int slot) {
 
 // launches the transport graph of mirror set m, for the items and closes written to that set, on
 // stream `s`
-int launch_graph(sg_batch b, int m, int maxl, cudaStream_t s) {
-  const int x = maxl > 2 ? 1 : 0;
+int launch_graph(sg_batch b, int m, int maxl, bool lean, cudaStream_t s) {
+  const int x = (maxl > 2 ? 1 : 0) + (lean ? 2 : 0);
   int rc = build_graph(b, m, x);
   if (rc) return rc;
   sg_batch_t::Graph& G = b->graph[m][x][b->reserving];
@@ -627,6 +637,7 @@ int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats
   std::vector<int> order(slots, slots + n);
   std::vector<char> seen(b->slots.size(), 0);
   int maxl = 2;
+  bool lean = true;
   long long hist = 0;
   for (int s : order) {
     int rc = check_slot(b, s);
@@ -634,6 +645,7 @@ int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats
     if (seen[s]) return b->fail(SG_ERR_BAD_ARG, "batch: a slot is listed twice");
     seen[s] = 1;
     maxl = std::max(maxl, b->slots[s].sp.maxl);
+    lean = lean && slot_lean(b->slots[s]);
     hist += (long long)b->slots[s].pop * b->slots[s].cycles;
   }
   auto size_of = [&](int x) { return (long long)b->slots[x].pop * b->slots[x].cycles; };
@@ -657,7 +669,7 @@ int32_t sg_batch_run(sg_batch b, const int32_t* slots, int32_t n, sg_batch_stats
   b->hInts[m][3] = 0;
   for (int i = 0; i < n; ++i) b->hClose[m][i] = order[i];
   BCK(cudaEventRecord(b->ev[2], b->stream));
-  int rc = launch_graph(b, m, maxl, b->stream);
+  int rc = launch_graph(b, m, maxl, lean, b->stream);
   if (rc) return rc;
   rc = run_closes(b, m, b->stream);
   if (rc) return rc;
@@ -763,11 +775,14 @@ int32_t sg_batch_autotune(sg_batch b, const int32_t* slots, int32_t n, sg_batch_
     if (pass == 0) for (int v : items) { sg_batch_tuning t = cur; t.item_histories = v; cands.push_back(t); }
     if (pass == 1) for (int v : blocks) { sg_batch_tuning t = cur; t.block_threads = v; cands.push_back(t); }
     if (pass == 2) {
-      int maxl = 2;
-      for (int i = 0; i < n; ++i) maxl = std::max(maxl, b->slots[slots[i]].sp.maxl);
+      int maxl = 2, lean = 1;
+      for (int i = 0; i < n; ++i) {
+        maxl = std::max(maxl, b->slots[slots[i]].sp.maxl);
+        lean = lean && slot_lean(b->slots[slots[i]]);
+      }
       const int dt = transport_op(b->cfg.transport);
-      const int occ = fp64(b) ? batch_occupancy<double>(maxl, dt, cur.block_threads)
-                              : batch_occupancy<float>(maxl, dt, cur.block_threads);
+      const int occ = fp64(b) ? batch_occupancy<double>(maxl, lean, dt, cur.block_threads)
+                              : batch_occupancy<float>(maxl, lean, dt, cur.block_threads);
       for (int v = std::max(1, occ / 2); v <= occ; ++v) { sg_batch_tuning t = cur; t.blocks_per_sm = v; cands.push_back(t); }
     }
     if (pass == 3) for (int v = 0; v <= 2; ++v) { sg_batch_tuning t = cur; t.order = v; cands.push_back(t); }
@@ -963,6 +978,7 @@ int launch_wave(sg_batch b) {
   w.mirror = m;
   long long budget = b->waveHist;
   int maxl = 2;
+  bool lean = true;
   std::vector<long long> take(b->active.size(), 0);
   // water-filling of the budget over the remaining work of the active requests
   for (int round = 0; round < 8 && budget > 0; ++round) {
@@ -988,6 +1004,7 @@ int launch_wave(sg_batch b) {
       r.next += take[i];
       w.histories += take[i];
       maxl = std::max(maxl, b->slots[r.slot].sp.maxl);
+      lean = lean && slot_lean(b->slots[r.slot]);
     }
     if (r.next >= r.total) w.closing.push_back(r);
     else still.push_back(r);
@@ -1005,7 +1022,7 @@ int launch_wave(sg_batch b) {
   // have ended (a request's earlier histories may be in the previous wave)
   BCK(cudaEventRecord(b->upl, b->stream));
   BCK(cudaStreamWaitEvent(b->ws[m], b->upl, 0));
-  int rc = launch_graph(b, m, maxl, b->ws[m]);
+  int rc = launch_graph(b, m, maxl, lean, b->ws[m]);
   if (rc) return rc;
   BCK(cudaEventRecord(b->kdone[m], b->ws[m]));
   BCK(cudaStreamWaitEvent(b->cstream, b->kdone[m], 0));

@@ -7,5 +7,7 @@ cudaError_t launch_batch_op<float, OP_DT>(const BatchLaunch& L, int grid, int bl
   return launch_batch_unit<float, OP_DT>(L, grid, block, s);
 }
 template <>
-int batch_occupancy_op<float, OP_DT>(int maxl, int block) { return batch_occupancy_unit<float, OP_DT>(maxl, block); }
+int batch_occupancy_op<float, OP_DT>(int maxl, int lean, int block) {
+  return batch_occupancy_unit<float, OP_DT>(maxl, lean != 0, block);
+}
 }  // namespace sg
