@@ -792,9 +792,11 @@ struct Geom {
   // tolerance rule decides it.  Points reached by a flight, a history start or a split release are
   // not on a surface; in the mixed form they are classified by the sign of each surface function.
   // There the tolerances are sized to FP32 crossing accuracy (~4e-6 cm), and the rule would assign
-  // a shell of that thickness around every surface by flight direction: with the net current out
-  // of fuel pins it shrank the fuel the flights saw and lowered k by 1.5e-5 (correlated runs of the
-  // two forms).  The FP64 form applies the rule everywhere, as SCONE does.
+  // a shell of that thickness around every surface by flight direction instead of by position.
+  // The FP64 form applies the rule everywhere, as SCONE does (its 1e-12 tolerance leaves no shell).
+  // (The global position stays FP64 in the mixed form too: keeping it as a pair of floats added
+  // with error-free two-sums removed the FP64 adds and conversions per flight but measured slower,
+  // -8 % on the lattice with delta tracking and -12 % on the uneven batch, same GB300.)
   __device__ __forceinline__ bool place(Coords<R, MAXL>& c, bool onSurface = true) const {
     c.uni[0] = g.root;
     c.base[0] = 0;
