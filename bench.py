@@ -218,6 +218,26 @@ def host_bank_dict(b, n):
     return {k: b[k][:n].copy() for k in ("wgt", "r", "dir", "G", "time", "brood_id")}
 
 
+def link_d2h_gbps(nbytes, reps=5):
+    """The host link's device-to-host copy rate for one pinned copy of nbytes (CUDA events around a
+    torch copy): what the end-to-end call's copy back of the normalised bank can reach."""
+    import torch
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    host = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        host.copy_(dev, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del dev, host
+    return nbytes / best / 1e6
+
+
 def pinned_bank(src, n, cap):
     """A HostBank in page-locked host memory (cudaHostAlloc through torch), filled from src."""
     import torch
@@ -785,6 +805,8 @@ def main():
                "h2d": "page-locked host bank read in place by the kernels across the host link (no staging copy)",
                "d2h": "normalised next-cycle bank, cudaMemcpyAsync after the cycle",
                "transport_kernel_ms_per_step": e_tr / a.steps, "call_device_ms_per_step": e_cyc / a.steps}
+        e2e["link_d2h_gbps"] = link_d2h_gbps(e2e["d2h_bytes_per_step"])
+        e2e["d2h_ms_at_link_rate"] = e2e["d2h_bytes_per_step"] / (e2e["link_d2h_gbps"] * 1e6)
         # the gen loop alone through sg_transport_bank (a shim that keeps normSize_Repr in Fortran)
         nxt_cap = cap
         b_next = pinned_bank(None, 0, nxt_cap)
