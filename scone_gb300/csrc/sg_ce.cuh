@@ -53,27 +53,54 @@ __device__ __forceinline__ R ce_interp(const R* __restrict__ x, long long i, R f
   return x[(i + 1) * 4 + k] * f + (R(1) - f) * x[i * 4 + k];
 }
 
-// One energy's lookup context: E and its hash bin in the nuclide table.
+// One energy's lookup context: E, its hash bin in the nuclide table and, with the union table, its
+// floor index u in the union grid (-1 outside it).
 struct CEPoint {
   double E;
   int b;
+  int u;
 };
 
 template <class R>
 __device__ __forceinline__ CEPoint ce_point(const DCE<R>& d, double E) {
   CEPoint p;
   p.E = E;
-  p.b = ce_hash_bin(__logf((float)E), d.hLogMin, d.hInvStep, d.nHash);
+  const float lg = __logf((float)E);
+  p.b = ce_hash_bin(lg, d.hLogMin, d.hInvStep, d.nHash);
+  p.u = -1;
+  if (d.lidx) {
+    p.u = ce_search(d.lu, d.nLU, d.luhash, ce_hash_bin(lg, d.luLogMin, d.luInvStep, d.nLUHash), E);
+    // E on the last union point: its own row (ce_search gives the last interval), so that a nuclide
+    // grid ending in a repeated point finds its last index and the closed rule below
+    if (p.u == d.nLU - 2 && __double_as_longlong(E) == __double_as_longlong(d.lu[d.nLU - 1])) p.u = d.nLU - 1;
+  }
   return p;
 }
 
-// nuclide search: returns the global index of the lower grid point (or -1) and f
+// nuclide search: returns the global index of the lower grid point (or -1) and f.
+// With the union table one search per energy (in ce_point) serves every nuclide: every point of a
+// nuclide's grid is a union point, so no nuclide point lies strictly between union points u and
+// u + 1, and the nuclide's floor index at E equals its floor index at union point u, which the
+// table holds.  At the top of a nuclide's grid the closed rule of binaryFloorIdxClosed applies: E
+// equal to its last point takes the last interval, anything above is outside.  The result is the
+// index ce_search would find, so both forms keep their results bit for bit.
 template <class R>
 __device__ __forceinline__ long long ce_nuc_search(const DCE<R>& d, int nuc, const CEPoint& p, R& f) {
   const long long o = d.off[nuc];
   const int n = (int)(d.off[nuc + 1] - o);
-  const int i = ce_search(d.e + o, n, d.hash + (long long)nuc * d.nHash, p.b, p.E);
-  if (i < 0) return -1;
+  int i;
+  if (d.lidx) {
+    if (p.u < 0) return -1;
+    i = d.lidx[(long long)p.u * d.nNuc + nuc];
+    if (i < 0) return -1;
+    if (i == n - 1) {
+      if (__double_as_longlong(p.E) != __double_as_longlong(d.e[o + n - 1])) return -1;
+      i = n - 2;
+    }
+  } else {
+    i = ce_search(d.e + o, n, d.hash + (long long)nuc * d.nHash, p.b, p.E);
+    if (i < 0) return -1;
+  }
   f = ce_factor<R>(d.e + o, i, p.E);
   return o + i;
 }

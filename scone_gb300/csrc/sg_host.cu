@@ -160,7 +160,9 @@ struct sg_handle_t {
   DArr<double> ceXs64, ceA64, ceKT64, ceDens64, ceMaj64;
   DArr<float> ceXsF, ceAF, ceKTF, ceDensF, ceMajF;
   DArr<long long> ceOff;
-  DArr<int2> ceHash, ceUHash;
+  DArr<int2> ceHash, ceUHash, ceLUHash;
+  DArr<double> ceLU;
+  DArr<int> ceLIdx;
   DArr<int> ceMatPtr, ceMatNuc, ceAct;
   DCE<double> ce64{};
   DCE<float> ceMx{};
@@ -857,6 +859,37 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
     uInvStep = (float)(nUHash / (std::log(ue.back()) - std::log(ue.front())));
     uhash = hash_brackets(ue.data(), (int)ue.size(), nUHash, uLogMin, uInvStep);
   }
+  // lookup union: every nuclide's grid points, sorted and de-duplicated, with each nuclide's floor
+  // index at every union point (a merge walk per nuclide).  Built when the table stays below 2^26
+  // entries (256 MB); otherwise the kernels search each nuclide's grid.
+  std::vector<double> lu;
+  std::vector<int> lidx;
+  std::vector<int2> luhash;
+  int nLUHash = 0;
+  float luLogMin = 0.f, luInvStep = 0.f;
+  {
+    lu.assign(d->e, d->e + nP);
+    std::sort(lu.begin(), lu.end());
+    lu.erase(std::unique(lu.begin(), lu.end()), lu.end());
+    if (lu.size() >= 2 && (double)lu.size() * nN <= (double)(1 << 26)) {
+      lidx.resize(lu.size() * (size_t)nN);
+      for (int n = 0; n < nN; ++n) {
+        const double* en = d->e + off[n];
+        const long long cnt = off[n + 1] - off[n];
+        long long j = 0;
+        for (size_t u = 0; u < lu.size(); ++u) {
+          while (j + 1 < cnt && en[j + 1] <= lu[u]) ++j;
+          lidx[u * nN + n] = (lu[u] < en[0]) ? -1 : (int)j;
+        }
+      }
+      nLUHash = (int)std::min<size_t>(1u << 18, std::max<size_t>(1024, lu.size() / 4));
+      luLogMin = (float)std::log(lu.front());
+      luInvStep = (float)(nLUHash / (std::log(lu.back()) - std::log(lu.front())));
+      luhash = hash_brackets(lu.data(), (int)lu.size(), nLUHash, luLogMin, luInvStep);
+    } else {
+      lu.clear();
+    }
+  }
   // uploads
   cudaStream_t st = h->stream;
   std::vector<double> e(d->e, d->e + nP), xs(d->xs, d->xs + 4 * nP), A(d->A, d->A + nN), kT(d->kT, d->kT + nN);
@@ -880,6 +913,11 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
   CK(h->ceMaj64.upload(umaj, st));
   CK(h->ceMajF.upload(std::vector<float>(umaj.begin(), umaj.end()), st));
   CK(h->ceUHash.upload(uhash, st));
+  if (!lidx.empty()) {
+    CK(h->ceLU.upload(lu, st));
+    CK(h->ceLIdx.upload(lidx, st));
+    CK(h->ceLUHash.upload(luhash, st));
+  }
   const double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
   auto fill = [&](auto& D, auto xsP, auto aP, auto ktP, auto densP, auto majP) {
     using RR = std::remove_reference_t<decltype(*xsP)>;
@@ -891,6 +929,11 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
     D.ue = h->ceUE.p; D.umaj = majP; D.uhash = h->ceUHash.p; D.nU = (int)ue.size(); D.nUHash = nUHash;
     D.uLogMin = uLogMin; D.uInvStep = uInvStep;
     D.act = h->ceAct.p; D.nAct = (int)act.size();
+    D.lu = lidx.empty() ? nullptr : h->ceLU.p;
+    D.lidx = lidx.empty() ? nullptr : h->ceLIdx.p;
+    D.luhash = lidx.empty() ? nullptr : h->ceLUHash.p;
+    D.nLU = (int)lu.size(); D.nLUHash = nLUHash;
+    D.luLogMin = luLogMin; D.luInvStep = luInvStep;
     D.minE = d->min_e; D.threshE = (RR)d->thresh_e; D.threshA = (RR)d->thresh_a; D.collisionXS = (RR)cxs;
   };
   fill(h->ce64, (const double*)h->ceXs64.p, (const double*)h->ceA64.p, (const double*)h->ceKT64.p,
@@ -1683,7 +1726,7 @@ int32_t sg_destroy(sg_handle h) {
   h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();
   h->ceE.free(); h->ceUE.free(); h->ceXs64.free(); h->ceA64.free(); h->ceKT64.free(); h->ceDens64.free();
   h->ceMaj64.free(); h->ceXsF.free(); h->ceAF.free(); h->ceKTF.free(); h->ceDensF.free(); h->ceMajF.free();
-  h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
+  h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceLUHash.free(); h->ceLU.free(); h->ceLIdx.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
   h->pE.free();
   h->wwLo64.free(); h->wwUp64.free(); h->wwLo32.free(); h->wwUp32.free(); h->dColl64.free(); h->dColl32.free();
   h->bufR.free(); h->bufE.free(); h->bufU64.free(); h->bufW64.free(); h->bufT64.free(); h->bufU32.free();

@@ -117,6 +117,13 @@ struct DCE {
   float uLogMin, uInvStep;
   const int* act;           // active materials (1-based), for the on-the-fly majorant
   int nAct;
+  // lookup acceleration: the union of every nuclide's grid and, per union point, each nuclide's
+  // floor index there ([nLU][nNuc], -1 below the nuclide's grid); null when not built
+  const double* lu;
+  const int* lidx;
+  const int2* luhash;
+  int nLU, nLUHash;
+  float luLogMin, luInvStep;
   double minE;              // neutronCEstd minEnergy cut-off
   R threshE, threshA;       // free-gas thresholds
   R collisionXS;

@@ -209,3 +209,25 @@ def test_scone_h1_table_on_the_device(gpu_mod, oracle_mod, transport):
     p = problems.Problem(gb.arrays(), None, ce=ce, source=dict(r=(0.0, 0.0, 0.0), E=1.0))
     bins = _history_parity(gpu_mod, oracle_mod, p, transport, 1500, [abi.clerk(abi.CLERK_COLLISION, axes=ax)])
     assert (bins[:, 1] > 0).sum() > 30                         # the spectrum spans the slowing-down range
+
+
+@pytest.mark.parametrize("where", ["top", "repeated"])
+@pytest.mark.parametrize("transport", [abi.TRANSPORT_ST, abi.TRANSPORT_DT])
+def test_ce_lookup_edges_fp64_parity(gpu_mod, oracle_mod, transport, where):
+    """The grid lookups at their edges, per history against the oracle: nuclide 0 gets a repeated
+    interior grid point (a step in its cross sections), and every history starts exactly on a grid
+    point -- the top of every grid (20 MeV: binaryFloorIdxClosed's closed end takes the last
+    interval) or the repeated point (the floor index is the later of the two)."""
+    p = problems.ce_slab_3layer(scale=0.05)
+    ce = dict(p.ce)
+    ptr, e, xs = np.asarray(ce["nuc_ptr"]), np.asarray(ce["e"]), np.asarray(ce["xs"])
+    k = int(ptr[1]) // 2
+    ce["e"] = np.insert(e, k + 1, e[k])
+    ce["xs"] = np.insert(xs, k + 1, xs[k] * 1.5, axis=0)
+    ptr2 = ptr.copy()
+    ptr2[1:] += 1
+    ce["nuc_ptr"] = ptr2
+    E = 20.0 if where == "top" else float(e[k])
+    q = problems.Problem(p.geometry, None, name="ce_slab_edges", ce=ce, source=dict(r=(15.0, 0.0, 0.0), E=E),
+                         tallies=p.tallies)
+    _history_parity(gpu_mod, oracle_mod, q, transport, 3000, q.tallies["current"])
