@@ -139,8 +139,19 @@ __device__ __forceinline__ bool ce_mat_macro(const DCE<R>& d, int mat, const CEP
 template <class R>
 __device__ __forceinline__ bool ce_majorant(const DCE<R>& d, const CEPoint& p, R& xs) {
   if (d.hasMajorant) {
-    const int b = ce_hash_bin(__logf((float)p.E), d.uLogMin, d.uInvStep, d.nUHash);
-    const int i = ce_search(d.ue, d.nU, d.uhash, b, p.E);
+    int i;
+    if (d.lmaj) {                      // every majorant grid point is a union point: a table read
+      if (p.u < 0) return false;
+      i = d.lmaj[p.u];
+      if (i < 0) return false;
+      if (i == d.nU - 1) {
+        if (__double_as_longlong(p.E) != __double_as_longlong(d.ue[d.nU - 1])) return false;
+        i = d.nU - 2;
+      }
+    } else {
+      const int b = ce_hash_bin(__logf((float)p.E), d.uLogMin, d.uInvStep, d.nUHash);
+      i = ce_search(d.ue, d.nU, d.uhash, b, p.E);
+    }
     if (i < 0) return false;
     const R f = ce_factor<R>(d.ue, i, p.E);
     xs = d.umaj[i + 1] * f + (R(1) - f) * d.umaj[i];

@@ -162,7 +162,7 @@ struct sg_handle_t {
   DArr<long long> ceOff;
   DArr<int2> ceHash, ceUHash, ceLUHash;
   DArr<double> ceLU;
-  DArr<int> ceLIdx;
+  DArr<int> ceLIdx, ceLMaj;
   DArr<int> ceMatPtr, ceMatNuc, ceAct;
   DCE<double> ce64{};
   DCE<float> ceMx{};
@@ -863,7 +863,7 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
   // index at every union point (a merge walk per nuclide).  Built when the table stays below 2^26
   // entries (256 MB); otherwise the kernels search each nuclide's grid.
   std::vector<double> lu;
-  std::vector<int> lidx;
+  std::vector<int> lidx, lmaj;
   std::vector<int2> luhash;
   int nLUHash = 0;
   float luLogMin = 0.f, luInvStep = 0.f;
@@ -886,6 +886,17 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
       luLogMin = (float)std::log(lu.front());
       luInvStep = (float)(nLUHash / (std::log(lu.back()) - std::log(lu.front())));
       luhash = hash_brackets(lu.data(), (int)lu.size(), nLUHash, luLogMin, luInvStep);
+      if (d->majorant) {               // the majorant grid's points are union points too
+        lmaj.resize(lu.size());
+        long long j = 0;
+        const long long cnt = (long long)ue.size();
+        for (size_t u = 0; u < lu.size(); ++u) {
+          while (j + 1 < cnt && ue[j + 1] <= lu[u]) ++j;
+          lmaj[u] = (lu[u] < ue[0]) ? -1 : (int)j;
+        }
+        for (double x : ue)            // guard: a majorant point outside the union disables the table
+          if (!std::binary_search(lu.begin(), lu.end(), x)) { lmaj.clear(); break; }
+      }
     } else {
       lu.clear();
     }
@@ -917,6 +928,7 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
     CK(h->ceLU.upload(lu, st));
     CK(h->ceLIdx.upload(lidx, st));
     CK(h->ceLUHash.upload(luhash, st));
+    if (!lmaj.empty()) CK(h->ceLMaj.upload(lmaj, st));
   }
   const double cxs = d->avg_dist > 0.0 ? 1.0 / d->avg_dist : 0.0;
   auto fill = [&](auto& D, auto xsP, auto aP, auto ktP, auto densP, auto majP) {
@@ -932,6 +944,7 @@ int build_ce(sg_handle h, const sg_ce_desc* d) {
     D.lu = lidx.empty() ? nullptr : h->ceLU.p;
     D.lidx = lidx.empty() ? nullptr : h->ceLIdx.p;
     D.luhash = lidx.empty() ? nullptr : h->ceLUHash.p;
+    D.lmaj = (lidx.empty() || lmaj.empty()) ? nullptr : h->ceLMaj.p;
     D.nLU = (int)lu.size(); D.nLUHash = nLUHash;
     D.luLogMin = luLogMin; D.luInvStep = luInvStep;
     D.minE = d->min_e; D.threshE = (RR)d->thresh_e; D.threshA = (RR)d->thresh_a; D.collisionXS = (RR)cxs;
@@ -1726,7 +1739,7 @@ int32_t sg_destroy(sg_handle h) {
   h->pGeo.free(); h->pInts.free(); h->pRng.free(); h->qT0.free(); h->qT1.free(); h->qC.free(); h->qCtr.free();
   h->ceE.free(); h->ceUE.free(); h->ceXs64.free(); h->ceA64.free(); h->ceKT64.free(); h->ceDens64.free();
   h->ceMaj64.free(); h->ceXsF.free(); h->ceAF.free(); h->ceKTF.free(); h->ceDensF.free(); h->ceMajF.free();
-  h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceLUHash.free(); h->ceLU.free(); h->ceLIdx.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
+  h->ceOff.free(); h->ceHash.free(); h->ceUHash.free(); h->ceLUHash.free(); h->ceLU.free(); h->ceLIdx.free(); h->ceLMaj.free(); h->ceMatPtr.free(); h->ceMatNuc.free(); h->ceAct.free();
   h->pE.free();
   h->wwLo64.free(); h->wwUp64.free(); h->wwLo32.free(); h->wwUp32.free(); h->dColl64.free(); h->dColl32.free();
   h->bufR.free(); h->bufE.free(); h->bufU64.free(); h->bufW64.free(); h->bufT64.free(); h->bufU32.free();

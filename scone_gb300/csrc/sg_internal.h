@@ -121,6 +121,7 @@ struct DCE {
   // floor index there ([nLU][nNuc], -1 below the nuclide's grid); null when not built
   const double* lu;
   const int* lidx;
+  const int* lmaj;          // [nLU] floor index of each union point in the majorant grid ue (-1 below)
   const int2* luhash;
   int nLU, nLUHash;
   float luLogMin, luInvStep;
