@@ -102,7 +102,7 @@ __device__ __forceinline__ void start_batched(Tracker<R, MAXL, OP, false, LEAN>&
 // LEAN: every problem of the launch runs without rotated universes, cell maps, current clerks or P1
 // scattering (BatchLaunch::lean), so the lean Tracker is compiled
 template <class R, int MAXL, int OP, bool LEAN = false>
-__global__ void __launch_bounds__(128, (history_min_blocks<R, false, OP>())) k_batch(const __grid_constant__ BatchLaunch L) {
+__global__ void __launch_bounds__(128, (batch_min_blocks<R, OP>())) k_batch(const __grid_constant__ BatchLaunch L) {
   __shared__ __align__(16) unsigned char s_rec[BATCH_MAX_WARPS][sizeof(BatchProblem<R>)];
   __shared__ __align__(8) unsigned long long s_bar[BATCH_MAX_WARPS];
   __shared__ RngJump s_jump;
