@@ -202,3 +202,46 @@ def test_load_balance_moves_particles_to_neighbours():
         t.join()
     assert [b.n for b in out] == [4, 4, 4]
     assert np.array_equal(np.concatenate([b["wgt"] for b in out]), np.arange(12, dtype=np.float64))
+
+
+def _balance(pops, tot):
+    comms = replicas.ThreadComm.group(len(pops))
+    start = np.cumsum([0] + pops)
+    out, errs = [None] * len(pops), []
+
+    def body(r):
+        n = pops[r]
+        ids = np.arange(start[r], start[r] + n, dtype=np.float64)
+        bank = abi.HostBank(n, dict(r=np.repeat(ids[:, None], 3, 1), dir=np.zeros((n, 3)), wgt=ids,
+                                    time=np.zeros(n), E=np.zeros(n), G=np.ones(n, np.int32),
+                                    brood_id=np.ones(n, np.int32)))
+        try:
+            out[r] = replicas.load_balance(comms[r], bank, n, tot, pops)
+        except RuntimeError as e:
+            errs.append(e)
+            comms[r].sh.barrier.abort()
+            for q in comms[r].sh.boxes.values():        # wake a neighbour blocked on a receive
+                q.put(np.zeros((0, 11)))
+
+    th = [threading.Thread(target=body, args=(r,)) for r in range(len(pops))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(timeout=60)
+    return out, errs
+
+
+def test_load_balance_from_a_middle_rank_holding_everything():
+    """All 12 particles on the middle one of 3 ranks: it passes 4 up and 4 down in one exchange."""
+    out, errs = _balance([0, 12, 0], 12)
+    assert not errs
+    assert [b.n for b in out] == [4, 4, 4]
+    assert np.array_equal(np.concatenate([b["wgt"] for b in out]), np.arange(12, dtype=np.float64))
+
+
+def test_load_balance_refuses_what_neighbour_passes_cannot_settle():
+    """All particles on the first of 3 ranks: the second would have to pass particles up before it
+    has received them.  SCONE's nearest-neighbour scheme assumes shares near the workshare (what
+    normSize_Repr leaves); here the exchange fails with an error instead of passing garbage."""
+    out, errs = _balance([12, 0, 0], 12)
+    assert errs and "more particles than it holds" in str(errs[0])
